@@ -1,0 +1,234 @@
+"""ctypes bindings for the CPU oracle (oracle/liboracle.so) and, where it was
+built, the reference objects (oracle/_ref/libffea_ref.so).
+
+TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's
+cpu_baseline / --impl reference legs use this module as the checker.  The
+product (ffea_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libffea_ref.so")
+REF_KAT = os.path.join(HERE, "_ref", "test_rngstream")
+REFERENCE_SRC = os.environ.get("FFEA_REFERENCE_SRC", "/root/reference")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+def build(ref: bool | None = None, quiet: bool = True) -> None:
+    """Compile the oracle (and the reference objects when their sources exist)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-C", HERE, "port"], check=True, stdout=out)
+    if ref is None:
+        ref = os.path.isdir(os.path.join(REFERENCE_SRC, "src"))
+    if ref:
+        subprocess.run(["make", "-C", HERE, "-j8", "ref", f"REF={REFERENCE_SRC}"], check=True, stdout=out)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def _declare(lib, prefix):
+    f = getattr(lib, prefix + "_blob_create")
+    f.restype = ctypes.c_void_p
+    f.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _ip, _dp, _dp, ctypes.c_int, _ip, _dp, _ip]
+    for name, res, args in [
+        ("_blob_destroy", None, [ctypes.c_void_p]),
+        ("_blob_seed", None, [ctypes.c_void_p, ctypes.c_int]),
+        ("_blob_step", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+        ("_blob_get_nodes", None, [ctypes.c_void_p, _dp, _dp, _dp]),
+        ("_blob_get_rhs", None, [ctypes.c_void_p, _dp]),
+        ("_blob_get_element_forces", None, [ctypes.c_void_p, _dp]),
+        ("_blob_last_inversions", ctypes.c_int, [ctypes.c_void_p]),
+    ]:
+        fn = getattr(lib, prefix + name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+_port = None
+_ref = None
+
+
+def port_lib():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_SO):
+            build(ref=False)
+        lib = ctypes.CDLL(PORT_SO)
+        _declare(lib, "orc")
+        lib.orc_blob_set_rng_state.argtypes = [ctypes.c_void_p, ctypes.c_int, _u64p]
+        lib.orc_blob_get_rng_state.argtypes = [ctypes.c_void_p, ctypes.c_int, _u64p]
+        lib.orc_blob_set_nodes.argtypes = [ctypes.c_void_p, _dp, _dp]
+        lib.orc_blob_last_cg_iters.restype = ctypes.c_int
+        lib.orc_blob_last_cg_iters.argtypes = [ctypes.c_void_p]
+        lib.orc_blob_energies.argtypes = [ctypes.c_void_p, _dp, _dp]
+        lib.orc_blob_apply_nomass.argtypes = [ctypes.c_void_p, _dp, _dp]
+        lib.orc_rng_draws.argtypes = [_u64p, ctypes.c_int64, _dp]
+        lib.orc_rng_jump.argtypes = [_u64p, ctypes.c_uint64]
+        lib.orc_rng_package_kat.restype = ctypes.c_double
+        lib.orc_ffea_seed.argtypes = [ctypes.c_int, _u64p]
+        lib.orc_ffea_thread_stream.argtypes = [_u64p, ctypes.c_int, _u64p]
+        lib.orc_num_threads_available.restype = ctypes.c_int
+        _port = lib
+    return _port
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        lib = ctypes.CDLL(REF_SO)
+        _declare(lib, "ref")
+        lib.ref_blob_set_rng_state.argtypes = [ctypes.c_void_p, _u64p]
+        lib.ref_blob_get_rng_state.argtypes = [ctypes.c_void_p, _u64p]
+        lib.ref_ffea_seed.argtypes = [ctypes.c_int, _u64p]
+        lib.ref_rng_draws.argtypes = [_u64p, ctypes.c_int64, _dp]
+        lib.ref_rng_advance.argtypes = [_u64p, ctypes.c_long, ctypes.c_long, _u64p]
+        _ref = lib
+    return _ref
+
+
+# ---------------------------------------------------------------- RNG helpers
+def ffea_seed(rng_seed: int) -> np.ndarray:
+    out = np.zeros(6, np.uint64)
+    port_lib().orc_ffea_seed(int(rng_seed), _ptr(out, _u64p))
+    return out
+
+
+def thread_stream(six, k: int) -> np.ndarray:
+    six = np.ascontiguousarray(six, dtype=np.uint64)
+    out = np.zeros(6, np.uint64)
+    port_lib().orc_ffea_thread_stream(_ptr(six, _u64p), int(k), _ptr(out, _u64p))
+    return out
+
+
+def rng_draws(state, n: int):
+    """(draws, state after) from a 6-word MRG32k3a state."""
+    st = np.ascontiguousarray(state, dtype=np.uint64).copy()
+    out = np.zeros(int(n), np.float64)
+    port_lib().orc_rng_draws(_ptr(st, _u64p), int(n), _ptr(out, _dp))
+    return out, st
+
+
+def rng_jump(state, n: int) -> np.ndarray:
+    st = np.ascontiguousarray(state, dtype=np.uint64).copy()
+    port_lib().orc_rng_jump(_ptr(st, _u64p), ctypes.c_uint64(int(n)))
+    return st
+
+
+def rng_package_kat() -> float:
+    return port_lib().orc_rng_package_kat()
+
+
+# ---------------------------------------------------------------- blobs
+class OracleBlob:
+    """One blob stepped by the oracle ("port") or by the reference objects ("ref")."""
+
+    def __init__(self, pos, topology, material, drag, pinned, dt, kT, epsilon2, max_iterations_cg=1000,
+                 calc_noise=1, calc_stokes=1, solver=0, num_threads=1, impl="port"):
+        self.impl = impl
+        self.lib = port_lib() if impl == "port" else ref_lib()
+        self.pfx = "orc" if impl == "port" else "ref"
+        self.pos0 = np.ascontiguousarray(pos, dtype=np.float64)
+        self.topo = np.ascontiguousarray(topology, dtype=np.int32)
+        self.mat = np.ascontiguousarray(material, dtype=np.float64)
+        self.drag = np.ascontiguousarray(drag, dtype=np.float64)
+        self.pinned = np.ascontiguousarray(pinned if pinned is not None else np.zeros(0), dtype=np.int32)
+        self.n = len(self.pos0)
+        self.e = len(self.topo)
+        fp = np.array([dt, kT, epsilon2], np.float64)
+        ip = np.array([max_iterations_cg, calc_noise, calc_stokes, solver, num_threads], np.int32)
+        self.h = getattr(self.lib, self.pfx + "_blob_create")(
+            self.n, self.e, _ptr(self.pos0, _dp), _ptr(self.topo, _ip), _ptr(self.mat, _dp),
+            _ptr(self.drag, _dp), len(self.pinned), _ptr(self.pinned, _ip), _ptr(fp, _dp), _ptr(ip, _ip))
+        if not self.h:
+            raise RuntimeError("oracle blob creation failed")
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            getattr(self.lib, self.pfx + "_blob_destroy")(h)
+            self.h = None
+
+    def seed(self, rng_seed: int):
+        getattr(self.lib, self.pfx + "_blob_seed")(self.h, int(rng_seed))
+
+    def set_rng_state(self, st, thread: int = 0):
+        st = np.ascontiguousarray(st, dtype=np.uint64)
+        if self.impl == "port":
+            self.lib.orc_blob_set_rng_state(self.h, thread, _ptr(st, _u64p))
+        else:
+            self.lib.ref_blob_set_rng_state(self.h, _ptr(st, _u64p))
+
+    def rng_state(self, thread: int = 0) -> np.ndarray:
+        st = np.zeros(6, np.uint64)
+        if self.impl == "port":
+            self.lib.orc_blob_get_rng_state(self.h, thread, _ptr(st, _u64p))
+        else:
+            self.lib.ref_blob_get_rng_state(self.h, _ptr(st, _u64p))
+        return st
+
+    def step(self, nsteps: int = 1) -> int:
+        return getattr(self.lib, self.pfx + "_blob_step")(self.h, int(nsteps))
+
+    def nodes(self):
+        pos = np.zeros((self.n, 3)); vel = np.zeros((self.n, 3)); frc = np.zeros((self.n, 3))
+        getattr(self.lib, self.pfx + "_blob_get_nodes")(self.h, _ptr(pos, _dp), _ptr(vel, _dp), _ptr(frc, _dp))
+        return pos, vel, frc
+
+    def set_nodes(self, pos=None, vel=None):
+        pos = None if pos is None else np.ascontiguousarray(pos, dtype=np.float64)
+        vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64)
+        self.lib.orc_blob_set_nodes(self.h, _ptr(pos, _dp), _ptr(vel, _dp))
+
+    def rhs(self):
+        out = np.zeros((self.n, 3))
+        getattr(self.lib, self.pfx + "_blob_get_rhs")(self.h, _ptr(out, _dp))
+        return out
+
+    def element_forces(self):
+        out = np.zeros((self.e, 4, 3))
+        getattr(self.lib, self.pfx + "_blob_get_element_forces")(self.h, _ptr(out, _dp))
+        return out
+
+    def last_inversions(self) -> int:
+        return getattr(self.lib, self.pfx + "_blob_last_inversions")(self.h)
+
+    def last_cg_iters(self) -> int:
+        return self.lib.orc_blob_last_cg_iters(self.h)
+
+    def energies(self):
+        s = ctypes.c_double(); k = ctypes.c_double()
+        self.lib.orc_blob_energies(self.h, ctypes.byref(s), ctypes.byref(k))
+        return s.value, k.value
+
+    def apply_nomass(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+        out = np.zeros_like(x)
+        self.lib.orc_blob_apply_nomass(self.h, _ptr(x, _dp), _ptr(out, _dp))
+        return out.reshape(-1, 3)
+
+
+def blob_from_spec(spec, impl="port", num_threads=1, epsilon2=None, seed=True):
+    """OracleBlob from an ffea_gb300.mesh.BlobSpec-like object."""
+    p = spec.params
+    b = OracleBlob(spec.mesh.pos, spec.mesh.topology, spec.material, spec.drag, spec.pinned, p.dt, p.kT,
+                   p.epsilon2 if epsilon2 is None else epsilon2, p.max_iterations_cg, p.calc_noise,
+                   p.calc_stokes, p.solver, num_threads, impl)
+    if seed:
+        b.seed(p.rng_seed)
+    return b
