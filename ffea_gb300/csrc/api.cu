@@ -1,0 +1,674 @@
+// api.cu -- the extern "C" boundary (include/ffea_gpu.h).
+//
+// A handle owns one packed batch of blobs in HBM, one CUDA stream and, in
+// graph mode, one instantiated CUDA graph per step:
+//   elements -> assemble -> nodes -> while(any blob iterating){ spmv, update, pupdate } -> euler
+// The CG loop runs as a device-side conditional WHILE node: the update
+// kernel's last CTA decides whether another iteration is needed, so a step
+// (and a run of steps) needs no host synchronisation.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ffea_gpu.h"
+#include "host_build.h"
+#include "kernels.h"
+
+using namespace ffea;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return FFEA_GPU_ERROR;
+}
+
+#define CK(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) return fail("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                  \
+    } while (0)
+
+struct DeviceArena {
+    std::vector<void *> ptrs;
+    ~DeviceArena()
+    {
+        for (void *p : ptrs) cudaFree(p);
+    }
+    template <typename T>
+    cudaError_t alloc(T *&out, size_t count)
+    {
+        void *p = nullptr;
+        size_t bytes = count * sizeof(T);
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) return e;
+        ptrs.push_back(p);
+        e = cudaMemset(p, 0, bytes);
+        out = static_cast<T *>(p);
+        return e;
+    }
+    cudaError_t alloc_bytes(void *&out, size_t bytes)
+    {
+        char *p = nullptr;
+        cudaError_t e = alloc(p, bytes);
+        out = p;
+        return e;
+    }
+};
+
+template <typename T>
+cudaError_t upload(DeviceArena &A, T *&dst, const std::vector<T> &src)
+{
+    cudaError_t e = A.alloc(dst, src.size());
+    if (e != cudaSuccess || src.empty()) return e;
+    return cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+// process-wide jump table per device (for ffea_gpu_rng_draws)
+std::mutex g_table_mu;
+std::vector<mrg::JumpMat *> g_tables;
+
+}  // namespace
+
+struct ffea_gpu {
+    HostBatch host;
+    DeviceBatch dev;
+    DeviceArena arena;
+    cudaStream_t stream = nullptr, side = nullptr;
+    cudaGraphExec_t step_exec = nullptr;
+    int graph_mode = 1;
+    int timing = 0;
+    double phase_ms[5] = {0, 0, 0, 0, 0};
+    cudaEvent_t ev[6] = {};
+    int32_t *running_host = nullptr;  // pinned
+    int last_iters = 8;
+    size_t tsize = 4;
+    std::vector<std::vector<double>> sec_vel;  // per blob: initial velocities of secondary nodes
+    ~ffea_gpu()
+    {
+        if (step_exec) cudaGraphExecDestroy(step_exec);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        if (running_host) cudaFreeHost(running_host);
+        if (stream) cudaStreamDestroy(stream);
+        if (side) cudaStreamDestroy(side);
+    }
+};
+
+namespace {
+
+int build_step_graph(ffea_gpu *h)
+{
+    DeviceBatch &d = h->dev;
+    cudaStream_t s = h->stream;
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t cap_graph = nullptr;
+    CK(cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap_graph, nullptr, nullptr, nullptr));
+    cudaGraphConditionalHandle cond;
+    CK(cudaGraphConditionalHandleCreate(&cond, cap_graph, 1, cudaGraphCondAssignDefault));
+    launch_elements(d, s, ELEM_STEP);
+    if (d.any_nomass) launch_assemble(d, s);
+    launch_nodes(d, s, 0, (unsigned long long)cond);
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    CK(cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap_graph, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    CK(cudaGraphAddNode(&cnode, cap_graph, deps, nullptr, ndeps, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(h->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    launch_cg_iteration(d, h->side, (unsigned long long)cond);
+    cudaGraph_t body_out = nullptr;
+    CK(cudaStreamEndCapture(h->side, &body_out));
+    CK(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    if (h->host.bp[0].true_residual) launch_true_residual(d, s);
+    launch_euler(d, s);
+    CK(cudaStreamEndCapture(s, &graph));
+    cudaError_t e = cudaGraphInstantiate(&h->step_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail("cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+    return FFEA_GPU_OK;
+}
+
+// CG loop driven from the host: launch chunks of iterations, check the
+// device flag between chunks.  Converged blobs make the kernels return early.
+int host_cg_loop(ffea_gpu *h)
+{
+    int chunk = h->last_iters > 4 ? h->last_iters : 4;
+    int total = 0;
+    int max_iter = 0;
+    for (auto &bp : h->host.bp) max_iter = bp.max_iter > max_iter ? bp.max_iter : max_iter;
+    while (total <= max_iter + 1) {
+        for (int i = 0; i < chunk; i++) launch_cg_iteration(h->dev, h->stream, 0);
+        total += chunk;
+        CK(cudaMemcpyAsync(h->running_host, h->dev.any_running, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (!*h->running_host) break;
+        chunk = 4;
+    }
+    h->last_iters = total;
+    return FFEA_GPU_OK;
+}
+
+int check_blob(ffea_gpu *h, int32_t blob)
+{
+    if (!h) return fail("null handle");
+    if (blob < 0 || blob >= h->host.num_blobs) return fail("blob index %d out of range [0, %d)", blob, h->host.num_blobs);
+    return FFEA_GPU_OK;
+}
+
+// device -> host copy of a T-typed array slice into doubles
+int copy_typed_to_double(ffea_gpu *h, const void *src, size_t offset, size_t count, std::vector<double> &out)
+{
+    out.resize(count);
+    if (h->dev.precision == PREC_FP64) {
+        CK(cudaMemcpy(out.data(), static_cast<const double *>(src) + offset, count * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> tmp(count);
+        CK(cudaMemcpy(tmp.data(), static_cast<const float *>(src) + offset, count * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < count; i++) out[i] = tmp[i];
+    }
+    return FFEA_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ffea_gpu_last_error(char *buf, size_t len)
+{
+    if (!buf || len == 0) return FFEA_GPU_ERROR;
+    std::snprintf(buf, len, "%s", g_last_error.c_str());
+    return FFEA_GPU_OK;
+}
+
+int64_t ffea_gpu_kernel_launches(void) { return kernel_launch_count(); }
+
+int ffea_gpu_ffea_seed(int32_t rng_seed, uint64_t out[6])
+{
+    if (!out) return fail("null output");
+    ffea_seed_words(rng_seed, out);
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_params *params,
+                          int32_t rng_mode, ffea_gpu_t **out)
+{
+    if (!out || !meshes || !params) return fail("null argument");
+    *out = nullptr;
+    if (rng_mode != FFEA_GPU_RNG_PER_BLOB && rng_mode != FFEA_GPU_RNG_SHARED) return fail("unknown rng_mode");
+    std::unique_ptr<ffea_gpu> h(new ffea_gpu());
+    std::string err;
+    if (!build_batch(num_blobs, meshes, params, rng_mode, h->host, err)) return fail("%s", err.c_str());
+    HostBatch &H = h->host;
+    DeviceBatch &d = h->dev;
+    DeviceArena &A = h->arena;
+    d.num_blobs = H.num_blobs;
+    d.nl_pad = H.nl_pad;
+    d.ne_pad = H.ne_pad;
+    d.n_edges = H.n_edges;
+    d.n_tiles = H.n_tiles;
+    d.n_etiles = H.n_etiles;
+    d.num_streams = H.num_streams;
+    d.precision = H.precision;
+    d.any_mass = H.any_mass;
+    d.any_nomass = H.any_nomass;
+    const size_t ts = H.precision == PREC_FP64 ? sizeof(double) : sizeof(float);
+    h->tsize = ts;
+    CK(upload(A, d.bp, H.bp));
+    CK(upload(A, d.mats, H.materials));
+    CK(upload(A, d.tile_blob, H.tile_blob));
+    CK(upload(A, d.etile_blob, H.etile_blob));
+    std::vector<mrg::JumpMat> table(mrg::JUMP_TABLE_ENTRIES);
+    mrg::build_jump_table(table.data());
+    CK(upload(A, d.jump_table, table));
+    CK(upload(A, d.stream_state, H.stream_state));
+    CK(upload(A, d.stream_step, H.stream_step));
+    CK(upload(A, d.pos, H.pos));
+    CK(upload(A, d.vel, H.vel));
+    CK(upload(A, d.drag, H.drag));
+    CK(upload(A, d.flags, H.flags));
+    CK(upload(A, d.orig, H.orig));
+    CK(upload(A, d.gather_ptr, H.gather_ptr));
+    CK(upload(A, d.gather_idx, H.gather_idx));
+    CK(upload(A, d.fold_ptr, H.fold_ptr));
+    CK(upload(A, d.fold_sec, H.fold_sec));
+    CK(upload(A, d.fold_drag, H.fold_drag));
+    CK(upload(A, d.conn, H.conn));
+    CK(upload(A, d.mat_id, H.mat_id));
+    CK(upload(A, d.edge_p, H.edge_p));
+    CK(upload(A, d.edge_q, H.edge_q));
+    CK(upload(A, d.edge_cptr, H.edge_cptr));
+    CK(upload(A, d.edge_cidx, H.edge_cidx));
+    CK(upload(A, d.up_ptr, H.up_ptr));
+    CK(upload(A, d.lo_ptr, H.lo_ptr));
+    CK(upload(A, d.lo_edge, H.lo_edge));
+    const size_t n3 = 3 * (size_t)H.nl_pad;
+    CK(A.alloc(d.rhs, n3));
+    CK(A.alloc(d.x, n3));
+    CK(A.alloc(d.r, n3));
+    CK(A.alloc_bytes(d.p, n3 * ts));
+    CK(A.alloc_bytes(d.q, n3 * ts));
+    CK(A.alloc_bytes(d.dinv, n3 * ts));
+    CK(A.alloc(d.det_sign, (size_t)H.ne_pad));
+    CK(A.alloc_bytes(d.jinv0, 9 * (size_t)H.ne_pad * ts));
+    CK(A.alloc_bytes(d.vol0, (size_t)H.ne_pad * ts));
+    CK(A.alloc_bytes(d.efrc, 12 * (size_t)H.ne_pad * ts));
+    CK(A.alloc_bytes(d.g, H.any_nomass ? 9 * (size_t)H.ne_pad * ts : 16));
+    CK(A.alloc_bytes(d.blocks, H.any_nomass ? 9 * (size_t)H.n_edges * ts : 16));
+    CK(A.alloc_bytes(d.mass_edge, H.any_mass ? (size_t)H.n_edges * ts : 16));
+    CK(A.alloc_bytes(d.mass_diag, H.any_mass ? (size_t)H.nl_pad * ts : 16));
+    CK(A.alloc(d.partials, 4 * (size_t)H.n_tiles));
+    CK(A.alloc(d.epartials, 2 * (size_t)H.n_etiles));
+    CK(A.alloc(d.cg, (size_t)H.num_blobs));
+    CK(A.alloc(d.counters, (size_t)CNT_COUNT));
+    CK(A.alloc(d.status, (size_t)H.num_blobs));
+    CK(A.alloc(d.inverted, (size_t)H.num_blobs));
+    CK(A.alloc(d.energy, 2 * (size_t)H.num_blobs));
+    CK(A.alloc(d.any_running, 1));
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+    CK(cudaMallocHost(&h->running_host, sizeof(int32_t)));
+    for (auto &e : h->ev) CK(cudaEventCreate(&e));
+    // secondary-node initial velocities (they never change: their rows are identity)
+    h->sec_vel.resize(num_blobs);
+    for (int b = 0; b < num_blobs; b++) {
+        const ffea_gpu_mesh &m = meshes[b];
+        h->sec_vel[b].assign(3 * (size_t)m.num_nodes, 0.0);
+        if (m.vel && params[b].solver == SOLVER_MASS)
+            for (int32_t n = 0; n < m.num_nodes; n++)
+                if (H.maps[b].lin_of_orig[n] < 0)
+                    for (int c = 0; c < 3; c++) h->sec_vel[b][3 * (size_t)n + c] = m.vel[3 * (size_t)n + c];
+    }
+    launch_rest_state(d, h->stream);
+    if (d.any_mass) launch_mass_matrix(d, h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
+    *out = h.release();
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_create(const ffea_gpu_mesh *mesh, const ffea_gpu_params *params, ffea_gpu_t **out)
+{
+    return ffea_gpu_create_batch(1, mesh, params, FFEA_GPU_RNG_PER_BLOB, out);
+}
+
+void ffea_gpu_destroy(ffea_gpu_t *h)
+{
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    delete h;
+}
+
+void *ffea_gpu_stream(ffea_gpu_t *h) { return h ? (void *)h->stream : nullptr; }
+
+int ffea_gpu_set_graph_mode(ffea_gpu_t *h, int32_t enable)
+{
+    if (!h) return fail("null handle");
+    h->graph_mode = enable ? 1 : 0;
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_set_timing(ffea_gpu_t *h, int32_t enable)
+{
+    if (!h) return fail("null handle");
+    h->timing = enable ? 1 : 0;
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_phase_times(ffea_gpu_t *h, double out_ms[5])
+{
+    if (!h || !out_ms) return fail("null argument");
+    for (int i = 0; i < 5; i++) out_ms[i] = h->phase_ms[i];
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_sizes(ffea_gpu_t *h, int64_t *linear_nodes, int64_t *elements, int64_t *edges)
+{
+    if (!h) return fail("null handle");
+    int64_t nl = 0, ne = 0;
+    for (auto &bp : h->host.bp) {
+        nl += bp.node_cnt;
+        ne += bp.elem_cnt;
+    }
+    if (linear_nodes) *linear_nodes = nl;
+    if (elements) *elements = ne;
+    if (edges) *edges = h->host.n_edges;
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_step(ffea_gpu_t *h, int32_t nsteps)
+{
+    if (!h) return fail("null handle");
+    if (nsteps < 0) return fail("nsteps must be >= 0");
+    DeviceBatch &d = h->dev;
+    for (int i = 0; i < 5; i++) h->phase_ms[i] = 0;
+    for (int32_t s = 0; s < nsteps; s++) {
+        if (h->graph_mode && !h->timing) {
+            if (!h->step_exec && build_step_graph(h) != FFEA_GPU_OK) return FFEA_GPU_ERROR;
+            CK(cudaGraphLaunch(h->step_exec, h->stream));
+            continue;
+        }
+        if (h->timing) CK(cudaEventRecord(h->ev[0], h->stream));
+        launch_elements(d, h->stream, ELEM_STEP);
+        if (h->timing) CK(cudaEventRecord(h->ev[1], h->stream));
+        if (d.any_nomass) launch_assemble(d, h->stream);
+        if (h->timing) CK(cudaEventRecord(h->ev[2], h->stream));
+        launch_nodes(d, h->stream, 0, 0);
+        if (h->timing) CK(cudaEventRecord(h->ev[3], h->stream));
+        if (host_cg_loop(h) != FFEA_GPU_OK) return FFEA_GPU_ERROR;
+        if (h->host.bp[0].true_residual) launch_true_residual(d, h->stream);
+        if (h->timing) CK(cudaEventRecord(h->ev[4], h->stream));
+        launch_euler(d, h->stream);
+        if (h->timing) {
+            CK(cudaEventRecord(h->ev[5], h->stream));
+            CK(cudaEventSynchronize(h->ev[5]));
+            for (int i = 0; i < 5; i++) {
+                float ms = 0;
+                CK(cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]));
+                h->phase_ms[i] += ms;
+            }
+        }
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
+    std::vector<int32_t> st(h->host.num_blobs);
+    CK(cudaMemcpy(st.data(), d.status, st.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    for (int b = 0; b < h->host.num_blobs; b++)
+        if (st[b]) {
+            const char *why = (st[b] & BLOB_FAIL_INVERSION) ? "an element inverted" : "the CG solve did not converge";
+            return fail("blob %d: %s (status bits %d); the blob is frozen at the failing step", b, why, st[b]);
+        }
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_get_nodes(ffea_gpu_t *h, int32_t blob, double *pos, double *vel, double *force)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    CK(cudaStreamSynchronize(h->stream));
+    const BlobParams &bp = h->host.bp[blob];
+    const BlobMap &map = h->host.maps[blob];
+    const size_t n3 = 3 * (size_t)bp.node_cnt, off = 3 * (size_t)bp.node_off;
+    std::vector<double> p(n3), v(n3), x(n3);
+    CK(cudaMemcpy(p.data(), h->dev.pos + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(v.data(), h->dev.vel + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(x.data(), h->dev.x + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    const int32_t N = map.num_nodes_total;
+    std::vector<double> P(3 * (size_t)N, 0.0);
+    for (int32_t n = 0; n < N; n++) {
+        const int32_t g = map.lin_of_orig[n];
+        if (g < 0) continue;
+        const size_t l = 3 * (size_t)(g - bp.node_off);
+        for (int c = 0; c < 3; c++) {
+            P[3 * (size_t)n + c] = p[l + c];
+            if (vel) vel[3 * (size_t)n + c] = v[l + c];
+            if (force) force[3 * (size_t)n + c] = x[l + c];
+        }
+    }
+    // midpoints in element order, last element wins (Blob::update_positions, src/Blob.cpp:759-761)
+    static const int mid[6][3] = {{4, 0, 1}, {5, 0, 2}, {6, 0, 3}, {7, 1, 2}, {8, 1, 3}, {9, 2, 3}};
+    for (int32_t e = 0; e < map.num_elements; e++) {
+        const int32_t *t = &map.topology[10 * (size_t)e];
+        for (int m = 0; m < 6; m++)
+            for (int c = 0; c < 3; c++)
+                P[3 * (size_t)t[mid[m][0]] + c] = .5 * (P[3 * (size_t)t[mid[m][1]] + c] + P[3 * (size_t)t[mid[m][2]] + c]);
+    }
+    for (int32_t n = 0; n < N; n++) {
+        if (map.lin_of_orig[n] >= 0) continue;
+        for (int c = 0; c < 3; c++) {
+            if (vel) vel[3 * (size_t)n + c] = (bp.solver == SOLVER_NOMASS) ? 0.0 : h->sec_vel[blob][3 * (size_t)n + c];
+            if (force) force[3 * (size_t)n + c] = 0.0;
+        }
+    }
+    if (pos) std::memcpy(pos, P.data(), P.size() * sizeof(double));
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const double *vel)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    CK(cudaStreamSynchronize(h->stream));
+    const BlobParams &bp = h->host.bp[blob];
+    const BlobMap &map = h->host.maps[blob];
+    const size_t n3 = 3 * (size_t)bp.node_cnt, off = 3 * (size_t)bp.node_off;
+    std::vector<double> p(n3), v(n3);
+    CK(cudaMemcpy(p.data(), h->dev.pos + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(v.data(), h->dev.vel + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int32_t n = 0; n < map.num_nodes_total; n++) {
+        const int32_t g = map.lin_of_orig[n];
+        if (g < 0) {
+            if (vel && bp.solver == SOLVER_MASS)
+                for (int c = 0; c < 3; c++) h->sec_vel[blob][3 * (size_t)n + c] = vel[3 * (size_t)n + c];
+            continue;
+        }
+        const size_t l = 3 * (size_t)(g - bp.node_off);
+        for (int c = 0; c < 3; c++) {
+            if (pos) p[l + c] = pos[3 * (size_t)n + c];
+            if (vel) v[l + c] = vel[3 * (size_t)n + c];
+        }
+    }
+    CK(cudaMemcpy(h->dev.pos + off, p.data(), n3 * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->dev.vel + off, v.data(), n3 * sizeof(double), cudaMemcpyHostToDevice));
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_get_rng_state(ffea_gpu_t *h, int32_t blob, uint64_t state[6])
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    if (!state) return fail("null state");
+    CK(cudaStreamSynchronize(h->stream));
+    uint32_t st[6];
+    CK(cudaMemcpy(st, h->dev.stream_state + 6 * h->host.bp[blob].stream, sizeof(st), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 6; i++) state[i] = st[i];
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_set_rng_state(ffea_gpu_t *h, int32_t blob, const uint64_t state[6])
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    if (!state) return fail("null state");
+    // RngStream::CheckSeed (src/RngStream.cpp:230-253): words below the moduli, not all zero per component
+    for (int i = 0; i < 6; i++)
+        if (state[i] >= (i < 3 ? mrg::M1 : mrg::M2)) return fail("seed word %d out of range", i);
+    if ((state[0] | state[1] | state[2]) == 0 || (state[3] | state[4] | state[5]) == 0)
+        return fail("seed component is all zero");
+    CK(cudaStreamSynchronize(h->stream));
+    uint32_t st[6];
+    for (int i = 0; i < 6; i++) st[i] = (uint32_t)state[i];
+    CK(cudaMemcpy(h->dev.stream_state + 6 * h->host.bp[blob].stream, st, sizeof(st), cudaMemcpyHostToDevice));
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_energies(ffea_gpu_t *h, int32_t blob, double *strain, double *kinetic)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    launch_energies(h->dev, h->stream);
+    double e[2];
+    CK(cudaMemcpyAsync(e, h->dev.energy + 2 * blob, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (strain) *strain = e[0];
+    if (kinetic) *kinetic = e[1];
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_status(ffea_gpu_t *h, int32_t blob, int32_t *inverted, int32_t *cg_iters, double *true_relres,
+                    int32_t *fail_bits)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    CK(cudaStreamSynchronize(h->stream));
+    CgScalars cg;
+    int32_t inv = 0, st = 0;
+    CK(cudaMemcpy(&cg, h->dev.cg + blob, sizeof(cg), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&inv, h->dev.inverted + blob, sizeof(inv), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&st, h->dev.status + blob, sizeof(st), cudaMemcpyDeviceToHost));
+    if (inverted) *inverted = inv;
+    if (cg_iters) *cg_iters = cg.iters;
+    if (true_relres) *true_relres = cg.true_relres2 >= 0 ? std::sqrt(cg.true_relres2) : NAN;
+    if (fail_bits) *fail_bits = st;
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_get_rhs(ffea_gpu_t *h, int32_t blob, double *rhs)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    if (!rhs) return fail("null output");
+    CK(cudaStreamSynchronize(h->stream));
+    const BlobParams &bp = h->host.bp[blob];
+    const BlobMap &map = h->host.maps[blob];
+    const size_t n3 = 3 * (size_t)bp.node_cnt;
+    std::vector<double> r(n3);
+    CK(cudaMemcpy(r.data(), h->dev.rhs + 3 * (size_t)bp.node_off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int32_t n = 0; n < map.num_nodes_total; n++) {
+        const int32_t g = map.lin_of_orig[n];
+        for (int c = 0; c < 3; c++) rhs[3 * (size_t)n + c] = g < 0 ? 0.0 : r[3 * (size_t)(g - bp.node_off) + c];
+    }
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_get_element_forces(ffea_gpu_t *h, int32_t blob, double *out)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    if (!out) return fail("null output");
+    CK(cudaStreamSynchronize(h->stream));
+    const BlobParams &bp = h->host.bp[blob];
+    std::vector<double> v;
+    if (copy_typed_to_double(h, h->dev.efrc, 12 * (size_t)bp.elem_off, 12 * (size_t)bp.elem_cnt, v)) return FFEA_GPU_ERROR;
+    std::memcpy(out, v.data(), v.size() * sizeof(double));
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_solver_solve(ffea_gpu_t *h, int32_t blob, const double *pos, double *x)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    if (!x) return fail("null rhs/solution");
+    if (pos && ffea_gpu_set_nodes(h, blob, pos, nullptr)) return FFEA_GPU_ERROR;
+    DeviceBatch &d = h->dev;
+    const BlobParams &bp = h->host.bp[blob];
+    const BlobMap &map = h->host.maps[blob];
+    std::vector<double> rhs(3 * (size_t)d.nl_pad, 0.0);
+    for (int32_t n = 0; n < map.num_nodes_total; n++) {
+        const int32_t g = map.lin_of_orig[n];
+        if (g < 0 || map.pinned_orig[n]) continue;
+        for (int c = 0; c < 3; c++) rhs[3 * (size_t)g + c] = x[3 * (size_t)n + c];
+    }
+    CK(cudaMemcpyAsync(d.rhs, rhs.data(), rhs.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_elements(d, h->stream, ELEM_MATRIX_ONLY);
+    if (d.any_nomass) launch_assemble(d, h->stream);
+    launch_nodes(d, h->stream, 1, 0);
+    if (host_cg_loop(h) != FFEA_GPU_OK) return FFEA_GPU_ERROR;
+    CK(cudaStreamSynchronize(h->stream));
+    CgScalars cg;
+    int32_t st = 0;
+    CK(cudaMemcpy(&cg, d.cg + blob, sizeof(cg), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&st, d.status + blob, sizeof(st), cudaMemcpyDeviceToHost));
+    std::vector<double> sol(3 * (size_t)bp.node_cnt);
+    CK(cudaMemcpy(sol.data(), d.x + 3 * (size_t)bp.node_off, sol.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int32_t n = 0; n < map.num_nodes_total; n++) {
+        const int32_t g = map.lin_of_orig[n];
+        for (int c = 0; c < 3; c++) {
+            double &xv = x[3 * (size_t)n + c];
+            if (map.pinned_orig[n] || (g < 0 && bp.solver == SOLVER_MASS)) continue;  // identity row: x = rhs
+            if (g >= 0) xv = sol[3 * (size_t)(g - bp.node_off) + c];
+            else xv = xv / (1.0 + (bp.calc_stokes == 1 ? map.drag_orig[n] : 0.0));
+            // secondary rows of the viscosity matrix hold one (+ the Stokes drag)
+            // on the diagonal only (src/NoMassCGSolver.cpp:109-139)
+        }
+    }
+    if (st) return fail("blob %d: solve failed (status bits %d)", blob, st);
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_solver_apply(ffea_gpu_t *h, int32_t blob, const double *in, double *out)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    if (!in || !out) return fail("null argument");
+    DeviceBatch &d = h->dev;
+    const BlobParams &bp = h->host.bp[blob];
+    const BlobMap &map = h->host.maps[blob];
+    std::vector<double> v(3 * (size_t)d.nl_pad, 0.0);
+    for (int32_t n = 0; n < map.num_nodes_total; n++) {
+        const int32_t g = map.lin_of_orig[n];
+        if (g < 0 || map.pinned_orig[n]) continue;
+        for (int c = 0; c < 3; c++) v[3 * (size_t)g + c] = in[3 * (size_t)n + c];
+    }
+    double *din = nullptr, *dout = nullptr;
+    CK(cudaMallocAsync(&din, v.size() * sizeof(double), h->stream));
+    CK(cudaMallocAsync(&dout, v.size() * sizeof(double), h->stream));
+    CK(cudaMemcpyAsync(din, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_apply(d, h->stream, din, dout);
+    CK(cudaMemcpyAsync(v.data(), dout, v.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaFreeAsync(din, h->stream));
+    CK(cudaFreeAsync(dout, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int32_t n = 0; n < map.num_nodes_total; n++) {
+        const int32_t g = map.lin_of_orig[n];
+        for (int c = 0; c < 3; c++) {
+            const size_t k = 3 * (size_t)n + c;
+            if (g >= 0 && !map.pinned_orig[n]) out[k] = v[3 * (size_t)g + c];
+            else out[k] = in[k];  // identity rows (pinned nodes; secondary nodes without drag)
+        }
+    }
+    (void)bp;
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_rng_draws(const uint64_t state[6], uint64_t offset, int64_t count, double *out)
+{
+    if (!state || (!out && count > 0)) return fail("null argument");
+    if (count <= 0) return FFEA_GPU_OK;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    mrg::JumpMat *table = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_table_mu);
+        if ((int)g_tables.size() <= dev) g_tables.resize(dev + 1, nullptr);
+        if (!g_tables[dev]) {
+            std::vector<mrg::JumpMat> t(mrg::JUMP_TABLE_ENTRIES);
+            mrg::build_jump_table(t.data());
+            CK(cudaMalloc(&g_tables[dev], t.size() * sizeof(mrg::JumpMat)));
+            CK(cudaMemcpy(g_tables[dev], t.data(), t.size() * sizeof(mrg::JumpMat), cudaMemcpyHostToDevice));
+        }
+        table = g_tables[dev];
+    }
+    uint32_t st[6];
+    for (int i = 0; i < 6; i++) st[i] = (uint32_t)state[i];
+    uint32_t *dst = nullptr;
+    double *dout = nullptr;
+    cudaStream_t s = nullptr;
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CK(cudaMallocAsync(&dst, sizeof(st), s));
+    CK(cudaMallocAsync(&dout, (size_t)count * sizeof(double), s));
+    CK(cudaMemcpyAsync(dst, st, sizeof(st), cudaMemcpyHostToDevice, s));
+    launch_rng_draws(table, dst, offset, count, dout, s);
+    CK(cudaMemcpyAsync(out, dout, (size_t)count * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaFreeAsync(dst, s));
+    CK(cudaFreeAsync(dout, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaStreamDestroy(s));
+    return FFEA_GPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,58 @@
+// host_build.h -- host-side preprocessing of FFEA blobs into the packed layout.
+#pragma once
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/ffea_gpu.h"
+#include "layout.h"
+
+namespace ffea {
+
+// How to rebuild the reference's node arrays of one blob.
+struct BlobMap {
+    int32_t num_nodes_total = 0;      // N_t
+    int32_t num_elements = 0;
+    std::vector<int32_t> lin_of_orig; // orig node -> global padded linear id, -1 for secondary
+    std::vector<int32_t> topology;    // 10 * E original indices (midpoint reconstruction)
+    std::vector<uint8_t> pinned_orig; // orig node pinned flag
+    std::vector<double> drag_orig;    // orig node Stokes drag
+};
+
+struct HostBatch {
+    int32_t num_blobs = 0;
+    int32_t precision = PREC_MIXED;
+    int32_t rng_mode = 0;
+    int32_t nl_pad = 0, ne_pad = 0, n_edges = 0, n_tiles = 0, n_etiles = 0;
+    int32_t any_mass = 0, any_nomass = 0;
+    std::vector<BlobParams> bp;
+    std::vector<Material> materials;
+    std::vector<uint16_t> mat_id;        // per padded element
+    std::vector<int32_t> conn;           // 4 per padded element (global linear ids)
+    std::vector<double> pos, vel;        // 3 per padded node
+    std::vector<double> drag;            // per padded node
+    std::vector<uint8_t> flags;          // per padded node
+    std::vector<int32_t> orig;           // per padded node: original index in its blob, -1 padding
+    std::vector<int32_t> gather_ptr, gather_idx;          // node -> (elem*4 + corner), element order
+    std::vector<int32_t> fold_ptr, fold_sec;              // node -> secondary nodes folded onto it
+    std::vector<double> fold_drag;
+    std::vector<int32_t> edge_p, edge_q;                  // edges (p < q), sorted by (p, q)
+    std::vector<int32_t> edge_cptr, edge_cidx;            // edge -> (elem*16 + a*4 + b), element order
+    std::vector<int32_t> up_ptr;                          // node p -> edges [up_ptr[p], up_ptr[p+1]) with p first
+    std::vector<int32_t> lo_ptr, lo_edge;                 // node q -> edges with q second
+    std::vector<int32_t> tile_blob, etile_blob;
+    int32_t num_streams = 0;
+    std::vector<uint32_t> stream_state;                   // 6 per stream
+    std::vector<mrg::JumpMat> stream_step;                // per stream: A^(draws per step)
+    std::vector<BlobMap> maps;
+};
+
+// Build the packed batch.  Returns false and sets err on invalid input.
+bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_params *params, int32_t rng_mode,
+                 HostBatch &out, std::string &err);
+
+// World::init's six seed words (src/World.cpp:299-305).
+void ffea_seed_words(int32_t rng_seed, uint64_t out[6]);
+
+}  // namespace ffea

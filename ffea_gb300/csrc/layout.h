@@ -1,0 +1,67 @@
+// layout.h -- the packed multi-blob layout in HBM, shared by host and device code.
+//
+// All blobs of a batch are concatenated.  Node-space arrays hold only the
+// LINEAR nodes of each blob (the 4 corner nodes that carry mechanics); the
+// secondary edge-midpoint nodes of FFEA's 10-node elements are reconstructed
+// on output.  Each blob's node range is padded to a multiple of NODE_TILE and
+// its element range to a multiple of ELEM_TILE so that every CTA of a
+// node-space or element-space kernel belongs to exactly one blob; padding rows
+// behave like pinned rows (zero force, identity matrix row).
+#pragma once
+#include <stdint.h>
+
+#include "mrg32k3a.cuh"
+
+namespace ffea {
+
+constexpr int NODE_TILE = 256;   // rows per CTA of node-space kernels
+constexpr int ELEM_TILE = 128;   // elements per CTA of the element kernel
+constexpr int EDGE_TILE = 256;
+constexpr int MAX_BLOBS = 1 << 20;
+
+enum SolverKind : int32_t { SOLVER_NOMASS = 0, SOLVER_MASS = 1 };
+enum Precision : int32_t { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+// node flag bits
+constexpr uint8_t NODE_PINNED = 1;   // pinned or padding: identity row, zero force
+
+// per-blob status bits
+constexpr int32_t BLOB_FAIL_INVERSION = 1;
+constexpr int32_t BLOB_FAIL_CG = 2;
+constexpr int32_t BLOB_FAIL_NAN = 4;
+
+struct BlobParams {
+    double dt, kT, epsilon2;
+    int32_t max_iter;
+    int32_t calc_noise, calc_stokes;
+    int32_t solver;
+    int32_t stream;            // index of the RNG stream this blob draws from
+    uint32_t elem_draw_base;   // draw offset of element 0 within a step
+    uint32_t node_draw_base;   // draw offset of node 0 (original numbering) within a step
+    int32_t node_off, node_cnt, node_pad;   // padded linear-node range
+    int32_t elem_off, elem_cnt, elem_pad;   // padded element range
+    int32_t tile_off, tile_cnt;             // node tiles (CTAs) of this blob
+    int32_t num_nodes_total;                // N_t of the reference (linear + secondary)
+    int32_t true_residual;
+};
+
+// material table entry (meso units, tetra_element_linear fields)
+struct Material {
+    double rho, A, B, G, E;
+};
+
+// Per-blob CG scalars, FP64.
+struct CgScalars {
+    double delta;      // r . z
+    double ff;         // f . f (rhs norm^2)
+    double pq;         // p . A p
+    double rr;         // r . r
+    double alpha, beta;
+    double true_relres2;
+    int32_t iters;
+    int32_t converged;  // 1 converged, 0 running
+    int32_t active;     // participates in the current solve
+    int32_t pad_;
+};
+
+}  // namespace ffea

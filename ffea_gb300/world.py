@@ -1,0 +1,258 @@
+"""Python side of the GB300 blob update, shaped like FFEA's own interface.
+
+``World`` holds one or many blobs in one device handle and runs the
+per-timestep update the way ``World::run`` drives ``Blob::update_internal_forces``
+and ``Blob::update_positions`` (src/World.cpp:2024-2043).  ``Blob`` is a view
+of one of them with the getters a caller of FFEA's Blob uses.
+``NoMassCGSolver`` / ``ConjugateGradientSolver`` mirror the Solver plugin
+(include/Solver.h:30-55): init, solve (rhs in, solution out) and apply_matrix.
+
+Errors map to ``FfeaGpuError`` -- the analogue of FFEA_ERROR -- with the
+library's message.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib as L
+from .params import PRECISION_MIXED, SOLVER_MASS, SOLVER_NOMASS, SimulationParams
+
+RNG_PER_BLOB = 0
+RNG_SHARED = 1
+
+
+class _Keep:
+    """Owns the numpy arrays a Mesh struct points into until creation returns."""
+
+    def __init__(self):
+        self.arrays = []
+
+    def arr(self, a, dtype):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dtype)
+        self.arrays.append(a)
+        return a
+
+
+def _mesh_struct(keep: _Keep, pos, topology, material, drag=None, pinned=None, vel=None) -> L.Mesh:
+    pos = keep.arr(np.asarray(pos).reshape(-1, 3), np.float64)
+    topo = keep.arr(np.asarray(topology).reshape(-1, 10), np.int32)
+    mat = keep.arr(np.asarray(material).reshape(-1, 5), np.float64)
+    drag = keep.arr(drag, np.float64)
+    vel = keep.arr(None if vel is None else np.asarray(vel).reshape(-1, 3), np.float64)
+    pins = keep.arr(np.zeros(0, np.int32) if pinned is None else pinned, np.int32)
+    if len(mat) != len(topo):
+        raise ValueError("material needs one row (rho, A, B, G, E) per element")
+    if drag is not None and len(drag) != len(pos):
+        raise ValueError("stokes_drag needs one value per node")
+    return L.Mesh(len(pos), len(topo), L.ptr(pos), L.ptr(vel), L.ptr(topo, L._ip), L.ptr(mat), L.ptr(drag),
+                  len(pins), L.ptr(pins, L._ip))
+
+
+def _params_struct(p: SimulationParams, true_residual: int = 0) -> L.Params:
+    return L.Params(p.dt, p.kT, p.epsilon2, p.max_iterations_cg, p.calc_noise, p.calc_stokes, p.solver, p.precision,
+                    p.rng_seed, true_residual)
+
+
+class World:
+    """A batch of blobs on the current CUDA device.
+
+    ``blobs``: sequence of objects with ``mesh`` (pos, topology), ``material``,
+    ``drag``, ``pinned`` and ``params`` attributes (ffea_gb300.mesh.BlobSpec), or
+    dicts with those keys.
+    """
+
+    def __init__(self, blobs: Sequence, rng_mode: int = RNG_PER_BLOB, true_residual: bool = False,
+                 graph: bool = True, velocities: Sequence | None = None):
+        keep = _Keep()
+        meshes, params = [], []
+        self.num_nodes = []
+        self.num_elements = []
+        self.solvers = []
+        for i, b in enumerate(blobs):
+            get = (lambda k: b[k]) if isinstance(b, dict) else (lambda k: getattr(b, k))
+            mesh = get("mesh")
+            pos = mesh.pos if hasattr(mesh, "pos") else mesh["pos"]
+            topo = mesh.topology if hasattr(mesh, "topology") else mesh["topology"]
+            vel = None if velocities is None else velocities[i]
+            meshes.append(_mesh_struct(keep, pos, topo, get("material"), get("drag"), get("pinned"), vel))
+            p = get("params")
+            params.append(_params_struct(p, int(true_residual)))
+            self.num_nodes.append(len(np.asarray(pos).reshape(-1, 3)))
+            self.num_elements.append(len(np.asarray(topo).reshape(-1, 10)))
+            self.solvers.append(p.solver)
+        n = len(meshes)
+        if n == 0:
+            raise ValueError("World needs at least one blob")
+        marr = (L.Mesh * n)(*meshes)
+        parr = (L.Params * n)(*params)
+        h = ctypes.c_void_p()
+        L.check(L.lib().ffea_gpu_create_batch(n, marr, parr, int(rng_mode), ctypes.byref(h)), "ffea_gpu_create_batch")
+        self._h = h
+        self.num_blobs = n
+        L.lib().ffea_gpu_set_graph_mode(self._h, 1 if graph else 0)
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().ffea_gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- stepping
+    def run(self, num_steps: int = 1) -> None:
+        """num_steps x (update_internal_forces + update_positions) for every blob."""
+        L.check(L.lib().ffea_gpu_step(self._h, int(num_steps)), "ffea_gpu_step")
+
+    def set_timing(self, on: bool):
+        L.check(L.lib().ffea_gpu_set_timing(self._h, 1 if on else 0))
+
+    def phase_times(self) -> np.ndarray:
+        out = np.zeros(5)
+        L.check(L.lib().ffea_gpu_phase_times(self._h, L.ptr(out)))
+        return out
+
+    def sizes(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        L.check(L.lib().ffea_gpu_sizes(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def stream(self) -> int:
+        return L.lib().ffea_gpu_stream(self._h) or 0
+
+    def blob(self, i: int) -> "Blob":
+        return Blob(self, i)
+
+
+class Blob:
+    """One blob of a World (the getters of FFEA's Blob)."""
+
+    def __init__(self, world: World, index: int):
+        if not 0 <= index < world.num_blobs:
+            raise IndexError(index)
+        self.world = world
+        self.index = index
+        self.n = world.num_nodes[index]
+        self.e = world.num_elements[index]
+
+    def get_nodes(self):
+        pos = np.zeros((self.n, 3)); vel = np.zeros((self.n, 3)); force = np.zeros((self.n, 3))
+        L.check(L.lib().ffea_gpu_get_nodes(self.world.handle, self.index, L.ptr(pos), L.ptr(vel), L.ptr(force)))
+        return pos, vel, force
+
+    def set_nodes(self, pos=None, vel=None):
+        pos = None if pos is None else np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+        L.check(L.lib().ffea_gpu_set_nodes(self.world.handle, self.index, L.ptr(pos), L.ptr(vel)))
+
+    def rng_state(self) -> np.ndarray:
+        st = np.zeros(6, np.uint64)
+        L.check(L.lib().ffea_gpu_get_rng_state(self.world.handle, self.index, L.ptr(st, L._u64p)))
+        return st
+
+    def set_rng_state(self, st):
+        st = np.ascontiguousarray(st, dtype=np.uint64)
+        L.check(L.lib().ffea_gpu_set_rng_state(self.world.handle, self.index, L.ptr(st, L._u64p)))
+
+    def energies(self):
+        s, k = ctypes.c_double(), ctypes.c_double()
+        L.check(L.lib().ffea_gpu_energies(self.world.handle, self.index, ctypes.byref(s), ctypes.byref(k)))
+        return s.value, k.value
+
+    def status(self):
+        inv, it, fb = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        rr = ctypes.c_double()
+        L.check(L.lib().ffea_gpu_status(self.world.handle, self.index, ctypes.byref(inv), ctypes.byref(it),
+                                        ctypes.byref(rr), ctypes.byref(fb)))
+        return {"inverted": inv.value, "cg_iters": it.value, "true_relres": rr.value, "fail_bits": fb.value}
+
+    def rhs(self) -> np.ndarray:
+        out = np.zeros((self.n, 3))
+        L.check(L.lib().ffea_gpu_get_rhs(self.world.handle, self.index, L.ptr(out)))
+        return out
+
+    def element_forces(self) -> np.ndarray:
+        out = np.zeros((self.e, 4, 3))
+        L.check(L.lib().ffea_gpu_get_element_forces(self.world.handle, self.index, L.ptr(out)))
+        return out
+
+
+class _GpuSolver:
+    """Solver plugin mirror (include/Solver.h:30-55) backed by a one-blob World."""
+
+    kind = SOLVER_NOMASS
+
+    def __init__(self):
+        self.world = None
+
+    def init(self, pos, topology, material, params: SimulationParams, drag=None, pinned=None):
+        p = SimulationParams(**{**params.__dict__, "solver": self.kind})
+        self.world = World([{"mesh": {"pos": pos, "topology": topology}, "material": material, "drag": drag,
+                             "pinned": pinned, "params": p}], graph=False)
+        self.n = len(np.asarray(pos).reshape(-1, 3))
+        return 0
+
+    def solve(self, x, pos=None):
+        """x: (N_t, 3) rhs on entry, solution on return (in place)."""
+        xx = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        pp = None if pos is None else np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        L.check(L.lib().ffea_gpu_solver_solve(self.world.handle, 0, L.ptr(pp), L.ptr(xx)), "solve")
+        if isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous:
+            x.reshape(-1, 3)[:] = xx
+        return xx
+
+    def apply_matrix(self, v):
+        vin = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros_like(vin)
+        L.check(L.lib().ffea_gpu_solver_apply(self.world.handle, 0, L.ptr(vin), L.ptr(out)), "apply_matrix")
+        return out
+
+
+class NoMassCGSolver(_GpuSolver):
+    kind = SOLVER_NOMASS
+
+
+class ConjugateGradientSolver(_GpuSolver):
+    kind = SOLVER_MASS
+
+
+def rng_draws(state, offset: int, count: int) -> np.ndarray:
+    """RngStream::RandU01 draws number offset .. offset+count-1 of a stream, on the GPU."""
+    st = np.ascontiguousarray(state, dtype=np.uint64)
+    out = np.zeros(int(count), np.float64)
+    L.check(L.lib().ffea_gpu_rng_draws(L.ptr(st, L._u64p), ctypes.c_uint64(int(offset)), int(count), L.ptr(out)),
+            "ffea_gpu_rng_draws")
+    return out
+
+
+def ffea_seed(rng_seed: int) -> np.ndarray:
+    out = np.zeros(6, np.uint64)
+    L.check(L.lib().ffea_gpu_ffea_seed(int(rng_seed), L.ptr(out, L._u64p)))
+    return out
+
+
+def kernel_launches() -> int:
+    return int(L.lib().ffea_gpu_kernel_launches())
+
+
+__all__ = ["World", "Blob", "NoMassCGSolver", "ConjugateGradientSolver", "rng_draws", "ffea_seed",
+           "kernel_launches", "RNG_PER_BLOB", "RNG_SHARED", "PRECISION_MIXED", "SOLVER_MASS", "SOLVER_NOMASS"]

@@ -1,0 +1,185 @@
+/*
+ * ffea_gpu.h -- C ABI of the GB300 blob update for FFEA.
+ *
+ * This library replaces FFEA's per-timestep blob update -- the pair
+ *   int Blob::update_internal_forces()   (include/Blob.h:130, src/Blob.cpp:638-735)
+ *   int Blob::update_positions()         (include/Blob.h:140, src/Blob.cpp:737-764)
+ * called for every blob by World::run (src/World.cpp:2024-2043) -- and the
+ * linear-solver plugin behind it,
+ *   class Solver { init(...); solve(vector3 *x); apply_matrix(scalar *in, scalar *result); }
+ *                                          (include/Solver.h:30-55)
+ * with its two CG implementations NoMassCGSolver (src/NoMassCGSolver.cpp)
+ * and ConjugateGradientSolver (src/ConjugateGradientSolver.cpp).
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Host arrays are copied; nothing is kept
+ *    from the caller's memory after a call returns.
+ *  - All quantities are in FFEA meso units (include/dimensions.h:30-41), i.e.
+ *    the values Blob and SimulationParams hold after loading.
+ *  - Node arrays use the reference's own node numbering (linear and
+ *    secondary nodes, N_t of them) and AoS x,y,z layout (vector3).
+ *  - Every function returns FFEA_GPU_OK (0) or FFEA_GPU_ERROR (-1), the values
+ *    of FFEA_OK / FFEA_ERROR (include/FFEA_return_codes.h:35-36).  The message
+ *    of the last error on the calling thread is available from
+ *    ffea_gpu_last_error().
+ *  - Calls on one handle are not thread-safe; different handles may be used
+ *    from different threads.  Each handle owns one CUDA stream.
+ */
+#ifndef FFEA_GPU_H
+#define FFEA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFEA_GPU_OK 0
+#define FFEA_GPU_ERROR (-1)
+
+#define FFEA_GPU_SOLVER_NOMASS 0   /* <solver = CG_nomass>: NoMassCGSolver */
+#define FFEA_GPU_SOLVER_MASS 1     /* <solver = CG>: ConjugateGradientSolver */
+
+#define FFEA_GPU_PRECISION_FP64 0  /* every kernel in FP64 */
+#define FFEA_GPU_PRECISION_MIXED 1 /* FP32 element forces and SpMV; FP64 positions, dots, residuals */
+
+#define FFEA_GPU_RNG_PER_BLOB 0    /* each blob draws from its own stream, seeded from its rng_seed */
+#define FFEA_GPU_RNG_SHARED 1      /* all blobs share stream 0 in FFEA's single-thread draw order */
+
+typedef struct ffea_gpu ffea_gpu_t;
+
+/* One blob's mesh: what Blob holds after Blob::init (src/Blob.cpp:270-420). */
+typedef struct {
+    int32_t num_nodes;          /* N_t: linear + secondary nodes (Blob::num_nodes) */
+    int32_t num_elements;       /* Blob::num_elements */
+    const double *pos;          /* 3*num_nodes, mesh_node::pos */
+    const double *vel;          /* 3*num_nodes, mesh_node::vel; NULL = at rest */
+    const int32_t *topology;    /* 10*num_elements, tetra_element_linear::n[j]->index */
+    const double *material;     /* 5*num_elements: rho, A, B, G, E (tetra_element_linear fields) */
+    const double *stokes_drag;  /* num_nodes, mesh_node::stokes_drag; NULL = no drag */
+    int32_t num_pinned;         /* Blob::num_pinned_nodes */
+    const int32_t *pinned;      /* Blob::pinned_nodes_list */
+} ffea_gpu_mesh;
+
+/* The SimulationParams fields the update reads (include/SimulationParams.h:76-131). */
+typedef struct {
+    double dt;                  /* SimulationParams::dt */
+    double kT;                  /* SimulationParams::kT */
+    double epsilon2;            /* SimulationParams::epsilon2 (= epsilon^2) */
+    int32_t max_iterations_cg;  /* SimulationParams::max_iterations_cg */
+    int32_t calc_noise;         /* SimulationParams::calc_noise */
+    int32_t calc_stokes;        /* SimulationParams::calc_stokes */
+    int32_t solver;             /* FFEA_GPU_SOLVER_* (Blob::linear_solver) */
+    int32_t precision;          /* FFEA_GPU_PRECISION_* */
+    int32_t rng_seed;           /* SimulationParams::rng_seed, seeded as World::init does */
+    int32_t true_residual;      /* 1: confirm every solve with an FP64 true residual */
+} ffea_gpu_params;
+
+/* --- handle lifetime ----------------------------------------------------- */
+
+/* One blob.  Replaces Blob::init's solver set-up (src/Blob.cpp:359-380) and
+ * World::init's RNG seeding for a single OpenMP thread (src/World.cpp:299-317). */
+int ffea_gpu_create(const ffea_gpu_mesh *mesh, const ffea_gpu_params *params, ffea_gpu_t **out);
+
+/* Many blobs in one handle, stepped together by one launch sequence.  With
+ * rng_mode FFEA_GPU_RNG_PER_BLOB blob b draws from its own stream seeded from
+ * params[b].rng_seed; with FFEA_GPU_RNG_SHARED all blobs share the stream of
+ * params[0].rng_seed in the order a one-thread World::run draws it
+ * (src/World.cpp:2024-2043).  All blobs must use the same precision. */
+int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_params *params,
+                          int32_t rng_mode, ffea_gpu_t **out);
+
+void ffea_gpu_destroy(ffea_gpu_t *h);
+
+/* --- stepping ------------------------------------------------------------ */
+
+/* nsteps x (Blob::update_internal_forces + Blob::update_positions) for every
+ * blob, with World::run's per-step force zeroing (src/World.cpp:1845,1907).
+ * Returns FFEA_GPU_ERROR if an element inverted or a solve did not converge
+ * in any blob; that blob stops at the failing step (see ffea_gpu_status). */
+int ffea_gpu_step(ffea_gpu_t *h, int32_t nsteps);
+
+/* --- state in / out (reference node numbering) --------------------------- */
+
+/* pos/vel: mesh_node pos and vel; force: Blob::force after the last solve
+ * (velocities for CG_nomass, accelerations for CG).  Any pointer may be NULL. */
+int ffea_gpu_get_nodes(ffea_gpu_t *h, int32_t blob, double *pos, double *vel, double *force);
+int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const double *vel);
+
+/* RngStream state words of a blob's stream (RngStream::GetState / SetSeed,
+ * src/RngStream.cpp:381-399,439-443); the .fcp checkpoint holds these. */
+int ffea_gpu_get_rng_state(ffea_gpu_t *h, int32_t blob, uint64_t state[6]);
+int ffea_gpu_set_rng_state(ffea_gpu_t *h, int32_t blob, const uint64_t state[6]);
+
+/* Strain and kinetic energy at the current state, as Blob::make_measurements
+ * computes them (src/Blob.cpp:1363-1432); kinetic is 0 for CG_nomass. */
+int ffea_gpu_energies(ffea_gpu_t *h, int32_t blob, double *strain, double *kinetic);
+
+/* Status of the last step: inverted-element count, CG iterations of the last
+ * solve, FP64 true relative residual ||b - A x|| / ||b|| of the last solve
+ * (NaN when the check is off), and the failure bits (1 inversion, 2 CG did
+ * not converge, 4 non-finite values). */
+int ffea_gpu_status(ffea_gpu_t *h, int32_t blob, int32_t *inverted, int32_t *cg_iters, double *true_relres,
+                    int32_t *fail_bits);
+
+/* rhs of the last solve: Blob::force handed to Solver::solve after the
+ * gather, Stokes terms, linearise_force and pinning (src/Blob.cpp:3826-3928). */
+int ffea_gpu_get_rhs(ffea_gpu_t *h, int32_t blob, double *rhs);
+
+/* Element nodal forces of the last step, 12 per element (corner 0..3 x,y,z):
+ * tetra_element_linear::node_force[0..3] (src/tetra_element_linear.cpp:474-489). */
+int ffea_gpu_get_element_forces(ffea_gpu_t *h, int32_t blob, double *out);
+
+/* --- Solver plugin (include/Solver.h:30-55) ------------------------------- */
+
+/* Solver::solve for the CURRENT node positions of `pos` (3*N_t): assembles
+ * the viscosity (CG_nomass) or mass (CG) matrix and overwrites x (3*N_t) --
+ * the rhs on entry -- with the solution.  Mirrors NoMassCGSolver::solve /
+ * ConjugateGradientSolver::solve (src/NoMassCGSolver.cpp:165-197,
+ * src/ConjugateGradientSolver.cpp:206-232). */
+int ffea_gpu_solver_solve(ffea_gpu_t *h, int32_t blob, const double *pos, double *x);
+
+/* Solver::apply_matrix: out = M in for the matrix of the last assembly,
+ * in/out 3*N_t (NoMassCGSolver's V->apply, src/SparseMatrixFixedPattern.cpp:148-191). */
+int ffea_gpu_solver_apply(ffea_gpu_t *h, int32_t blob, const double *in, double *out);
+
+/* --- RNG ----------------------------------------------------------------- */
+
+/* count draws of RngStream::RandU01 starting `offset` draws after `state`,
+ * generated on the GPU with jump-ahead (for checks against RngStream). */
+int ffea_gpu_rng_draws(const uint64_t state[6], uint64_t offset, int64_t count, double *out);
+
+/* World::init's six seed words for an rng_seed (src/World.cpp:299-305). */
+int ffea_gpu_ffea_seed(int32_t rng_seed, uint64_t out[6]);
+
+/* --- diagnostics --------------------------------------------------------- */
+
+/* Copies the last error message of the calling thread (NUL-terminated). */
+int ffea_gpu_last_error(char *buf, size_t len);
+
+/* Number of kernel launches the library issued so far (all handles). */
+int64_t ffea_gpu_kernel_launches(void);
+
+/* Sizes of a handle: total linear nodes, elements and edges across blobs. */
+int ffea_gpu_sizes(ffea_gpu_t *h, int64_t *linear_nodes, int64_t *elements, int64_t *edges);
+
+/* Per-phase timing of the last ffea_gpu_step call, measured with CUDA events
+ * on the handle's stream (milliseconds): elements, assembly, node gather,
+ * CG solve, update.  Only filled when timing was enabled. */
+int ffea_gpu_set_timing(ffea_gpu_t *h, int32_t enable);
+int ffea_gpu_phase_times(ffea_gpu_t *h, double out_ms[5]);
+
+/* The handle's CUDA stream (cudaStream_t), for callers that order their own
+ * work after a step. */
+void *ffea_gpu_stream(ffea_gpu_t *h);
+
+/* Execution mode: 1 = one CUDA graph per step with a device-side conditional
+ * loop for the CG iterations (default); 0 = host-driven launches. */
+int ffea_gpu_set_graph_mode(ffea_gpu_t *h, int32_t enable);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFEA_GPU_H */

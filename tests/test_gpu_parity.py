@@ -1,0 +1,124 @@
+"""GPU blob update vs the CPU oracle (FFEA's algorithm restated), through the C ABI.
+
+Tolerances:
+  - RNG draws: bit-exact.
+  - FP64 precision mode: positions to 1e-10 absolute (meso), velocities and
+    rhs to 1e-9 relative (2-norm) -- the remaining differences are CG
+    round-off with both sides solving to epsilon 1e-12.
+  - mixed FP32/FP64 mode: per-step velocity and force error <= 1e-5 relative
+    (2-norm) over the first 100 steps, the spec parity bar.
+"""
+import numpy as np
+import pytest
+
+from ffea_gb300 import params as P
+from tests.helpers import rel, spec
+
+pytestmark = pytest.mark.gpu
+
+
+def _world(specs, **kw):
+    from ffea_gb300.world import World
+    return World(specs, **kw)
+
+
+def test_rng_draws_bit_exact(gpulib, oracle):
+    from ffea_gb300.world import rng_draws
+    st = oracle.ffea_seed(44)
+    ref, _ = oracle.rng_draws(st, 5000)
+    got = rng_draws(st, 0, 5000)
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+    # arbitrary offsets via jump-ahead, including beyond 2^32
+    for off in (1, 255, 256, 65537, 7 * 823968 + 5, 2**31 + 3, 2**32 + 17, 3 * 2**32 + 1):
+        jumped = oracle.rng_jump(st, off)
+        ref, _ = oracle.rng_draws(jumped, 64)
+        got = rng_draws(st, off, 64)
+        assert np.array_equal(got.view(np.uint64), ref.view(np.uint64)), off
+
+
+@pytest.mark.parametrize("solver", [P.SOLVER_NOMASS, P.SOLVER_MASS])
+def test_fp64_matches_oracle_10_steps(gpulib, oracle, solver):
+    s = spec(radius_nm=3.0, solver=solver)
+    ref = oracle.blob_from_spec(s)
+    with _world([s]) as w:
+        b = w.blob(0)
+        for step in range(10):
+            w.run(1)
+            assert ref.step(1) == 0
+            pos, vel, force = b.get_nodes()
+            rpos, rvel, rforce = ref.nodes()
+            assert np.array_equal(b.rng_state(), ref.rng_state()), step
+            assert rel(b.rhs(), ref.rhs()) < 1e-9, step
+            assert rel(vel, rvel) < 1e-9, step
+            assert np.abs(pos - rpos).max() < 1e-10, step
+
+
+def test_fp64_pinned_nodes(gpulib, oracle):
+    s = spec(radius_nm=3.0, pinned=[0, 3, 10, 11])
+    ref = oracle.blob_from_spec(s)
+    with _world([s]) as w:
+        w.run(5)
+        assert ref.step(5) == 0
+        pos, vel, _ = w.blob(0).get_nodes()
+        rpos, rvel, _ = ref.nodes()
+        assert np.abs(vel[[0, 3, 10, 11]]).max() == 0.0
+        assert rel(vel, rvel) < 1e-9
+        assert np.abs(pos - rpos).max() < 1e-10
+
+
+def test_secondary_drag_folding(gpulib, oracle):
+    """Stokes radii on every node (as in hand-made .stokes files): the midpoint
+    nodes' noise is folded onto the corners like Blob::linearise_force."""
+    s = spec(radius_nm=3.0)
+    s.drag = s.drag.copy()
+    s.drag[s.mesh.num_linear:] = 0.5 * s.drag[0]
+    ref = oracle.blob_from_spec(s)
+    with _world([s]) as w:
+        w.run(3)
+        assert ref.step(3) == 0
+        _, vel, _ = w.blob(0).get_nodes()
+        _, rvel, _ = ref.nodes()
+        assert rel(vel, rvel) < 1e-9
+
+
+@pytest.mark.parametrize("solver", [P.SOLVER_NOMASS, P.SOLVER_MASS])
+def test_mixed_precision_100_steps(gpulib, oracle, solver):
+    s = spec(radius_nm=4.0, solver=solver, precision=P.PRECISION_MIXED)
+    ref = oracle.blob_from_spec(s)
+    worst_v = worst_f = 0.0
+    with _world([s]) as w:
+        b = w.blob(0)
+        for step in range(100):
+            w.run(1)
+            assert ref.step(1) == 0
+            _, vel, _ = b.get_nodes()
+            _, rvel, _ = ref.nodes()
+            worst_v = max(worst_v, rel(vel, rvel))
+            worst_f = max(worst_f, rel(b.rhs(), ref.rhs()))
+    assert worst_v <= 1e-5, worst_v
+    assert worst_f <= 1e-5, worst_f
+
+
+def test_batch_equals_independent_blobs(gpulib):
+    specs = [spec(radius_nm=r, seed=i, rng_seed=100 + i, precision=P.PRECISION_MIXED) for i, r in enumerate((2.5, 4.0, 3.0))]
+    with _world(specs) as w:
+        w.run(4)
+        batch = [w.blob(i).get_nodes() for i in range(3)]
+    for i, s in enumerate(specs):
+        with _world([s]) as w1:
+            w1.run(4)
+            single = w1.blob(0).get_nodes()
+        for a, c in zip(batch[i], single):
+            assert np.array_equal(a, c), i
+
+
+def test_deterministic_and_graph_equals_host_loop(gpulib):
+    s = spec(radius_nm=4.0, precision=P.PRECISION_MIXED)
+    outs = []
+    for graph in (True, True, False):
+        with _world([s], graph=graph) as w:
+            w.run(5)
+            outs.append(w.blob(0).get_nodes())
+    for o in outs[1:]:
+        for a, c in zip(outs[0], o):
+            assert np.array_equal(a, c)
