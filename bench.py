@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Throughput of FFEA's per-timestep blob update on GB300.
+
+Metric: node-steps/s (linear nodes advanced one timestep per second) with
+every CG solve run to relative residual 1e-6.
+
+Workload (default): a 64^3-cell grid split into 6 tetrahedra per cell and
+cut to a 40 nm-radius sphere (146,737 linear nodes, 823,968 elements,
+1,135,891 nodes with the edge midpoints), node positions jittered by
+N(0, 0.05 cell) from a seed; density 1.5e3 kg/m^3, shear/bulk modulus
+3.7e8/1.1e9 Pa, shear/bulk viscosity 1e-3 Pa s, kT at 300 K, dt 1e-14 s,
+thermal noise on, Stokes drag on, CG_nomass solver with Jacobi-PCG to
+epsilon 1e-6, FP32 element forces and SpMV with FP64 dot products.
+Synthetic, seeded inputs stand in for a real protein mesh.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs under torchrun, one replica blob per GPU with its own RNG stream
+(the path does not shard a single blob: replicas only, weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "sphere40": dict(radius_nm=40.0, cell_nm=1.25, desc="64^3-cell Freudenthal grid cut to a 40 nm sphere"),
+    "sphere20": dict(radius_nm=20.0, cell_nm=1.25, desc="32^3-cell Freudenthal grid cut to a 20 nm sphere"),
+    "sphere10": dict(radius_nm=10.0, cell_nm=1.25, desc="16^3-cell Freudenthal grid cut to a 10 nm sphere"),
+}
+METRIC = "node-steps/s at CG rel-res 1e-6"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sphere40")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the cpu_baseline sample")
+    return ap.parse_args()
+
+
+def build_spec(workload: str, rank: int, precision: str):
+    from ffea_gb300 import params as P
+    from ffea_gb300.mesh import make_blob, sphere_mesh
+    w = WORKLOADS[workload]
+    mesh = sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0)
+    prm = P.SimulationParams.from_si(dt=1e-14, kT=P.kT_at(300.0) * P.MESO_ENERGY, epsilon=1e-6,
+                                     max_iterations_cg=10000, rng_seed=44 + rank, solver=P.SOLVER_NOMASS,
+                                     precision=P.PRECISION_MIXED if precision == "mixed" else P.PRECISION_FP64)
+    return make_blob(mesh, prm)
+
+
+def config_of(args, spec, world_size):
+    m = spec.mesh
+    return {
+        "workload": f"{args.workload}: {WORKLOADS[args.workload]['desc']}",
+        "linear_nodes": int(m.num_linear),
+        "elements": int(m.num_elements),
+        "total_nodes": int(m.num_nodes),
+        "solver": "CG_nomass Jacobi-PCG, epsilon 1e-6, convergence confirmed by an FP64 true residual",
+        "precision": "FP32 element forces + SpMV, FP64 positions/dots" if args.precision == "mixed" else "FP64",
+        "noise": "on (MRG32k3a, RngStream-exact)",
+        "replicas": world_size,
+        "l2": "L2 flushed (256 MiB write) between timed steps",
+    }
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm_, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm_)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- roofline
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cg_iteration_bytes(num_linear: int, num_edges: int) -> int:
+    """Algorithmic bytes of one Jacobi-PCG iteration in the minimum-traffic
+    model (FP32 values, int32 indices): SpMV over the block-sparse matrix with
+    B = N + 2 edges 3x3 blocks (36 B values + 4 B column each, 4 B row pointer
+    and 12 + 12 B for the input and output vectors per row), the solution /
+    residual update (48 N + 24 N) and the direction update (36 N + 12 N):
+    40 B + 148 N."""
+    B = num_linear + 2 * num_edges
+    return 40 * B + 148 * num_linear
+
+
+def ncu_traffic(kernel="k_cg", workload="sphere40"):
+    """Per-launch DRAM bytes from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    try:
+        with open(path) as fh:
+            m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", fh.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_baseline(spec, budget_s: float):
+    """Oracle (C restatement of FFEA's path) on all host cores, bounded sample."""
+    from oracle import oracle as O
+    O.build(ref=False)
+    threads = os.cpu_count() or 1
+    b = O.blob_from_spec(spec, num_threads=threads)
+    t0 = time.perf_counter()
+    rc = b.step(1)
+    first = time.perf_counter() - t0
+    steps, total = 1, first
+    while rc == 0 and total + first < budget_s:
+        t = time.perf_counter()
+        rc = b.step(1)
+        total += time.perf_counter() - t
+        steps += 1
+    if rc != 0:
+        raise RuntimeError("oracle step failed in the CPU baseline")
+    v = spec.mesh.num_linear * steps / total
+    return {"value": v, "unit": "node-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} timestep(s) of the full workload after set-up, {total:.1f} s, OpenMP "
+                      f"{threads} threads, per-thread RNG streams as FFEA_PARALLEL_WITHIN_BLOB",
+            "steps": steps, "seconds": total}
+
+
+# ---------------------------------------------------------------- arms
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    spec = build_spec(args.workload, 0, args.precision)
+    base = cpu_baseline(spec, budget_s=max(args.cpu_seconds, 30.0))
+    line = {
+        "metric": METRIC, "value": base["value"], "unit": "node-steps/s", "n_gpus": args.gpus,
+        "steps": base["steps"], "warmup": 0, "ms_per_step": 1e3 * base["seconds"] / base["steps"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_of(args, spec, 1), "impl": "reference",
+        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": base["value"], "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    line["config"]["l2"] = "n/a (CPU)"
+    line["config"]["precision"] = "FP64 (the reference algorithm on the host cores)"
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from ffea_gb300.world import World, kernel_launches
+
+    spec = build_spec(args.workload, rank, args.precision)
+    N = spec.mesh.num_linear
+    w = World([spec], graph=True, true_residual=True)
+    nl, ne, nedges = w.sizes()
+    stream = torch.cuda.ExternalStream(w.stream())
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    w.run(max(args.warmup, 3) if args.warmup >= 0 else 3)
+    K = args.steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    loops0 = w.cg_loop_count()
+    launches0 = kernel_launches()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    torch.cuda.synchronize()
+    for k in range(K):
+        starts[k].record(stream)
+        w.run_async(1)
+        ends[k].record(stream)
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+    w.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+    loops = w.cg_loop_count() - loops0
+    launches = kernel_launches() - launches0
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = N * K * world / (total_ms / 1e3)
+
+    # end to end through the C ABI with host buffers: set_nodes (H2D) + step + get_nodes (D2H)
+    blob = w.blob(0)
+    pos, vel, _ = blob.get_nodes()
+    Ke = args.e2e_steps or max(3, K // 2)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        blob.set_nodes(pos, vel)
+        w.run(1)
+        pos, vel, _ = blob.get_nodes()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": N * Ke * world / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": 2 * 3 * 8 * N,
+           "d2h_bytes_per_step": 3 * 3 * 8 * N, "steps": Ke}
+
+    # profile pass: direct launches with CUDA events around each kernel of a step
+    prof_steps = 3
+    loops_p0 = w.cg_loop_count()
+    w.set_timing(True)
+    w.run(prof_steps)
+    phases = w.phase_times() / prof_steps
+    w.set_timing(False)
+    iters_p = (w.cg_loop_count() - loops_p0) / prof_steps
+    cg_ms = float(phases[3])
+    alg = int(iters_p * cg_iteration_bytes(nl, nedges))
+    peak, peak_kind = measured_peak()
+    achieved = alg / (cg_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_cg", "achieved": round(achieved, 1), "peak": peak,
+                "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": ncu_traffic(), "algorithmic_bytes_per_launch": alg,
+                "avg_launch_us": round(cg_ms * 1e3, 1), "cg_iters_per_launch": iters_p,
+                "bytes_per_iteration": cg_iteration_bytes(nl, nedges)}
+    if rank != 0:
+        w.close()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": config_of(args, spec, world), "e2e": e2e, "gpu_launches": int(launches),
+        "cg_iters_per_step": loops / K, "roofline": roofline, "clocks": clocks,
+        "phase_ms_per_step": {"elements": float(phases[0]), "assemble": float(phases[1]),
+                              "nodes": float(phases[2]), "cg": float(phases[3]), "euler": float(phases[4])},
+        "cg_us_per_iteration": 1e3 * cg_ms / max(iters_p, 1),
+    }
+    line["config"]["edges"] = int(nedges)
+    if world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(spec, args.cpu_seconds)
+        line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    w.close()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -77,6 +77,9 @@ SIGNATURES = {
     "ffea_gpu_phase_times": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "ffea_gpu_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "ffea_gpu_set_graph_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "ffea_gpu_step_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "ffea_gpu_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "ffea_gpu_cg_loop_count": (ctypes.c_int64, [ctypes.c_void_p]),
 }
 
 _lib = None

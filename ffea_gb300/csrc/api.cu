@@ -2,12 +2,13 @@
 //
 // A handle owns one packed batch of blobs in HBM, one CUDA stream and, in
 // graph mode, one instantiated CUDA graph per step:
-//   elements -> assemble -> nodes -> while(any blob iterating){ spmv, update, pupdate } -> euler
-// The CG loop runs as a device-side conditional WHILE node: the update
-// kernel's last CTA decides whether another iteration is needed, so a step
-// (and a run of steps) needs no host synchronisation.
+//   elements -> assemble -> nodes -> cg (persistent, cooperative) -> euler
+// The whole CG solve of every blob runs inside one cooperative launch that
+// iterates until each blob has converged, so a step (and a run of steps)
+// needs no host synchronisation.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -91,14 +92,13 @@ struct ffea_gpu {
     HostBatch host;
     DeviceBatch dev;
     DeviceArena arena;
-    cudaStream_t stream = nullptr, side = nullptr;
+    cudaStream_t stream = nullptr;
     cudaGraphExec_t step_exec = nullptr;
     int graph_mode = 1;
     int timing = 0;
     double phase_ms[5] = {0, 0, 0, 0, 0};
     cudaEvent_t ev[6] = {};
-    int32_t *running_host = nullptr;  // pinned
-    int last_iters = 8;
+    int64_t fixed_per_step = 0;  // kernels of a step graph outside the CG loop
     size_t tsize = 4;
     std::vector<std::vector<double>> sec_vel;  // per blob: initial velocities of secondary nodes
     ~ffea_gpu()
@@ -106,9 +106,7 @@ struct ffea_gpu {
         if (step_exec) cudaGraphExecDestroy(step_exec);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
-        if (running_host) cudaFreeHost(running_host);
         if (stream) cudaStreamDestroy(stream);
-        if (side) cudaStreamDestroy(side);
     }
 };
 
@@ -120,56 +118,21 @@ int build_step_graph(ffea_gpu *h)
     cudaStream_t s = h->stream;
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    cudaStreamCaptureStatus cst;
-    cudaGraph_t cap_graph = nullptr;
-    CK(cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap_graph, nullptr, nullptr, nullptr));
-    cudaGraphConditionalHandle cond;
-    CK(cudaGraphConditionalHandleCreate(&cond, cap_graph, 1, cudaGraphCondAssignDefault));
     launch_elements(d, s, ELEM_STEP);
     if (d.any_nomass) launch_assemble(d, s);
-    launch_nodes(d, s, 0, (unsigned long long)cond);
-    const cudaGraphNode_t *deps = nullptr;
-    size_t ndeps = 0;
-    CK(cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap_graph, &deps, nullptr, &ndeps));
-    cudaGraphNodeParams cp = {};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = cond;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    cudaGraphNode_t cnode;
-    CK(cudaGraphAddNode(&cnode, cap_graph, deps, nullptr, ndeps, &cp));
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    CK(cudaStreamBeginCaptureToGraph(h->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    launch_cg_iteration(d, h->side, (unsigned long long)cond);
-    cudaGraph_t body_out = nullptr;
-    CK(cudaStreamEndCapture(h->side, &body_out));
-    CK(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
-    if (h->host.bp[0].true_residual) launch_true_residual(d, s);
+    launch_nodes(d, s, 0);
+    cudaError_t le = launch_cg(d, s);
     launch_euler(d, s);
-    CK(cudaStreamEndCapture(s, &graph));
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return fail("capturing the step graph failed: %s / %s", cudaGetErrorString(le), cudaGetErrorString(ce));
+    }
+    h->fixed_per_step = 4 + (d.any_nomass ? 1 : 0);
     cudaError_t e = cudaGraphInstantiate(&h->step_exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail("cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
-    return FFEA_GPU_OK;
-}
-
-// CG loop driven from the host: launch chunks of iterations, check the
-// device flag between chunks.  Converged blobs make the kernels return early.
-int host_cg_loop(ffea_gpu *h)
-{
-    int chunk = h->last_iters > 4 ? h->last_iters : 4;
-    int total = 0;
-    int max_iter = 0;
-    for (auto &bp : h->host.bp) max_iter = bp.max_iter > max_iter ? bp.max_iter : max_iter;
-    while (total <= max_iter + 1) {
-        for (int i = 0; i < chunk; i++) launch_cg_iteration(h->dev, h->stream, 0);
-        total += chunk;
-        CK(cudaMemcpyAsync(h->running_host, h->dev.any_running, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
-        CK(cudaStreamSynchronize(h->stream));
-        if (!*h->running_host) break;
-        chunk = 4;
-    }
-    h->last_iters = total;
     return FFEA_GPU_OK;
 }
 
@@ -263,23 +226,23 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(upload(A, d.edge_q, H.edge_q));
     CK(upload(A, d.edge_cptr, H.edge_cptr));
     CK(upload(A, d.edge_cidx, H.edge_cidx));
-    CK(upload(A, d.up_ptr, H.up_ptr));
-    CK(upload(A, d.lo_ptr, H.lo_ptr));
-    CK(upload(A, d.lo_edge, H.lo_edge));
+    CK(upload(A, d.edge_pos_pq, H.edge_pos_pq));
+    CK(upload(A, d.edge_pos_qp, H.edge_pos_qp));
+    CK(upload(A, d.slice_ptr, H.slice_ptr));
+    CK(upload(A, d.slice_len, H.slice_len));
+    CK(upload(A, d.sell_col, H.sell_col));
+    d.n_slices = (int32_t)H.slice_len.size();
+    d.n_entries = (int32_t)H.sell_col.size();
     const size_t n3 = 3 * (size_t)H.nl_pad;
     CK(A.alloc(d.rhs, n3));
-    CK(A.alloc(d.x, n3));
-    CK(A.alloc(d.r, n3));
-    CK(A.alloc_bytes(d.p, n3 * ts));
-    CK(A.alloc_bytes(d.q, n3 * ts));
-    CK(A.alloc_bytes(d.dinv, n3 * ts));
+    for (void **v : {&d.x, &d.r, &d.u, &d.w, &d.p, &d.s, &d.dinv}) CK(A.alloc_bytes(*v, n3 * ts));
     CK(A.alloc(d.det_sign, (size_t)H.ne_pad));
     CK(A.alloc_bytes(d.jinv0, 9 * (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.vol0, (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.efrc, 12 * (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.g, H.any_nomass ? 9 * (size_t)H.ne_pad * ts : 16));
-    CK(A.alloc_bytes(d.blocks, H.any_nomass ? 9 * (size_t)H.n_edges * ts : 16));
-    CK(A.alloc_bytes(d.mass_edge, H.any_mass ? (size_t)H.n_edges * ts : 16));
+    CK(A.alloc_bytes(d.sell_val, H.any_nomass ? 9 * (size_t)d.n_entries * ts : 16));
+    CK(A.alloc_bytes(d.sell_mval, H.any_mass ? (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.mass_diag, H.any_mass ? (size_t)H.nl_pad * ts : 16));
     CK(A.alloc(d.partials, 4 * (size_t)H.n_tiles));
     CK(A.alloc(d.epartials, 2 * (size_t)H.n_etiles));
@@ -288,10 +251,9 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(A.alloc(d.status, (size_t)H.num_blobs));
     CK(A.alloc(d.inverted, (size_t)H.num_blobs));
     CK(A.alloc(d.energy, 2 * (size_t)H.num_blobs));
-    CK(A.alloc(d.any_running, 1));
+    CK(A.alloc(d.bar, 8));
+    CK(A.alloc(d.loop_count, 1));
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
-    CK(cudaMallocHost(&h->running_host, sizeof(int32_t)));
     for (auto &e : h->ev) CK(cudaEventCreate(&e));
     // secondary-node initial velocities (they never change: their rows are identity)
     h->sec_vel.resize(num_blobs);
@@ -303,6 +265,12 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
                 if (H.maps[b].lin_of_orig[n] < 0)
                     for (int c = 0; c < 3; c++) h->sec_vel[b][3 * (size_t)n + c] = m.vel[3 * (size_t)n + c];
     }
+    // persistent CG kernel: all CTAs co-resident, at most CG_MAX_TILES node tiles each
+    const int max_grid = cg_max_grid(d.precision);
+    if (max_grid <= 0) return fail("cannot size the persistent CG kernel on this device");
+    d.cg_grid = std::min(max_grid, d.n_tiles);
+    if ((int64_t)d.cg_grid * CG_MAX_TILES < d.n_tiles)
+        return fail("batch too large: %d node tiles need more than %d co-resident CTAs", d.n_tiles, max_grid);
     launch_rest_state(d, h->stream);
     if (d.any_mass) launch_mass_matrix(d, h->stream);
     CK(cudaStreamSynchronize(h->stream));
@@ -360,27 +328,30 @@ int ffea_gpu_sizes(ffea_gpu_t *h, int64_t *linear_nodes, int64_t *elements, int6
     return FFEA_GPU_OK;
 }
 
-int ffea_gpu_step(ffea_gpu_t *h, int32_t nsteps)
+namespace {
+int enqueue_steps(ffea_gpu *h, int32_t nsteps, bool allow_direct)
 {
-    if (!h) return fail("null handle");
-    if (nsteps < 0) return fail("nsteps must be >= 0");
     DeviceBatch &d = h->dev;
-    for (int i = 0; i < 5; i++) h->phase_ms[i] = 0;
     for (int32_t s = 0; s < nsteps; s++) {
         if (h->graph_mode && !h->timing) {
-            if (!h->step_exec && build_step_graph(h) != FFEA_GPU_OK) return FFEA_GPU_ERROR;
-            CK(cudaGraphLaunch(h->step_exec, h->stream));
-            continue;
+            if (!h->step_exec && build_step_graph(h) != FFEA_GPU_OK) {
+                // fall back to direct launches when the graph cannot be built
+                h->graph_mode = 0;
+            } else {
+                CK(cudaGraphLaunch(h->step_exec, h->stream));
+                count_launches(h->fixed_per_step);
+                continue;
+            }
         }
+        if (!allow_direct) return fail("asynchronous stepping needs graph mode without timing");
         if (h->timing) CK(cudaEventRecord(h->ev[0], h->stream));
         launch_elements(d, h->stream, ELEM_STEP);
         if (h->timing) CK(cudaEventRecord(h->ev[1], h->stream));
         if (d.any_nomass) launch_assemble(d, h->stream);
         if (h->timing) CK(cudaEventRecord(h->ev[2], h->stream));
-        launch_nodes(d, h->stream, 0, 0);
+        launch_nodes(d, h->stream, 0);
         if (h->timing) CK(cudaEventRecord(h->ev[3], h->stream));
-        if (host_cg_loop(h) != FFEA_GPU_OK) return FFEA_GPU_ERROR;
-        if (h->host.bp[0].true_residual) launch_true_residual(d, h->stream);
+        CK(launch_cg(d, h->stream));
         if (h->timing) CK(cudaEventRecord(h->ev[4], h->stream));
         launch_euler(d, h->stream);
         if (h->timing) {
@@ -393,16 +364,52 @@ int ffea_gpu_step(ffea_gpu_t *h, int32_t nsteps)
             }
         }
     }
+    return FFEA_GPU_OK;
+}
+
+int sync_and_check(ffea_gpu *h)
+{
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
     std::vector<int32_t> st(h->host.num_blobs);
-    CK(cudaMemcpy(st.data(), d.status, st.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(st.data(), h->dev.status, st.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
     for (int b = 0; b < h->host.num_blobs; b++)
         if (st[b]) {
             const char *why = (st[b] & BLOB_FAIL_INVERSION) ? "an element inverted" : "the CG solve did not converge";
             return fail("blob %d: %s (status bits %d); the blob is frozen at the failing step", b, why, st[b]);
         }
     return FFEA_GPU_OK;
+}
+}  // namespace
+
+int ffea_gpu_step(ffea_gpu_t *h, int32_t nsteps)
+{
+    if (!h) return fail("null handle");
+    if (nsteps < 0) return fail("nsteps must be >= 0");
+    for (int i = 0; i < 5; i++) h->phase_ms[i] = 0;
+    if (enqueue_steps(h, nsteps, true) != FFEA_GPU_OK) return FFEA_GPU_ERROR;
+    return sync_and_check(h);
+}
+
+int ffea_gpu_step_async(ffea_gpu_t *h, int32_t nsteps)
+{
+    if (!h) return fail("null handle");
+    if (nsteps < 0) return fail("nsteps must be >= 0");
+    return enqueue_steps(h, nsteps, false);
+}
+
+int ffea_gpu_synchronize(ffea_gpu_t *h)
+{
+    if (!h) return fail("null handle");
+    return sync_and_check(h);
+}
+
+int64_t ffea_gpu_cg_loop_count(ffea_gpu_t *h)
+{
+    if (!h) return -1;
+    unsigned long long c = 0;
+    if (cudaMemcpy(&c, h->dev.loop_count, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return (int64_t)c;
 }
 
 int ffea_gpu_get_nodes(ffea_gpu_t *h, int32_t blob, double *pos, double *vel, double *force)
@@ -412,10 +419,10 @@ int ffea_gpu_get_nodes(ffea_gpu_t *h, int32_t blob, double *pos, double *vel, do
     const BlobParams &bp = h->host.bp[blob];
     const BlobMap &map = h->host.maps[blob];
     const size_t n3 = 3 * (size_t)bp.node_cnt, off = 3 * (size_t)bp.node_off;
-    std::vector<double> p(n3), v(n3), x(n3);
+    std::vector<double> p(n3), v(n3), x;
     CK(cudaMemcpy(p.data(), h->dev.pos + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(v.data(), h->dev.vel + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(x.data(), h->dev.x + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    if (copy_typed_to_double(h, h->dev.x, off, n3, x)) return FFEA_GPU_ERROR;
     const int32_t N = map.num_nodes_total;
     std::vector<double> P(3 * (size_t)N, 0.0);
     for (int32_t n = 0; n < N; n++) {
@@ -455,8 +462,9 @@ int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const dou
     const BlobMap &map = h->host.maps[blob];
     const size_t n3 = 3 * (size_t)bp.node_cnt, off = 3 * (size_t)bp.node_off;
     std::vector<double> p(n3), v(n3);
-    CK(cudaMemcpy(p.data(), h->dev.pos + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(v.data(), h->dev.vel + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    // every linear entry is overwritten when both arrays are given: no read-back then
+    if (!pos) CK(cudaMemcpy(p.data(), h->dev.pos + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    if (!vel) CK(cudaMemcpy(v.data(), h->dev.vel + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
     for (int32_t n = 0; n < map.num_nodes_total; n++) {
         const int32_t g = map.lin_of_orig[n];
         if (g < 0) {
@@ -577,15 +585,15 @@ int ffea_gpu_solver_solve(ffea_gpu_t *h, int32_t blob, const double *pos, double
     CK(cudaMemcpyAsync(d.rhs, rhs.data(), rhs.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     launch_elements(d, h->stream, ELEM_MATRIX_ONLY);
     if (d.any_nomass) launch_assemble(d, h->stream);
-    launch_nodes(d, h->stream, 1, 0);
-    if (host_cg_loop(h) != FFEA_GPU_OK) return FFEA_GPU_ERROR;
+    launch_nodes(d, h->stream, 1);
+    CK(launch_cg(d, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     CgScalars cg;
     int32_t st = 0;
     CK(cudaMemcpy(&cg, d.cg + blob, sizeof(cg), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&st, d.status + blob, sizeof(st), cudaMemcpyDeviceToHost));
-    std::vector<double> sol(3 * (size_t)bp.node_cnt);
-    CK(cudaMemcpy(sol.data(), d.x + 3 * (size_t)bp.node_off, sol.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<double> sol;
+    if (copy_typed_to_double(h, d.x, 3 * (size_t)bp.node_off, 3 * (size_t)bp.node_cnt, sol)) return FFEA_GPU_ERROR;
     for (int32_t n = 0; n < map.num_nodes_total; n++) {
         const int32_t g = map.lin_of_orig[n];
         for (int c = 0; c < 3; c++) {

@@ -351,20 +351,48 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
             err = "too many edge terms";
             return false;
         }
-        H.up_ptr.assign(H.nl_pad + 1, 0);
-        std::vector<int32_t> locnt(H.nl_pad + 1, 0);
+        // SELL-32 rows: neighbours in ascending column order
+        std::vector<int32_t> deg(H.nl_pad + 1, 0);
         for (int32_t e = 0; e < H.n_edges; e++) {
-            H.up_ptr[H.edge_p[e] + 1]++;
-            locnt[H.edge_q[e] + 1]++;
+            deg[H.edge_p[e] + 1]++;
+            deg[H.edge_q[e] + 1]++;
         }
-        std::partial_sum(H.up_ptr.begin(), H.up_ptr.end(), H.up_ptr.begin());
-        std::partial_sum(locnt.begin(), locnt.end(), locnt.begin());
-        H.lo_ptr = locnt;
-        H.lo_edge.assign(H.n_edges, 0);
+        std::partial_sum(deg.begin(), deg.end(), deg.begin());
+        std::vector<int64_t> adj(deg.back());  // (col << 32) | edge
         std::vector<int32_t> fill(H.nl_pad, 0);
         for (int32_t e = 0; e < H.n_edges; e++) {
-            int32_t q = H.edge_q[e];
-            H.lo_edge[H.lo_ptr[q] + fill[q]++] = e;
+            const int32_t p = H.edge_p[e], q = H.edge_q[e];
+            adj[deg[p] + fill[p]++] = ((int64_t)q << 32) | (uint32_t)e;
+            adj[deg[q] + fill[q]++] = ((int64_t)p << 32) | (uint32_t)e;
+        }
+        for (int32_t r = 0; r < H.nl_pad; r++) std::sort(adj.begin() + deg[r], adj.begin() + deg[r + 1]);
+        const int32_t nslices = H.nl_pad / 32;
+        H.slice_ptr.assign(nslices + 1, 0);
+        H.slice_len.assign(nslices, 0);
+        for (int32_t sl = 0; sl < nslices; sl++) {
+            int32_t L = 0;
+            for (int32_t r = 32 * sl; r < 32 * sl + 32; r++) L = std::max(L, deg[r + 1] - deg[r]);
+            H.slice_len[sl] = L;
+            if ((int64_t)H.slice_ptr[sl] + 32ll * L >= (1ll << 31)) {
+                err = "matrix too large for 32-bit SELL offsets";
+                return false;
+            }
+            H.slice_ptr[sl + 1] = H.slice_ptr[sl] + 32 * L;
+        }
+        H.sell_col.assign(H.slice_ptr[nslices], 0);
+        H.edge_pos_pq.assign(H.n_edges, 0);
+        H.edge_pos_qp.assign(H.n_edges, 0);
+        for (int32_t r = 0; r < H.nl_pad; r++) {
+            const int32_t sl = r / 32, lane = r % 32;
+            for (int32_t j = 0; j < H.slice_len[sl]; j++) H.sell_col[H.slice_ptr[sl] + 32 * j + lane] = r;  // padding: own row
+            for (int32_t j = 0; j < deg[r + 1] - deg[r]; j++) {
+                const int64_t v = adj[deg[r] + j];
+                const int32_t col = (int32_t)(v >> 32), e = (int32_t)(v & 0xffffffff);
+                const int32_t off = H.slice_ptr[sl] + 32 * j + lane;
+                H.sell_col[off] = col;
+                if (r == H.edge_p[e]) H.edge_pos_pq[e] = off;
+                else H.edge_pos_qp[e] = off;
+            }
         }
     }
 

@@ -39,8 +39,10 @@ struct HostBatch {
     std::vector<double> fold_drag;
     std::vector<int32_t> edge_p, edge_q;                  // edges (p < q), sorted by (p, q)
     std::vector<int32_t> edge_cptr, edge_cidx;            // edge -> (elem*16 + a*4 + b), element order
-    std::vector<int32_t> up_ptr;                          // node p -> edges [up_ptr[p], up_ptr[p+1]) with p first
-    std::vector<int32_t> lo_ptr, lo_edge;                 // node q -> edges with q second
+    // SELL-32 layout of the node-node matrix: slices of 32 consecutive rows,
+    // slot j of row r at entry slice_ptr[r/32] + 32*j + r%32, columns ascending
+    std::vector<int32_t> slice_ptr, slice_len, sell_col;
+    std::vector<int32_t> edge_pos_pq, edge_pos_qp;        // entry of (p,q) in row p and of (q,p) in row q
     std::vector<int32_t> tile_blob, etile_blob;
     int32_t num_streams = 0;
     std::vector<uint32_t> stream_state;                   // 6 per stream

@@ -7,19 +7,19 @@
 //                scaled gradients g = sqrt(vol) dpsi for the assembly
 //                (tetra_element_linear.cpp:193-489, Blob.cpp:638-735)
 //   k_assemble   per mesh edge: the 3x3 viscosity block as a fixed-order sum
-//                over the elements sharing the edge (NoMassCGSolver::init +
-//                SparseMatrixFixedPattern::build, without pointer chasing)
+//                over the elements sharing the edge, written into both rows of
+//                the SELL-32 matrix (NoMassCGSolver::init + SparseMatrixFixedPattern::build)
 //   k_nodes      per linear node: deterministic gather of element forces,
 //                Stokes drag and noise, midpoint folding, pins, Jacobi
 //                diagonal, and the CG start (Blob.cpp:3826-3928,
 //                NoMassCGSolver.cpp:205-230)
-//   k_spmv / k_update / k_pupdate    one Jacobi-PCG iteration
-//                (NoMassCGSolver.cpp:165-197, ConjugateGradientSolver.cpp:206-232)
+//   k_cg         the whole Jacobi-PCG solve in one persistent cooperative
+//                launch (NoMassCGSolver.cpp:165-197, ConjugateGradientSolver.cpp:206-232)
 //   k_euler      velocity / position update and RNG stream advance
 //                (Blob.cpp:3937-3969)
-// Reductions are deterministic: a fixed butterfly inside each CTA, one
-// partial per CTA, and a fixed-order per-blob sum done by the last CTA to
-// finish.  No floating-point atomics are used anywhere.
+// Reductions are deterministic: fixed butterflies inside warps and CTAs, one
+// partial per node tile, and fixed-order per-blob sums.  No floating-point
+// atomics are used anywhere.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -31,35 +31,36 @@ namespace ffea {
 
 static std::atomic<int64_t> g_launches{0};
 int64_t kernel_launch_count() { return g_launches.load(); }
+void count_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 #define FFEA_LAUNCHED() g_launches.fetch_add(1, std::memory_order_relaxed)
 
 namespace {
 
 // ---------------------------------------------------------------- reductions
-__device__ __forceinline__ double warp_sum(double v)
+template <typename A>
+__device__ __forceinline__ A warp_sum(A v)
 {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
-// Sum NV values over the CTA; result valid in thread 0.  Fixed order.
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double *smem)
+// Sum NV per-thread values over the CTA; the butterfly inside each warp runs
+// in W (float for the mixed path: GB300's FP64 rate is a small fraction of
+// FP32), the per-warp results are summed in FP64.  Result valid in thread 0.
+template <int NV, typename W>
+__device__ __forceinline__ void block_sum(const W (&in)[NV], double (&out)[NV], double *smem)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-    for (int k = 0; k < NV; k++) v[k] = warp_sum(v[k]);
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NV; k++) smem[k * 32 + warp] = v[k];
+    for (int k = 0; k < NV; k++) {
+        const W s = warp_sum<W>(in[k]);
+        if (lane == 0) smem[k * 32 + warp] = (double)s;
+    }
     __syncthreads();
     if (warp == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) {
-            double t = lane < nw ? smem[k * 32 + lane] : 0.0;
-            v[k] = warp_sum(t);
-        }
+        for (int k = 0; k < NV; k++) out[k] = warp_sum<double>(lane < nw ? smem[k * 32 + lane] : 0.0);
     }
     __syncthreads();
 }
@@ -79,29 +80,10 @@ __device__ __forceinline__ bool last_block(unsigned int *counter, unsigned int t
     return is_last != 0;
 }
 
-// Per-blob fixed-order sums of NV partials (stride 4 per tile) over the
-// blob's node tiles; one warp per blob.  fin(b, sums) runs in lane 0.
-template <int NV, typename Fin>
-__device__ __forceinline__ void reduce_node_tiles(const DeviceBatch &d, Fin fin)
+// SELL-32 value index of component k (0..8 row-major 3x3) of entry `off`
+__device__ __forceinline__ size_t sell_vidx(int off, int k)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int b = warp; b < d.num_blobs; b += nw) {
-        const int t0 = d.bp[b].tile_off, tc = d.bp[b].tile_cnt;
-        double s[NV];
-#pragma unroll
-        for (int k = 0; k < NV; k++) s[k] = 0.0;
-        for (int t = lane; t < tc; t += 32)
-#pragma unroll
-            for (int k = 0; k < NV; k++) s[k] += __ldcg(&d.partials[4 * (size_t)(t0 + t) + k]);
-#pragma unroll
-        for (int k = 0; k < NV; k++) s[k] = warp_sum(s[k]);
-        if (lane == 0) fin(b, s);
-    }
-}
-
-__device__ __forceinline__ void set_condition(unsigned long long cond, unsigned int v)
-{
-    if (cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, v);
+    return (size_t)(off & ~31) * 9 + (size_t)k * 32 + (off & 31);
 }
 
 // ---------------------------------------------------------------- element math
@@ -322,9 +304,10 @@ __global__ void __launch_bounds__(ELEM_TILE) k_elements(DeviceBatch d, int mode)
             fo[3 * a + i] = -(vol * (dpsi[a] * S[i][0] + dpsi[4 + a] * S[i][1] + dpsi[8 + a] * S[i][2]));
 }
 
-// Edge blocks of the viscosity matrix: K_pq = sum over elements e holding
-// edge (p,q) of vol_e [A (delta_ik dpsi_a.dpsi_b + dpsi_a,k dpsi_b,i) + B dpsi_a,i dpsi_b,k]
-// (include/tetra_element_linear.h:55-116 + add_diffusion_matrix).
+// Viscosity blocks: K_pq = sum over elements e holding edge (p,q) of
+// vol_e [A (delta_ik dpsi_a.dpsi_b + dpsi_a,k dpsi_b,i) + B dpsi_a,i dpsi_b,k]
+// (include/tetra_element_linear.h:55-116 + add_diffusion_matrix), written to
+// row p as K_pq and to row q as K_pq^T.
 template <typename T>
 __global__ void __launch_bounds__(EDGE_TILE) k_assemble(DeviceBatch d)
 {
@@ -348,9 +331,15 @@ __global__ void __launch_bounds__(EDGE_TILE) k_assemble(DeviceBatch d)
 #pragma unroll
             for (int j = 0; j < 3; j++) K[3 * i + j] += A * ((i == j ? gab : (T)0) + ga[j] * gb[i]) + B * ga[i] * gb[j];
     }
-    T *out = static_cast<T *>(d.blocks) + 9 * (size_t)e;
+    T *val = static_cast<T *>(d.sell_val);
+    const int opq = d.edge_pos_pq[e], oqp = d.edge_pos_qp[e];
 #pragma unroll
-    for (int i = 0; i < 9; i++) out[i] = K[i];
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            val[sell_vidx(opq, 3 * i + j)] = K[3 * i + j];
+            val[sell_vidx(oqp, 3 * j + i)] = K[3 * i + j];
+        }
 }
 
 // Mass matrix (ConjugateGradientSolver::init, src/ConjugateGradientSolver.cpp:62-204):
@@ -366,7 +355,9 @@ __global__ void k_mass_matrix(DeviceBatch d)
             s += .05 * d.mats[d.mat_id[el]].rho * (double)static_cast<const T *>(d.vol0)[el];
         }
         const bool pinned = (d.flags[d.edge_p[i]] | d.flags[d.edge_q[i]]) & NODE_PINNED;
-        static_cast<T *>(d.mass_edge)[i] = pinned ? (T)0 : (T)s;
+        T *mv = static_cast<T *>(d.sell_mval);
+        mv[d.edge_pos_pq[i]] = pinned ? (T)0 : (T)s;
+        mv[d.edge_pos_qp[i]] = pinned ? (T)0 : (T)s;
     }
     if (i < d.nl_pad) {
         double s = 0.0;
@@ -374,17 +365,17 @@ __global__ void k_mass_matrix(DeviceBatch d)
             const int el = d.gather_idx[k] >> 2;
             s += .1 * d.mats[d.mat_id[el]].rho * (double)static_cast<const T *>(d.vol0)[el];
         }
-        const bool pinned = d.flags[i] & NODE_PINNED;
+        const bool pinned = (d.flags[i] & NODE_PINNED) || s == 0.0;
         static_cast<T *>(d.mass_diag)[i] = pinned ? (T)1 : (T)s;
-        static_cast<T *>(d.dinv)[3 * (size_t)i] = pinned ? (T)1 : (T)(1.0 / s);
-        static_cast<T *>(d.dinv)[3 * (size_t)i + 1] = pinned ? (T)1 : (T)(1.0 / s);
-        static_cast<T *>(d.dinv)[3 * (size_t)i + 2] = pinned ? (T)1 : (T)(1.0 / s);
+        T *dinv = static_cast<T *>(d.dinv);
+#pragma unroll
+        for (int c = 0; c < 3; c++) dinv[3 * (size_t)i + c] = pinned ? (T)1 : (T)(1.0 / s);
     }
 }
 
 // Node kernel: rhs and the CG start.
 template <typename T>
-__global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_given_rhs, unsigned long long cond)
+__global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_given_rhs)
 {
     __shared__ double red[2 * 32];
     const int tile = blockIdx.x;
@@ -456,102 +447,147 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
 #pragma unroll
         for (int i = 0; i < 3; i++) dinv[3 * (size_t)row + i] = valid ? (T)(1.0 / (D[i] + drag)) : (T)1;
     }
-    double rz = 0.0, ff = 0.0;
-    T *p = static_cast<T *>(d.p);
+    // CG start (Chronopoulos-Gear form): x = 0, r = f, u = D^-1 r, p = s = w = 0
+    T *x = static_cast<T *>(d.x), *r = static_cast<T *>(d.r), *u = static_cast<T *>(d.u);
+    T *p = static_cast<T *>(d.p), *sv = static_cast<T *>(d.s), *w = static_cast<T *>(d.w);
+    double gam = 0.0, ff = 0.0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const size_t k = 3 * (size_t)row + i;
         const double fi = valid ? f[i] : 0.0;
         if (!use_given_rhs) d.rhs[k] = fi;
-        d.x[k] = 0.0;
-        d.r[k] = fi;
-        const double z = (double)dinv[k] * fi;
-        p[k] = (T)z;
-        rz += fi * z;
+        const T ri = (T)fi;
+        const T ui = dinv[k] * ri;
+        x[k] = (T)0;
+        r[k] = ri;
+        u[k] = ui;
+        p[k] = (T)0;
+        sv[k] = (T)0;
+        w[k] = (T)0;
+        gam += (double)ri * (double)ui;
         ff += fi * fi;
     }
-    double v[2] = {rz, ff};
-    block_sum<2>(v, red);
+    const double in[2] = {gam, ff};
+    double sums[2];
+    block_sum<2, double>(in, sums, red);
     if (threadIdx.x == 0) {
-        d.partials[4 * (size_t)tile] = v[0];
-        d.partials[4 * (size_t)tile + 1] = v[1];
+        d.partials[4 * (size_t)tile] = sums[0];
+        d.partials[4 * (size_t)tile + 1] = sums[1];
     }
     if (last_block(&d.counters[CNT_NODES], gridDim.x)) {
-        __shared__ int running;
+        __shared__ unsigned int running;
         if (threadIdx.x == 0) running = 0;
         __syncthreads();
-        reduce_node_tiles<2>(d, [&](int bb, const double *s) {
-            CgScalars &cg = d.cg[bb];
-            cg.delta = s[0];
-            cg.ff = s[1];
-            cg.pq = cg.rr = cg.alpha = cg.beta = 0.0;
-            cg.iters = 0;
-            cg.true_relres2 = -1.0;
-            const bool done = (d.status[bb] != 0) || s[1] == 0.0;
-            cg.converged = done ? 1 : 0;
-            cg.active = 1;
-            if (!done) atomicOr(&running, 1);
-        });
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int bb = warp; bb < d.num_blobs; bb += nw) {
+            const int t0 = d.bp[bb].tile_off, tc = d.bp[bb].tile_cnt;
+            double s0 = 0.0, s1 = 0.0;
+            for (int t = lane; t < tc; t += 32) {
+                s0 += __ldcg(&d.partials[4 * (size_t)(t0 + t)]);
+                s1 += __ldcg(&d.partials[4 * (size_t)(t0 + t) + 1]);
+            }
+            s0 = warp_sum<double>(s0);
+            s1 = warp_sum<double>(s1);
+            if (lane == 0) {
+                CgScalars &cg = d.cg[bb];
+                cg.gamma = s0;
+                cg.ff = s1;
+                cg.delta = cg.rr = cg.alpha = cg.beta = 0.0;
+                cg.iters = 0;
+                cg.restarts = 0;
+                cg.true_relres2 = -1.0;
+                const bool done = (d.status[bb] != 0) || s1 == 0.0;
+                cg.state = done ? CG_CONVERGED : CG_ACTIVE;
+                if (!done) atomicAdd(&running, 1u);
+            }
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
-            *d.any_running = running;
-            set_condition(cond, running ? 1u : 0u);
+            d.bar[0] = 0;          // arrival count
+            d.bar[2] = running;    // blobs still iterating
+            d.bar[3] = running;
+            d.bar[4] = 0;          // barrier time-out flag
             d.counters[CNT_NODES] = 0;
         }
     }
 }
 
-// q = A p for one row (difference form for the viscosity matrix), T arithmetic.
-template <typename T>
-__device__ __forceinline__ void row_apply(const DeviceBatch &d, int row, bool nomass, double drag, const T *p, T out[3])
+// ---------------------------------------------------------------- persistent CG
+constexpr unsigned int kSpinLimit = 1u << 24;  // ~1 s of 64 ns sleeps, then give up
+constexpr int kMaxRestarts = 4;
+
+// Grid-wide barrier of the persistent kernel (all CTAs co-resident by the
+// cooperative launch).  The last CTA to arrive publishes the running-blob
+// count, so every CTA leaves with the same value.  A wait that exceeds the
+// spin limit raises the time-out flag instead of hanging.
+__device__ __forceinline__ unsigned int grid_barrier(unsigned int *bar, int *s_err, unsigned int *s_pub)
 {
-    const T p0 = p[3 * (size_t)row], p1 = p[3 * (size_t)row + 1], p2 = p[3 * (size_t)row + 2];
-    T a0 = 0, a1 = 0, a2 = 0;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vb = bar;
+        const unsigned int gen = vb[1];
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&bar[0], 1u);
+        if (arrived == gridDim.x - 1) {
+            vb[3] = vb[2];
+            vb[0] = 0;
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        } else {
+            unsigned int spins = 0;
+            while (vb[1] == gen) {
+                if (++spins > kSpinLimit || vb[4]) {
+                    *s_err = 1;
+                    atomicExch(&bar[4], 1u);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        *s_pub = vb[3];
+    }
+    __syncthreads();
+    return *s_pub;
+}
+
+// q = A v for one row: NoMass in difference form sum_q K_pq (v_q - v_p) + drag v_p,
+// mass sum_q m_pq v_q + m_pp v_p.  v is read through L2 (written by other CTAs).
+template <typename T>
+__device__ __forceinline__ void sell_row(const DeviceBatch &d, int row, bool nomass, T diag, const T *v, T out[3])
+{
+    const int sl = row >> 5, lane = row & 31;
+    const int L = __ldg(&d.slice_len[sl]);
+    const int base = __ldg(&d.slice_ptr[sl]);
+    const T v0 = __ldcg(&v[3 * (size_t)row]), v1 = __ldcg(&v[3 * (size_t)row + 1]), v2 = __ldcg(&v[3 * (size_t)row + 2]);
+    T a0 = diag * v0, a1 = diag * v1, a2 = diag * v2;
     if (nomass) {
-        const T *blk = static_cast<const T *>(d.blocks);
-        // edges (row, q), q > row: K_pq = stored block
-        for (int e = d.up_ptr[row]; e < d.up_ptr[row + 1]; e++) {
-            const int qn = d.edge_q[e];
-            const T d0 = p[3 * (size_t)qn] - p0, d1 = p[3 * (size_t)qn + 1] - p1, d2 = p[3 * (size_t)qn + 2] - p2;
-            const T *K = blk + 9 * (size_t)e;
+        const T *val = static_cast<const T *>(d.sell_val);
+#pragma unroll 2
+        for (int j = 0; j < L; j++) {
+            const int off = base + 32 * j + lane;
+            const int q = __ldg(&d.sell_col[off]);
+            const size_t vb = (size_t)(base + 32 * j) * 9 + lane;
+            T K[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) K[k] = __ldg(&val[vb + 32 * k]);
+            const T d0 = __ldcg(&v[3 * (size_t)q]) - v0, d1 = __ldcg(&v[3 * (size_t)q + 1]) - v1,
+                    d2 = __ldcg(&v[3 * (size_t)q + 2]) - v2;
             a0 += K[0] * d0 + K[1] * d1 + K[2] * d2;
             a1 += K[3] * d0 + K[4] * d1 + K[5] * d2;
             a2 += K[6] * d0 + K[7] * d1 + K[8] * d2;
         }
-        // edges (q, row), q < row: K_pq = (stored block)^T
-        for (int k = d.lo_ptr[row]; k < d.lo_ptr[row + 1]; k++) {
-            const int e = d.lo_edge[k];
-            const int qn = d.edge_p[e];
-            const T d0 = p[3 * (size_t)qn] - p0, d1 = p[3 * (size_t)qn + 1] - p1, d2 = p[3 * (size_t)qn + 2] - p2;
-            const T *K = blk + 9 * (size_t)e;
-            a0 += K[0] * d0 + K[3] * d1 + K[6] * d2;
-            a1 += K[1] * d0 + K[4] * d1 + K[7] * d2;
-            a2 += K[2] * d0 + K[5] * d1 + K[8] * d2;
-        }
-        const T dr = (T)drag;
-        a0 += dr * p0;
-        a1 += dr * p1;
-        a2 += dr * p2;
     } else {
-        const T *me = static_cast<const T *>(d.mass_edge);
-        const T md = static_cast<const T *>(d.mass_diag)[row];
-        a0 = md * p0;
-        a1 = md * p1;
-        a2 = md * p2;
-        for (int e = d.up_ptr[row]; e < d.up_ptr[row + 1]; e++) {
-            const int qn = d.edge_q[e];
-            const T m = me[e];
-            a0 += m * p[3 * (size_t)qn];
-            a1 += m * p[3 * (size_t)qn + 1];
-            a2 += m * p[3 * (size_t)qn + 2];
-        }
-        for (int k = d.lo_ptr[row]; k < d.lo_ptr[row + 1]; k++) {
-            const int e = d.lo_edge[k];
-            const int qn = d.edge_p[e];
-            const T m = me[e];
-            a0 += m * p[3 * (size_t)qn];
-            a1 += m * p[3 * (size_t)qn + 1];
-            a2 += m * p[3 * (size_t)qn + 2];
+        const T *mv = static_cast<const T *>(d.sell_mval);
+#pragma unroll 2
+        for (int j = 0; j < L; j++) {
+            const int off = base + 32 * j + lane;
+            const int q = __ldg(&d.sell_col[off]);
+            const T m = __ldg(&mv[off]);
+            a0 += m * __ldcg(&v[3 * (size_t)q]);
+            a1 += m * __ldcg(&v[3 * (size_t)q + 1]);
+            a2 += m * __ldcg(&v[3 * (size_t)q + 2]);
         }
     }
     out[0] = a0;
@@ -559,143 +595,322 @@ __device__ __forceinline__ void row_apply(const DeviceBatch &d, int row, bool no
     out[2] = a2;
 }
 
+// b - A x for one row with FP64 products and accumulation (x is T).
 template <typename T>
-__global__ void __launch_bounds__(NODE_TILE) k_spmv(DeviceBatch d)
+__device__ __forceinline__ void true_residual_row(const DeviceBatch &d, int row, bool nomass, double diag, const T *x,
+                                                  double out[3])
 {
-    __shared__ double red[32];
-    const int tile = blockIdx.x;
-    const int b = d.tile_blob[tile];
-    const BlobParams &bp = d.bp[b];
-    const bool run = d.cg[b].converged == 0;
-    double pq = 0.0;
-    if (run) {
-        const int row = tile * NODE_TILE + threadIdx.x;
-        const bool valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
-        const T *p = static_cast<const T *>(d.p);
-        T q[3] = {0, 0, 0};
-        if (valid) {
-            const double drag = bp.calc_stokes == 1 ? d.drag[row] : 0.0;
-            row_apply<T>(d, row, bp.solver == SOLVER_NOMASS, drag, p, q);
-            pq = (double)p[3 * (size_t)row] * (double)q[0] + (double)p[3 * (size_t)row + 1] * (double)q[1] +
-                 (double)p[3 * (size_t)row + 2] * (double)q[2];
+    const int sl = row >> 5, lane = row & 31;
+    const int L = __ldg(&d.slice_len[sl]);
+    const int base = __ldg(&d.slice_ptr[sl]);
+    const double x0 = (double)__ldcg(&x[3 * (size_t)row]), x1 = (double)__ldcg(&x[3 * (size_t)row + 1]),
+                 x2 = (double)__ldcg(&x[3 * (size_t)row + 2]);
+    double a0 = diag * x0, a1 = diag * x1, a2 = diag * x2;
+    for (int j = 0; j < L; j++) {
+        const int off = base + 32 * j + lane;
+        const int q = __ldg(&d.sell_col[off]);
+        const double y0 = (double)__ldcg(&x[3 * (size_t)q]), y1 = (double)__ldcg(&x[3 * (size_t)q + 1]),
+                     y2 = (double)__ldcg(&x[3 * (size_t)q + 2]);
+        if (nomass) {
+            const T *val = static_cast<const T *>(d.sell_val);
+            const size_t vb = (size_t)(base + 32 * j) * 9 + lane;
+            double K[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) K[k] = (double)__ldg(&val[vb + 32 * k]);
+            const double d0 = y0 - x0, d1 = y1 - x1, d2 = y2 - x2;
+            a0 += K[0] * d0 + K[1] * d1 + K[2] * d2;
+            a1 += K[3] * d0 + K[4] * d1 + K[5] * d2;
+            a2 += K[6] * d0 + K[7] * d1 + K[8] * d2;
+        } else {
+            const double m = (double)__ldg(&static_cast<const T *>(d.sell_mval)[off]);
+            a0 += m * y0;
+            a1 += m * y1;
+            a2 += m * y2;
         }
-        T *qo = static_cast<T *>(d.q);
-        qo[3 * (size_t)row] = q[0];
-        qo[3 * (size_t)row + 1] = q[1];
-        qo[3 * (size_t)row + 2] = q[2];
     }
-    double v[1] = {pq};
-    block_sum<1>(v, red);
-    if (threadIdx.x == 0) d.partials[4 * (size_t)tile + 2] = v[0];
-    if (last_block(&d.counters[CNT_SPMV], gridDim.x)) {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int bb = warp; bb < d.num_blobs; bb += nw) {
-            if (d.cg[bb].converged) continue;
-            const int t0 = d.bp[bb].tile_off, tc = d.bp[bb].tile_cnt;
-            double s = 0.0;
-            for (int t = lane; t < tc; t += 32) s += __ldcg(&d.partials[4 * (size_t)(t0 + t) + 2]);
-            s = warp_sum(s);
-            if (lane == 0) {
-                d.cg[bb].pq = s;
-                d.cg[bb].alpha = d.cg[bb].delta / s;
-            }
-        }
-        if (threadIdx.x == 0) d.counters[CNT_SPMV] = 0;
-    }
+    out[0] = d.rhs[3 * (size_t)row] - a0;
+    out[1] = d.rhs[3 * (size_t)row + 1] - a1;
+    out[2] = d.rhs[3 * (size_t)row + 2] - a2;
 }
 
+// The whole solve of every blob: Chronopoulos-Gear PCG (one pair of
+// reductions per iteration), x0 = 0, stopping on sum r^2 / sum f^2 < eps^2
+// like residual2() (src/NoMassCGSolver.cpp:233-247).  With true_residual on,
+// a recursive convergence is confirmed by an FP64 b - A x; a failed check
+// restarts CG from that residual.  CTA c owns node tiles
+// [n_tiles*c/G, n_tiles*(c+1)/G); thread t owns row t of each of its tiles.
 template <typename T>
-__global__ void __launch_bounds__(NODE_TILE) k_update(DeviceBatch d, unsigned long long cond)
+__global__ void __launch_bounds__(CG_THREADS) k_cg(DeviceBatch d)
 {
-    __shared__ double red[2 * 32];
-    const int tile = blockIdx.x;
-    const int b = d.tile_blob[tile];
-    const bool run = d.cg[b].converged == 0;
-    double rr = 0.0, rz = 0.0;
-    if (run) {
-        const int row = tile * NODE_TILE + threadIdx.x;
-        const double alpha = d.cg[b].alpha;
-        const T *p = static_cast<const T *>(d.p);
-        const T *q = static_cast<const T *>(d.q);
-        const T *dinv = static_cast<const T *>(d.dinv);
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            const size_t k = 3 * (size_t)row + i;
-            d.x[k] += alpha * (double)p[k];
-            const double r = d.r[k] + (-alpha) * (double)q[k];
-            d.r[k] = r;
-            rr += r * r;
-            rz += r * ((double)dinv[k] * r);
-        }
-    }
-    double v[2] = {rr, rz};
-    block_sum<2>(v, red);
-    if (threadIdx.x == 0) {
-        d.partials[4 * (size_t)tile] = v[0];
-        d.partials[4 * (size_t)tile + 1] = v[1];
-    }
-    if (last_block(&d.counters[CNT_UPDATE], gridDim.x)) {
-        __shared__ int running;
-        if (threadIdx.x == 0) running = 0;
-        __syncthreads();
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int bb = warp; bb < d.num_blobs; bb += nw) {
-            CgScalars &cg = d.cg[bb];
-            if (cg.converged) continue;
-            const int t0 = d.bp[bb].tile_off, tc = d.bp[bb].tile_cnt;
-            double s0 = 0.0, s1 = 0.0;
-            for (int t = lane; t < tc; t += 32) {
-                s0 += __ldcg(&d.partials[4 * (size_t)(t0 + t)]);
-                s1 += __ldcg(&d.partials[4 * (size_t)(t0 + t) + 1]);
+    using W = T;
+    __shared__ double red[4 * 32];
+    __shared__ int s_nt, s_nb, s_err;
+    __shared__ unsigned int s_pub;
+    __shared__ int s_tslot[CG_MAX_TILES];
+    __shared__ int s_blob[CG_MAX_TILES], s_state[CG_MAX_TILES], s_iters[CG_MAX_TILES], s_restarts[CG_MAX_TILES];
+    __shared__ int s_owner[CG_MAX_TILES], s_limit[CG_MAX_TILES], s_tr[CG_MAX_TILES], s_nomass[CG_MAX_TILES];
+    __shared__ double s_alpha[CG_MAX_TILES], s_beta[CG_MAX_TILES], s_gamma[CG_MAX_TILES], s_ff[CG_MAX_TILES];
+    __shared__ double s_gnew[CG_MAX_TILES], s_eps2[CG_MAX_TILES], s_trr[CG_MAX_TILES], s_rr[CG_MAX_TILES];
+    __shared__ double s_sum[2][CG_MAX_TILES];
+
+    const int G = gridDim.x, c = blockIdx.x, tid = threadIdx.x;
+    const int T0 = (int)(((long long)d.n_tiles * c) / G), T1 = (int)(((long long)d.n_tiles * (c + 1)) / G);
+    if (tid == 0) {
+        s_err = 0;
+        int nb = 0;
+        for (int j = 0; j < T1 - T0; j++) {
+            const int b = d.tile_blob[T0 + j];
+            if (nb == 0 || s_blob[nb - 1] != b) {
+                const CgScalars cg = d.cg[b];
+                const BlobParams &bp = d.bp[b];
+                s_blob[nb] = b;
+                s_state[nb] = cg.state;
+                s_gamma[nb] = cg.gamma;
+                s_ff[nb] = cg.ff;
+                s_alpha[nb] = s_beta[nb] = 0.0;
+                s_iters[nb] = 0;
+                s_restarts[nb] = 0;
+                s_trr[nb] = -1.0;
+                s_rr[nb] = 0.0;
+                s_owner[nb] = bp.tile_off == T0 + j;
+                s_limit[nb] = bp.solver == SOLVER_MASS ? bp.max_iter - 1 : bp.max_iter;
+                s_tr[nb] = bp.true_residual;
+                s_nomass[nb] = bp.solver == SOLVER_NOMASS;
+                s_eps2[nb] = bp.epsilon2;
+                nb++;
             }
-            s0 = warp_sum(s0);
-            s1 = warp_sum(s1);
+            s_tslot[j] = nb - 1;
+        }
+        s_nt = T1 - T0;
+        s_nb = nb;
+    }
+    __syncthreads();
+    const int nt = s_nt, nb = s_nb;
+    T *x = static_cast<T *>(d.x), *r = static_cast<T *>(d.r), *u = static_cast<T *>(d.u);
+    T *w = static_cast<T *>(d.w), *p = static_cast<T *>(d.p), *sv = static_cast<T *>(d.s);
+    const T *dinv = static_cast<const T *>(d.dinv);
+
+    // per-blob fixed-order sums of two partial slots; one warp per distinct
+    // blob, 8 loads per lane in flight per pass (the partials live in L2)
+    auto reduce2 = [&](int slot0) {
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int k = warp; k < nb; k += CG_THREADS / 32) {
+            const int b = s_blob[k];
+            const int t0 = d.bp[b].tile_off, tc = d.bp[b].tile_cnt;
+            double a0 = 0.0, a1 = 0.0;
+            for (int base = 0; base < tc; base += 8 * 32) {
+                double v0[8], v1[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int t = base + 32 * q + lane;
+                    const double2 pv = t < tc ? __ldcg(reinterpret_cast<const double2 *>(
+                                                    &d.partials[4 * (size_t)(t0 + t) + slot0]))
+                                              : make_double2(0.0, 0.0);
+                    v0[q] = pv.x;
+                    v1[q] = pv.y;
+                }
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    a0 += v0[q];
+                    a1 += v1[q];
+                }
+            }
+            a0 = warp_sum<double>(a0);
+            a1 = warp_sum<double>(a1);
             if (lane == 0) {
-                cg.iters += 1;
-                cg.rr = s0;
-                // residual2() = sum r^2 / sum f^2 (src/NoMassCGSolver.cpp:233-247)
-                const double res = (cg.ff == 0.0) ? 0.0 : s0 / cg.ff;
-                const int limit = d.bp[bb].solver == SOLVER_MASS ? d.bp[bb].max_iter - 1 : d.bp[bb].max_iter;
-                if (res < d.bp[bb].epsilon2) {
-                    cg.converged = 1;
-                } else if (!(res == res) || cg.iters >= limit) {
-                    cg.converged = 1;
-                    atomicOr(&d.status[bb], (res == res) ? BLOB_FAIL_CG : (BLOB_FAIL_CG | BLOB_FAIL_NAN));
-                } else {
-                    cg.beta = s1 / cg.delta;
-                    cg.delta = s1;
-                    atomicOr(&running, 1);
+                s_sum[0][k] = a0;
+                s_sum[1][k] = a1;
+            }
+        }
+        __syncthreads();
+    };
+    auto finish_blob = [&](int k, int state, int bits) {
+        s_state[k] = state;
+        if (s_owner[k]) {
+            atomicSub(&d.bar[2], 1u);
+            if (bits) atomicOr(&d.status[s_blob[k]], bits);
+        }
+    };
+    // SpMV phase for ACTIVE / RESTART blobs: w = A u, partial delta = w . u  -> slot 2;
+    // VERIFY blobs: r = b - A x (FP64), u = D^-1 r, partials r.r -> slot 2, r.u -> slot 3
+    auto spmv_phase = [&]() {
+        for (int j = 0; j < nt; j++) {
+            const int t = T0 + j, k = s_tslot[j], st = s_state[k];
+            const int row = t * NODE_TILE + tid;
+            const BlobParams &bp = d.bp[s_blob[k]];
+            const bool valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
+            W wd = 0, wg = 0;
+            double vd = 0.0, vg = 0.0;
+            if ((st == CG_ACTIVE || st == CG_RESTART) && valid) {
+                const T diag = s_nomass[k] ? (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0)
+                                           : static_cast<const T *>(d.mass_diag)[row];
+                T q[3];
+                sell_row<T>(d, row, s_nomass[k], diag, u, q);
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    w[3 * (size_t)row + i] = q[i];
+                    wd += q[i] * __ldcg(&u[3 * (size_t)row + i]);
+                }
+            } else if (st == CG_VERIFY && valid) {
+                const double diag = s_nomass[k] ? (bp.calc_stokes == 1 ? d.drag[row] : 0.0)
+                                                : (double)static_cast<const T *>(d.mass_diag)[row];
+                double rt[3];
+                true_residual_row<T>(d, row, s_nomass[k], diag, x, rt);
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    const size_t kk = 3 * (size_t)row + i;
+                    const T ri = (T)rt[i];
+                    const T ui = dinv[kk] * ri;
+                    r[kk] = ri;
+                    u[kk] = ui;
+                    vd += rt[i] * rt[i];
+                    vg += (double)ri * (double)ui;
+                }
+            }
+            double out[2];
+            if (st == CG_VERIFY) {
+                const double in[2] = {vd, vg};
+                block_sum<2, double>(in, out, red);
+            } else {
+                const W in[2] = {wd, wg};
+                block_sum<2, W>(in, out, red);
+            }
+            if (tid == 0) {
+                d.partials[4 * (size_t)t + 2] = out[0];
+                d.partials[4 * (size_t)t + 3] = out[1];
+            }
+        }
+    };
+
+    // prologue: w0 = A u0, delta0, alpha0 = gamma0 / delta0
+    spmv_phase();
+    unsigned int running = grid_barrier(d.bar, &s_err, &s_pub);
+    long long loops = 0;
+    if (!s_err) {
+        reduce2(2);
+        if (tid == 0)
+            for (int k = 0; k < nb; k++)
+                if (s_state[k] == CG_ACTIVE) {
+                    s_alpha[k] = s_gamma[k] / s_sum[0][k];
+                    s_beta[k] = 0.0;
+                }
+        __syncthreads();
+    }
+    while (!s_err && running > 0) {
+        // phase A: p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = D^-1 r
+        for (int j = 0; j < nt; j++) {
+            const int t = T0 + j, k = s_tslot[j];
+            const int row = t * NODE_TILE + tid;
+            W gam = 0, rr = 0;
+            if (s_state[k] == CG_ACTIVE) {
+                const T alpha = (T)s_alpha[k], beta = (T)s_beta[k];
+                const bool first = s_beta[k] == 0.0;
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    const size_t kk = 3 * (size_t)row + i;
+                    const T ui = u[kk], wi = w[kk];
+                    const T pi = first ? ui : ui + beta * p[kk];
+                    const T si = first ? wi : wi + beta * sv[kk];
+                    p[kk] = pi;
+                    sv[kk] = si;
+                    x[kk] += alpha * pi;
+                    const T ri = r[kk] - alpha * si;
+                    r[kk] = ri;
+                    const T un = dinv[kk] * ri;
+                    u[kk] = un;
+                    gam += ri * un;
+                    rr += ri * ri;
+                }
+            }
+            const W in[2] = {gam, rr};
+            double out[2];
+            block_sum<2, W>(in, out, red);
+            if (tid == 0) {
+                d.partials[4 * (size_t)t] = out[0];
+                d.partials[4 * (size_t)t + 1] = out[1];
+            }
+        }
+        loops++;
+        running = grid_barrier(d.bar, &s_err, &s_pub);
+        if (s_err || running == 0) break;
+        reduce2(0);
+        if (tid == 0) {
+            for (int k = 0; k < nb; k++) {
+                if (s_state[k] != CG_ACTIVE) continue;
+                s_iters[k] += 1;
+                const double rr = s_sum[1][k];
+                s_rr[k] = rr;
+                s_gnew[k] = s_sum[0][k];
+                const double res = (s_ff[k] == 0.0) ? 0.0 : rr / s_ff[k];
+                if (res < s_eps2[k]) {
+                    if (s_tr[k]) s_state[k] = CG_VERIFY;
+                    else finish_blob(k, CG_CONVERGED, 0);
+                } else if (!(res == res)) {
+                    finish_blob(k, CG_FAILED, BLOB_FAIL_CG | BLOB_FAIL_NAN);
+                } else if (s_iters[k] >= s_limit[k]) {
+                    finish_blob(k, CG_FAILED, BLOB_FAIL_CG);
                 }
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            *d.any_running = running;
-            set_condition(cond, running ? 1u : 0u);
-            d.counters[CNT_UPDATE] = 0;
+        // phase B: w = A u (or the FP64 true residual for blobs being verified)
+        spmv_phase();
+        running = grid_barrier(d.bar, &s_err, &s_pub);
+        if (s_err) break;
+        reduce2(2);
+        if (tid == 0) {
+            for (int k = 0; k < nb; k++) {
+                const int st = s_state[k];
+                if (st == CG_ACTIVE) {
+                    const double gnew = s_gnew[k], delta = s_sum[0][k];
+                    const double beta = gnew / s_gamma[k];
+                    s_alpha[k] = gnew / (delta - beta * gnew / s_alpha[k]);
+                    s_beta[k] = beta;
+                    s_gamma[k] = gnew;
+                } else if (st == CG_RESTART) {
+                    s_alpha[k] = s_gamma[k] / s_sum[0][k];
+                    s_beta[k] = 0.0;
+                    s_state[k] = CG_ACTIVE;
+                } else if (st == CG_VERIFY) {
+                    const double trr = s_sum[0][k];
+                    s_trr[k] = (s_ff[k] == 0.0) ? 0.0 : trr / s_ff[k];
+                    if (s_trr[k] < s_eps2[k]) {
+                        finish_blob(k, CG_CONVERGED, 0);
+                    } else if (s_restarts[k] >= kMaxRestarts || s_iters[k] >= s_limit[k]) {
+                        finish_blob(k, CG_FAILED, BLOB_FAIL_CG);
+                    } else {
+                        s_restarts[k] += 1;
+                        s_gamma[k] = s_sum[1][k];
+                        s_state[k] = CG_RESTART;
+                    }
+                }
+            }
         }
+        __syncthreads();
+        if (running == 0) break;
     }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(NODE_TILE) k_pupdate(DeviceBatch d)
-{
-    const int tile = blockIdx.x;
-    const int b = d.tile_blob[tile];
-    if (d.cg[b].converged) return;
-    const double beta = d.cg[b].beta;
-    const int row = tile * NODE_TILE + threadIdx.x;
-    T *p = static_cast<T *>(d.p);
-    const T *dinv = static_cast<const T *>(d.dinv);
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const size_t k = 3 * (size_t)row + i;
-        // vec3_scale_and_add: p = beta p + z (src/mat_vec_fns.cpp:265-275)
-        p[k] = (T)(beta * (double)p[k] + (double)dinv[k] * d.r[k]);
+    if (tid == 0) {
+        if (s_err) {
+            for (int k = 0; k < nb; k++) atomicOr(&d.status[s_blob[k]], BLOB_FAIL_CG | BLOB_FAIL_TIMEOUT);
+        }
+        for (int k = 0; k < nb; k++) {
+            if (!s_owner[k]) continue;
+            CgScalars &cg = d.cg[s_blob[k]];
+            cg.state = s_state[k];
+            cg.iters = s_iters[k];
+            cg.restarts = s_restarts[k];
+            cg.alpha = s_alpha[k];
+            cg.beta = s_beta[k];
+            cg.gamma = s_gamma[k];
+            cg.rr = s_rr[k];
+            cg.true_relres2 = s_trr[k];
+        }
+        if (c == 0) *d.loop_count += (unsigned long long)loops;
     }
 }
 
 // Euler update (src/Blob.cpp:3937-3969) and the RNG advance to the next step.
+template <typename T>
 __global__ void __launch_bounds__(NODE_TILE) k_euler(DeviceBatch d)
 {
     const int tile = blockIdx.x;
@@ -717,19 +932,63 @@ __global__ void __launch_bounds__(NODE_TILE) k_euler(DeviceBatch d)
     }
     if (row - bp.node_off >= bp.node_cnt || d.status[b]) return;
     const double dt = bp.dt;
+    const T *x = static_cast<const T *>(d.x);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const size_t k = 3 * (size_t)row + i;
+        const double xi = (double)x[k];
         if (bp.solver == SOLVER_NOMASS) {
-            const double x = d.x[k];
-            d.vel[k] = x;
-            d.pos[k] += x * dt;
+            d.vel[k] = xi;
+            d.pos[k] += xi * dt;
         } else {
-            const double v = d.vel[k] + d.x[k] * dt;
+            const double v = d.vel[k] + xi * dt;
             d.vel[k] = v;
             d.pos[k] += v * dt;
         }
     }
+}
+
+// out = A in (FP64 vectors and arithmetic); pinned rows and padding give 0.
+template <typename T>
+__global__ void __launch_bounds__(NODE_TILE) k_apply(DeviceBatch d, const double *in, double *out)
+{
+    const int tile = blockIdx.x;
+    const int b = d.tile_blob[tile];
+    const BlobParams &bp = d.bp[b];
+    const int row = tile * NODE_TILE + threadIdx.x;
+    const bool valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
+    double acc[3] = {0.0, 0.0, 0.0};
+    if (valid) {
+        const bool nomass = bp.solver == SOLVER_NOMASS;
+        const double diag = nomass ? (bp.calc_stokes == 1 ? d.drag[row] : 0.0)
+                                   : (double)static_cast<const T *>(d.mass_diag)[row];
+        const int sl = row >> 5, lane = row & 31;
+        const int L = d.slice_len[sl], base = d.slice_ptr[sl];
+        const double v0 = in[3 * (size_t)row], v1 = in[3 * (size_t)row + 1], v2 = in[3 * (size_t)row + 2];
+        acc[0] = diag * v0;
+        acc[1] = diag * v1;
+        acc[2] = diag * v2;
+        for (int j = 0; j < L; j++) {
+            const int off = base + 32 * j + lane;
+            const int q = d.sell_col[off];
+            const double y0 = in[3 * (size_t)q], y1 = in[3 * (size_t)q + 1], y2 = in[3 * (size_t)q + 2];
+            if (nomass) {
+                const T *val = static_cast<const T *>(d.sell_val);
+                double K[9];
+                for (int k = 0; k < 9; k++) K[k] = (double)val[sell_vidx(off, k)];
+                const double d0 = y0 - v0, d1 = y1 - v1, d2 = y2 - v2;
+                acc[0] += K[0] * d0 + K[1] * d1 + K[2] * d2;
+                acc[1] += K[3] * d0 + K[4] * d1 + K[5] * d2;
+                acc[2] += K[6] * d0 + K[7] * d1 + K[8] * d2;
+            } else {
+                const double m = (double)static_cast<const T *>(d.sell_mval)[off];
+                acc[0] += m * y0;
+                acc[1] += m * y1;
+                acc[2] += m * y2;
+            }
+        }
+    }
+    for (int i = 0; i < 3; i++) out[3 * (size_t)row + i] = acc[i];
 }
 
 // Strain (and kinetic) energy at the current state, FP64
@@ -772,8 +1031,9 @@ __global__ void __launch_bounds__(ELEM_TILE) k_energies(DeviceBatch d)
                 }
         }
     }
-    double v[2] = {se, ke};
-    block_sum<2>(v, red);
+    const double ein[2] = {se, ke};
+    double v[2];
+    block_sum<2, double>(ein, v, red);
     if (threadIdx.x == 0) {
         d.epartials[2 * (size_t)tile] = v[0];
         d.epartials[2 * (size_t)tile + 1] = v[1];
@@ -787,142 +1047,14 @@ __global__ void __launch_bounds__(ELEM_TILE) k_energies(DeviceBatch d)
                 s0 += __ldcg(&d.epartials[2 * (size_t)(t0 + t)]);
                 s1 += __ldcg(&d.epartials[2 * (size_t)(t0 + t) + 1]);
             }
-            s0 = warp_sum(s0);
-            s1 = warp_sum(s1);
+            s0 = warp_sum<double>(s0);
+            s1 = warp_sum<double>(s1);
             if (lane == 0) {
                 d.energy[2 * bb] = 0.5 * s0;
                 d.energy[2 * bb + 1] = 0.5 * s1;
             }
         }
         if (threadIdx.x == 0) d.counters[CNT_ENERGY] = 0;
-    }
-}
-
-// out = A in (FP64 vectors), pinned rows and padding excluded (callers handle them).
-template <typename T>
-__global__ void __launch_bounds__(NODE_TILE) k_apply(DeviceBatch d, const double *in, double *out)
-{
-    const int tile = blockIdx.x;
-    const int b = d.tile_blob[tile];
-    const BlobParams &bp = d.bp[b];
-    const int row = tile * NODE_TILE + threadIdx.x;
-    const bool valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
-    double acc[3] = {0.0, 0.0, 0.0};
-    if (valid) {
-        const double drag = bp.calc_stokes == 1 ? d.drag[row] : 0.0;
-        const double p0 = in[3 * (size_t)row], p1 = in[3 * (size_t)row + 1], p2 = in[3 * (size_t)row + 2];
-        if (bp.solver == SOLVER_NOMASS) {
-            const T *blk = static_cast<const T *>(d.blocks);
-            for (int e = d.up_ptr[row]; e < d.up_ptr[row + 1]; e++) {
-                const int qn = d.edge_q[e];
-                const double d0 = in[3 * (size_t)qn] - p0, d1 = in[3 * (size_t)qn + 1] - p1, d2 = in[3 * (size_t)qn + 2] - p2;
-                const T *K = blk + 9 * (size_t)e;
-                acc[0] += (double)K[0] * d0 + (double)K[1] * d1 + (double)K[2] * d2;
-                acc[1] += (double)K[3] * d0 + (double)K[4] * d1 + (double)K[5] * d2;
-                acc[2] += (double)K[6] * d0 + (double)K[7] * d1 + (double)K[8] * d2;
-            }
-            for (int k = d.lo_ptr[row]; k < d.lo_ptr[row + 1]; k++) {
-                const int e = d.lo_edge[k];
-                const int qn = d.edge_p[e];
-                const double d0 = in[3 * (size_t)qn] - p0, d1 = in[3 * (size_t)qn + 1] - p1, d2 = in[3 * (size_t)qn + 2] - p2;
-                const T *K = blk + 9 * (size_t)e;
-                acc[0] += (double)K[0] * d0 + (double)K[3] * d1 + (double)K[6] * d2;
-                acc[1] += (double)K[1] * d0 + (double)K[4] * d1 + (double)K[7] * d2;
-                acc[2] += (double)K[2] * d0 + (double)K[5] * d1 + (double)K[8] * d2;
-            }
-            acc[0] += drag * p0;
-            acc[1] += drag * p1;
-            acc[2] += drag * p2;
-        } else {
-            const T *me = static_cast<const T *>(d.mass_edge);
-            const double md = (double)static_cast<const T *>(d.mass_diag)[row];
-            acc[0] = md * p0;
-            acc[1] = md * p1;
-            acc[2] = md * p2;
-            for (int e = d.up_ptr[row]; e < d.up_ptr[row + 1]; e++) {
-                const int qn = d.edge_q[e];
-                for (int i = 0; i < 3; i++) acc[i] += (double)me[e] * in[3 * (size_t)qn + i];
-            }
-            for (int k = d.lo_ptr[row]; k < d.lo_ptr[row + 1]; k++) {
-                const int e = d.lo_edge[k];
-                const int qn = d.edge_p[e];
-                for (int i = 0; i < 3; i++) acc[i] += (double)me[e] * in[3 * (size_t)qn + i];
-            }
-        }
-    }
-    for (int i = 0; i < 3; i++) out[3 * (size_t)row + i] = acc[i];
-}
-
-// FP64 true residual of the last solve: || rhs - A x ||^2 / ||rhs||^2 per blob.
-template <typename T>
-__global__ void __launch_bounds__(NODE_TILE) k_true_residual(DeviceBatch d)
-{
-    __shared__ double red[32];
-    const int tile = blockIdx.x;
-    const int b = d.tile_blob[tile];
-    const BlobParams &bp = d.bp[b];
-    const int row = tile * NODE_TILE + threadIdx.x;
-    const bool valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED) && d.status[b] == 0;
-    double rr = 0.0;
-    if (valid) {
-        // A x with FP64 accumulation; x is FP64, blocks T.
-        const double drag = bp.calc_stokes == 1 ? d.drag[row] : 0.0;
-        const double *x = d.x;
-        const double x0 = x[3 * (size_t)row], x1 = x[3 * (size_t)row + 1], x2 = x[3 * (size_t)row + 2];
-        double a[3] = {0.0, 0.0, 0.0};
-        if (bp.solver == SOLVER_NOMASS) {
-            const T *blk = static_cast<const T *>(d.blocks);
-            for (int e = d.up_ptr[row]; e < d.up_ptr[row + 1]; e++) {
-                const int qn = d.edge_q[e];
-                const double d0 = x[3 * (size_t)qn] - x0, d1 = x[3 * (size_t)qn + 1] - x1, d2 = x[3 * (size_t)qn + 2] - x2;
-                const T *K = blk + 9 * (size_t)e;
-                a[0] += (double)K[0] * d0 + (double)K[1] * d1 + (double)K[2] * d2;
-                a[1] += (double)K[3] * d0 + (double)K[4] * d1 + (double)K[5] * d2;
-                a[2] += (double)K[6] * d0 + (double)K[7] * d1 + (double)K[8] * d2;
-            }
-            for (int k = d.lo_ptr[row]; k < d.lo_ptr[row + 1]; k++) {
-                const int e = d.lo_edge[k];
-                const int qn = d.edge_p[e];
-                const double d0 = x[3 * (size_t)qn] - x0, d1 = x[3 * (size_t)qn + 1] - x1, d2 = x[3 * (size_t)qn + 2] - x2;
-                const T *K = blk + 9 * (size_t)e;
-                a[0] += (double)K[0] * d0 + (double)K[3] * d1 + (double)K[6] * d2;
-                a[1] += (double)K[1] * d0 + (double)K[4] * d1 + (double)K[7] * d2;
-                a[2] += (double)K[2] * d0 + (double)K[5] * d1 + (double)K[8] * d2;
-            }
-            a[0] += drag * x0;
-            a[1] += drag * x1;
-            a[2] += drag * x2;
-        } else {
-            const T *me = static_cast<const T *>(d.mass_edge);
-            const double md = (double)static_cast<const T *>(d.mass_diag)[row];
-            a[0] = md * x0;
-            a[1] = md * x1;
-            a[2] = md * x2;
-            for (int e = d.up_ptr[row]; e < d.up_ptr[row + 1]; e++)
-                for (int i = 0; i < 3; i++) a[i] += (double)me[e] * x[3 * (size_t)d.edge_q[e] + i];
-            for (int k = d.lo_ptr[row]; k < d.lo_ptr[row + 1]; k++) {
-                const int e = d.lo_edge[k];
-                for (int i = 0; i < 3; i++) a[i] += (double)me[e] * x[3 * (size_t)d.edge_p[e] + i];
-            }
-        }
-        for (int i = 0; i < 3; i++) {
-            const double r = d.rhs[3 * (size_t)row + i] - a[i];
-            rr += r * r;
-        }
-    }
-    double v[1] = {rr};
-    block_sum<1>(v, red);
-    if (threadIdx.x == 0) d.partials[4 * (size_t)tile + 3] = v[0];
-    if (last_block(&d.counters[CNT_TRUERES], gridDim.x)) {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int bb = warp; bb < d.num_blobs; bb += nw) {
-            const int t0 = d.bp[bb].tile_off, tc = d.bp[bb].tile_cnt;
-            double s = 0.0;
-            for (int t = lane; t < tc; t += 32) s += __ldcg(&d.partials[4 * (size_t)(t0 + t) + 3]);
-            s = warp_sum(s);
-            if (lane == 0) d.cg[bb].true_relres2 = d.cg[bb].ff == 0.0 ? 0.0 : s / d.cg[bb].ff;
-        }
-        if (threadIdx.x == 0) d.counters[CNT_TRUERES] = 0;
     }
 }
 
@@ -944,6 +1076,7 @@ __global__ void k_rng_draws(const mrg::JumpMat *table, const uint32_t *state, ui
     mrg::jump(table, (uint32_t)off, st);
     out[i] = mrg::u01(st);
 }
+
 
 inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
@@ -981,22 +1114,43 @@ void launch_assemble(const DeviceBatch &d, cudaStream_t s)
     PREC_DISPATCH(d, k_assemble, blocks_for(d.n_edges, EDGE_TILE), EDGE_TILE, s, d);
 }
 
-void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs, unsigned long long cond)
+void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs)
 {
-    PREC_DISPATCH(d, k_nodes, d.n_tiles, NODE_TILE, s, d, use_given_rhs, cond);
+    PREC_DISPATCH(d, k_nodes, d.n_tiles, NODE_TILE, s, d, use_given_rhs);
 }
 
-void launch_cg_iteration(const DeviceBatch &d, cudaStream_t s, unsigned long long cond)
+int cg_max_grid(int precision)
 {
-    PREC_DISPATCH(d, k_spmv, d.n_tiles, NODE_TILE, s, d);
-    PREC_DISPATCH(d, k_update, d.n_tiles, NODE_TILE, s, d, cond);
-    PREC_DISPATCH(d, k_pupdate, d.n_tiles, NODE_TILE, s, d);
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    cudaError_t e = precision == PREC_FP64
+                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double>, CG_THREADS, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float>, CG_THREADS, 0);
+    if (e != cudaSuccess) return 0;
+    return sms * per_sm;
+}
+
+cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)d.cg_grid);
+    cfg.blockDim = dim3(CG_THREADS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FFEA_LAUNCHED();
+    if (d.precision == PREC_FP64) return cudaLaunchKernelEx(&cfg, k_cg<double>, d);
+    return cudaLaunchKernelEx(&cfg, k_cg<float>, d);
 }
 
 void launch_euler(const DeviceBatch &d, cudaStream_t s)
 {
-    k_euler<<<d.n_tiles, NODE_TILE, 0, s>>>(d);
-    FFEA_LAUNCHED();
+    PREC_DISPATCH(d, k_euler, d.n_tiles, NODE_TILE, s, d);
 }
 
 void launch_energies(const DeviceBatch &d, cudaStream_t s)
@@ -1007,11 +1161,6 @@ void launch_energies(const DeviceBatch &d, cudaStream_t s)
 void launch_apply(const DeviceBatch &d, cudaStream_t s, const double *in, double *out)
 {
     PREC_DISPATCH(d, k_apply, d.n_tiles, NODE_TILE, s, d, in, out);
-}
-
-void launch_true_residual(const DeviceBatch &d, cudaStream_t s)
-{
-    PREC_DISPATCH(d, k_true_residual, d.n_tiles, NODE_TILE, s, d);
 }
 
 void launch_rng_draws(const mrg::JumpMat *table, const uint32_t *state, uint64_t offset, int64_t count, double *out,

@@ -11,8 +11,10 @@ namespace ffea {
 // precision-dependent type T (float in PREC_MIXED, double in PREC_FP64).
 struct DeviceBatch {
     int32_t num_blobs = 0, nl_pad = 0, ne_pad = 0, n_edges = 0, n_tiles = 0, n_etiles = 0, num_streams = 0;
+    int32_t n_slices = 0, n_entries = 0;
     int32_t precision = PREC_MIXED;
     int32_t any_mass = 0, any_nomass = 0;
+    int32_t cg_grid = 0;          // CTAs of the persistent CG kernel
     // blobs
     BlobParams *bp = nullptr;
     Material *mats = nullptr;
@@ -21,55 +23,65 @@ struct DeviceBatch {
     mrg::JumpMat *jump_table = nullptr;
     uint32_t *stream_state = nullptr;
     mrg::JumpMat *stream_step = nullptr;
-    // nodes
-    double *pos = nullptr, *vel = nullptr, *drag = nullptr, *rhs = nullptr, *x = nullptr, *r = nullptr;
+    // nodes (FP64 state and rhs)
+    double *pos = nullptr, *vel = nullptr, *drag = nullptr, *rhs = nullptr;
     uint8_t *flags = nullptr;
     int32_t *orig = nullptr;
     int32_t *gather_ptr = nullptr, *gather_idx = nullptr;
     int32_t *fold_ptr = nullptr, *fold_sec = nullptr;
     double *fold_drag = nullptr;
-    void *p = nullptr, *q = nullptr, *dinv = nullptr;
+    // CG vectors, T-typed, 3 per padded node: solution x, residual r,
+    // preconditioned residual u, w = A u, directions p and s = A p, Jacobi dinv
+    void *x = nullptr, *r = nullptr, *u = nullptr, *w = nullptr, *p = nullptr, *s = nullptr, *dinv = nullptr;
     // elements
     int32_t *conn = nullptr;
     uint16_t *mat_id = nullptr;
     int8_t *det_sign = nullptr;
     void *jinv0 = nullptr, *vol0 = nullptr, *efrc = nullptr, *g = nullptr;
-    // edges
+    // edges and the SELL-32 matrix
     int32_t *edge_p = nullptr, *edge_q = nullptr, *edge_cptr = nullptr, *edge_cidx = nullptr;
-    int32_t *up_ptr = nullptr, *lo_ptr = nullptr, *lo_edge = nullptr;
-    void *blocks = nullptr, *mass_edge = nullptr, *mass_diag = nullptr;
+    int32_t *edge_pos_pq = nullptr, *edge_pos_qp = nullptr;
+    int32_t *slice_ptr = nullptr, *slice_len = nullptr, *sell_col = nullptr;
+    void *sell_val = nullptr;     // 9 T per entry: (slot base)*9 + k*32 + lane
+    void *sell_mval = nullptr;    // mass matrix: 1 T per entry
+    void *mass_diag = nullptr;    // T per node
     // reductions / status
     double *partials = nullptr;     // 4 per node tile
     CgScalars *cg = nullptr;        // per blob
     unsigned int *counters = nullptr;  // one per reduction site
+    unsigned int *bar = nullptr;    // grid barrier: arrival count, generation
     int32_t *status = nullptr;      // per blob failure bits
     int32_t *inverted = nullptr;    // per blob inverted-element count of the last step
     double *energy = nullptr;       // per blob: strain, kinetic
     double *epartials = nullptr;    // 2 per element tile
-    int32_t *any_running = nullptr; // host-visible "some blob still iterating" flag
+    unsigned long long *loop_count = nullptr;  // CG iterations executed by the persistent kernel (max over blobs)
 };
 
 // reduction counter slots
-enum CounterSlot { CNT_NODES = 0, CNT_SPMV = 1, CNT_UPDATE = 2, CNT_ENERGY = 3, CNT_TRUERES = 4, CNT_COUNT = 8 };
+enum CounterSlot { CNT_NODES = 0, CNT_ENERGY = 1, CNT_COUNT = 4 };
 
 // element kernel modes
 enum ElemMode { ELEM_STEP = 0, ELEM_MATRIX_ONLY = 1 };
 
-// Launchers (all asynchronous on `s`).  `cond` is a graph conditional handle
-// (0 when not inside a conditional body).
+constexpr int CG_THREADS = NODE_TILE;   // one row per thread and tile
+constexpr int CG_MAX_TILES = 64;        // node tiles per CTA of the persistent kernel
+
+// Launchers (all asynchronous on `s`).
 void launch_rest_state(const DeviceBatch &d, cudaStream_t s);
 void launch_mass_matrix(const DeviceBatch &d, cudaStream_t s);
 void launch_elements(const DeviceBatch &d, cudaStream_t s, int mode);
 void launch_assemble(const DeviceBatch &d, cudaStream_t s);
-void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs, unsigned long long cond);
-void launch_cg_iteration(const DeviceBatch &d, cudaStream_t s, unsigned long long cond);
+void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs);
+cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s);
 void launch_euler(const DeviceBatch &d, cudaStream_t s);
 void launch_energies(const DeviceBatch &d, cudaStream_t s);
 void launch_apply(const DeviceBatch &d, cudaStream_t s, const double *in, double *out);
-void launch_true_residual(const DeviceBatch &d, cudaStream_t s);
 void launch_rng_draws(const mrg::JumpMat *table, const uint32_t *state, uint64_t offset, int64_t count, double *out,
                       cudaStream_t s);
+// CTAs of the persistent CG kernel that fit co-resident on the current device
+int cg_max_grid(int precision);
 
 int64_t kernel_launch_count();
+void count_launches(int64_t n);
 
 }  // namespace ffea

@@ -29,6 +29,7 @@ constexpr uint8_t NODE_PINNED = 1;   // pinned or padding: identity row, zero fo
 constexpr int32_t BLOB_FAIL_INVERSION = 1;
 constexpr int32_t BLOB_FAIL_CG = 2;
 constexpr int32_t BLOB_FAIL_NAN = 4;
+constexpr int32_t BLOB_FAIL_TIMEOUT = 8;   // a grid barrier of the CG kernel gave up waiting
 
 struct BlobParams {
     double dt, kT, epsilon2;
@@ -50,17 +51,20 @@ struct Material {
     double rho, A, B, G, E;
 };
 
-// Per-blob CG scalars, FP64.
+// CG state of a blob during a solve
+enum CgState : int32_t { CG_ACTIVE = 0, CG_VERIFY = 1, CG_RESTART = 2, CG_CONVERGED = 3, CG_FAILED = 4 };
+
+// Per-blob CG scalars, FP64 (Chronopoulos-Gear recurrences).
 struct CgScalars {
-    double delta;      // r . z
-    double ff;         // f . f (rhs norm^2)
-    double pq;         // p . A p
+    double gamma;      // r . u   (u = D^-1 r)
+    double delta;      // w . u   (w = A u)
+    double ff;         // f . f   (rhs norm^2)
     double rr;         // r . r
     double alpha, beta;
-    double true_relres2;
-    int32_t iters;
-    int32_t converged;  // 1 converged, 0 running
-    int32_t active;     // participates in the current solve
+    double true_relres2;   // ||b - A x||^2 / ||b||^2 of the last verification, -1 if none
+    int32_t iters;         // matrix-vector products of this solve (the reference's iteration count)
+    int32_t state;         // CgState
+    int32_t restarts;
     int32_t pad_;
 };
 

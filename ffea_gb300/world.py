@@ -123,6 +123,16 @@ class World:
         """num_steps x (update_internal_forces + update_positions) for every blob."""
         L.check(L.lib().ffea_gpu_step(self._h, int(num_steps)), "ffea_gpu_step")
 
+    def run_async(self, num_steps: int = 1) -> None:
+        """Enqueue steps on the handle's stream without waiting (graph mode)."""
+        L.check(L.lib().ffea_gpu_step_async(self._h, int(num_steps)), "ffea_gpu_step_async")
+
+    def synchronize(self) -> None:
+        L.check(L.lib().ffea_gpu_synchronize(self._h), "ffea_gpu_synchronize")
+
+    def cg_loop_count(self) -> int:
+        return int(L.lib().ffea_gpu_cg_loop_count(self._h))
+
     def set_timing(self, on: bool):
         L.check(L.lib().ffea_gpu_set_timing(self._h, 1 if on else 0))
 

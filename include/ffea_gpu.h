@@ -174,9 +174,18 @@ int ffea_gpu_phase_times(ffea_gpu_t *h, double out_ms[5]);
  * work after a step. */
 void *ffea_gpu_stream(ffea_gpu_t *h);
 
-/* Execution mode: 1 = one CUDA graph per step with a device-side conditional
- * loop for the CG iterations (default); 0 = host-driven launches. */
+/* Execution mode: 1 = one CUDA graph per step (default); 0 = direct launches. */
 int ffea_gpu_set_graph_mode(ffea_gpu_t *h, int32_t enable);
+
+/* Enqueue nsteps steps on the handle's stream and return without waiting
+ * (graph mode only); ffea_gpu_synchronize waits and reports failures the way
+ * ffea_gpu_step does. */
+int ffea_gpu_step_async(ffea_gpu_t *h, int32_t nsteps);
+int ffea_gpu_synchronize(ffea_gpu_t *h);
+
+/* Iterations of the CG loop (each one SpMV and one vector update over every
+ * blob still iterating) that the handle's persistent solver kernel executed. */
+int64_t ffea_gpu_cg_loop_count(ffea_gpu_t *h);
 
 #ifdef __cplusplus
 }
