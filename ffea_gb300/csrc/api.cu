@@ -88,6 +88,11 @@ std::vector<mrg::JumpMat *> g_tables;
 
 }  // namespace
 
+namespace ffea {
+// lets the other translation units of the library report through ffea_gpu_last_error
+void set_last_error(const char *msg) { g_last_error = msg; }
+}  // namespace ffea
+
 struct ffea_gpu {
     HostBatch host;
     DeviceBatch dev;

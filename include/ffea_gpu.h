@@ -153,6 +153,30 @@ int ffea_gpu_rng_draws(const uint64_t state[6], uint64_t offset, int64_t count, 
 /* World::init's six seed words for an rng_seed (src/World.cpp:299-305). */
 int ffea_gpu_ffea_seed(int32_t rng_seed, uint64_t out[6]);
 
+/* --- allocation-free measurement ------------------------------------------ */
+
+/* Strain and kinetic energy of one blob, like ffea_gpu_energies, for callers
+ * that cannot allocate device memory where they measure (for instance a host
+ * code's own time-step loop, where cudaMalloc would synchronise the device
+ * and fragment a pool the host manages).  This entry point has no counterpart
+ * in FFEA; it allocates nothing.
+ *   Inputs and output are DEVICE pointers owned by the caller: pos, vel (may
+ *   be NULL), rest_pos (positions the rest state is taken from) -- 3*N_t
+ *   doubles each in the reference node numbering --, topology (10 int32 per
+ *   element), material (rho, A, B, G, E per element), out (2 doubles: strain,
+ *   kinetic).  solver selects whether the kinetic term is evaluated (mass path).
+ *   Scratch is a static device array of the library sized for at most
+ *   2,097,152 elements; larger meshes are rejected with an error.  Every GPU
+ *   that loads the library holds that array (256 KiB) until the process exits.
+ *   The first call on a device looks the array up on that device; make that
+ *   first call before any stream capture.  All calls share the array: calls
+ *   that overlap on the GPU (different streams, no ordering) race.
+ *   Work is enqueued on `stream` (a cudaStream_t; NULL = legacy default
+ *   stream); the result is ready when the stream reaches that point. */
+int ffea_gpu_energies_noalloc(const double *pos, const double *vel, const int32_t *topology, const double *rest_pos,
+                              const double *material, int32_t num_elements, int32_t solver, double *out,
+                              void *stream);
+
 /* --- diagnostics --------------------------------------------------------- */
 
 /* Copies the last error message of the calling thread (NUL-terminated). */
