@@ -64,7 +64,7 @@ def build_spec(workload: str, rank: int, precision: str):
     w = WORKLOADS[workload]
     mesh = sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0)
     prm = P.SimulationParams.from_si(dt=1e-14, kT=P.kT_at(300.0) * P.MESO_ENERGY, epsilon=1e-6,
-                                     max_iterations_cg=10000, rng_seed=44 + rank, solver=P.SOLVER_NOMASS,
+                                     max_iterations_cg=10000, rng_seed=replica_seed(rank), solver=P.SOLVER_NOMASS,
                                      precision=P.PRECISION_MIXED if precision == "mixed" else P.PRECISION_FP64)
     return make_blob(mesh, prm)
 
@@ -203,6 +203,26 @@ def dist_env():
     return rank, world, local
 
 
+def replica_seed(rank: int) -> int:
+    """Each rank steps its own replica blob with its own RNG stream (no exchange)."""
+    return 44 + rank
+
+
+def max_over_ranks(x: float, world: int, device="cuda") -> float:
+    """The slowest rank's time: the whole job is done when the last replica is."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_throughput(nodes_per_replica: int, steps: int, world: int, seconds: float) -> float:
+    """Whole-job node-steps/s: every replica advances all its linear nodes each step."""
+    return nodes_per_replica * steps * world / seconds
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -266,11 +286,8 @@ def run_gb300(args):
     total_ms = float(sum(step_ms))
     loops = w.cg_loop_count() - loops0
     launches = kernel_launches() - launches0
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = N * K * world / (total_ms / 1e3)
+    total_ms = max_over_ranks(total_ms, world)
+    value = aggregate_throughput(N, K, world, total_ms / 1e3)
 
     # end to end through the C ABI with host buffers: set_nodes (H2D) + step + get_nodes (D2H)
     blob = w.blob(0)
@@ -284,11 +301,8 @@ def run_gb300(args):
         w.run(1)
         pos, vel, _ = blob.get_nodes()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": N * Ke * world / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": 2 * 3 * 8 * N,
+    e2e_s = max_over_ranks(e2e_s, world)
+    e2e = {"value": aggregate_throughput(N, Ke, world, e2e_s), "unit": "node-steps/s", "h2d_bytes_per_step": 2 * 3 * 8 * N,
            "d2h_bytes_per_step": 3 * 3 * 8 * N, "steps": Ke}
 
     # profile pass: direct launches with CUDA events around each kernel of a step

@@ -145,7 +145,7 @@ def write_blob(prefix, files: BlobFiles):
         for k, p in enumerate(files.pos):
             if k == files.num_surface_nodes:
                 fh.write("interior nodes:\n")
-            fh.write(f"{p[0]!r} {p[1]!r} {p[2]!r}\n")
+            fh.write(f"{float(p[0])!r} {float(p[1])!r} {float(p[2])!r}\n")
     with open(prefix + ".top", "w") as fh:
         fh.write("ffea topology file\n")
         fh.write(f"num_elements {e}\nnum_surface_elements {files.num_surface_elements}\n")

@@ -194,6 +194,24 @@ void orc_rng_draws(uint64_t *state, int64_t n, double *out)
     for (int i = 0; i < 6; i++) state[i] = (uint64_t)Cg[i];
 }
 
+/* Sequential sum and FNV-style hash (h = (h ^ bits) * 0x100000001b3 from
+ * 0xcbf29ce484222325) of n draws: a fingerprint of a whole stream. */
+void orc_rng_fingerprint(const uint64_t *state, int64_t n, double *sum, uint64_t *hash)
+{
+    double Cg[6], s = 0.0;
+    uint64_t h = 0xcbf29ce484222325ULL;
+    for (int i = 0; i < 6; i++) Cg[i] = (double)state[i];
+    for (int64_t i = 0; i < n; i++) {
+        double u = orc_u01(Cg);
+        uint64_t bits;
+        memcpy(&bits, &u, sizeof(bits));
+        h = (h ^ bits) * 0x100000001b3ULL;
+        s += u;
+    }
+    *sum = s;
+    *hash = h;
+}
+
 void orc_rng_jump(uint64_t *state, uint64_t n)
 {
     double Cg[6];

@@ -76,6 +76,7 @@ def port_lib():
         lib.orc_blob_apply_nomass.argtypes = [ctypes.c_void_p, _dp, _dp]
         lib.orc_rng_draws.argtypes = [_u64p, ctypes.c_int64, _dp]
         lib.orc_rng_jump.argtypes = [_u64p, ctypes.c_uint64]
+        lib.orc_rng_fingerprint.argtypes = [_u64p, ctypes.c_int64, _dp, _u64p]
         lib.orc_rng_package_kat.restype = ctypes.c_double
         lib.orc_ffea_seed.argtypes = [ctypes.c_int, _u64p]
         lib.orc_ffea_thread_stream.argtypes = [_u64p, ctypes.c_int, _u64p]
@@ -128,6 +129,15 @@ def rng_jump(state, n: int) -> np.ndarray:
     st = np.ascontiguousarray(state, dtype=np.uint64).copy()
     port_lib().orc_rng_jump(_ptr(st, _u64p), ctypes.c_uint64(int(n)))
     return st
+
+
+def rng_fingerprint(state, n: int):
+    """(sequential sum, FNV-style hash) of n draws from a state."""
+    st = np.ascontiguousarray(state, dtype=np.uint64)
+    s = ctypes.c_double()
+    h = ctypes.c_uint64()
+    port_lib().orc_rng_fingerprint(_ptr(st, _u64p), int(n), ctypes.byref(s), ctypes.byref(h))
+    return s.value, h.value
 
 
 def rng_package_kat() -> float:
