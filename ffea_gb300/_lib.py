@@ -80,6 +80,7 @@ SIGNATURES = {
     "ffea_gpu_step_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ffea_gpu_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "ffea_gpu_cg_loop_count": (ctypes.c_int64, [ctypes.c_void_p]),
+    "ffea_gpu_diag_spmv": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _dp]),
     "ffea_gpu_energies_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 5 + [ctypes.c_int32, ctypes.c_int32,
                                                                           ctypes.c_void_p, ctypes.c_void_p]),
 }

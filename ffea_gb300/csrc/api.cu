@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -240,7 +241,8 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     d.n_entries = (int32_t)H.sell_col.size();
     const size_t n3 = 3 * (size_t)H.nl_pad;
     CK(A.alloc(d.rhs, n3));
-    for (void **v : {&d.x, &d.r, &d.u, &d.w, &d.p, &d.s, &d.dinv}) CK(A.alloc_bytes(*v, n3 * ts));
+    for (void **v : {&d.x, &d.r, &d.u, &d.w, &d.p, &d.s, &d.dinv, &d.m, &d.z, &d.q, &d.m2})
+        CK(A.alloc_bytes(*v, n3 * ts));
     CK(A.alloc(d.det_sign, (size_t)H.ne_pad));
     CK(A.alloc_bytes(d.jinv0, 9 * (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.vol0, (size_t)H.ne_pad * ts));
@@ -249,7 +251,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(A.alloc_bytes(d.sell_val, H.any_nomass ? 9 * (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.sell_mval, H.any_mass ? (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.mass_diag, H.any_mass ? (size_t)H.nl_pad * ts : 16));
-    CK(A.alloc(d.partials, 4 * (size_t)H.n_tiles));
+    CK(A.alloc(d.partials, 8 * (size_t)H.n_tiles));
     CK(A.alloc(d.epartials, 2 * (size_t)H.n_etiles));
     CK(A.alloc(d.cg, (size_t)H.num_blobs));
     CK(A.alloc(d.counters, (size_t)CNT_COUNT));
@@ -271,9 +273,23 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
                     for (int c = 0; c < 3; c++) h->sec_vel[b][3 * (size_t)n + c] = m.vel[3 * (size_t)n + c];
     }
     // persistent CG kernel: all CTAs co-resident, at most CG_MAX_TILES node tiles each
-    const int max_grid = cg_max_grid(d.precision);
+    // register-resident variant when every node tile gets a CTA of its own
+    const int reg_grid = cg_max_grid(d.precision, 1);
+    const int max_grid = cg_max_grid(d.precision, 0);
     if (max_grid <= 0) return fail("cannot size the persistent CG kernel on this device");
-    d.cg_grid = std::min(max_grid, d.n_tiles);
+    const char *force_mem = std::getenv("FFEA_GPU_CG_MEMORY_STATE");
+    if (reg_grid >= d.n_tiles && !(force_mem && force_mem[0] == '1')) {
+        d.cg_reg = 1;
+        d.cg_grid = d.n_tiles;
+    } else {
+        d.cg_reg = 0;
+        d.cg_grid = std::min(max_grid, d.n_tiles);
+    }
+    // local reduction (every CTA sums all partials, no serial last-arriver
+    // step) while that read stays small
+    const char *force_last = std::getenv("FFEA_GPU_CG_LAST_ARRIVER");
+    d.cg_local = d.num_blobs <= CG_LOCAL_MAX_BLOBS && d.n_tiles <= CG_LOCAL_MAX_TILES &&
+                 !(force_last && force_last[0] == '1');
     if ((int64_t)d.cg_grid * CG_MAX_TILES < d.n_tiles)
         return fail("batch too large: %d node tiles need more than %d co-resident CTAs", d.n_tiles, max_grid);
     launch_rest_state(d, h->stream);
@@ -685,3 +701,19 @@ int ffea_gpu_rng_draws(const uint64_t state[6], uint64_t offset, int64_t count, 
 }
 
 }  // extern "C"
+
+extern "C" int ffea_gpu_diag_spmv(ffea_gpu_t *h, int32_t variant, int32_t reps, double *us_per_spmv)
+{
+    if (!h || !us_per_spmv || reps <= 0) return fail("bad arguments");
+    if (variant < 0 || variant > 3) return fail("SpMV variant must be 0..3");
+    launch_spmv_variant(h->dev, h->stream, variant);  // warm-up
+    CK(cudaEventRecord(h->ev[0], h->stream));
+    for (int i = 0; i < reps; i++) launch_spmv_variant(h->dev, h->stream, variant);
+    CK(cudaEventRecord(h->ev[1], h->stream));
+    CK(cudaEventSynchronize(h->ev[1]));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+    CK(cudaGetLastError());
+    *us_per_spmv = 1e3 * (double)ms / reps;
+    return FFEA_GPU_OK;
+}

@@ -447,9 +447,10 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
 #pragma unroll
         for (int i = 0; i < 3; i++) dinv[3 * (size_t)row + i] = valid ? (T)(1.0 / (D[i] + drag)) : (T)1;
     }
-    // CG start (Chronopoulos-Gear form): x = 0, r = f, u = D^-1 r, p = s = w = 0
+    // CG start (pipelined form): x = 0, r = f, u = D^-1 r, w = m = z = q = s = p = 0
     T *x = static_cast<T *>(d.x), *r = static_cast<T *>(d.r), *u = static_cast<T *>(d.u);
     T *p = static_cast<T *>(d.p), *sv = static_cast<T *>(d.s), *w = static_cast<T *>(d.w);
+    T *mv = static_cast<T *>(d.m), *zv = static_cast<T *>(d.z), *qv = static_cast<T *>(d.q);
     double gam = 0.0, ff = 0.0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -464,6 +465,9 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
         p[k] = (T)0;
         sv[k] = (T)0;
         w[k] = (T)0;
+        mv[k] = (T)0;
+        zv[k] = (T)0;
+        qv[k] = (T)0;
         gam += (double)ri * (double)ui;
         ff += fi * fi;
     }
@@ -507,6 +511,7 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
             d.bar[2] = running;    // blobs still iterating
             d.bar[3] = running;
             d.bar[4] = 0;          // barrier time-out flag
+            d.bar[5] = 0;          // arrivals at counting barriers (monotonic within a solve)
             d.counters[CNT_NODES] = 0;
         }
     }
@@ -516,44 +521,38 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
 constexpr unsigned int kSpinLimit = 1u << 24;  // ~1 s of 64 ns sleeps, then give up
 constexpr int kMaxRestarts = 4;
 
-// Grid-wide barrier of the persistent kernel (all CTAs co-resident by the
-// cooperative launch).  The last CTA to arrive publishes the running-blob
-// count, so every CTA leaves with the same value.  A wait that exceeds the
-// spin limit raises the time-out flag instead of hanging.
-__device__ __forceinline__ unsigned int grid_barrier(unsigned int *bar, int *s_err, unsigned int *s_pub)
+// Grid-wide barrier on a counter that only grows during a solve: each CTA
+// adds one and waits until the count reaches `target` (the number of CTAs
+// times the barriers passed so far, including this one).  The waiters see the
+// last arrival directly, one L2 round trip sooner than with a separate
+// release word.  The CTAs are co-resident (cooperative launch); a wait that
+// exceeds the spin limit raises the time-out flag instead of hanging.
+__device__ __forceinline__ void counting_barrier(unsigned int *bar, unsigned int target, int *s_err)
 {
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned int *vb = bar;
-        const unsigned int gen = vb[1];
         __threadfence();
-        const unsigned int arrived = atomicAdd(&bar[0], 1u);
-        if (arrived == gridDim.x - 1) {
-            vb[3] = vb[2];
-            vb[0] = 0;
-            __threadfence();
-            atomicAdd(&bar[1], 1u);
-        } else {
-            unsigned int spins = 0;
-            while (vb[1] == gen) {
-                if (++spins > kSpinLimit || vb[4]) {
-                    *s_err = 1;
-                    atomicExch(&bar[4], 1u);
-                    break;
-                }
-                __nanosleep(64);
+        atomicAdd(&bar[5], 1u);
+        volatile unsigned int *vb = bar;
+        unsigned int spins = 0;
+        while ((int)(vb[5] - target) < 0) {
+            if (++spins > kSpinLimit || vb[4]) {
+                *s_err = 1;
+                atomicExch(&bar[4], 1u);
+                break;
             }
+            __nanosleep(32);
         }
         __threadfence();
-        *s_pub = vb[3];
     }
     __syncthreads();
-    return *s_pub;
 }
 
 // q = A v for one row: NoMass in difference form sum_q K_pq (v_q - v_p) + drag v_p,
 // mass sum_q m_pq v_q + m_pp v_p.  v is read through L2 (written by other CTAs).
+// Slots are processed in groups of 4: the column indices of a group are
+// loaded together, then the 12 neighbour components, so a group costs about
+// two L2 round trips instead of one or two per slot.
 template <typename T>
 __device__ __forceinline__ void sell_row(const DeviceBatch &d, int row, bool nomass, T diag, const T *v, T out[3])
 {
@@ -562,37 +561,100 @@ __device__ __forceinline__ void sell_row(const DeviceBatch &d, int row, bool nom
     const int base = __ldg(&d.slice_ptr[sl]);
     const T v0 = __ldcg(&v[3 * (size_t)row]), v1 = __ldcg(&v[3 * (size_t)row + 1]), v2 = __ldcg(&v[3 * (size_t)row + 2]);
     T a0 = diag * v0, a1 = diag * v1, a2 = diag * v2;
-    if (nomass) {
-        const T *val = static_cast<const T *>(d.sell_val);
-#pragma unroll 2
-        for (int j = 0; j < L; j++) {
-            const int off = base + 32 * j + lane;
-            const int q = __ldg(&d.sell_col[off]);
-            const size_t vb = (size_t)(base + 32 * j) * 9 + lane;
-            T K[9];
+    const T *val = static_cast<const T *>(d.sell_val);
+    const T *mv = static_cast<const T *>(d.sell_mval);
+    constexpr int GRP = 4;
+    for (int j0 = 0; j0 < L; j0 += GRP) {
+        int q[GRP];
 #pragma unroll
-            for (int k = 0; k < 9; k++) K[k] = __ldg(&val[vb + 32 * k]);
-            const T d0 = __ldcg(&v[3 * (size_t)q]) - v0, d1 = __ldcg(&v[3 * (size_t)q + 1]) - v1,
-                    d2 = __ldcg(&v[3 * (size_t)q + 2]) - v2;
-            a0 += K[0] * d0 + K[1] * d1 + K[2] * d2;
-            a1 += K[3] * d0 + K[4] * d1 + K[5] * d2;
-            a2 += K[6] * d0 + K[7] * d1 + K[8] * d2;
+        for (int g = 0; g < GRP; g++) q[g] = (j0 + g < L) ? __ldg(&d.sell_col[base + 32 * (j0 + g) + lane]) : row;
+        T y[GRP][3];
+#pragma unroll
+        for (int g = 0; g < GRP; g++) {
+            y[g][0] = __ldcg(&v[3 * (size_t)q[g]]);
+            y[g][1] = __ldcg(&v[3 * (size_t)q[g] + 1]);
+            y[g][2] = __ldcg(&v[3 * (size_t)q[g] + 2]);
         }
-    } else {
-        const T *mv = static_cast<const T *>(d.sell_mval);
-#pragma unroll 2
-        for (int j = 0; j < L; j++) {
-            const int off = base + 32 * j + lane;
-            const int q = __ldg(&d.sell_col[off]);
-            const T m = __ldg(&mv[off]);
-            a0 += m * __ldcg(&v[3 * (size_t)q]);
-            a1 += m * __ldcg(&v[3 * (size_t)q + 1]);
-            a2 += m * __ldcg(&v[3 * (size_t)q + 2]);
+#pragma unroll
+        for (int g = 0; g < GRP; g++) {
+            if (j0 + g >= L) break;
+            const int off = base + 32 * (j0 + g) + lane;
+            if (nomass) {
+                const size_t vb = (size_t)(base + 32 * (j0 + g)) * 9 + lane;
+                T K[9];
+#pragma unroll
+                for (int k = 0; k < 9; k++) K[k] = __ldg(&val[vb + 32 * k]);
+                const T d0 = y[g][0] - v0, d1 = y[g][1] - v1, d2 = y[g][2] - v2;
+                a0 += K[0] * d0 + K[1] * d1 + K[2] * d2;
+                a1 += K[3] * d0 + K[4] * d1 + K[5] * d2;
+                a2 += K[6] * d0 + K[7] * d1 + K[8] * d2;
+            } else {
+                const T m = __ldg(&mv[off]);
+                a0 += m * y[g][0];
+                a1 += m * y[g][1];
+                a2 += m * y[g][2];
+            }
         }
     }
     out[0] = a0;
     out[1] = a1;
     out[2] = a2;
+}
+
+// Standalone w = A u over every row of every blob, for timing SpMV variants:
+// TPR threads per row (slots j with j % TPR == sub), GROUPED = the grouped
+// loads of sell_row (TPR 1 only).  NoMass blobs only; other rows are skipped.
+template <typename T, int TPR, bool GROUPED>
+__global__ void __launch_bounds__(256) k_spmv_variant(DeviceBatch d, const T *__restrict__ v, T *__restrict__ out)
+{
+    const int lane = threadIdx.x & 31;
+    const int rows_per_warp = 32 / TPR;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int sub = lane / rows_per_warp;
+    const int row = gwarp * rows_per_warp + (lane % rows_per_warp);
+    if (row >= d.nl_pad) return;
+    const int b = d.tile_blob[row / NODE_TILE];
+    const BlobParams &bp = d.bp[b];
+    const bool valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED) && bp.solver == SOLVER_NOMASS;
+    T a[3] = {0, 0, 0};
+    if (valid) {
+        const T diag = (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0);
+        if (TPR == 1 && GROUPED) {
+            sell_row<T>(d, row, true, diag, v, a);
+        } else {
+            const int sl = row >> 5, rl = row & 31;
+            const int L = __ldg(&d.slice_len[sl]);
+            const int base = __ldg(&d.slice_ptr[sl]);
+            const T v0 = __ldcg(&v[3 * (size_t)row]), v1 = __ldcg(&v[3 * (size_t)row + 1]), v2 = __ldcg(&v[3 * (size_t)row + 2]);
+            if (sub == 0) {
+                a[0] = diag * v0;
+                a[1] = diag * v1;
+                a[2] = diag * v2;
+            }
+            const T *val = static_cast<const T *>(d.sell_val);
+#pragma unroll 2
+            for (int j = sub; j < L; j += TPR) {
+                const int off = base + 32 * j + rl;
+                const int q = __ldg(&d.sell_col[off]);
+                const size_t vb = (size_t)(base + 32 * j) * 9 + rl;
+                T K[9];
+#pragma unroll
+                for (int k = 0; k < 9; k++) K[k] = __ldg(&val[vb + 32 * k]);
+                const T d0 = __ldcg(&v[3 * (size_t)q]) - v0, d1 = __ldcg(&v[3 * (size_t)q + 1]) - v1,
+                        d2 = __ldcg(&v[3 * (size_t)q + 2]) - v2;
+                a[0] += K[0] * d0 + K[1] * d1 + K[2] * d2;
+                a[1] += K[3] * d0 + K[4] * d1 + K[5] * d2;
+                a[2] += K[6] * d0 + K[7] * d1 + K[8] * d2;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = rows_per_warp; o < 32; o <<= 1)
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) a[cc] += __shfl_xor_sync(0xffffffffu, a[cc], o);
+    if (sub == 0)
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) out[3 * (size_t)row + cc] = a[cc];
 }
 
 // b - A x for one row with FP64 products and accumulation (x is T).
@@ -633,278 +695,582 @@ __device__ __forceinline__ void true_residual_row(const DeviceBatch &d, int row,
     out[2] = d.rhs[3 * (size_t)row + 2] - a2;
 }
 
-// The whole solve of every blob: Chronopoulos-Gear PCG (one pair of
-// reductions per iteration), x0 = 0, stopping on sum r^2 / sum f^2 < eps^2
-// like residual2() (src/NoMassCGSolver.cpp:233-247).  With true_residual on,
-// a recursive convergence is confirmed by an FP64 b - A x; a failed check
-// restarts CG from that residual.  CTA c owns node tiles
-// [n_tiles*c/G, n_tiles*(c+1)/G); thread t owns row t of each of its tiles.
+// Per-row state of the CG recurrences (3 components each).
 template <typename T>
-__global__ void __launch_bounds__(CG_THREADS) k_cg(DeviceBatch d)
+struct RowState {
+    T x[3], r[3], u[3], w[3], s[3], p[3], dinv[3];
+};
+
+template <typename T>
+__device__ __forceinline__ void load_row(const DeviceBatch &d, int row, RowState<T> &S)
+{
+    const size_t o = 3 * (size_t)row;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        S.x[c] = static_cast<const T *>(d.x)[o + c];
+        S.r[c] = static_cast<const T *>(d.r)[o + c];
+        S.u[c] = static_cast<const T *>(d.u)[o + c];
+        S.w[c] = static_cast<const T *>(d.w)[o + c];
+        S.s[c] = static_cast<const T *>(d.s)[o + c];
+        S.p[c] = static_cast<const T *>(d.p)[o + c];
+        S.dinv[c] = static_cast<const T *>(d.dinv)[o + c];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void store_row(const DeviceBatch &d, int row, const RowState<T> &S)
+{
+    const size_t o = 3 * (size_t)row;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        static_cast<T *>(d.x)[o + c] = S.x[c];
+        static_cast<T *>(d.r)[o + c] = S.r[c];
+        static_cast<T *>(d.u)[o + c] = S.u[c];
+        static_cast<T *>(d.w)[o + c] = S.w[c];
+        static_cast<T *>(d.s)[o + c] = S.s[c];
+        static_cast<T *>(d.p)[o + c] = S.p[c];
+    }
+}
+
+// Double-float accumulation (Knuth's TwoSum, error-free in FP32): sums with
+// ~48-bit precision on the FP32 pipes, which on GB300 run many times faster
+// than FP64.
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF df_add(DF a, DF b)
+{
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float err = (a.hi - (s - bb)) + (b.hi - bb);
+    err += a.lo + b.lo;
+    const float hi = s + err;
+    return DF{hi, err - (hi - s)};
+}
+
+__device__ __forceinline__ DF df_warp_sum(DF v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        DF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+        v = df_add(v, w);
+    }
+    return v;
+}
+
+// Partial sums of a node tile: three quantities, each a (hi, lo) float pair,
+// in the 32 bytes of the tile's partials slot.  Per thread and per warp the
+// sums run in W; tid 0 adds the warp sums in FP64 and splits the result.
+template <typename W>
+__device__ __forceinline__ void tile_partials(double *part, int tile, const W (&in)[3], int mask, double *smem)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const W s = warp_sum<W>(in[k]);
+        if (lane == 0) smem[k * 32 + warp] = (double)s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float *P = reinterpret_cast<float *>(part) + 8 * (size_t)tile;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            if (!(mask & (1 << k))) continue;
+            double a = 0.0;
+            for (int w = 0; w < nw; w++) a += smem[k * 32 + w];
+            const float hi = (float)a;
+            P[2 * k] = hi;
+            P[2 * k + 1] = (float)(a - (double)hi);
+        }
+    }
+    __syncthreads();
+}
+
+// Loads of tile partials in flight per thread before they are added.
+constexpr int kSumUnroll = 4;
+
+// Adds the partials of tiles t0 + first, t0 + first + stride, ... (< tc) to
+// a[0..2] in that order; kSumUnroll loads are issued before the adds.
+__device__ __forceinline__ void add_tile_partials(const double *part, int t0, int tc, int first, int stride,
+                                                  DF a[3])
+{
+    for (int t = first; t < tc; t += kSumUnroll * stride) {
+        float4 v01[kSumUnroll];
+        float2 v2[kSumUnroll];
+#pragma unroll
+        for (int u = 0; u < kSumUnroll; u++) {
+            const int tt = t + u * stride;
+            if (tt < tc) {
+                v01[u] = __ldcg(reinterpret_cast<const float4 *>(part) + 2 * (size_t)(t0 + tt));
+                v2[u] = __ldcg(reinterpret_cast<const float2 *>(part) + 4 * (size_t)(t0 + tt) + 2);
+            } else {
+                v01[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                v2[u] = make_float2(0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kSumUnroll; u++) {
+            a[0] = df_add(a[0], DF{v01[u].x, v01[u].y});
+            a[1] = df_add(a[1], DF{v01[u].z, v01[u].w});
+            a[2] = df_add(a[2], DF{v2[u].x, v2[u].y});
+        }
+    }
+}
+
+// Sum of the three partial slots over a blob's node tiles, by the calling
+// warp (lane-strided, then a butterfly): fixed order, so deterministic.
+__device__ __forceinline__ void warp_blob_sums(const DeviceBatch &d, const double *part, int b, double out[3])
+{
+    DF a[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    add_tile_partials(part, d.bp[b].tile_off, d.bp[b].tile_cnt, threadIdx.x & 31, 32, a);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const DF s = df_warp_sum(a[k]);
+        out[k] = (double)s.hi + (double)s.lo;
+    }
+}
+
+// The same for one blob with the whole CTA (CG_THREADS = 8 warps): thread-
+// strided sums, a butterfly per warp, then warp 0 combines the 8 warp sums of
+// each quantity with a butterfly over lanes 8k .. 8k+7.  The result is valid
+// in warp 0 only (every lane of it); the caller synchronises before reusing sm.
+__device__ __forceinline__ void block_blob_sums(const DeviceBatch &d, const double *part, int b, double out[3],
+                                                float *sm)
+{
+    static_assert(CG_THREADS == 256, "block_blob_sums combines 8 warps");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    DF a[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    add_tile_partials(part, d.bp[b].tile_off, d.bp[b].tile_cnt, threadIdx.x, CG_THREADS, a);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const DF s = df_warp_sum(a[k]);
+        if (lane == 0) {
+            sm[2 * (k * 8 + warp)] = s.hi;
+            sm[2 * (k * 8 + warp) + 1] = s.lo;
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // lane 8k + w holds warp w's sum of quantity k (lanes 24..31 idle)
+        DF v = lane < 24 ? DF{sm[2 * lane], sm[2 * lane + 1]} : DF{0.f, 0.f};
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            const DF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+            v = df_add(v, w);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float hi = __shfl_sync(0xffffffffu, v.hi, 8 * k), lo = __shfl_sync(0xffffffffu, v.lo, 8 * k);
+            out[k] = (double)hi + (double)lo;
+        }
+    }
+}
+
+// One CG transition of a blob from its three sums:
+//   ACTIVE   sums r.u, w.u, r.r: stop test, then alpha / beta of the next update
+//   VERIFY   sums r.u, -, |b - A x|^2: converged, or restart from that residual
+//   RESTART  sums -, w.u, -: alpha of the first restarted update, beta = 0
+// Returns true when the blob stops (cg.state is then CONVERGED or FAILED) and
+// sets *fail_bits to the failure bits (0 if none).
+__device__ __forceinline__ bool transition_core(CgScalars &cg, const BlobParams &bp, const double sums[3],
+                                                int *fail_bits)
+{
+    const int limit = bp.solver == SOLVER_MASS ? bp.max_iter - 1 : bp.max_iter;
+    const double ff = cg.ff;
+    int finish = 0, bits = 0;
+    if (cg.state == CG_ACTIVE) {
+        const double g = sums[0], dl = sums[1], rr = sums[2];
+        cg.rr = rr;
+        const double res = (ff == 0.0) ? 0.0 : rr / ff;
+        if (cg.iters > 0 && res < bp.epsilon2) {
+            if (bp.true_residual) cg.state = CG_VERIFY;
+            else finish = CG_CONVERGED;
+        } else if (!(res == res) || !(g == g) || !(dl == dl)) {
+            finish = CG_FAILED;
+            bits = BLOB_FAIL_CG | BLOB_FAIL_NAN;
+        } else if (cg.iters >= limit) {
+            finish = CG_FAILED;
+            bits = BLOB_FAIL_CG;
+        } else {
+            if (cg.iters == 0) {
+                cg.beta = 0.0;
+                cg.alpha = g / dl;
+            } else {
+                const double beta = g / cg.gamma;
+                cg.alpha = g / (dl - beta * g / cg.alpha);
+                cg.beta = beta;
+            }
+            cg.gamma = g;
+            cg.iters += 1;
+        }
+    } else if (cg.state == CG_VERIFY) {
+        cg.true_relres2 = (ff == 0.0) ? 0.0 : sums[2] / ff;
+        if (cg.true_relres2 < bp.epsilon2) {
+            finish = CG_CONVERGED;
+        } else if (cg.restarts >= kMaxRestarts || cg.iters >= limit) {
+            finish = CG_FAILED;
+            bits = BLOB_FAIL_CG;
+        } else {
+            cg.restarts += 1;
+            cg.gamma = sums[0];
+            cg.state = CG_RESTART;
+        }
+    } else if (cg.state == CG_RESTART) {
+        cg.state = CG_ACTIVE;
+        cg.beta = 0.0;
+        cg.alpha = cg.gamma / sums[1];
+        cg.iters += 1;
+        if (!(cg.alpha == cg.alpha)) {
+            finish = CG_FAILED;
+            bits = BLOB_FAIL_CG | BLOB_FAIL_NAN;
+        }
+    }
+    if (finish) cg.state = finish;
+    *fail_bits = bits;
+    return finish != 0;
+}
+
+// The transition run by the CTA that arrived last at a reducing barrier
+// (exactly once per blob), on the blob's record in global memory.
+__device__ __forceinline__ void cg_transition(const DeviceBatch &d, int b, const double sums[3])
+{
+    // read through L2: the record may have been written by another SM's last CTA
+    CgScalars cg;
+    {
+        static_assert(sizeof(CgScalars) % 8 == 0, "CgScalars must be 8-byte words");
+        const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&d.cg[b]);
+        unsigned long long *dst = reinterpret_cast<unsigned long long *>(&cg);
+#pragma unroll
+        for (int i = 0; i < (int)(sizeof(CgScalars) / 8); i++) dst[i] = __ldcg(src + i);
+    }
+    int bits;
+    if (transition_core(cg, d.bp[b], sums, &bits)) {
+        atomicSub(&d.bar[2], 1u);
+        if (bits) atomicOr(&d.status[b], bits);
+    }
+    d.cg[b] = cg;
+}
+
+// Grid barrier whose last arriving CTA first reduces the partial sums of
+// every busy blob and runs its CG transition, then publishes the count of
+// blobs still iterating and releases the others.  Bounded waits as in
+// counting_barrier.
+__device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, int *s_err, unsigned int *s_pub,
+                                                         int *s_last, float *sm)
+{
+    unsigned int *bar = d.bar;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vb = bar;
+        s_last[1] = (int)vb[1];  // generation before arriving
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&bar[0], 1u);
+        s_last[0] = arrived == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last[0]) {
+        __threadfence();
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (d.num_blobs < 8) {
+            for (int b = 0; b < d.num_blobs; b++) {
+                const int st = __ldcg(&d.cg[b].state);
+                if (st == CG_CONVERGED || st == CG_FAILED) continue;
+                double sums[3];
+                block_blob_sums(d, d.partials, b, sums, sm);
+                if (threadIdx.x == 0) cg_transition(d, b, sums);
+                __syncthreads();  // sm reused by the next blob
+            }
+        } else {
+            for (int b = warp; b < d.num_blobs; b += blockDim.x >> 5) {
+                const int st = __ldcg(&d.cg[b].state);
+                if (st == CG_CONVERGED || st == CG_FAILED) continue;
+                double sums[3];
+                warp_blob_sums(d, d.partials, b, sums);
+                if (lane == 0) cg_transition(d, b, sums);
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            volatile unsigned int *vb = bar;
+            __threadfence();
+            vb[3] = vb[2];
+            vb[0] = 0;
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        }
+    } else if (threadIdx.x == 0) {
+        volatile unsigned int *vb = bar;
+        const unsigned int gen = (unsigned int)s_last[1];
+        unsigned int spins = 0;
+        while (vb[1] == gen) {
+            if (++spins > kSpinLimit || vb[4]) {
+                *s_err = 1;
+                atomicExch(&bar[4], 1u);
+                break;
+            }
+            __nanosleep(32);
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        *s_pub = ((volatile unsigned int *)bar)[3];
+    }
+    __syncthreads();
+    return *s_pub;
+}
+
+// Reduction without a serial step: after a plain grid barrier every CTA sums
+// the partials of every busy blob itself, in the same fixed order, and runs
+// the transitions on its own copy of the blob records in shared memory, so
+// all CTAs reach bit-identical states.  CTA 0 alone records failure bits.
+// Returns the number of blobs still iterating.
+__device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const double *part, CgScalars *s_cg,
+                                                     float *sm, unsigned int *s_run)
+{
+    const int nbl = d.num_blobs, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (nbl < 8) {
+        for (int b = 0; b < nbl; b++) {
+            const int st = s_cg[b].state;
+            if (st == CG_CONVERGED || st == CG_FAILED) continue;  // CTA-uniform
+            double sums[3];
+            block_blob_sums(d, part, b, sums, sm);
+            if (threadIdx.x == 0) {
+                int bits;
+                if (transition_core(s_cg[b], d.bp[b], sums, &bits) && bits && blockIdx.x == 0)
+                    atomicOr(&d.status[b], bits);
+            }
+            __syncthreads();  // s_cg[b] visible; sm reused by the next blob
+        }
+    } else {
+        for (int b = warp; b < nbl; b += blockDim.x >> 5) {
+            const int st = s_cg[b].state;
+            if (st == CG_CONVERGED || st == CG_FAILED) continue;  // warp-uniform
+            double sums[3];
+            warp_blob_sums(d, part, b, sums);
+            if (lane == 0) {
+                int bits;
+                if (transition_core(s_cg[b], d.bp[b], sums, &bits) && bits && blockIdx.x == 0)
+                    atomicOr(&d.status[b], bits);
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        unsigned int n = 0;
+        for (int b = 0; b < nbl; b++) n += !(s_cg[b].state == CG_CONVERGED || s_cg[b].state == CG_FAILED);
+        *s_run = n;
+    }
+    __syncthreads();
+    return *s_run;
+}
+
+// The whole solve of every blob in one cooperative launch: Jacobi-PCG in the
+// Chronopoulos-Gear form (one SpMV and one group of dot products per
+// iteration), x0 = 0, stopping on residual2() = sum r^2 / sum f^2 < eps^2
+// after each update (src/NoMassCGSolver.cpp:180-189, :233-247).  Per
+// iteration: phase A updates p, s, x, r and u = D^-1 r of the own rows; a
+// plain grid barrier makes u visible; phase B computes w = A u; then r.u, r.r
+// and w.u are summed per blob and each blob's CG state advances.  With few
+// tiles and blobs (cg_local) every CTA does that sum itself after a plain
+// barrier, from partials double-buffered by iteration parity (a fast CTA's
+// next phase A must not overwrite what a slow CTA is still summing); else a
+// reducing barrier does it once, in the last CTA to arrive.  With true_residual on, a recursive
+// convergence is confirmed by an FP64 b - A x and a failed check restarts the
+// recurrences from that residual.  CTA c owns node tiles
+// [n_tiles*c/G, n_tiles*(c+1)/G); thread t owns row t of each.  With one tile
+// per CTA (REG) the row state stays in registers for the whole solve; only u
+// and x go to memory, for the neighbours.
+template <typename T, bool REG>
+__global__ void __launch_bounds__(CG_THREADS, 4) k_cg(DeviceBatch d)
 {
     using W = T;
-    __shared__ double red[4 * 32];
-    __shared__ int s_nt, s_nb, s_err;
+    __shared__ double red[3 * 32];
+    __shared__ float sm_df[2 * 3 * 32];
+    __shared__ int s_nt, s_nb, s_err, s_last[2];
     __shared__ unsigned int s_pub;
     __shared__ int s_tslot[CG_MAX_TILES];
-    __shared__ int s_blob[CG_MAX_TILES], s_state[CG_MAX_TILES], s_iters[CG_MAX_TILES], s_restarts[CG_MAX_TILES];
-    __shared__ int s_owner[CG_MAX_TILES], s_limit[CG_MAX_TILES], s_tr[CG_MAX_TILES], s_nomass[CG_MAX_TILES];
-    __shared__ double s_alpha[CG_MAX_TILES], s_beta[CG_MAX_TILES], s_gamma[CG_MAX_TILES], s_ff[CG_MAX_TILES];
-    __shared__ double s_gnew[CG_MAX_TILES], s_eps2[CG_MAX_TILES], s_trr[CG_MAX_TILES], s_rr[CG_MAX_TILES];
-    __shared__ double s_sum[2][CG_MAX_TILES];
+    __shared__ int s_blob[CG_MAX_TILES], s_state[CG_MAX_TILES];
+    __shared__ double s_alpha[CG_MAX_TILES], s_beta[CG_MAX_TILES];
+    __shared__ CgScalars s_cg[CG_LOCAL_MAX_BLOBS];
+    __shared__ unsigned int s_run;
 
     const int G = gridDim.x, c = blockIdx.x, tid = threadIdx.x;
+    const bool local = d.cg_local;
     const int T0 = (int)(((long long)d.n_tiles * c) / G), T1 = (int)(((long long)d.n_tiles * (c + 1)) / G);
     if (tid == 0) {
         s_err = 0;
         int nb = 0;
         for (int j = 0; j < T1 - T0; j++) {
             const int b = d.tile_blob[T0 + j];
-            if (nb == 0 || s_blob[nb - 1] != b) {
-                const CgScalars cg = d.cg[b];
-                const BlobParams &bp = d.bp[b];
-                s_blob[nb] = b;
-                s_state[nb] = cg.state;
-                s_gamma[nb] = cg.gamma;
-                s_ff[nb] = cg.ff;
-                s_alpha[nb] = s_beta[nb] = 0.0;
-                s_iters[nb] = 0;
-                s_restarts[nb] = 0;
-                s_trr[nb] = -1.0;
-                s_rr[nb] = 0.0;
-                s_owner[nb] = bp.tile_off == T0 + j;
-                s_limit[nb] = bp.solver == SOLVER_MASS ? bp.max_iter - 1 : bp.max_iter;
-                s_tr[nb] = bp.true_residual;
-                s_nomass[nb] = bp.solver == SOLVER_NOMASS;
-                s_eps2[nb] = bp.epsilon2;
-                nb++;
-            }
+            if (nb == 0 || s_blob[nb - 1] != b) s_blob[nb++] = b;
             s_tslot[j] = nb - 1;
         }
         s_nt = T1 - T0;
         s_nb = nb;
     }
+    if (local)
+        for (int b = tid; b < d.num_blobs; b += CG_THREADS) s_cg[b] = d.cg[b];
     __syncthreads();
     const int nt = s_nt, nb = s_nb;
-    T *x = static_cast<T *>(d.x), *r = static_cast<T *>(d.r), *u = static_cast<T *>(d.u);
-    T *w = static_cast<T *>(d.w), *p = static_cast<T *>(d.p), *sv = static_cast<T *>(d.s);
-    const T *dinv = static_cast<const T *>(d.dinv);
-
-    // per-blob fixed-order sums of two partial slots; one warp per distinct
-    // blob, 8 loads per lane in flight per pass (the partials live in L2)
-    auto reduce2 = [&](int slot0) {
-        const int lane = tid & 31, warp = tid >> 5;
-        for (int k = warp; k < nb; k += CG_THREADS / 32) {
-            const int b = s_blob[k];
-            const int t0 = d.bp[b].tile_off, tc = d.bp[b].tile_cnt;
-            double a0 = 0.0, a1 = 0.0;
-            for (int base = 0; base < tc; base += 8 * 32) {
-                double v0[8], v1[8];
-#pragma unroll
-                for (int q = 0; q < 8; q++) {
-                    const int t = base + 32 * q + lane;
-                    const double2 pv = t < tc ? __ldcg(reinterpret_cast<const double2 *>(
-                                                    &d.partials[4 * (size_t)(t0 + t) + slot0]))
-                                              : make_double2(0.0, 0.0);
-                    v0[q] = pv.x;
-                    v1[q] = pv.y;
-                }
-#pragma unroll
-                for (int q = 0; q < 8; q++) {
-                    a0 += v0[q];
-                    a1 += v1[q];
-                }
-            }
-            a0 = warp_sum<double>(a0);
-            a1 = warp_sum<double>(a1);
-            if (lane == 0) {
-                s_sum[0][k] = a0;
-                s_sum[1][k] = a1;
-            }
-        }
-        __syncthreads();
-    };
-    auto finish_blob = [&](int k, int state, int bits) {
-        s_state[k] = state;
-        if (s_owner[k]) {
-            atomicSub(&d.bar[2], 1u);
-            if (bits) atomicOr(&d.status[s_blob[k]], bits);
-        }
-    };
-    // SpMV phase for ACTIVE / RESTART blobs: w = A u, partial delta = w . u  -> slot 2;
-    // VERIFY blobs: r = b - A x (FP64), u = D^-1 r, partials r.r -> slot 2, r.u -> slot 3
-    auto spmv_phase = [&]() {
-        for (int j = 0; j < nt; j++) {
-            const int t = T0 + j, k = s_tslot[j], st = s_state[k];
-            const int row = t * NODE_TILE + tid;
-            const BlobParams &bp = d.bp[s_blob[k]];
-            const bool valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
-            W wd = 0, wg = 0;
-            double vd = 0.0, vg = 0.0;
-            if ((st == CG_ACTIVE || st == CG_RESTART) && valid) {
-                const T diag = s_nomass[k] ? (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0)
-                                           : static_cast<const T *>(d.mass_diag)[row];
-                T q[3];
-                sell_row<T>(d, row, s_nomass[k], diag, u, q);
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    w[3 * (size_t)row + i] = q[i];
-                    wd += q[i] * __ldcg(&u[3 * (size_t)row + i]);
-                }
-            } else if (st == CG_VERIFY && valid) {
-                const double diag = s_nomass[k] ? (bp.calc_stokes == 1 ? d.drag[row] : 0.0)
-                                                : (double)static_cast<const T *>(d.mass_diag)[row];
-                double rt[3];
-                true_residual_row<T>(d, row, s_nomass[k], diag, x, rt);
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    const size_t kk = 3 * (size_t)row + i;
-                    const T ri = (T)rt[i];
-                    const T ui = dinv[kk] * ri;
-                    r[kk] = ri;
-                    u[kk] = ui;
-                    vd += rt[i] * rt[i];
-                    vg += (double)ri * (double)ui;
-                }
-            }
-            double out[2];
-            if (st == CG_VERIFY) {
-                const double in[2] = {vd, vg};
-                block_sum<2, double>(in, out, red);
+    // the CG state of this CTA's blobs: its own records (local) or as
+    // published by the last reducing barrier
+    auto refresh = [&]() {
+        for (int k = tid; k < nb; k += CG_THREADS) {
+            if (local) {
+                const CgScalars &cg = s_cg[s_blob[k]];
+                s_state[k] = cg.state;
+                s_alpha[k] = cg.alpha;
+                s_beta[k] = cg.beta;
             } else {
-                const W in[2] = {wd, wg};
-                block_sum<2, W>(in, out, red);
+                const CgScalars *cg = &d.cg[s_blob[k]];
+                s_state[k] = __ldcg(&cg->state);
+                s_alpha[k] = __ldcg(&cg->alpha);
+                s_beta[k] = __ldcg(&cg->beta);
             }
-            if (tid == 0) {
-                d.partials[4 * (size_t)t + 2] = out[0];
-                d.partials[4 * (size_t)t + 3] = out[1];
+        }
+        __syncthreads();
+    };
+    // partials buffer of the current iteration
+    int parity = 0;
+    auto part = [&]() { return d.partials + (size_t)parity * 4 * d.n_tiles; };
+    refresh();
+    T *X = static_cast<T *>(d.x), *U = static_cast<T *>(d.u);
+
+    // per-thread constants of the row in REG mode (the CTA's only tile)
+    RowState<T> reg;
+    bool reg_valid = false;
+    T reg_diag = 0;
+    if (REG) {
+        const int row = T0 * NODE_TILE + tid;
+        const BlobParams &bp = d.bp[s_blob[0]];
+        reg_valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
+        reg_diag = bp.solver == SOLVER_NOMASS ? (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0)
+                                              : static_cast<const T *>(d.mass_diag)[row];
+        load_row<T>(d, row, reg);
+    }
+    auto row_info = [&](int j, int row, bool &valid, T &diag, bool &nomass) {
+        const BlobParams &bp = d.bp[s_blob[s_tslot[j]]];
+        nomass = bp.solver == SOLVER_NOMASS;
+        if (REG) {
+            valid = reg_valid;
+            diag = reg_diag;
+        } else {
+            valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
+            diag = nomass ? (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0) : static_cast<const T *>(d.mass_diag)[row];
+        }
+    };
+    // phase A of tile j: p = u + beta p; s = w + beta s; x += alpha p;
+    // r -= alpha s; u = D^-1 r.  Partials: slot 0 r.u, slot 2 r.r.
+    auto phase_a = [&](int j) {
+        const int t = T0 + j, k = s_tslot[j];
+        if (s_state[k] != CG_ACTIVE) return;  // CTA-uniform
+        const int row = t * NODE_TILE + tid;
+        bool valid, nomass;
+        T diag;
+        row_info(j, row, valid, diag, nomass);
+        W pg = 0, pr = 0;
+        RowState<T> loc;
+        RowState<T> &S = REG ? reg : loc;
+        if (!REG && valid) load_row<T>(d, row, loc);
+        if (valid) {
+            const T a = (T)s_alpha[k], b = (T)s_beta[k];
+            const bool first = s_beta[k] == 0.0;
+            const size_t o = 3 * (size_t)row;
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) {
+                S.p[cc] = first ? S.u[cc] : S.u[cc] + b * S.p[cc];
+                S.s[cc] = first ? S.w[cc] : S.w[cc] + b * S.s[cc];
+                S.x[cc] += a * S.p[cc];
+                S.r[cc] -= a * S.s[cc];
+                S.u[cc] = S.dinv[cc] * S.r[cc];
+                U[o + cc] = S.u[cc];
+                X[o + cc] = S.x[cc];
+                pg += S.r[cc] * S.u[cc];
+                pr += S.r[cc] * S.r[cc];
             }
+        }
+        if (!REG && valid) store_row<T>(d, row, loc);
+        const W in[3] = {pg, (W)0, pr};
+        tile_partials<W>(part(), t, in, 5, red);
+    };
+    // phase B of tile j: ACTIVE / RESTART and the prologue: w = A u, slot 1
+    // w.u (the prologue and RESTART also fill slots 0 and 2); VERIFY: the
+    // FP64 b - A x becomes the new residual, slot 0 r.u, slot 2 |b - A x|^2.
+    auto phase_b = [&](int j, bool prologue) {
+        const int t = T0 + j, k = s_tslot[j], state = s_state[k];
+        if (!(state == CG_ACTIVE || state == CG_VERIFY || state == CG_RESTART)) return;  // CTA-uniform
+        const int row = t * NODE_TILE + tid;
+        bool valid, nomass;
+        T diag;
+        row_info(j, row, valid, diag, nomass);
+        W pg = 0, pd = 0, pr = 0;
+        double vr = 0.0, vg = 0.0;
+        RowState<T> loc;
+        RowState<T> &S = REG ? reg : loc;
+        if (!REG && valid) load_row<T>(d, row, loc);
+        if (valid) {
+            const size_t o = 3 * (size_t)row;
+            if (state != CG_VERIFY) {
+                T au[3];
+                sell_row<T>(d, row, nomass, diag, U, au);
+#pragma unroll
+                for (int cc = 0; cc < 3; cc++) {
+                    S.w[cc] = au[cc];
+                    pd += au[cc] * S.u[cc];
+                    pg += S.r[cc] * S.u[cc];
+                    pr += S.r[cc] * S.r[cc];
+                }
+            } else {
+                double rt[3];
+                true_residual_row<T>(d, row, nomass, (double)diag, X, rt);
+#pragma unroll
+                for (int cc = 0; cc < 3; cc++) {
+                    S.r[cc] = (T)rt[cc];
+                    S.u[cc] = S.dinv[cc] * S.r[cc];
+                    U[o + cc] = S.u[cc];
+                    vr += rt[cc] * rt[cc];
+                    vg += (double)S.r[cc] * (double)S.u[cc];
+                }
+            }
+        }
+        if (!REG && valid) store_row<T>(d, row, loc);
+        if (state == CG_VERIFY) {
+            const double in[3] = {vg, 0.0, vr};
+            tile_partials<double>(part(), t, in, 5, red);
+        } else {
+            const W in[3] = {pg, pd, pr};
+            tile_partials<W>(part(), t, in, (prologue || state == CG_RESTART) ? 7 : 2, red);
         }
     };
 
-    // prologue: w0 = A u0, delta0, alpha0 = gamma0 / delta0
-    spmv_phase();
-    unsigned int running = grid_barrier(d.bar, &s_err, &s_pub);
+    unsigned int n_bar = 0;  // counting barriers passed
+    // sums of the iteration's partials and the transitions; the running-blob count
+    auto reduce = [&]() -> unsigned int {
+        if (!local) return reducing_barrier(d, &s_err, &s_pub, s_last, sm_df);
+        counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
+        if (s_err) return 0u;
+        return local_reduce(d, part(), s_cg, sm_df, &s_run);
+    };
+    for (int j = 0; j < nt; j++) phase_b(j, true);
+    unsigned int running = reduce();
     long long loops = 0;
-    if (!s_err) {
-        reduce2(2);
-        if (tid == 0)
-            for (int k = 0; k < nb; k++)
-                if (s_state[k] == CG_ACTIVE) {
-                    s_alpha[k] = s_gamma[k] / s_sum[0][k];
-                    s_beta[k] = 0.0;
-                }
-        __syncthreads();
-    }
     while (!s_err && running > 0) {
-        // phase A: p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = D^-1 r
-        for (int j = 0; j < nt; j++) {
-            const int t = T0 + j, k = s_tslot[j];
-            const int row = t * NODE_TILE + tid;
-            W gam = 0, rr = 0;
-            if (s_state[k] == CG_ACTIVE) {
-                const T alpha = (T)s_alpha[k], beta = (T)s_beta[k];
-                const bool first = s_beta[k] == 0.0;
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    const size_t kk = 3 * (size_t)row + i;
-                    const T ui = u[kk], wi = w[kk];
-                    const T pi = first ? ui : ui + beta * p[kk];
-                    const T si = first ? wi : wi + beta * sv[kk];
-                    p[kk] = pi;
-                    sv[kk] = si;
-                    x[kk] += alpha * pi;
-                    const T ri = r[kk] - alpha * si;
-                    r[kk] = ri;
-                    const T un = dinv[kk] * ri;
-                    u[kk] = un;
-                    gam += ri * un;
-                    rr += ri * ri;
-                }
-            }
-            const W in[2] = {gam, rr};
-            double out[2];
-            block_sum<2, W>(in, out, red);
-            if (tid == 0) {
-                d.partials[4 * (size_t)t] = out[0];
-                d.partials[4 * (size_t)t + 1] = out[1];
-            }
-        }
-        loops++;
-        running = grid_barrier(d.bar, &s_err, &s_pub);
-        if (s_err || running == 0) break;
-        reduce2(0);
-        if (tid == 0) {
-            for (int k = 0; k < nb; k++) {
-                if (s_state[k] != CG_ACTIVE) continue;
-                s_iters[k] += 1;
-                const double rr = s_sum[1][k];
-                s_rr[k] = rr;
-                s_gnew[k] = s_sum[0][k];
-                const double res = (s_ff[k] == 0.0) ? 0.0 : rr / s_ff[k];
-                if (res < s_eps2[k]) {
-                    if (s_tr[k]) s_state[k] = CG_VERIFY;
-                    else finish_blob(k, CG_CONVERGED, 0);
-                } else if (!(res == res)) {
-                    finish_blob(k, CG_FAILED, BLOB_FAIL_CG | BLOB_FAIL_NAN);
-                } else if (s_iters[k] >= s_limit[k]) {
-                    finish_blob(k, CG_FAILED, BLOB_FAIL_CG);
-                }
-            }
-        }
-        __syncthreads();
-        // phase B: w = A u (or the FP64 true residual for blobs being verified)
-        spmv_phase();
-        running = grid_barrier(d.bar, &s_err, &s_pub);
+        if (local) parity ^= 1;
+        refresh();
+        for (int j = 0; j < nt; j++) phase_a(j);
+        counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) break;
-        reduce2(2);
-        if (tid == 0) {
-            for (int k = 0; k < nb; k++) {
-                const int st = s_state[k];
-                if (st == CG_ACTIVE) {
-                    const double gnew = s_gnew[k], delta = s_sum[0][k];
-                    const double beta = gnew / s_gamma[k];
-                    s_alpha[k] = gnew / (delta - beta * gnew / s_alpha[k]);
-                    s_beta[k] = beta;
-                    s_gamma[k] = gnew;
-                } else if (st == CG_RESTART) {
-                    s_alpha[k] = s_gamma[k] / s_sum[0][k];
-                    s_beta[k] = 0.0;
-                    s_state[k] = CG_ACTIVE;
-                } else if (st == CG_VERIFY) {
-                    const double trr = s_sum[0][k];
-                    s_trr[k] = (s_ff[k] == 0.0) ? 0.0 : trr / s_ff[k];
-                    if (s_trr[k] < s_eps2[k]) {
-                        finish_blob(k, CG_CONVERGED, 0);
-                    } else if (s_restarts[k] >= kMaxRestarts || s_iters[k] >= s_limit[k]) {
-                        finish_blob(k, CG_FAILED, BLOB_FAIL_CG);
-                    } else {
-                        s_restarts[k] += 1;
-                        s_gamma[k] = s_sum[1][k];
-                        s_state[k] = CG_RESTART;
-                    }
-                }
-            }
-        }
-        __syncthreads();
-        if (running == 0) break;
+        for (int j = 0; j < nt; j++) phase_b(j, false);
+        loops++;
+        running = reduce();
     }
+    if (local && c == 0)
+        for (int b = tid; b < d.num_blobs; b += CG_THREADS) d.cg[b] = s_cg[b];
     if (tid == 0) {
-        if (s_err) {
+        if (s_err)
             for (int k = 0; k < nb; k++) atomicOr(&d.status[s_blob[k]], BLOB_FAIL_CG | BLOB_FAIL_TIMEOUT);
-        }
-        for (int k = 0; k < nb; k++) {
-            if (!s_owner[k]) continue;
-            CgScalars &cg = d.cg[s_blob[k]];
-            cg.state = s_state[k];
-            cg.iters = s_iters[k];
-            cg.restarts = s_restarts[k];
-            cg.alpha = s_alpha[k];
-            cg.beta = s_beta[k];
-            cg.gamma = s_gamma[k];
-            cg.rr = s_rr[k];
-            cg.true_relres2 = s_trr[k];
-        }
         if (c == 0) *d.loop_count += (unsigned long long)loops;
     }
 }
@@ -1119,14 +1485,18 @@ void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs)
     PREC_DISPATCH(d, k_nodes, d.n_tiles, NODE_TILE, s, d, use_given_rhs);
 }
 
-int cg_max_grid(int precision)
+int cg_max_grid(int precision, int reg)
 {
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    cudaError_t e = precision == PREC_FP64
-                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double>, CG_THREADS, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float>, CG_THREADS, 0);
+    cudaError_t e;
+    if (precision == PREC_FP64)
+        e = reg ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double, true>, CG_THREADS, 0)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double, false>, CG_THREADS, 0);
+    else
+        e = reg ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float, true>, CG_THREADS, 0)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float, false>, CG_THREADS, 0);
     if (e != cudaSuccess) return 0;
     return sms * per_sm;
 }
@@ -1144,8 +1514,9 @@ cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s)
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     FFEA_LAUNCHED();
-    if (d.precision == PREC_FP64) return cudaLaunchKernelEx(&cfg, k_cg<double>, d);
-    return cudaLaunchKernelEx(&cfg, k_cg<float>, d);
+    if (d.precision == PREC_FP64)
+        return d.cg_reg ? cudaLaunchKernelEx(&cfg, k_cg<double, true>, d) : cudaLaunchKernelEx(&cfg, k_cg<double, false>, d);
+    return d.cg_reg ? cudaLaunchKernelEx(&cfg, k_cg<float, true>, d) : cudaLaunchKernelEx(&cfg, k_cg<float, false>, d);
 }
 
 void launch_euler(const DeviceBatch &d, cudaStream_t s)
@@ -1156,6 +1527,27 @@ void launch_euler(const DeviceBatch &d, cudaStream_t s)
 void launch_energies(const DeviceBatch &d, cudaStream_t s)
 {
     PREC_DISPATCH(d, k_energies, d.n_etiles, ELEM_TILE, s, d);
+}
+
+template <typename T>
+static void spmv_variant_dispatch(const DeviceBatch &d, cudaStream_t s, int variant)
+{
+    const T *v = static_cast<const T *>(d.u);
+    T *o = static_cast<T *>(d.w);
+    const int64_t rows = d.nl_pad;
+    switch (variant) {
+    case 0: k_spmv_variant<T, 1, true><<<blocks_for(rows, 256), 256, 0, s>>>(d, v, o); break;
+    case 1: k_spmv_variant<T, 1, false><<<blocks_for(rows, 256), 256, 0, s>>>(d, v, o); break;
+    case 2: k_spmv_variant<T, 2, false><<<blocks_for(rows * 2, 256), 256, 0, s>>>(d, v, o); break;
+    default: k_spmv_variant<T, 4, false><<<blocks_for(rows * 4, 256), 256, 0, s>>>(d, v, o); break;
+    }
+    FFEA_LAUNCHED();
+}
+
+void launch_spmv_variant(const DeviceBatch &d, cudaStream_t s, int variant)
+{
+    if (d.precision == PREC_FP64) spmv_variant_dispatch<double>(d, s, variant);
+    else spmv_variant_dispatch<float>(d, s, variant);
 }
 
 void launch_apply(const DeviceBatch &d, cudaStream_t s, const double *in, double *out)

@@ -15,6 +15,8 @@ struct DeviceBatch {
     int32_t precision = PREC_MIXED;
     int32_t any_mass = 0, any_nomass = 0;
     int32_t cg_grid = 0;          // CTAs of the persistent CG kernel
+    int32_t cg_reg = 0;           // 1: one node tile per CTA, CG state kept in registers
+    int32_t cg_local = 0;         // 1: every CTA reduces the dot products itself (few tiles and blobs)
     // blobs
     BlobParams *bp = nullptr;
     Material *mats = nullptr;
@@ -30,9 +32,12 @@ struct DeviceBatch {
     int32_t *gather_ptr = nullptr, *gather_idx = nullptr;
     int32_t *fold_ptr = nullptr, *fold_sec = nullptr;
     double *fold_drag = nullptr;
-    // CG vectors, T-typed, 3 per padded node: solution x, residual r,
-    // preconditioned residual u, w = A u, directions p and s = A p, Jacobi dinv
+    // CG vectors, T-typed, 3 per padded node (pipelined PCG): solution x,
+    // residual r, u = D^-1 r, w = A u, m = D^-1 w, and the recurrences
+    // z, q, s, p; Jacobi dinv
     void *x = nullptr, *r = nullptr, *u = nullptr, *w = nullptr, *p = nullptr, *s = nullptr, *dinv = nullptr;
+    void *m = nullptr, *z = nullptr, *q = nullptr;
+    void *m2 = nullptr;           // second buffer of m: iteration i reads m[i&1] and writes m[(i+1)&1]
     // elements
     int32_t *conn = nullptr;
     uint16_t *mat_id = nullptr;
@@ -46,7 +51,7 @@ struct DeviceBatch {
     void *sell_mval = nullptr;    // mass matrix: 1 T per entry
     void *mass_diag = nullptr;    // T per node
     // reductions / status
-    double *partials = nullptr;     // 4 per node tile
+    double *partials = nullptr;     // 8 per node tile: two buffers of 4, alternating between CG iterations
     CgScalars *cg = nullptr;        // per blob
     unsigned int *counters = nullptr;  // one per reduction site
     unsigned int *bar = nullptr;    // grid barrier: arrival count, generation
@@ -65,6 +70,8 @@ enum ElemMode { ELEM_STEP = 0, ELEM_MATRIX_ONLY = 1 };
 
 constexpr int CG_THREADS = NODE_TILE;   // one row per thread and tile
 constexpr int CG_MAX_TILES = 64;        // node tiles per CTA of the persistent kernel
+constexpr int CG_LOCAL_MAX_BLOBS = 64;  // local reduction: blob records kept in shared memory
+constexpr int CG_LOCAL_MAX_TILES = 4096;  // local reduction: partial sums every CTA reads per iteration
 
 // Launchers (all asynchronous on `s`).
 void launch_rest_state(const DeviceBatch &d, cudaStream_t s);
@@ -76,10 +83,13 @@ cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s);
 void launch_euler(const DeviceBatch &d, cudaStream_t s);
 void launch_energies(const DeviceBatch &d, cudaStream_t s);
 void launch_apply(const DeviceBatch &d, cudaStream_t s, const double *in, double *out);
+// standalone w = A u with one of the SpMV variants (0..3), for timing
+void launch_spmv_variant(const DeviceBatch &d, cudaStream_t s, int variant);
 void launch_rng_draws(const mrg::JumpMat *table, const uint32_t *state, uint64_t offset, int64_t count, double *out,
                       cudaStream_t s);
-// CTAs of the persistent CG kernel that fit co-resident on the current device
-int cg_max_grid(int precision);
+// CTAs of the persistent CG kernel (register-resident variant or not) that fit
+// co-resident on the current device
+int cg_max_grid(int precision, int reg);
 
 int64_t kernel_launch_count();
 void count_launches(int64_t n);

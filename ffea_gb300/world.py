@@ -133,6 +133,12 @@ class World:
     def cg_loop_count(self) -> int:
         return int(L.lib().ffea_gpu_cg_loop_count(self._h))
 
+    def diag_spmv(self, variant: int, reps: int = 50) -> float:
+        """Microseconds per standalone SpMV of the current matrix (variant 0..3)."""
+        us = ctypes.c_double()
+        L.check(L.lib().ffea_gpu_diag_spmv(self._h, int(variant), int(reps), ctypes.byref(us)), "diag_spmv")
+        return us.value
+
     def set_timing(self, on: bool):
         L.check(L.lib().ffea_gpu_set_timing(self._h, 1 if on else 0))
 

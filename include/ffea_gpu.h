@@ -182,6 +182,13 @@ int ffea_gpu_energies_noalloc(const double *pos, const double *vel, const int32_
 /* Copies the last error message of the calling thread (NUL-terminated). */
 int ffea_gpu_last_error(char *buf, size_t len);
 
+/* Average time (microseconds) of one standalone w = A u over every row of
+ * the handle's last assembled viscosity matrix, for SpMV variant 0..3
+ * (0: one thread per row with grouped loads, 1: one thread per row,
+ * 2: two threads per row, 3: four threads per row).  Overwrites the solver's
+ * scratch vector w. */
+int ffea_gpu_diag_spmv(ffea_gpu_t *h, int32_t variant, int32_t reps, double *us_per_spmv);
+
 /* Number of kernel launches the library issued so far (all handles). */
 int64_t ffea_gpu_kernel_launches(void);
 

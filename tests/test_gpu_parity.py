@@ -122,3 +122,52 @@ def test_deterministic_and_graph_equals_host_loop(gpulib):
     for o in outs[1:]:
         for a, c in zip(outs[0], o):
             assert np.array_equal(a, c)
+
+
+def test_register_and_memory_cg_state_agree(gpulib, monkeypatch):
+    """The persistent solver keeps per-row CG state in registers when every
+    node tile has a CTA; the memory-resident variant (used for larger meshes)
+    must give the same iterates."""
+    s = spec(radius_nm=4.0, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    outs = []
+    for mem in ("0", "1"):
+        monkeypatch.setenv("FFEA_GPU_CG_MEMORY_STATE", mem)
+        with _world([s], true_residual=True) as w:
+            w.run(3)
+            outs.append(w.blob(0).get_nodes())
+            st = w.blob(0).status()
+            assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6
+    for a, c in zip(outs[0], outs[1]):
+        assert np.array_equal(a, c)
+
+
+@pytest.mark.parametrize("num_blobs", [1, 9])
+def test_local_and_last_arriver_reduction_agree(gpulib, monkeypatch, num_blobs):
+    """The CG sums are reduced either redundantly by every CTA (few tiles and
+    blobs) or once by the last CTA at a barrier; both sum the same partials
+    in the same order (a CTA per blob below 8 blobs, a warp per blob from 8),
+    so the iterates must be bit-identical."""
+    specs = [spec(radius_nm=2.5 + 0.25 * i, seed=i, rng_seed=60 + i, precision=P.PRECISION_MIXED, epsilon=1e-6)
+             for i in range(num_blobs)]
+    outs = []
+    for last in ("0", "1"):
+        monkeypatch.setenv("FFEA_GPU_CG_LAST_ARRIVER", last)
+        with _world(specs, true_residual=True) as w:
+            w.run(3)
+            outs.append([w.blob(i).get_nodes() for i in range(num_blobs)])
+            for i in range(num_blobs):
+                st = w.blob(i).status()
+                assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (i, st)
+    for i in range(num_blobs):
+        for a, c in zip(outs[0][i], outs[1][i]):
+            assert np.array_equal(a, c), i
+
+
+def test_true_residual_confirms_convergence(gpulib, oracle):
+    s = spec(radius_nm=4.0, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    with _world([s], true_residual=True) as w:
+        for _ in range(5):
+            w.run(1)
+            st = w.blob(0).status()
+            assert st["fail_bits"] == 0
+            assert st["true_relres"] < 1e-6, st
