@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdlib>
+#include <limits>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -195,6 +196,28 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     HostBatch &H = h->host;
     DeviceBatch &d = h->dev;
     DeviceArena &A = h->arena;
+    // persistent CG kernel: all CTAs co-resident (cooperative launch); the
+    // register-resident variant when every CG segment gets a CTA of its own.
+    // FFEA_GPU_CG_MAX_CTAS caps the grid, FFEA_GPU_CG_MEMORY_STATE=1 keeps the
+    // segments but runs the memory-resident variant (both for tests).
+    const int reg_grid = cg_max_grid(H.precision, 1);
+    const int max_grid = cg_max_grid(H.precision, 0);
+    if (reg_grid <= 0 || max_grid <= 0) return fail("cannot size the persistent CG kernel on this device");
+    int cap = std::numeric_limits<int>::max();
+    if (const char *e = std::getenv("FFEA_GPU_CG_MAX_CTAS")) cap = std::max(1, std::atoi(e));
+    const int reg_cap = std::min(reg_grid, cap), mem_cap = std::min(max_grid, cap);
+    const int32_t n_segs = plan_cg_segments(H, reg_cap, CG_THREADS);
+    const char *force_mem = std::getenv("FFEA_GPU_CG_MEMORY_STATE");
+    d.n_segs = n_segs;
+    d.cg_reg = n_segs <= reg_cap && !(force_mem && force_mem[0] == '1');
+    d.cg_grid = n_segs <= reg_cap ? n_segs : std::min(mem_cap, n_segs);
+    if ((int64_t)d.cg_grid * CG_MAX_SEGS < n_segs)
+        return fail("batch too large: %d CG segments need more than %d co-resident CTAs", n_segs, mem_cap);
+    // local reduction (every CTA sums all partials, no serial last-arriver
+    // step) while that read stays small
+    const char *force_last = std::getenv("FFEA_GPU_CG_LAST_ARRIVER");
+    d.cg_local = H.num_blobs <= CG_LOCAL_MAX_BLOBS && n_segs <= CG_LOCAL_MAX_SEGS &&
+                 !(force_last && force_last[0] == '1');
     d.num_blobs = H.num_blobs;
     d.nl_pad = H.nl_pad;
     d.ne_pad = H.ne_pad;
@@ -210,6 +233,9 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(upload(A, d.bp, H.bp));
     CK(upload(A, d.mats, H.materials));
     CK(upload(A, d.tile_blob, H.tile_blob));
+    CK(upload(A, d.seg_row0, H.seg_row0));
+    CK(upload(A, d.seg_rows, H.seg_rows));
+    CK(upload(A, d.seg_blob, H.seg_blob));
     CK(upload(A, d.etile_blob, H.etile_blob));
     std::vector<mrg::JumpMat> table(mrg::JUMP_TABLE_ENTRIES);
     mrg::build_jump_table(table.data());
@@ -251,7 +277,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(A.alloc_bytes(d.sell_val, H.any_nomass ? 9 * (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.sell_mval, H.any_mass ? (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.mass_diag, H.any_mass ? (size_t)H.nl_pad * ts : 16));
-    CK(A.alloc(d.partials, 8 * (size_t)H.n_tiles));
+    CK(A.alloc(d.partials, std::max(4 * (size_t)H.n_tiles, 8 * (size_t)n_segs)));
     CK(A.alloc(d.epartials, 2 * (size_t)H.n_etiles));
     CK(A.alloc(d.cg, (size_t)H.num_blobs));
     CK(A.alloc(d.counters, (size_t)CNT_COUNT));
@@ -272,26 +298,6 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
                 if (H.maps[b].lin_of_orig[n] < 0)
                     for (int c = 0; c < 3; c++) h->sec_vel[b][3 * (size_t)n + c] = m.vel[3 * (size_t)n + c];
     }
-    // persistent CG kernel: all CTAs co-resident, at most CG_MAX_TILES node tiles each
-    // register-resident variant when every node tile gets a CTA of its own
-    const int reg_grid = cg_max_grid(d.precision, 1);
-    const int max_grid = cg_max_grid(d.precision, 0);
-    if (max_grid <= 0) return fail("cannot size the persistent CG kernel on this device");
-    const char *force_mem = std::getenv("FFEA_GPU_CG_MEMORY_STATE");
-    if (reg_grid >= d.n_tiles && !(force_mem && force_mem[0] == '1')) {
-        d.cg_reg = 1;
-        d.cg_grid = d.n_tiles;
-    } else {
-        d.cg_reg = 0;
-        d.cg_grid = std::min(max_grid, d.n_tiles);
-    }
-    // local reduction (every CTA sums all partials, no serial last-arriver
-    // step) while that read stays small
-    const char *force_last = std::getenv("FFEA_GPU_CG_LAST_ARRIVER");
-    d.cg_local = d.num_blobs <= CG_LOCAL_MAX_BLOBS && d.n_tiles <= CG_LOCAL_MAX_TILES &&
-                 !(force_last && force_last[0] == '1');
-    if ((int64_t)d.cg_grid * CG_MAX_TILES < d.n_tiles)
-        return fail("batch too large: %d node tiles need more than %d co-resident CTAs", d.n_tiles, max_grid);
     launch_rest_state(d, h->stream);
     if (d.any_mass) launch_mass_matrix(d, h->stream);
     CK(cudaStreamSynchronize(h->stream));

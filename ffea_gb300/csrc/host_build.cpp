@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <queue>
 #include <numeric>
 
 namespace ffea {
@@ -59,6 +60,49 @@ const int kMid[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
 int32_t round_up(int32_t x, int32_t m) { return (x + m - 1) / m * m; }
 
 }  // namespace
+
+int32_t plan_cg_segments(HostBatch &H, int32_t ctas, int32_t max_rows)
+{
+    const int nb = H.num_blobs;
+    const int32_t max_slices = std::max(1, max_rows / 32);
+    std::vector<int32_t> slices(nb), k(nb);
+    int64_t total = 0;
+    for (int b = 0; b < nb; b++) {
+        slices[b] = std::max(1, (H.bp[b].node_cnt + 31) / 32);
+        k[b] = (slices[b] + max_slices - 1) / max_slices;
+        total += k[b];
+    }
+    if (total <= ctas) {
+        // longest segment first: (slices per segment rounded up, blob)
+        std::priority_queue<std::pair<int32_t, int>> q;
+        for (int b = 0; b < nb; b++) q.push({(slices[b] + k[b] - 1) / k[b], -b});
+        while (total < ctas && !q.empty()) {
+            const int b = -q.top().second;
+            q.pop();
+            if (k[b] >= slices[b]) continue;  // one slice per segment already
+            k[b]++;
+            total++;
+            q.push({(slices[b] + k[b] - 1) / k[b], -b});
+        }
+    }
+    H.seg_row0.clear();
+    H.seg_rows.clear();
+    H.seg_blob.clear();
+    for (int b = 0; b < nb; b++) {
+        BlobParams &bp = H.bp[b];
+        bp.seg_off = (int32_t)H.seg_row0.size();
+        bp.seg_cnt = k[b];
+        for (int j = 0; j < k[b]; j++) {
+            const int64_t s0 = (int64_t)slices[b] * j / k[b], s1 = (int64_t)slices[b] * (j + 1) / k[b];
+            const int32_t r0 = (int32_t)(32 * s0);
+            const int32_t r1 = (int32_t)std::min<int64_t>(32 * s1, bp.node_cnt);
+            H.seg_row0.push_back(bp.node_off + r0);
+            H.seg_rows.push_back(std::max(0, r1 - r0));
+            H.seg_blob.push_back(b);
+        }
+    }
+    return (int32_t)H.seg_row0.size();
+}
 
 void ffea_seed_words(int32_t rng_seed, uint64_t out[6])
 {

@@ -44,6 +44,9 @@ struct HostBatch {
     std::vector<int32_t> slice_ptr, slice_len, sell_col;
     std::vector<int32_t> edge_pos_pq, edge_pos_qp;        // entry of (p,q) in row p and of (q,p) in row q
     std::vector<int32_t> tile_blob, etile_blob;
+    // CG segments: contiguous row ranges of one blob, 32-row aligned, one
+    // per CTA of the persistent CG kernel (or several per CTA)
+    std::vector<int32_t> seg_row0, seg_rows, seg_blob;
     int32_t num_streams = 0;
     std::vector<uint32_t> stream_state;                   // 6 per stream
     std::vector<mrg::JumpMat> stream_step;                // per stream: A^(draws per step)
@@ -53,6 +56,15 @@ struct HostBatch {
 // Build the packed batch.  Returns false and sets err on invalid input.
 bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_params *params, int32_t rng_mode,
                  HostBatch &out, std::string &err);
+
+// Split every blob's rows into CG segments of at most max_rows rows (a
+// multiple of 32), starting on 32-row boundaries.  When the minimum number of
+// segments fits `ctas`, segments are added where they are longest until there
+// are `ctas` of them (each CTA then runs one, and the longest segment is as
+// short as the 32-row granularity allows); otherwise every blob gets the
+// minimum.  Fills H.seg_* and H.bp[b].seg_off / seg_cnt; returns the number of
+// segments.
+int32_t plan_cg_segments(HostBatch &H, int32_t ctas, int32_t max_rows);
 
 // World::init's six seed words (src/World.cpp:299-305).
 void ffea_seed_words(int32_t rng_seed, uint64_t out[6]);

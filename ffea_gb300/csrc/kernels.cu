@@ -759,11 +759,12 @@ __device__ __forceinline__ DF df_warp_sum(DF v)
     return v;
 }
 
-// Partial sums of a node tile: three quantities, each a (hi, lo) float pair,
-// in the 32 bytes of the tile's partials slot.  Per thread and per warp the
-// sums run in W; tid 0 adds the warp sums in FP64 and splits the result.
+// Partial sums of a CG segment: three quantities, each a (hi, lo) float pair,
+// in the 32 bytes of the segment's partials slot.  Per thread and per warp the
+// sums run in W; warp 0 adds the warp sums in FP64 (a butterfly over the
+// CTA's warps) and lane 0 splits the results.
 template <typename W>
-__device__ __forceinline__ void tile_partials(double *part, int tile, const W (&in)[3], int mask, double *smem)
+__device__ __forceinline__ void seg_partials(double *part, int seg, const W (&in)[3], int mask, double *smem)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -772,38 +773,39 @@ __device__ __forceinline__ void tile_partials(double *part, int tile, const W (&
         if (lane == 0) smem[k * 32 + warp] = (double)s;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float *P = reinterpret_cast<float *>(part) + 8 * (size_t)tile;
+    if (warp == 0) {
+        float *P = reinterpret_cast<float *>(part) + 8 * (size_t)seg;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             if (!(mask & (1 << k))) continue;
-            double a = 0.0;
-            for (int w = 0; w < nw; w++) a += smem[k * 32 + w];
-            const float hi = (float)a;
-            P[2 * k] = hi;
-            P[2 * k + 1] = (float)(a - (double)hi);
+            double a = lane < nw ? smem[k * 32 + lane] : 0.0;
+            a = warp_sum<double>(a);
+            if (lane == 0) {
+                const float hi = (float)a;
+                P[2 * k] = hi;
+                P[2 * k + 1] = (float)(a - (double)hi);
+            }
         }
     }
     __syncthreads();
 }
 
-// Loads of tile partials in flight per thread before they are added.
+// Loads of segment partials in flight per thread before they are added.
 constexpr int kSumUnroll = 4;
 
-// Adds the partials of tiles t0 + first, t0 + first + stride, ... (< tc) to
-// a[0..2] in that order; kSumUnroll loads are issued before the adds.
-__device__ __forceinline__ void add_tile_partials(const double *part, int t0, int tc, int first, int stride,
-                                                  DF a[3])
+// Adds the partials of segments s0 + first, s0 + first + stride, ... (< cnt)
+// to a[0..2] in that order; kSumUnroll loads are issued before the adds.
+__device__ __forceinline__ void add_seg_partials(const double *part, int s0, int cnt, int first, int stride, DF a[3])
 {
-    for (int t = first; t < tc; t += kSumUnroll * stride) {
+    for (int t = first; t < cnt; t += kSumUnroll * stride) {
         float4 v01[kSumUnroll];
         float2 v2[kSumUnroll];
 #pragma unroll
         for (int u = 0; u < kSumUnroll; u++) {
             const int tt = t + u * stride;
-            if (tt < tc) {
-                v01[u] = __ldcg(reinterpret_cast<const float4 *>(part) + 2 * (size_t)(t0 + tt));
-                v2[u] = __ldcg(reinterpret_cast<const float2 *>(part) + 4 * (size_t)(t0 + tt) + 2);
+            if (tt < cnt) {
+                v01[u] = __ldcg(reinterpret_cast<const float4 *>(part) + 2 * (size_t)(s0 + tt));
+                v2[u] = __ldcg(reinterpret_cast<const float2 *>(part) + 4 * (size_t)(s0 + tt) + 2);
             } else {
                 v01[u] = make_float4(0.f, 0.f, 0.f, 0.f);
                 v2[u] = make_float2(0.f, 0.f);
@@ -818,12 +820,12 @@ __device__ __forceinline__ void add_tile_partials(const double *part, int t0, in
     }
 }
 
-// Sum of the three partial slots over a blob's node tiles, by the calling
+// Sum of the three partial slots over a blob's CG segments, by the calling
 // warp (lane-strided, then a butterfly): fixed order, so deterministic.
 __device__ __forceinline__ void warp_blob_sums(const DeviceBatch &d, const double *part, int b, double out[3])
 {
     DF a[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    add_tile_partials(part, d.bp[b].tile_off, d.bp[b].tile_cnt, threadIdx.x & 31, 32, a);
+    add_seg_partials(part, d.bp[b].seg_off, d.bp[b].seg_cnt, threadIdx.x & 31, 32, a);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const DF s = df_warp_sum(a[k]);
@@ -831,38 +833,31 @@ __device__ __forceinline__ void warp_blob_sums(const DeviceBatch &d, const doubl
     }
 }
 
-// The same for one blob with the whole CTA (CG_THREADS = 8 warps): thread-
-// strided sums, a butterfly per warp, then warp 0 combines the 8 warp sums of
-// each quantity with a butterfly over lanes 8k .. 8k+7.  The result is valid
-// in warp 0 only (every lane of it); the caller synchronises before reusing sm.
+// The same for one blob with the whole CTA: thread-strided sums, a butterfly
+// per warp, then warp 0 combines the warp sums of each quantity with a
+// butterfly.  The result is valid in warp 0 only (every lane of it); the
+// caller synchronises before reusing sm (2 * 3 * 32 floats).
 __device__ __forceinline__ void block_blob_sums(const DeviceBatch &d, const double *part, int b, double out[3],
                                                 float *sm)
 {
-    static_assert(CG_THREADS == 256, "block_blob_sums combines 8 warps");
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     DF a[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    add_tile_partials(part, d.bp[b].tile_off, d.bp[b].tile_cnt, threadIdx.x, CG_THREADS, a);
+    add_seg_partials(part, d.bp[b].seg_off, d.bp[b].seg_cnt, threadIdx.x, blockDim.x, a);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const DF s = df_warp_sum(a[k]);
         if (lane == 0) {
-            sm[2 * (k * 8 + warp)] = s.hi;
-            sm[2 * (k * 8 + warp) + 1] = s.lo;
+            sm[2 * (k * 32 + warp)] = s.hi;
+            sm[2 * (k * 32 + warp) + 1] = s.lo;
         }
     }
     __syncthreads();
     if (warp == 0) {
-        // lane 8k + w holds warp w's sum of quantity k (lanes 24..31 idle)
-        DF v = lane < 24 ? DF{sm[2 * lane], sm[2 * lane + 1]} : DF{0.f, 0.f};
-#pragma unroll
-        for (int o = 4; o > 0; o >>= 1) {
-            const DF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
-            v = df_add(v, w);
-        }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const float hi = __shfl_sync(0xffffffffu, v.hi, 8 * k), lo = __shfl_sync(0xffffffffu, v.lo, 8 * k);
-            out[k] = (double)hi + (double)lo;
+            const DF v = lane < nw ? DF{sm[2 * (k * 32 + lane)], sm[2 * (k * 32 + lane) + 1]} : DF{0.f, 0.f};
+            const DF s = df_warp_sum(v);
+            out[k] = (double)s.hi + (double)s.lo;
         }
     }
 }
@@ -1071,43 +1066,48 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
 // iteration), x0 = 0, stopping on residual2() = sum r^2 / sum f^2 < eps^2
 // after each update (src/NoMassCGSolver.cpp:180-189, :233-247).  Per
 // iteration: phase A updates p, s, x, r and u = D^-1 r of the own rows; a
-// plain grid barrier makes u visible; phase B computes w = A u; then r.u, r.r
-// and w.u are summed per blob and each blob's CG state advances.  With few
-// tiles and blobs (cg_local) every CTA does that sum itself after a plain
+// grid barrier makes u visible; phase B computes w = A u; then r.u, r.r and
+// w.u are summed per blob and each blob's CG state advances.  With few
+// segments and blobs (cg_local) every CTA does that sum itself after a plain
 // barrier, from partials double-buffered by iteration parity (a fast CTA's
 // next phase A must not overwrite what a slow CTA is still summing); else a
-// reducing barrier does it once, in the last CTA to arrive.  With true_residual on, a recursive
-// convergence is confirmed by an FP64 b - A x and a failed check restarts the
-// recurrences from that residual.  CTA c owns node tiles
-// [n_tiles*c/G, n_tiles*(c+1)/G); thread t owns row t of each.  With one tile
-// per CTA (REG) the row state stays in registers for the whole solve; only u
-// and x go to memory, for the neighbours.
+// reducing barrier does it once, in the last CTA to arrive.  With
+// true_residual on, a recursive convergence is confirmed by an FP64 b - A x
+// and a failed check restarts the recurrences from that residual.
+//
+// Work split: the rows of each blob are cut into segments (32-row aligned, at
+// most CG_THREADS rows); CTA c owns segments [n_segs*c/G, n_segs*(c+1)/G) and
+// thread t row t of each.  With one segment per CTA (REG) the row state stays
+// in registers for the whole solve; only u and x go to memory, for the
+// neighbours.
 template <typename T, bool REG>
-__global__ void __launch_bounds__(CG_THREADS, 4) k_cg(DeviceBatch d)
+__global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
 {
     using W = T;
     __shared__ double red[3 * 32];
     __shared__ float sm_df[2 * 3 * 32];
     __shared__ int s_nt, s_nb, s_err, s_last[2];
     __shared__ unsigned int s_pub;
-    __shared__ int s_tslot[CG_MAX_TILES];
-    __shared__ int s_blob[CG_MAX_TILES], s_state[CG_MAX_TILES];
-    __shared__ double s_alpha[CG_MAX_TILES], s_beta[CG_MAX_TILES];
+    __shared__ int s_tslot[CG_MAX_SEGS], s_row0[CG_MAX_SEGS], s_rows[CG_MAX_SEGS];
+    __shared__ int s_blob[CG_MAX_SEGS], s_state[CG_MAX_SEGS];
+    __shared__ double s_alpha[CG_MAX_SEGS], s_beta[CG_MAX_SEGS];
     __shared__ CgScalars s_cg[CG_LOCAL_MAX_BLOBS];
     __shared__ unsigned int s_run;
 
     const int G = gridDim.x, c = blockIdx.x, tid = threadIdx.x;
     const bool local = d.cg_local;
-    const int T0 = (int)(((long long)d.n_tiles * c) / G), T1 = (int)(((long long)d.n_tiles * (c + 1)) / G);
+    const int S0 = (int)(((long long)d.n_segs * c) / G), S1 = (int)(((long long)d.n_segs * (c + 1)) / G);
     if (tid == 0) {
         s_err = 0;
         int nb = 0;
-        for (int j = 0; j < T1 - T0; j++) {
-            const int b = d.tile_blob[T0 + j];
+        for (int j = 0; j < S1 - S0; j++) {
+            const int b = d.seg_blob[S0 + j];
             if (nb == 0 || s_blob[nb - 1] != b) s_blob[nb++] = b;
             s_tslot[j] = nb - 1;
+            s_row0[j] = d.seg_row0[S0 + j];
+            s_rows[j] = d.seg_rows[S0 + j];
         }
-        s_nt = T1 - T0;
+        s_nt = S1 - S0;
         s_nb = nb;
     }
     if (local)
@@ -1134,41 +1134,51 @@ __global__ void __launch_bounds__(CG_THREADS, 4) k_cg(DeviceBatch d)
     };
     // partials buffer of the current iteration
     int parity = 0;
-    auto part = [&]() { return d.partials + (size_t)parity * 4 * d.n_tiles; };
+    auto part = [&]() { return d.partials + (size_t)parity * 4 * d.n_segs; };
     refresh();
     T *X = static_cast<T *>(d.x), *U = static_cast<T *>(d.u);
 
-    // per-thread constants of the row in REG mode (the CTA's only tile)
-    RowState<T> reg;
-    bool reg_valid = false;
-    T reg_diag = 0;
-    if (REG) {
-        const int row = T0 * NODE_TILE + tid;
-        const BlobParams &bp = d.bp[s_blob[0]];
-        reg_valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
-        reg_diag = bp.solver == SOLVER_NOMASS ? (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0)
-                                              : static_cast<const T *>(d.mass_diag)[row];
-        load_row<T>(d, row, reg);
-    }
-    auto row_info = [&](int j, int row, bool &valid, T &diag, bool &nomass) {
+    // row of this thread in segment j, and whether it is a free (unpinned) row
+    auto row_of = [&](int j, bool &valid) {
+        const int row = s_row0[j] + tid;
+        valid = tid < s_rows[j] && !(d.flags[row] & NODE_PINNED);
+        return row;
+    };
+    auto diag_of = [&](int j, int row, bool &nomass) {
         const BlobParams &bp = d.bp[s_blob[s_tslot[j]]];
         nomass = bp.solver == SOLVER_NOMASS;
+        return nomass ? (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0) : static_cast<const T *>(d.mass_diag)[row];
+    };
+    // per-thread constants of the row in REG mode (the CTA's only segment)
+    RowState<T> reg;
+    bool reg_valid = false, reg_nomass = true;
+    T reg_diag = 0;
+    if (REG) {
+        const int row = row_of(0, reg_valid);
+        if (tid < s_rows[0]) {
+            reg_diag = diag_of(0, row, reg_nomass);
+            load_row<T>(d, row, reg);
+        }
+    }
+    auto row_info = [&](int j, int &row, bool &valid, T &diag, bool &nomass) {
         if (REG) {
+            row = s_row0[0] + tid;
             valid = reg_valid;
             diag = reg_diag;
+            nomass = reg_nomass;
         } else {
-            valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
-            diag = nomass ? (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0) : static_cast<const T *>(d.mass_diag)[row];
+            row = row_of(j, valid);
+            if (valid) diag = diag_of(j, row, nomass);
         }
     };
-    // phase A of tile j: p = u + beta p; s = w + beta s; x += alpha p;
+    // phase A of segment j: p = u + beta p; s = w + beta s; x += alpha p;
     // r -= alpha s; u = D^-1 r.  Partials: slot 0 r.u, slot 2 r.r.
     auto phase_a = [&](int j) {
-        const int t = T0 + j, k = s_tslot[j];
+        const int k = s_tslot[j];
         if (s_state[k] != CG_ACTIVE) return;  // CTA-uniform
-        const int row = t * NODE_TILE + tid;
-        bool valid, nomass;
-        T diag;
+        int row;
+        bool valid, nomass = true;
+        T diag = 0;
         row_info(j, row, valid, diag, nomass);
         W pg = 0, pr = 0;
         RowState<T> loc;
@@ -1193,17 +1203,17 @@ __global__ void __launch_bounds__(CG_THREADS, 4) k_cg(DeviceBatch d)
         }
         if (!REG && valid) store_row<T>(d, row, loc);
         const W in[3] = {pg, (W)0, pr};
-        tile_partials<W>(part(), t, in, 5, red);
+        seg_partials<W>(part(), S0 + j, in, 5, red);
     };
-    // phase B of tile j: ACTIVE / RESTART and the prologue: w = A u, slot 1
+    // phase B of segment j: ACTIVE / RESTART and the prologue: w = A u, slot 1
     // w.u (the prologue and RESTART also fill slots 0 and 2); VERIFY: the
     // FP64 b - A x becomes the new residual, slot 0 r.u, slot 2 |b - A x|^2.
     auto phase_b = [&](int j, bool prologue) {
-        const int t = T0 + j, k = s_tslot[j], state = s_state[k];
+        const int k = s_tslot[j], state = s_state[k];
         if (!(state == CG_ACTIVE || state == CG_VERIFY || state == CG_RESTART)) return;  // CTA-uniform
-        const int row = t * NODE_TILE + tid;
-        bool valid, nomass;
-        T diag;
+        int row;
+        bool valid, nomass = true;
+        T diag = 0;
         row_info(j, row, valid, diag, nomass);
         W pg = 0, pd = 0, pr = 0;
         double vr = 0.0, vg = 0.0;
@@ -1238,10 +1248,10 @@ __global__ void __launch_bounds__(CG_THREADS, 4) k_cg(DeviceBatch d)
         if (!REG && valid) store_row<T>(d, row, loc);
         if (state == CG_VERIFY) {
             const double in[3] = {vg, 0.0, vr};
-            tile_partials<double>(part(), t, in, 5, red);
+            seg_partials<double>(part(), S0 + j, in, 5, red);
         } else {
             const W in[3] = {pg, pd, pr};
-            tile_partials<W>(part(), t, in, (prologue || state == CG_RESTART) ? 7 : 2, red);
+            seg_partials<W>(part(), S0 + j, in, (prologue || state == CG_RESTART) ? 7 : 2, red);
         }
     };
 

@@ -12,15 +12,17 @@ namespace ffea {
 struct DeviceBatch {
     int32_t num_blobs = 0, nl_pad = 0, ne_pad = 0, n_edges = 0, n_tiles = 0, n_etiles = 0, num_streams = 0;
     int32_t n_slices = 0, n_entries = 0;
+    int32_t n_segs = 0;           // CG segments
     int32_t precision = PREC_MIXED;
     int32_t any_mass = 0, any_nomass = 0;
     int32_t cg_grid = 0;          // CTAs of the persistent CG kernel
-    int32_t cg_reg = 0;           // 1: one node tile per CTA, CG state kept in registers
+    int32_t cg_reg = 0;           // 1: one CG segment per CTA, row state kept in registers
     int32_t cg_local = 0;         // 1: every CTA reduces the dot products itself (few tiles and blobs)
     // blobs
     BlobParams *bp = nullptr;
     Material *mats = nullptr;
     int32_t *tile_blob = nullptr, *etile_blob = nullptr;
+    int32_t *seg_row0 = nullptr, *seg_rows = nullptr, *seg_blob = nullptr;   // CG segments
     // RNG
     mrg::JumpMat *jump_table = nullptr;
     uint32_t *stream_state = nullptr;
@@ -51,7 +53,7 @@ struct DeviceBatch {
     void *sell_mval = nullptr;    // mass matrix: 1 T per entry
     void *mass_diag = nullptr;    // T per node
     // reductions / status
-    double *partials = nullptr;     // 8 per node tile: two buffers of 4, alternating between CG iterations
+    double *partials = nullptr;     // 4 per node tile (node kernel); CG: two buffers of 4 per segment
     CgScalars *cg = nullptr;        // per blob
     unsigned int *counters = nullptr;  // one per reduction site
     unsigned int *bar = nullptr;    // grid barrier: arrival count, generation
@@ -68,10 +70,10 @@ enum CounterSlot { CNT_NODES = 0, CNT_ENERGY = 1, CNT_COUNT = 4 };
 // element kernel modes
 enum ElemMode { ELEM_STEP = 0, ELEM_MATRIX_ONLY = 1 };
 
-constexpr int CG_THREADS = NODE_TILE;   // one row per thread and tile
-constexpr int CG_MAX_TILES = 64;        // node tiles per CTA of the persistent kernel
+constexpr int CG_THREADS = 1024;        // threads per CTA of the CG kernel = maximum rows of a segment
+constexpr int CG_MAX_SEGS = 64;         // segments per CTA of the persistent kernel
 constexpr int CG_LOCAL_MAX_BLOBS = 64;  // local reduction: blob records kept in shared memory
-constexpr int CG_LOCAL_MAX_TILES = 4096;  // local reduction: partial sums every CTA reads per iteration
+constexpr int CG_LOCAL_MAX_SEGS = 2048; // local reduction: partial sums every CTA reads per iteration
 
 // Launchers (all asynchronous on `s`).
 void launch_rest_state(const DeviceBatch &d, cudaStream_t s);
@@ -88,7 +90,7 @@ void launch_spmv_variant(const DeviceBatch &d, cudaStream_t s, int variant);
 void launch_rng_draws(const mrg::JumpMat *table, const uint32_t *state, uint64_t offset, int64_t count, double *out,
                       cudaStream_t s);
 // CTAs of the persistent CG kernel (register-resident variant or not) that fit
-// co-resident on the current device
+// co-resident on the current device, 0 on error
 int cg_max_grid(int precision, int reg);
 
 int64_t kernel_launch_count();

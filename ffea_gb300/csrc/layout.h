@@ -42,6 +42,7 @@ struct BlobParams {
     int32_t node_off, node_cnt, node_pad;   // padded linear-node range
     int32_t elem_off, elem_cnt, elem_pad;   // padded element range
     int32_t tile_off, tile_cnt;             // node tiles (CTAs) of this blob
+    int32_t seg_off, seg_cnt;               // CG segments of this blob
     int32_t num_nodes_total;                // N_t of the reference (linear + secondary)
     int32_t true_residual;
 };

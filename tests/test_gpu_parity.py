@@ -141,6 +141,26 @@ def test_register_and_memory_cg_state_agree(gpulib, monkeypatch):
         assert np.array_equal(a, c)
 
 
+@pytest.mark.parametrize("max_ctas", ["1", "3"])
+def test_several_segments_per_cta_match_oracle(gpulib, oracle, monkeypatch, max_ctas):
+    """A grid capped below the segment count runs the memory-resident CG
+    variant with several segments per CTA (the layout of batches too large
+    for one segment per CTA); FP64 results must still follow the oracle."""
+    monkeypatch.setenv("FFEA_GPU_CG_MAX_CTAS", max_ctas)
+    s = spec(radius_nm=8.0)
+    ref = oracle.blob_from_spec(s)
+    with _world([s]) as w:
+        b = w.blob(0)
+        for step in range(4):
+            w.run(1)
+            assert ref.step(1) == 0
+            pos, vel, _ = b.get_nodes()
+            rpos, rvel, _ = ref.nodes()
+            assert b.status()["fail_bits"] == 0
+            assert rel(vel, rvel) < 1e-9, step
+            assert np.abs(pos - rpos).max() < 1e-10, step
+
+
 @pytest.mark.parametrize("num_blobs", [1, 9])
 def test_local_and_last_arriver_reduction_agree(gpulib, monkeypatch, num_blobs):
     """The CG sums are reduced either redundantly by every CTA (few tiles and
