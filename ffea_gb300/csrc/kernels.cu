@@ -497,6 +497,9 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
                 cg.gamma = s0;
                 cg.ff = s1;
                 cg.delta = cg.rr = cg.alpha = cg.beta = 0.0;
+                cg.gamma_f = (float)s0;
+                cg.pap_f = cg.alpha_f = cg.beta_f = 0.f;
+                cg.stop_f = (float)(d.bp[bb].epsilon2 * s1);
                 cg.iters = 0;
                 cg.restarts = 0;
                 cg.true_relres2 = -1.0;
@@ -764,13 +767,14 @@ __device__ __forceinline__ DF df_warp_sum(DF v)
 // sums run in W; warp 0 adds the warp sums in FP64 (a butterfly over the
 // CTA's warps) and lane 0 splits the results.
 template <typename W>
-__device__ __forceinline__ void seg_partials(double *part, int seg, const W (&in)[3], int mask, double *smem)
+__device__ __forceinline__ void seg_partials(double *part, int seg, const W (&in)[3], int mask, double *smem_raw)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    W *smem = reinterpret_cast<W *>(smem_raw);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const W s = warp_sum<W>(in[k]);
-        if (lane == 0) smem[k * 32 + warp] = (double)s;
+        if (lane == 0) smem[k * 32 + warp] = s;
     }
     __syncthreads();
     if (warp == 0) {
@@ -778,12 +782,21 @@ __device__ __forceinline__ void seg_partials(double *part, int seg, const W (&in
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             if (!(mask & (1 << k))) continue;
-            double a = lane < nw ? smem[k * 32 + lane] : 0.0;
-            a = warp_sum<double>(a);
+            float hi, lo;
+            if (sizeof(W) == 4) {
+                // FP32 warp sums added in double-float on the FP32 pipes (an
+                // FP64 butterfly or conversion here costs ~0.5 us per phase)
+                const DF v = df_warp_sum(DF{lane < nw ? (float)smem[k * 32 + lane] : 0.f, 0.f});
+                hi = v.hi;
+                lo = v.lo;
+            } else {
+                const double a = warp_sum<double>(lane < nw ? (double)smem[k * 32 + lane] : 0.0);
+                hi = (float)a;
+                lo = (float)(a - (double)hi);
+            }
             if (lane == 0) {
-                const float hi = (float)a;
                 P[2 * k] = hi;
-                P[2 * k + 1] = (float)(a - (double)hi);
+                P[2 * k + 1] = lo;
             }
         }
     }
@@ -822,22 +835,19 @@ __device__ __forceinline__ void add_seg_partials(const double *part, int s0, int
 
 // Sum of the three partial slots over a blob's CG segments, by the calling
 // warp (lane-strided, then a butterfly): fixed order, so deterministic.
-__device__ __forceinline__ void warp_blob_sums(const DeviceBatch &d, const double *part, int b, double out[3])
+__device__ __forceinline__ void warp_blob_sums(const DeviceBatch &d, const double *part, int b, DF out[3])
 {
     DF a[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     add_seg_partials(part, d.bp[b].seg_off, d.bp[b].seg_cnt, threadIdx.x & 31, 32, a);
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const DF s = df_warp_sum(a[k]);
-        out[k] = (double)s.hi + (double)s.lo;
-    }
+    for (int k = 0; k < 3; k++) out[k] = df_warp_sum(a[k]);
 }
 
 // The same for one blob with the whole CTA: thread-strided sums, a butterfly
 // per warp, then warp 0 combines the warp sums of each quantity with a
 // butterfly.  The result is valid in warp 0 only (every lane of it); the
 // caller synchronises before reusing sm (2 * 3 * 32 floats).
-__device__ __forceinline__ void block_blob_sums(const DeviceBatch &d, const double *part, int b, double out[3],
+__device__ __forceinline__ void block_blob_sums(const DeviceBatch &d, const double *part, int b, DF out[3],
                                                 float *sm)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -856,8 +866,7 @@ __device__ __forceinline__ void block_blob_sums(const DeviceBatch &d, const doub
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const DF v = lane < nw ? DF{sm[2 * (k * 32 + lane)], sm[2 * (k * 32 + lane) + 1]} : DF{0.f, 0.f};
-            const DF s = df_warp_sum(v);
-            out[k] = (double)s.hi + (double)s.lo;
+            out[k] = df_warp_sum(v);
         }
     }
 }
@@ -868,39 +877,70 @@ __device__ __forceinline__ void block_blob_sums(const DeviceBatch &d, const doub
 //   RESTART  sums -, w.u, -: alpha of the first restarted update, beta = 0
 // Returns true when the blob stops (cg.state is then CONVERGED or FAILED) and
 // sets *fail_bits to the failure bits (0 if none).
-__device__ __forceinline__ bool transition_core(CgScalars &cg, const BlobParams &bp, const double sums[3],
-                                                int *fail_bits)
+//
+// FP64 precision runs the recurrence in FP64: alpha = r.u / (w.u - beta r.u /
+// alpha_prev), beta = r.u / r.u_prev, stop when r.r / f.f < eps^2.  Mixed
+// precision (`fast`) applies alpha and beta in FP32 anyway and runs it in
+// FP32 as alpha = r.u / p.Ap with p.Ap = w.u - beta^2 (p.Ap)_prev (the same
+// recurrence), stop when r.r < eps^2 f.f: FP64 arithmetic and conversions run
+// at 1/64 of the FP32 rate and would sit on the critical path of every
+// iteration.  VERIFY (once per solve) stays in FP64.
+__device__ __forceinline__ bool transition_core(CgScalars &cg, const BlobParams &bp, const DF sums[3],
+                                                int *fail_bits, bool fast)
 {
     const int limit = bp.solver == SOLVER_MASS ? bp.max_iter - 1 : bp.max_iter;
-    const double ff = cg.ff;
     int finish = 0, bits = 0;
     if (cg.state == CG_ACTIVE) {
-        const double g = sums[0], dl = sums[1], rr = sums[2];
-        cg.rr = rr;
-        const double res = (ff == 0.0) ? 0.0 : rr / ff;
-        if (cg.iters > 0 && res < bp.epsilon2) {
+        bool conv, nan;
+        if (fast) {
+            const float g = sums[0].hi + sums[0].lo, dl = sums[1].hi + sums[1].lo, rr = sums[2].hi + sums[2].lo;
+            conv = rr < cg.stop_f;
+            nan = !(rr == rr) || !(g == g) || !(dl == dl);
+            if (!(cg.iters > 0 && conv) && !nan && cg.iters < limit) {
+                if (cg.iters == 0) {
+                    cg.beta_f = 0.f;
+                    cg.pap_f = dl;
+                } else {
+                    cg.beta_f = g / cg.gamma_f;
+                    cg.pap_f = fmaf(-cg.beta_f * cg.beta_f, cg.pap_f, dl);
+                }
+                cg.alpha_f = g / cg.pap_f;
+                cg.gamma_f = g;
+            }
+        } else {
+            const double g = (double)sums[0].hi + (double)sums[0].lo, dl = (double)sums[1].hi + (double)sums[1].lo;
+            const double rr = (double)sums[2].hi + (double)sums[2].lo;
+            cg.rr = rr;
+            const double res = (cg.ff == 0.0) ? 0.0 : rr / cg.ff;
+            conv = res < bp.epsilon2;
+            nan = !(res == res) || !(g == g) || !(dl == dl);
+            if (!(cg.iters > 0 && conv) && !nan && cg.iters < limit) {
+                if (cg.iters == 0) {
+                    cg.beta = 0.0;
+                    cg.alpha = g / dl;
+                } else {
+                    const double beta = g / cg.gamma;
+                    cg.alpha = g / (dl - beta * g / cg.alpha);
+                    cg.beta = beta;
+                }
+                cg.gamma = g;
+            }
+        }
+        if (cg.iters > 0 && conv) {
             if (bp.true_residual) cg.state = CG_VERIFY;
             else finish = CG_CONVERGED;
-        } else if (!(res == res) || !(g == g) || !(dl == dl)) {
+        } else if (nan) {
             finish = CG_FAILED;
             bits = BLOB_FAIL_CG | BLOB_FAIL_NAN;
         } else if (cg.iters >= limit) {
             finish = CG_FAILED;
             bits = BLOB_FAIL_CG;
         } else {
-            if (cg.iters == 0) {
-                cg.beta = 0.0;
-                cg.alpha = g / dl;
-            } else {
-                const double beta = g / cg.gamma;
-                cg.alpha = g / (dl - beta * g / cg.alpha);
-                cg.beta = beta;
-            }
-            cg.gamma = g;
             cg.iters += 1;
         }
     } else if (cg.state == CG_VERIFY) {
-        cg.true_relres2 = (ff == 0.0) ? 0.0 : sums[2] / ff;
+        const double tr = (double)sums[2].hi + (double)sums[2].lo;
+        cg.true_relres2 = (cg.ff == 0.0) ? 0.0 : tr / cg.ff;
         if (cg.true_relres2 < bp.epsilon2) {
             finish = CG_CONVERGED;
         } else if (cg.restarts >= kMaxRestarts || cg.iters >= limit) {
@@ -908,15 +948,25 @@ __device__ __forceinline__ bool transition_core(CgScalars &cg, const BlobParams 
             bits = BLOB_FAIL_CG;
         } else {
             cg.restarts += 1;
-            cg.gamma = sums[0];
+            cg.gamma = (double)sums[0].hi + (double)sums[0].lo;
+            cg.gamma_f = sums[0].hi + sums[0].lo;
             cg.state = CG_RESTART;
         }
     } else if (cg.state == CG_RESTART) {
         cg.state = CG_ACTIVE;
-        cg.beta = 0.0;
-        cg.alpha = cg.gamma / sums[1];
         cg.iters += 1;
-        if (!(cg.alpha == cg.alpha)) {
+        bool nan;
+        if (fast) {
+            cg.beta_f = 0.f;
+            cg.pap_f = sums[1].hi + sums[1].lo;
+            cg.alpha_f = cg.gamma_f / cg.pap_f;
+            nan = !(cg.alpha_f == cg.alpha_f);
+        } else {
+            cg.beta = 0.0;
+            cg.alpha = cg.gamma / ((double)sums[1].hi + (double)sums[1].lo);
+            nan = !(cg.alpha == cg.alpha);
+        }
+        if (nan) {
             finish = CG_FAILED;
             bits = BLOB_FAIL_CG | BLOB_FAIL_NAN;
         }
@@ -926,9 +976,25 @@ __device__ __forceinline__ bool transition_core(CgScalars &cg, const BlobParams 
     return finish != 0;
 }
 
+// The coefficients of the next update in the arithmetic type of the vectors.
+template <typename T>
+__device__ __forceinline__ void cg_coefs(const CgScalars &cg, T &alpha, T &beta);
+template <>
+__device__ __forceinline__ void cg_coefs<float>(const CgScalars &cg, float &alpha, float &beta)
+{
+    alpha = cg.alpha_f;
+    beta = cg.beta_f;
+}
+template <>
+__device__ __forceinline__ void cg_coefs<double>(const CgScalars &cg, double &alpha, double &beta)
+{
+    alpha = cg.alpha;
+    beta = cg.beta;
+}
+
 // The transition run by the CTA that arrived last at a reducing barrier
 // (exactly once per blob), on the blob's record in global memory.
-__device__ __forceinline__ void cg_transition(const DeviceBatch &d, int b, const double sums[3])
+__device__ __forceinline__ void cg_transition(const DeviceBatch &d, int b, const DF sums[3])
 {
     // read through L2: the record may have been written by another SM's last CTA
     CgScalars cg;
@@ -940,7 +1006,7 @@ __device__ __forceinline__ void cg_transition(const DeviceBatch &d, int b, const
         for (int i = 0; i < (int)(sizeof(CgScalars) / 8); i++) dst[i] = __ldcg(src + i);
     }
     int bits;
-    if (transition_core(cg, d.bp[b], sums, &bits)) {
+    if (transition_core(cg, d.bp[b], sums, &bits, d.precision == PREC_MIXED)) {
         atomicSub(&d.bar[2], 1u);
         if (bits) atomicOr(&d.status[b], bits);
     }
@@ -972,7 +1038,7 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, i
             for (int b = 0; b < d.num_blobs; b++) {
                 const int st = __ldcg(&d.cg[b].state);
                 if (st == CG_CONVERGED || st == CG_FAILED) continue;
-                double sums[3];
+                DF sums[3];
                 block_blob_sums(d, d.partials, b, sums, sm);
                 if (threadIdx.x == 0) cg_transition(d, b, sums);
                 __syncthreads();  // sm reused by the next blob
@@ -981,7 +1047,7 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, i
             for (int b = warp; b < d.num_blobs; b += blockDim.x >> 5) {
                 const int st = __ldcg(&d.cg[b].state);
                 if (st == CG_CONVERGED || st == CG_FAILED) continue;
-                double sums[3];
+                DF sums[3];
                 warp_blob_sums(d, d.partials, b, sums);
                 if (lane == 0) cg_transition(d, b, sums);
             }
@@ -1020,33 +1086,39 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, i
 // the partials of every busy blob itself, in the same fixed order, and runs
 // the transitions on its own copy of the blob records in shared memory, so
 // all CTAs reach bit-identical states.  CTA 0 alone records failure bits.
-// Returns the number of blobs still iterating.
+// Also refreshes the CTA's view (state, alpha, beta of its nb blobs) and
+// returns the number of blobs still iterating.
+template <typename T>
 __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const double *part, CgScalars *s_cg,
-                                                     float *sm, unsigned int *s_run)
+                                                     float *sm, unsigned int *s_run, int nb, const int *s_blob,
+                                                     int *s_state, T *s_alpha, T *s_beta)
 {
     const int nbl = d.num_blobs, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr bool fast = sizeof(T) == 4;
     if (nbl < 8) {
+        // one blob after the other with the whole CTA; thread 0 (in warp 0,
+        // which holds the sums) runs every transition
         for (int b = 0; b < nbl; b++) {
             const int st = s_cg[b].state;
             if (st == CG_CONVERGED || st == CG_FAILED) continue;  // CTA-uniform
-            double sums[3];
+            DF sums[3];
             block_blob_sums(d, part, b, sums, sm);
             if (threadIdx.x == 0) {
                 int bits;
-                if (transition_core(s_cg[b], d.bp[b], sums, &bits) && bits && blockIdx.x == 0)
+                if (transition_core(s_cg[b], d.bp[b], sums, &bits, fast) && bits && blockIdx.x == 0)
                     atomicOr(&d.status[b], bits);
             }
-            __syncthreads();  // s_cg[b] visible; sm reused by the next blob
+            if (b + 1 < nbl) __syncthreads();  // sm reused by the next blob
         }
     } else {
         for (int b = warp; b < nbl; b += blockDim.x >> 5) {
             const int st = s_cg[b].state;
             if (st == CG_CONVERGED || st == CG_FAILED) continue;  // warp-uniform
-            double sums[3];
+            DF sums[3];
             warp_blob_sums(d, part, b, sums);
             if (lane == 0) {
                 int bits;
-                if (transition_core(s_cg[b], d.bp[b], sums, &bits) && bits && blockIdx.x == 0)
+                if (transition_core(s_cg[b], d.bp[b], sums, &bits, fast) && bits && blockIdx.x == 0)
                     atomicOr(&d.status[b], bits);
             }
         }
@@ -1056,6 +1128,11 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
         unsigned int n = 0;
         for (int b = 0; b < nbl; b++) n += !(s_cg[b].state == CG_CONVERGED || s_cg[b].state == CG_FAILED);
         *s_run = n;
+        for (int k = 0; k < nb; k++) {
+            const CgScalars &cg = s_cg[s_blob[k]];
+            s_state[k] = cg.state;
+            cg_coefs<T>(cg, s_alpha[k], s_beta[k]);
+        }
     }
     __syncthreads();
     return *s_run;
@@ -1090,7 +1167,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     __shared__ unsigned int s_pub;
     __shared__ int s_tslot[CG_MAX_SEGS], s_row0[CG_MAX_SEGS], s_rows[CG_MAX_SEGS];
     __shared__ int s_blob[CG_MAX_SEGS], s_state[CG_MAX_SEGS];
-    __shared__ double s_alpha[CG_MAX_SEGS], s_beta[CG_MAX_SEGS];
+    __shared__ T s_alpha[CG_MAX_SEGS], s_beta[CG_MAX_SEGS];
     __shared__ CgScalars s_cg[CG_LOCAL_MAX_BLOBS];
     __shared__ unsigned int s_run;
 
@@ -1121,13 +1198,17 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             if (local) {
                 const CgScalars &cg = s_cg[s_blob[k]];
                 s_state[k] = cg.state;
-                s_alpha[k] = cg.alpha;
-                s_beta[k] = cg.beta;
+                cg_coefs<T>(cg, s_alpha[k], s_beta[k]);
             } else {
                 const CgScalars *cg = &d.cg[s_blob[k]];
                 s_state[k] = __ldcg(&cg->state);
-                s_alpha[k] = __ldcg(&cg->alpha);
-                s_beta[k] = __ldcg(&cg->beta);
+                if (sizeof(T) == 4) {
+                    s_alpha[k] = (T)__ldcg(&cg->alpha_f);
+                    s_beta[k] = (T)__ldcg(&cg->beta_f);
+                } else {
+                    s_alpha[k] = (T)__ldcg(&cg->alpha);
+                    s_beta[k] = (T)__ldcg(&cg->beta);
+                }
             }
         }
         __syncthreads();
@@ -1185,8 +1266,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         RowState<T> &S = REG ? reg : loc;
         if (!REG && valid) load_row<T>(d, row, loc);
         if (valid) {
-            const T a = (T)s_alpha[k], b = (T)s_beta[k];
-            const bool first = s_beta[k] == 0.0;
+            const T a = s_alpha[k], b = s_beta[k];
+            const bool first = b == (T)0;
             const size_t o = 3 * (size_t)row;
 #pragma unroll
             for (int cc = 0; cc < 3; cc++) {
@@ -1261,14 +1342,14 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         if (!local) return reducing_barrier(d, &s_err, &s_pub, s_last, sm_df);
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) return 0u;
-        return local_reduce(d, part(), s_cg, sm_df, &s_run);
+        return local_reduce<T>(d, part(), s_cg, sm_df, &s_run, nb, s_blob, s_state, s_alpha, s_beta);
     };
     for (int j = 0; j < nt; j++) phase_b(j, true);
     unsigned int running = reduce();
     long long loops = 0;
     while (!s_err && running > 0) {
         if (local) parity ^= 1;
-        refresh();
+        else refresh();  // the local reduction refreshed already
         for (int j = 0; j < nt; j++) phase_a(j);
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) break;

@@ -58,15 +58,18 @@ enum CgState : int32_t { CG_ACTIVE = 0, CG_VERIFY = 1, CG_RESTART = 2, CG_CONVER
 // Per-blob CG scalars, FP64 (Chronopoulos-Gear recurrences).
 struct CgScalars {
     double gamma;      // r . u   (u = D^-1 r)
-    double delta;      // w . u   (w = A u)
+    double delta;      // p . A p of the last update (w . u at the first)
     double ff;         // f . f   (rhs norm^2)
     double rr;         // r . r
     double alpha, beta;
     double true_relres2;   // ||b - A x||^2 / ||b||^2 of the last verification, -1 if none
+    // mixed precision: the recurrences in FP32 (no FP64 instruction on the
+    // per-iteration path; FP64 runs at 1/64 of the FP32 rate)
+    float gamma_f, pap_f, alpha_f, beta_f;
+    float stop_f;          // eps^2 f.f: stop when r.r < stop_f
     int32_t iters;         // matrix-vector products of this solve (the reference's iteration count)
     int32_t state;         // CgState
     int32_t restarts;
-    int32_t pad_;
 };
 
 }  // namespace ffea
