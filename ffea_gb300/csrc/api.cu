@@ -200,8 +200,17 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     // register-resident variant when every CG segment gets a CTA of its own.
     // FFEA_GPU_CG_MAX_CTAS caps the grid, FFEA_GPU_CG_MEMORY_STATE=1 keeps the
     // segments but runs the memory-resident variant (both for tests).
-    const int reg_grid = cg_max_grid(H.precision, 1);
-    const int max_grid = cg_max_grid(H.precision, 0);
+    // FFEA_GPU_CG_SMEM_SLOTS caps the matrix slots per row held in shared memory
+    int max_slots = 64;
+    if (const char *e = std::getenv("FFEA_GPU_CG_SMEM_SLOTS")) max_slots = std::max(0, std::atoi(e));
+    int max_cols = 0;
+    for (int32_t L : H.slice_len) max_cols = std::max(max_cols, (int)L);
+    size_t dyn_bytes = 0;
+    int cache_slots = 0, cache_cols = 0;
+    if (cg_smem_plan(H.precision, max_slots, max_cols, &cache_slots, &cache_cols, &dyn_bytes) != 0)
+        return fail("cannot size the shared memory of the CG kernel");
+    const int reg_grid = cg_max_grid(H.precision, 1, dyn_bytes);
+    const int max_grid = cg_max_grid(H.precision, 0, 0);
     if (reg_grid <= 0 || max_grid <= 0) return fail("cannot size the persistent CG kernel on this device");
     int cap = std::numeric_limits<int>::max();
     if (const char *e = std::getenv("FFEA_GPU_CG_MAX_CTAS")) cap = std::max(1, std::atoi(e));
@@ -211,6 +220,9 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     d.n_segs = n_segs;
     d.cg_reg = n_segs <= reg_cap && !(force_mem && force_mem[0] == '1');
     d.cg_grid = n_segs <= reg_cap ? n_segs : std::min(mem_cap, n_segs);
+    d.cg_cache_slots = d.cg_reg ? cache_slots : 0;
+    d.cg_cache_cols = d.cg_reg ? cache_cols : 0;
+    d.cg_dyn_smem = d.cg_reg ? (int32_t)dyn_bytes : 0;
     if ((int64_t)d.cg_grid * CG_MAX_SEGS < n_segs)
         return fail("batch too large: %d CG segments need more than %d co-resident CTAs", n_segs, mem_cap);
     // local reduction (every CTA sums all partials, no serial last-arriver
@@ -267,8 +279,9 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     d.n_entries = (int32_t)H.sell_col.size();
     const size_t n3 = 3 * (size_t)H.nl_pad;
     CK(A.alloc(d.rhs, n3));
-    for (void **v : {&d.x, &d.r, &d.u, &d.w, &d.p, &d.s, &d.dinv, &d.m, &d.z, &d.q, &d.m2})
+    for (void **v : {&d.x, &d.r, &d.u, &d.w, &d.p, &d.s, &d.dinv})
         CK(A.alloc_bytes(*v, n3 * ts));
+    CK(A.alloc_bytes(d.u4, 4 * (size_t)H.nl_pad * ts));
     CK(A.alloc(d.det_sign, (size_t)H.ne_pad));
     CK(A.alloc_bytes(d.jinv0, 9 * (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.vol0, (size_t)H.ne_pad * ts));

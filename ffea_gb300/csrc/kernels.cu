@@ -27,6 +27,9 @@
 
 #include "kernels.h"
 
+#include <algorithm>
+#include <type_traits>
+
 namespace ffea {
 
 static std::atomic<int64_t> g_launches{0};
@@ -447,10 +450,9 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
 #pragma unroll
         for (int i = 0; i < 3; i++) dinv[3 * (size_t)row + i] = valid ? (T)(1.0 / (D[i] + drag)) : (T)1;
     }
-    // CG start (pipelined form): x = 0, r = f, u = D^-1 r, w = m = z = q = s = p = 0
+    // CG start: x = 0, r = f, u = D^-1 r, w = s = p = 0
     T *x = static_cast<T *>(d.x), *r = static_cast<T *>(d.r), *u = static_cast<T *>(d.u);
     T *p = static_cast<T *>(d.p), *sv = static_cast<T *>(d.s), *w = static_cast<T *>(d.w);
-    T *mv = static_cast<T *>(d.m), *zv = static_cast<T *>(d.z), *qv = static_cast<T *>(d.q);
     double gam = 0.0, ff = 0.0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -465,9 +467,6 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
         p[k] = (T)0;
         sv[k] = (T)0;
         w[k] = (T)0;
-        mv[k] = (T)0;
-        zv[k] = (T)0;
-        qv[k] = (T)0;
         gam += (double)ri * (double)ui;
         ff += fi * fi;
     }
@@ -598,6 +597,122 @@ __device__ __forceinline__ void sell_row(const DeviceBatch &d, int row, bool nom
                 a2 += m * y[g][2];
             }
         }
+    }
+    out[0] = a0;
+    out[1] = a1;
+    out[2] = a2;
+}
+
+// Vector of 4 T: the published copy of u in the CG kernel (x, y, z, 0), one
+// 16-byte (FP32) load per neighbour instead of three 4-byte loads that each
+// touch the same sectors.
+struct alignas(16) Dbl4 {
+    double x, y, z, w;
+};
+template <typename T> struct Vec4T;
+template <> struct Vec4T<float> { using type = float4; };
+template <> struct Vec4T<double> { using type = Dbl4; };
+
+__device__ __forceinline__ float4 ldcg4(const float4 *p) { return __ldcg(p); }
+__device__ __forceinline__ Dbl4 ldcg4(const Dbl4 *p)
+{
+    const double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldcg(reinterpret_cast<const double2 *>(p) + 1);
+    return Dbl4{a.x, a.y, b.x, b.y};
+}
+
+// On-chip copy of a CTA's matrix rows for one solve (register-resident CG
+// variant): the column indices of slots j < JC (col[j * CG_THREADS + t] for
+// thread t) and the 9 values of slots j < J as four pairs and a single
+// (kv2[(4 j + m) * CG_THREADS + t], kv1[j * CG_THREADS + t]).  The matrix is
+// constant during a solve; each slot held on chip saves its L2 reads in every
+// iteration, and cached column indices take the index -> neighbour dependency
+// off the critical path of the gathers.
+template <typename T>
+struct CgCache {
+    using T2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+    const int *col = nullptr;
+    const T2 *kv2 = nullptr;
+    const T *kv1 = nullptr;
+    int J = 0, JC = 0;
+};
+
+// One 3x3 block times a difference vector, added with explicit FMAs so that
+// every code path gives the same bits.
+template <typename T>
+__device__ __forceinline__ void block_fma(const T K[9], T d0, T d1, T d2, T &a0, T &a1, T &a2)
+{
+    a0 = fma(K[2], d2, fma(K[1], d1, fma(K[0], d0, a0)));
+    a1 = fma(K[5], d2, fma(K[4], d1, fma(K[3], d0, a1)));
+    a2 = fma(K[8], d2, fma(K[7], d1, fma(K[6], d0, a2)));
+}
+
+// q = A u for one row of the CG kernel (sell_row's arithmetic): slots with
+// values on chip in groups of 4 (only the neighbour loads go to L2), then the
+// rest in groups of 2 (values and neighbours from L2, issued together).
+template <typename T>
+__device__ __forceinline__ void sell_row_cg(const DeviceBatch &d, int row, bool nomass, T diag,
+                                            const typename Vec4T<T>::type *u4, T out[3], const CgCache<T> &cc)
+{
+    const int sl = row >> 5, lane = row & 31, t = threadIdx.x;
+    const int L = __ldg(&d.slice_len[sl]);
+    const int base = __ldg(&d.slice_ptr[sl]);
+    const auto me = ldcg4(&u4[row]);
+    T a0 = diag * me.x, a1 = diag * me.y, a2 = diag * me.z;
+    auto col_of = [&](int j) {
+        return j < cc.JC ? cc.col[j * CG_THREADS + t] : __ldg(&d.sell_col[base + 32 * j + lane]);
+    };
+    if (!nomass) {
+        const T *mv = static_cast<const T *>(d.sell_mval);
+        for (int j = 0; j < L; j++) {
+            const auto y = ldcg4(&u4[col_of(j)]);
+            const T m = __ldg(&mv[base + 32 * j + lane]);
+            a0 = fma(m, y.x, a0);
+            a1 = fma(m, y.y, a1);
+            a2 = fma(m, y.z, a2);
+        }
+        out[0] = a0;
+        out[1] = a1;
+        out[2] = a2;
+        return;
+    }
+    const int Jk = min(cc.J, L);
+    constexpr int G1 = 4;
+    for (int j0 = 0; j0 < Jk; j0 += G1) {
+        typename Vec4T<T>::type y[G1];
+#pragma unroll
+        for (int g = 0; g < G1; g++) y[g] = ldcg4(&u4[j0 + g < Jk ? col_of(j0 + g) : row]);
+#pragma unroll
+        for (int g = 0; g < G1; g++) {
+            const int j = j0 + g;
+            if (j >= Jk) break;
+            T K[9];
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                const auto kp = cc.kv2[(4 * j + m) * CG_THREADS + t];
+                K[2 * m] = kp.x;
+                K[2 * m + 1] = kp.y;
+            }
+            K[8] = cc.kv1[j * CG_THREADS + t];
+            block_fma(K, y[g].x - me.x, y[g].y - me.y, y[g].z - me.z, a0, a1, a2);
+        }
+    }
+    const T *val = static_cast<const T *>(d.sell_val);
+    constexpr int G2 = 2;
+    for (int j0 = Jk; j0 < L; j0 += G2) {
+        typename Vec4T<T>::type y[G2];
+        T K[G2][9];
+#pragma unroll
+        for (int g = 0; g < G2; g++) {
+            const int j = j0 + g;
+            y[g] = ldcg4(&u4[j < L ? col_of(j) : row]);
+            const size_t vb = (size_t)(base + 32 * j) * 9 + lane;
+#pragma unroll
+            for (int k = 0; k < 9; k++) K[g][k] = j < L ? __ldg(&val[vb + 32 * k]) : (T)0;
+        }
+#pragma unroll
+        for (int g = 0; g < G2; g++)
+            if (j0 + g < L) block_fma(K[g], y[g].x - me.x, y[g].y - me.y, y[g].z - me.z, a0, a1, a2);
     }
     out[0] = a0;
     out[1] = a1;
@@ -1171,6 +1286,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     __shared__ CgScalars s_cg[CG_LOCAL_MAX_BLOBS];
     __shared__ unsigned int s_run;
 
+    extern __shared__ __align__(16) unsigned char cg_dyn[];
     const int G = gridDim.x, c = blockIdx.x, tid = threadIdx.x;
     const bool local = d.cg_local;
     const int S0 = (int)(((long long)d.n_segs * c) / G), S1 = (int)(((long long)d.n_segs * (c + 1)) / G);
@@ -1217,7 +1333,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     int parity = 0;
     auto part = [&]() { return d.partials + (size_t)parity * 4 * d.n_segs; };
     refresh();
-    T *X = static_cast<T *>(d.x), *U = static_cast<T *>(d.u);
+    using V4 = typename Vec4T<T>::type;
+    using T2 = typename CgCache<T>::T2;
+    T *X = static_cast<T *>(d.x);
+    V4 *U4 = static_cast<V4 *>(d.u4);
 
     // row of this thread in segment j, and whether it is a free (unpinned) row
     auto row_of = [&](int j, bool &valid) {
@@ -1230,15 +1349,58 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         nomass = bp.solver == SOLVER_NOMASS;
         return nomass ? (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0) : static_cast<const T *>(d.mass_diag)[row];
     };
-    // per-thread constants of the row in REG mode (the CTA's only segment)
+    // REG: r, u, w, s, p of the CTA's only segment in registers; x, D^-1 and
+    // the on-chip matrix copy in dynamic shared memory:
+    //   sx[3 CG_THREADS] T | sdinv[3 CG_THREADS] T | col[JC CG_THREADS] int |
+    //   kv2[4 J CG_THREADS] T2 | kv1[J CG_THREADS] T
     RowState<T> reg;
     bool reg_valid = false, reg_nomass = true;
     T reg_diag = 0;
+    T *sx = reinterpret_cast<T *>(cg_dyn);
+    T *sdinv = sx + 3 * CG_THREADS;
+    CgCache<T> cc;
     if (REG) {
+        cc.J = d.cg_cache_slots;
+        cc.JC = d.cg_cache_cols;
+        cc.col = reinterpret_cast<const int *>(sdinv + 3 * CG_THREADS);
+        cc.kv2 = reinterpret_cast<const T2 *>(cc.col + (size_t)cc.JC * CG_THREADS);
+        cc.kv1 = reinterpret_cast<const T *>(cc.kv2 + 4 * (size_t)cc.J * CG_THREADS);
         const int row = row_of(0, reg_valid);
+        const size_t o = 3 * (size_t)row;
         if (tid < s_rows[0]) {
             reg_diag = diag_of(0, row, reg_nomass);
-            load_row<T>(d, row, reg);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                reg.r[k] = static_cast<const T *>(d.r)[o + k];
+                reg.u[k] = static_cast<const T *>(d.u)[o + k];
+                reg.w[k] = static_cast<const T *>(d.w)[o + k];
+                reg.s[k] = static_cast<const T *>(d.s)[o + k];
+                reg.p[k] = static_cast<const T *>(d.p)[o + k];
+                sx[k * CG_THREADS + tid] = static_cast<const T *>(d.x)[o + k];
+                sdinv[k * CG_THREADS + tid] = static_cast<const T *>(d.dinv)[o + k];
+            }
+        }
+        // every free row (NoMass or mass) reads its column indices from the
+        // copy; only NoMass rows read values from it
+        if (reg_valid) {
+            const int sl = row >> 5, lane = row & 31;
+            const int L = d.slice_len[sl], base = d.slice_ptr[sl];
+            const T *val = static_cast<const T *>(d.sell_val);
+            int *col = const_cast<int *>(cc.col);
+            T2 *kv2 = const_cast<T2 *>(cc.kv2);
+            T *kv1 = const_cast<T *>(cc.kv1);
+            for (int j = 0; j < min(cc.JC, L); j++) col[j * CG_THREADS + tid] = d.sell_col[base + 32 * j + lane];
+            for (int j = 0; reg_nomass && j < min(cc.J, L); j++) {
+                const size_t vb = (size_t)(base + 32 * j) * 9 + lane;
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    T2 kp;
+                    kp.x = val[vb + 32 * (2 * m)];
+                    kp.y = val[vb + 32 * (2 * m + 1)];
+                    kv2[(4 * j + m) * CG_THREADS + tid] = kp;
+                }
+                kv1[j * CG_THREADS + tid] = val[vb + 32 * 8];
+            }
         }
     }
     auto row_info = [&](int j, int &row, bool &valid, T &diag, bool &nomass) {
@@ -1250,6 +1412,18 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         } else {
             row = row_of(j, valid);
             if (valid) diag = diag_of(j, row, nomass);
+        }
+    };
+    // x and D^-1 of the thread's row (component k)
+    auto xref = [&](RowState<T> &S, int k) -> T & { return REG ? sx[k * CG_THREADS + tid] : S.x[k]; };
+    auto dinv_of = [&](const RowState<T> &S, int k) -> T { return REG ? sdinv[k * CG_THREADS + tid] : S.dinv[k]; };
+    // REG: x of the own rows to global memory (for the FP64 true residual and
+    // the Euler update; the memory-resident variant keeps it there)
+    auto publish_x = [&]() {
+        if (REG && reg_valid) {
+            const size_t o = 3 * (size_t)(s_row0[0] + tid);
+#pragma unroll
+            for (int k = 0; k < 3; k++) X[o + k] = sx[k * CG_THREADS + tid];
         }
     };
     // phase A of segment j: p = u + beta p; s = w + beta s; x += alpha p;
@@ -1268,19 +1442,17 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         if (valid) {
             const T a = s_alpha[k], b = s_beta[k];
             const bool first = b == (T)0;
-            const size_t o = 3 * (size_t)row;
 #pragma unroll
-            for (int cc = 0; cc < 3; cc++) {
-                S.p[cc] = first ? S.u[cc] : S.u[cc] + b * S.p[cc];
-                S.s[cc] = first ? S.w[cc] : S.w[cc] + b * S.s[cc];
-                S.x[cc] += a * S.p[cc];
-                S.r[cc] -= a * S.s[cc];
-                S.u[cc] = S.dinv[cc] * S.r[cc];
-                U[o + cc] = S.u[cc];
-                X[o + cc] = S.x[cc];
-                pg += S.r[cc] * S.u[cc];
-                pr += S.r[cc] * S.r[cc];
+            for (int cc2 = 0; cc2 < 3; cc2++) {
+                S.p[cc2] = first ? S.u[cc2] : S.u[cc2] + b * S.p[cc2];
+                S.s[cc2] = first ? S.w[cc2] : S.w[cc2] + b * S.s[cc2];
+                xref(S, cc2) += a * S.p[cc2];
+                S.r[cc2] -= a * S.s[cc2];
+                S.u[cc2] = dinv_of(S, cc2) * S.r[cc2];
+                pg += S.r[cc2] * S.u[cc2];
+                pr += S.r[cc2] * S.r[cc2];
             }
+            U4[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
         }
         if (!REG && valid) store_row<T>(d, row, loc);
         const W in[3] = {pg, (W)0, pr};
@@ -1302,28 +1474,27 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         RowState<T> &S = REG ? reg : loc;
         if (!REG && valid) load_row<T>(d, row, loc);
         if (valid) {
-            const size_t o = 3 * (size_t)row;
             if (state != CG_VERIFY) {
                 T au[3];
-                sell_row<T>(d, row, nomass, diag, U, au);
+                sell_row_cg<T>(d, row, nomass, diag, U4, au, cc);
 #pragma unroll
-                for (int cc = 0; cc < 3; cc++) {
-                    S.w[cc] = au[cc];
-                    pd += au[cc] * S.u[cc];
-                    pg += S.r[cc] * S.u[cc];
-                    pr += S.r[cc] * S.r[cc];
+                for (int cc2 = 0; cc2 < 3; cc2++) {
+                    S.w[cc2] = au[cc2];
+                    pd += au[cc2] * S.u[cc2];
+                    pg += S.r[cc2] * S.u[cc2];
+                    pr += S.r[cc2] * S.r[cc2];
                 }
             } else {
                 double rt[3];
                 true_residual_row<T>(d, row, nomass, (double)diag, X, rt);
 #pragma unroll
-                for (int cc = 0; cc < 3; cc++) {
-                    S.r[cc] = (T)rt[cc];
-                    S.u[cc] = S.dinv[cc] * S.r[cc];
-                    U[o + cc] = S.u[cc];
-                    vr += rt[cc] * rt[cc];
-                    vg += (double)S.r[cc] * (double)S.u[cc];
+                for (int cc2 = 0; cc2 < 3; cc2++) {
+                    S.r[cc2] = (T)rt[cc2];
+                    S.u[cc2] = dinv_of(S, cc2) * S.r[cc2];
+                    vr += rt[cc2] * rt[cc2];
+                    vg += (double)S.r[cc2] * (double)S.u[cc2];
                 }
+                U4[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
             }
         }
         if (!REG && valid) store_row<T>(d, row, loc);
@@ -1344,12 +1515,24 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         if (s_err) return 0u;
         return local_reduce<T>(d, part(), s_cg, sm_df, &s_run, nb, s_blob, s_state, s_alpha, s_beta);
     };
-    for (int j = 0; j < nt; j++) phase_b(j, true);
-    unsigned int running = reduce();
+    // publish u of the own rows for the neighbours (the k_nodes start value;
+    // zero on pinned rows) before the first product
+    for (int j = 0; j < nt; j++) {
+        const int row = s_row0[j] + tid;
+        if (tid < s_rows[j]) {
+            const T *u = static_cast<const T *>(d.u) + 3 * (size_t)row;
+            U4[row] = V4{u[0], u[1], u[2], (T)0};
+        }
+    }
+    counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
+    if (!s_err)
+        for (int j = 0; j < nt; j++) phase_b(j, true);
+    unsigned int running = s_err ? 0u : reduce();
     long long loops = 0;
     while (!s_err && running > 0) {
         if (local) parity ^= 1;
         else refresh();  // the local reduction refreshed already
+        if (REG && s_state[0] == CG_VERIFY) publish_x();
         for (int j = 0; j < nt; j++) phase_a(j);
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) break;
@@ -1357,6 +1540,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         loops++;
         running = reduce();
     }
+    publish_x();
     if (local && c == 0)
         for (int b = tid; b < d.num_blobs; b += CG_THREADS) d.cg[b] = s_cg[b];
     if (tid == 0) {
@@ -1576,17 +1760,49 @@ void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs)
     PREC_DISPATCH(d, k_nodes, d.n_tiles, NODE_TILE, s, d, use_given_rhs);
 }
 
-int cg_max_grid(int precision, int reg)
+template <typename T>
+static int cg_smem_plan_t(int max_slots, int max_cols, int *J, int *JC, size_t *dyn_bytes)
+{
+    int dev = 0, optin = 0;
+    *J = *JC = 0;
+    *dyn_bytes = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k_cg<T, true>) != cudaSuccess) return -1;
+    const size_t reserve = 1024;  // per-CTA system use
+    const size_t state = 6 * (size_t)CG_THREADS * sizeof(T);  // x and D^-1
+    const size_t fixed = fa.sharedSizeBytes + reserve + state;
+    if ((size_t)optin < fixed) return -1;
+    size_t room = optin - fixed;
+    const size_t per_col = (size_t)CG_THREADS * sizeof(int), per_slot = (size_t)CG_THREADS * 9 * sizeof(T);
+    *JC = (int)std::min<size_t>(room / per_col, (size_t)std::max(0, max_cols));
+    room -= (size_t)*JC * per_col;
+    *J = (int)std::min<size_t>(room / per_slot, (size_t)std::max(0, std::min(max_slots, *JC)));
+    *dyn_bytes = state + (size_t)*JC * per_col + (size_t)*J * per_slot;
+    if (cudaFuncSetAttribute(k_cg<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*dyn_bytes) !=
+        cudaSuccess)
+        return -1;
+    return 0;
+}
+
+int cg_smem_plan(int precision, int max_slots, int max_cols, int *J, int *JC, size_t *dyn_bytes)
+{
+    return precision == PREC_FP64 ? cg_smem_plan_t<double>(max_slots, max_cols, J, JC, dyn_bytes)
+                                  : cg_smem_plan_t<float>(max_slots, max_cols, J, JC, dyn_bytes);
+}
+
+int cg_max_grid(int precision, int reg, size_t dyn_bytes)
 {
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
     cudaError_t e;
     if (precision == PREC_FP64)
-        e = reg ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double, true>, CG_THREADS, 0)
+        e = reg ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double, true>, CG_THREADS, dyn_bytes)
                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double, false>, CG_THREADS, 0);
     else
-        e = reg ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float, true>, CG_THREADS, 0)
+        e = reg ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float, true>, CG_THREADS, dyn_bytes)
                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float, false>, CG_THREADS, 0);
     if (e != cudaSuccess) return 0;
     return sms * per_sm;
@@ -1597,7 +1813,7 @@ cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s)
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)d.cg_grid);
     cfg.blockDim = dim3(CG_THREADS);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = d.cg_reg ? (size_t)d.cg_dyn_smem : 0;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

@@ -17,7 +17,10 @@ struct DeviceBatch {
     int32_t any_mass = 0, any_nomass = 0;
     int32_t cg_grid = 0;          // CTAs of the persistent CG kernel
     int32_t cg_reg = 0;           // 1: one CG segment per CTA, row state kept in registers
-    int32_t cg_local = 0;         // 1: every CTA reduces the dot products itself (few tiles and blobs)
+    int32_t cg_local = 0;         // 1: every CTA reduces the dot products itself (few segments and blobs)
+    int32_t cg_cache_slots = 0;   // REG: matrix slots per row whose values are copied to shared memory
+    int32_t cg_cache_cols = 0;    // REG: matrix slots per row whose column indices are copied
+    int32_t cg_dyn_smem = 0;      // REG: dynamic shared memory bytes of that copy
     // blobs
     BlobParams *bp = nullptr;
     Material *mats = nullptr;
@@ -34,12 +37,10 @@ struct DeviceBatch {
     int32_t *gather_ptr = nullptr, *gather_idx = nullptr;
     int32_t *fold_ptr = nullptr, *fold_sec = nullptr;
     double *fold_drag = nullptr;
-    // CG vectors, T-typed, 3 per padded node (pipelined PCG): solution x,
-    // residual r, u = D^-1 r, w = A u, m = D^-1 w, and the recurrences
-    // z, q, s, p; Jacobi dinv
+    // CG vectors, T-typed, 3 per padded node: solution x, residual r,
+    // u = D^-1 r, w = A u, the recurrences s, p; Jacobi dinv
     void *x = nullptr, *r = nullptr, *u = nullptr, *w = nullptr, *p = nullptr, *s = nullptr, *dinv = nullptr;
-    void *m = nullptr, *z = nullptr, *q = nullptr;
-    void *m2 = nullptr;           // second buffer of m: iteration i reads m[i&1] and writes m[(i+1)&1]
+    void *u4 = nullptr;           // CG kernel: u published for the neighbours, 4 T per padded node (x, y, z, 0)
     // elements
     int32_t *conn = nullptr;
     uint16_t *mat_id = nullptr;
@@ -89,9 +90,15 @@ void launch_apply(const DeviceBatch &d, cudaStream_t s, const double *in, double
 void launch_spmv_variant(const DeviceBatch &d, cudaStream_t s, int variant);
 void launch_rng_draws(const mrg::JumpMat *table, const uint32_t *state, uint64_t offset, int64_t count, double *out,
                       cudaStream_t s);
-// CTAs of the persistent CG kernel (register-resident variant or not) that fit
-// co-resident on the current device, 0 on error
-int cg_max_grid(int precision, int reg);
+// Shared-memory plan of the register-resident CG kernel on the current
+// device: column indices of JC slots per row (at most max_cols) and values of
+// J slots (at most max_slots), plus x and D^-1; dyn_bytes is the dynamic
+// shared memory that takes (also set as the kernel's limit).  -1 on error.
+int cg_smem_plan(int precision, int max_slots, int max_cols, int *J, int *JC, size_t *dyn_bytes);
+// CTAs of the persistent CG kernel (register-resident variant with dyn_bytes
+// of dynamic shared memory, or not) that fit co-resident on the current
+// device, 0 on error
+int cg_max_grid(int precision, int reg, size_t dyn_bytes);
 
 int64_t kernel_launch_count();
 void count_launches(int64_t n);

@@ -141,6 +141,23 @@ def test_register_and_memory_cg_state_agree(gpulib, monkeypatch):
         assert np.array_equal(a, c)
 
 
+@pytest.mark.parametrize("precision", [P.PRECISION_MIXED, P.PRECISION_FP64])
+def test_shared_memory_matrix_copy_is_exact(gpulib, monkeypatch, precision):
+    """Matrix slots read from the per-solve shared-memory copy enter the SpMV
+    in the same order as slots read from global memory: identical iterates
+    with the copy on or off."""
+    s = spec(radius_nm=8.0, precision=precision, epsilon=1e-6 if precision == P.PRECISION_MIXED else 1e-12)
+    outs = []
+    for slots in ("0", "64"):
+        monkeypatch.setenv("FFEA_GPU_CG_SMEM_SLOTS", slots)
+        with _world([s]) as w:
+            w.run(3)
+            outs.append(w.blob(0).get_nodes())
+            assert w.blob(0).status()["fail_bits"] == 0
+    for a, c in zip(outs[0], outs[1]):
+        assert np.array_equal(a, c)
+
+
 @pytest.mark.parametrize("max_ctas", ["1", "3"])
 def test_several_segments_per_cta_match_oracle(gpulib, oracle, monkeypatch, max_ctas):
     """A grid capped below the segment count runs the memory-resident CG
