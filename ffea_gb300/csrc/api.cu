@@ -192,14 +192,26 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     if (rng_mode != FFEA_GPU_RNG_PER_BLOB && rng_mode != FFEA_GPU_RNG_SHARED) return fail("unknown rng_mode");
     std::unique_ptr<ffea_gpu> h(new ffea_gpu());
     std::string err;
-    if (!build_batch(num_blobs, meshes, params, rng_mode, h->host, err)) return fail("%s", err.c_str());
-    HostBatch &H = h->host;
-    DeviceBatch &d = h->dev;
-    DeviceArena &A = h->arena;
     // persistent CG kernel: all CTAs co-resident (cooperative launch); the
     // register-resident variant when every CG segment gets a CTA of its own.
     // FFEA_GPU_CG_MAX_CTAS caps the grid, FFEA_GPU_CG_MEMORY_STATE=1 keeps the
     // segments but runs the memory-resident variant (both for tests).
+    if (num_blobs <= 0) return fail("num_blobs must be >= 1");
+    const int prec = params[0].precision;
+    const int reg_grid0 = cg_max_grid(prec, 1, 0);
+    const int max_grid = cg_max_grid(prec, 0, 0);
+    const bool sized = reg_grid0 > 0 && max_grid > 0;
+    int cap = std::numeric_limits<int>::max();
+    if (const char *e = std::getenv("FFEA_GPU_CG_MAX_CTAS")) cap = std::max(1, std::atoi(e));
+    const int mem_cap = std::min(max_grid, cap);
+    // the input is validated first, so that its errors are reported even
+    // where no device is usable
+    if (!build_batch(num_blobs, meshes, params, rng_mode, sized ? std::min(reg_grid0, cap) : 1, h->host, err))
+        return fail("%s", err.c_str());
+    if (!sized) return fail("cannot size the persistent CG kernel on this device");
+    HostBatch &H = h->host;
+    DeviceBatch &d = h->dev;
+    DeviceArena &A = h->arena;
     // FFEA_GPU_CG_SMEM_SLOTS caps the matrix slots per row held in shared memory
     int max_slots = 64;
     if (const char *e = std::getenv("FFEA_GPU_CG_SMEM_SLOTS")) max_slots = std::max(0, std::atoi(e));
@@ -210,12 +222,9 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     if (cg_smem_plan(H.precision, max_slots, max_cols, &cache_slots, &cache_cols, &dyn_bytes) != 0)
         return fail("cannot size the shared memory of the CG kernel");
     const int reg_grid = cg_max_grid(H.precision, 1, dyn_bytes);
-    const int max_grid = cg_max_grid(H.precision, 0, 0);
-    if (reg_grid <= 0 || max_grid <= 0) return fail("cannot size the persistent CG kernel on this device");
-    int cap = std::numeric_limits<int>::max();
-    if (const char *e = std::getenv("FFEA_GPU_CG_MAX_CTAS")) cap = std::max(1, std::atoi(e));
-    const int reg_cap = std::min(reg_grid, cap), mem_cap = std::min(max_grid, cap);
-    const int32_t n_segs = plan_cg_segments(H, reg_cap, CG_THREADS);
+    if (reg_grid <= 0) return fail("cannot size the persistent CG kernel on this device");
+    const int reg_cap = std::min(reg_grid, cap);
+    const int32_t n_segs = plan_cg_segments(H);
     const char *force_mem = std::getenv("FFEA_GPU_CG_MEMORY_STATE");
     d.n_segs = n_segs;
     d.cg_reg = n_segs <= reg_cap && !(force_mem && force_mem[0] == '1');

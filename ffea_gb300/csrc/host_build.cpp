@@ -61,14 +61,14 @@ int32_t round_up(int32_t x, int32_t m) { return (x + m - 1) / m * m; }
 
 }  // namespace
 
-int32_t plan_cg_segments(HostBatch &H, int32_t ctas, int32_t max_rows)
+std::vector<int32_t> plan_parts(const std::vector<int32_t> &counts, int32_t ctas, int32_t max_rows)
 {
-    const int nb = H.num_blobs;
+    const int nb = (int)counts.size();
     const int32_t max_slices = std::max(1, max_rows / 32);
     std::vector<int32_t> slices(nb), k(nb);
     int64_t total = 0;
     for (int b = 0; b < nb; b++) {
-        slices[b] = std::max(1, (H.bp[b].node_cnt + 31) / 32);
+        slices[b] = std::max(1, (counts[b] + 31) / 32);
         k[b] = (slices[b] + max_slices - 1) / max_slices;
         total += k[b];
     }
@@ -85,17 +85,72 @@ int32_t plan_cg_segments(HostBatch &H, int32_t ctas, int32_t max_rows)
             q.push({(slices[b] + k[b] - 1) / k[b], -b});
         }
     }
+    return k;
+}
+
+namespace {
+
+// First row of part j when n rows are cut into k parts on 32-row boundaries.
+int32_t part_start(int32_t n, int32_t k, int32_t j)
+{
+    const int64_t slices = std::max(1, (n + 31) / 32);
+    return (int32_t)std::min<int64_t>(32 * (slices * j / k), n);
+}
+
+// Recursive coordinate bisection of ids[begin, end) into parts [p0, p1): the
+// set is sorted along its longest extent and split at the row count of the
+// first half of the parts.  Inside a part, rows run lexicographically over a
+// grid of spacing h (x slowest, z fastest), so consecutive rows are mostly
+// neighbours.  Ties break on the id: the order is the same on every host.
+void rcb(const double *pos, std::vector<int32_t> &ids, int32_t begin, int32_t end, int32_t n, int32_t k, int32_t p0,
+         int32_t p1, double h)
+{
+    if (end - begin <= 1) return;
+    if (p1 - p0 == 1) {
+        auto cell = [&](int32_t i, int c) { return (int64_t)std::floor(pos[3 * (size_t)i + c] / h); };
+        std::sort(ids.begin() + begin, ids.begin() + end, [&](int32_t a, int32_t b) {
+            for (int c = 0; c < 3; c++) {
+                const int64_t ca = cell(a, c), cb = cell(b, c);
+                if (ca != cb) return ca < cb;
+            }
+            return a < b;
+        });
+        return;
+    }
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int32_t i = begin; i < end; i++)
+        for (int c = 0; c < 3; c++) {
+            lo[c] = std::min(lo[c], pos[3 * (size_t)ids[i] + c]);
+            hi[c] = std::max(hi[c], pos[3 * (size_t)ids[i] + c]);
+        }
+    int axis = 0;
+    for (int c = 1; c < 3; c++)
+        if (hi[c] - lo[c] > hi[axis] - lo[axis]) axis = c;
+    std::sort(ids.begin() + begin, ids.begin() + end, [&](int32_t a, int32_t b) {
+        const double xa = pos[3 * (size_t)a + axis], xb = pos[3 * (size_t)b + axis];
+        if (xa != xb) return xa < xb;
+        return a < b;
+    });
+    const int32_t pm = (p0 + p1) / 2;
+    const int32_t mid = begin + (part_start(n, k, pm) - part_start(n, k, p0));
+    rcb(pos, ids, begin, mid, n, k, p0, pm, h);
+    rcb(pos, ids, mid, end, n, k, pm, p1, h);
+}
+
+}  // namespace
+
+int32_t plan_cg_segments(HostBatch &H)
+{
     H.seg_row0.clear();
     H.seg_rows.clear();
     H.seg_blob.clear();
-    for (int b = 0; b < nb; b++) {
+    for (int b = 0; b < H.num_blobs; b++) {
         BlobParams &bp = H.bp[b];
+        const int32_t k = H.parts[b];
         bp.seg_off = (int32_t)H.seg_row0.size();
-        bp.seg_cnt = k[b];
-        for (int j = 0; j < k[b]; j++) {
-            const int64_t s0 = (int64_t)slices[b] * j / k[b], s1 = (int64_t)slices[b] * (j + 1) / k[b];
-            const int32_t r0 = (int32_t)(32 * s0);
-            const int32_t r1 = (int32_t)std::min<int64_t>(32 * s1, bp.node_cnt);
+        bp.seg_cnt = k;
+        for (int j = 0; j < k; j++) {
+            const int32_t r0 = part_start(bp.node_cnt, k, j), r1 = part_start(bp.node_cnt, k, j + 1);
             H.seg_row0.push_back(bp.node_off + r0);
             H.seg_rows.push_back(std::max(0, r1 - r0));
             H.seg_blob.push_back(b);
@@ -119,7 +174,7 @@ void ffea_seed_words(int32_t rng_seed, uint64_t out[6])
 }
 
 bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_params *params, int32_t rng_mode,
-                 HostBatch &out, std::string &err)
+                 int32_t cg_ctas, HostBatch &out, std::string &err)
 {
     if (num_blobs <= 0 || num_blobs > MAX_BLOBS) {
         err = "num_blobs must be in [1, 2^20]";
@@ -191,7 +246,7 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
         lin_ids[b].assign(m.num_nodes, -1);
         int32_t cnt = 0;
         for (int32_t n = 0; n < m.num_nodes; n++)
-            if (kind[n] == 1) lin_ids[b][n] = cnt++;
+            if (kind[n] == 1) lin_ids[b][n] = cnt++;  // provisional: original order
         nl[b] = cnt;
         ne[b] = m.num_elements;
         BlobParams &bp = H.bp[b];
@@ -226,6 +281,42 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
     H.ne_pad = elem_off;
     H.n_tiles = tile_off;
     H.n_etiles = elem_off / ELEM_TILE;
+
+    // ---- linear node order: each blob's CG segments are compact blocks ---------
+    H.parts = plan_parts(nl, std::max(1, cg_ctas), CG_SEG_MAX_ROWS);
+    for (int b = 0; b < num_blobs; b++) {
+        const ffea_gpu_mesh &m = meshes[b];
+        const int32_t n = nl[b];
+        std::vector<double> lp(3 * (size_t)n);
+        std::vector<int32_t> orig_of(n);
+        for (int32_t v = 0; v < m.num_nodes; v++) {
+            const int32_t l = lin_ids[b][v];
+            if (l < 0) continue;
+            orig_of[l] = v;
+            for (int c = 0; c < 3; c++) lp[3 * (size_t)l + c] = m.pos[3 * (size_t)v + c];
+        }
+        // grid spacing of the in-segment order: mean corner-edge length
+        double hsum = 0.0;
+        int64_t hcnt = 0;
+        for (int64_t e = 0; e < std::min<int64_t>(m.num_elements, 4096); e++) {
+            const int32_t *t = &m.topology[10 * e];
+            for (int a = 0; a < 4; a++)
+                for (int c = a + 1; c < 4; c++) {
+                    double d2 = 0.0;
+                    for (int x = 0; x < 3; x++) {
+                        const double dd = m.pos[3 * (size_t)t[a] + x] - m.pos[3 * (size_t)t[c] + x];
+                        d2 += dd * dd;
+                    }
+                    hsum += std::sqrt(d2);
+                    hcnt++;
+                }
+        }
+        const double h = hcnt && hsum > 0 ? hsum / (double)hcnt : 1.0;
+        std::vector<int32_t> ids(n);
+        std::iota(ids.begin(), ids.end(), 0);
+        rcb(lp.data(), ids, 0, n, n, H.parts[b], 0, H.parts[b], h);
+        for (int32_t r = 0; r < n; r++) lin_ids[b][orig_of[ids[r]]] = r;
+    }
 
     // ---- materials (deduplicated table) ---------------------------------------
     std::map<std::vector<double>, uint16_t> mat_index;

@@ -47,24 +47,30 @@ struct HostBatch {
     // CG segments: contiguous row ranges of one blob, 32-row aligned, one
     // per CTA of the persistent CG kernel (or several per CTA)
     std::vector<int32_t> seg_row0, seg_rows, seg_blob;
+    std::vector<int32_t> parts;                            // CG segments per blob
     int32_t num_streams = 0;
     std::vector<uint32_t> stream_state;                   // 6 per stream
     std::vector<mrg::JumpMat> stream_step;                // per stream: A^(draws per step)
     std::vector<BlobMap> maps;
 };
 
-// Build the packed batch.  Returns false and sets err on invalid input.
-bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_params *params, int32_t rng_mode,
-                 HostBatch &out, std::string &err);
+// CG segments per blob for the given linear-node counts: at least enough of
+// at most max_rows rows (a multiple of 32); when those fit `ctas`, segments
+// are added where they are longest until there are `ctas` of them (each CTA
+// then runs one, and the longest is as short as the 32-row granularity
+// allows).
+std::vector<int32_t> plan_parts(const std::vector<int32_t> &counts, int32_t ctas, int32_t max_rows);
 
-// Split every blob's rows into CG segments of at most max_rows rows (a
-// multiple of 32), starting on 32-row boundaries.  When the minimum number of
-// segments fits `ctas`, segments are added where they are longest until there
-// are `ctas` of them (each CTA then runs one, and the longest segment is as
-// short as the 32-row granularity allows); otherwise every blob gets the
-// minimum.  Fills H.seg_* and H.bp[b].seg_off / seg_cnt; returns the number of
-// segments.
-int32_t plan_cg_segments(HostBatch &H, int32_t ctas, int32_t max_rows);
+// Build the packed batch for a persistent CG kernel of `cg_ctas` co-resident
+// CTAs: each blob's linear nodes are numbered so that its CG segments
+// (plan_parts) are compact blocks.  Returns false and sets err on invalid
+// input.
+bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_params *params, int32_t rng_mode,
+                 int32_t cg_ctas, HostBatch &out, std::string &err);
+
+// The CG segments of the batch (H.parts per blob, 32-row aligned row ranges):
+// fills H.seg_* and H.bp[b].seg_off / seg_cnt; returns the number of segments.
+int32_t plan_cg_segments(HostBatch &H);
 
 // World::init's six seed words (src/World.cpp:299-305).
 void ffea_seed_words(int32_t rng_seed, uint64_t out[6]);

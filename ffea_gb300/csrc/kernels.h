@@ -71,7 +71,7 @@ enum CounterSlot { CNT_NODES = 0, CNT_ENERGY = 1, CNT_COUNT = 4 };
 // element kernel modes
 enum ElemMode { ELEM_STEP = 0, ELEM_MATRIX_ONLY = 1 };
 
-constexpr int CG_THREADS = 1024;        // threads per CTA of the CG kernel = maximum rows of a segment
+constexpr int CG_THREADS = CG_SEG_MAX_ROWS;  // threads per CTA of the CG kernel = maximum rows of a segment
 constexpr int CG_MAX_SEGS = 64;         // segments per CTA of the persistent kernel
 constexpr int CG_LOCAL_MAX_BLOBS = 64;  // local reduction: blob records kept in shared memory
 constexpr int CG_LOCAL_MAX_SEGS = 2048; // local reduction: partial sums every CTA reads per iteration

@@ -18,6 +18,7 @@ constexpr int NODE_TILE = 256;   // rows per CTA of node-space kernels
 constexpr int ELEM_TILE = 128;   // elements per CTA of the element kernel
 constexpr int EDGE_TILE = 256;
 constexpr int MAX_BLOBS = 1 << 20;
+constexpr int CG_SEG_MAX_ROWS = 1024;  // rows of a CG segment (one per thread of a CG CTA)
 
 enum SolverKind : int32_t { SOLVER_NOMASS = 0, SOLVER_MASS = 1 };
 enum Precision : int32_t { PREC_FP64 = 0, PREC_MIXED = 1 };
