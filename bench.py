@@ -41,6 +41,7 @@ WORKLOADS = {
     "sphere10": dict(radius_nm=10.0, cell_nm=1.25, desc="16^3-cell Freudenthal grid cut to a 10 nm sphere"),
 }
 METRIC = "node-steps/s at CG rel-res 1e-6"
+PRECONDS = {"jacobi": 0, "two-level": 1, "learned": 2}
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -55,6 +56,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the cpu_baseline sample")
+    ap.add_argument("--precond", choices=sorted(PRECONDS), default="jacobi")
     return ap.parse_args()
 
 
@@ -253,7 +255,7 @@ def run_gb300(args):
 
     spec = build_spec(args.workload, rank, args.precision)
     N = spec.mesh.num_linear
-    w = World([spec], graph=True, true_residual=True)
+    w = World([spec], graph=True, true_residual=True, preconditioner=PRECONDS[args.precond])
     nl, ne, nedges = w.sizes()
     stream = torch.cuda.ExternalStream(w.stream())
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -334,6 +336,7 @@ def run_gb300(args):
         "phase_ms_per_step": {"elements": float(phases[0]), "assemble": float(phases[1]),
                               "nodes": float(phases[2]), "cg": float(phases[3]), "euler": float(phases[4])},
         "cg_us_per_iteration": 1e3 * cg_ms / max(iters_p, 1),
+        "preconditioner": {v: k for k, v in PRECONDS.items()}[w.preconditioner()],
     }
     line["config"]["edges"] = int(nedges)
     if world == 1 and not args.no_cpu_baseline:

@@ -47,6 +47,7 @@ class Params(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("rng_seed", ctypes.c_int32),
         ("true_residual", ctypes.c_int32),
+        ("preconditioner", ctypes.c_int32),
     ]
 
 
@@ -81,6 +82,9 @@ SIGNATURES = {
     "ffea_gpu_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "ffea_gpu_cg_loop_count": (ctypes.c_int64, [ctypes.c_void_p]),
     "ffea_gpu_diag_spmv": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _dp]),
+    "ffea_gpu_preconditioner": (ctypes.c_int, [ctypes.c_void_p]),
+    "ffea_gpu_set_smoother_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32,
+                                                     ctypes.POINTER(ctypes.c_float)]),
     "ffea_gpu_energies_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 5 + [ctypes.c_int32, ctypes.c_int32,
                                                                           ctypes.c_void_p, ctypes.c_void_p]),
 }

@@ -1,7 +1,8 @@
 """Build recipe for libffea_gb300.so (sm_103a), in-tree.
 
-Three translation units compiled in parallel with nvcc, linked into one
-shared library next to this file.  No cmake, no torch extension machinery:
+The translation units are compiled in parallel with nvcc and linked into one
+shared library next to this file (with cuBLAS, for the plain FP32 GEMMs of
+the coarse-space inverse).  No cmake, no torch extension machinery:
 the library exposes only the C ABI of include/ffea_gpu.h.
 """
 from __future__ import annotations
@@ -15,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT_DIR, "libffea_gb300.so")
-SOURCES = ["kernels.cu", "api.cu", "host_build.cpp", "noalloc.cu"]
+SOURCES = ["kernels.cu", "api.cu", "host_build.cpp", "noalloc.cu", "coarse.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -61,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
     tmp = LIB + ".tmp"
-    link = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    link = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lcublas"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))

@@ -6,6 +6,7 @@
 // The whole CG solve of every blob runs inside one cooperative launch that
 // iterates until each blob has converged, so a step (and a run of steps)
 // needs no host synchronisation.
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -108,8 +109,11 @@ struct ffea_gpu {
     int64_t fixed_per_step = 0;  // kernels of a step graph outside the CG loop
     size_t tsize = 4;
     std::vector<std::vector<double>> sec_vel;  // per blob: initial velocities of secondary nodes
+    int precond = FFEA_GPU_PRECOND_JACOBI;     // in use, after fall-backs
+    cublasHandle_t cublas = nullptr;           // coarse-space GEMMs
     ~ffea_gpu()
     {
+        if (cublas) cublasDestroy(cublas);
         if (step_exec) cudaGraphExecDestroy(step_exec);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
@@ -119,6 +123,20 @@ struct ffea_gpu {
 
 namespace {
 
+constexpr size_t kCublasWorkspace = 4u << 20;  // a fixed workspace makes the GEMMs capturable
+constexpr int kCoarseInitIterations = 40;      // Newton-Schulz from I / ||A_c||: log2(cond) + a few
+
+// The coarse matrix of the current mesh and one Newton-Schulz update of its
+// inverse (after the matrix assembly of every step or solve).
+int refresh_coarse(ffea_gpu *h, cudaStream_t s, int iterations, bool init)
+{
+    if (!h->dev.coarse) return FFEA_GPU_OK;
+    launch_coarse_assemble(h->dev, s);
+    if (coarse_refresh(h->dev, h->host.bp, h->cublas, s, iterations, init) != 0)
+        return fail("coarse-space refresh failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return FFEA_GPU_OK;
+}
+
 int build_step_graph(ffea_gpu *h)
 {
     DeviceBatch &d = h->dev;
@@ -127,16 +145,17 @@ int build_step_graph(ffea_gpu *h)
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     launch_elements(d, s, ELEM_STEP);
     if (d.any_nomass) launch_assemble(d, s);
+    int rc = refresh_coarse(h, s, 1, false);
     launch_nodes(d, s, 0);
     cudaError_t le = launch_cg(d, s);
     launch_euler(d, s);
     cudaError_t ce = cudaStreamEndCapture(s, &graph);
-    if (le != cudaSuccess || ce != cudaSuccess) {
+    if (rc != FFEA_GPU_OK || le != cudaSuccess || ce != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         cudaGetLastError();
         return fail("capturing the step graph failed: %s / %s", cudaGetErrorString(le), cudaGetErrorString(ce));
     }
-    h->fixed_per_step = 4 + (d.any_nomass ? 1 : 0);
+    h->fixed_per_step = 4 + (d.any_nomass ? 1 : 0) + (d.coarse ? 2 : 0);
     cudaError_t e = cudaGraphInstantiate(&h->step_exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail("cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
@@ -217,14 +236,27 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     if (const char *e = std::getenv("FFEA_GPU_CG_SMEM_SLOTS")) max_slots = std::max(0, std::atoi(e));
     int max_cols = 0;
     for (int32_t L : H.slice_len) max_cols = std::max(max_cols, (int)L);
+    const int32_t n_segs = plan_cg_segments(H);
+    // two-level preconditioner: NoMass blobs, mixed precision, one segment
+    // per CTA with local reductions, at most CG_THREADS coarse dofs per blob
+    const int want = params[0].preconditioner;
+    for (int b = 1; b < num_blobs; b++)
+        if (params[b].preconditioner != want) return fail("all blobs of a batch must use the same preconditioner");
+    if (want < FFEA_GPU_PRECOND_JACOBI || want > FFEA_GPU_PRECOND_LEARNED) return fail("unknown preconditioner");
+    const int64_t coarse_total = build_coarse(H);
+    int coarse_nmax = 0;
+    bool coarse_ok = want != FFEA_GPU_PRECOND_JACOBI && H.precision == PREC_MIXED && !H.any_mass;
+    for (const BlobParams &bp : H.bp) coarse_nmax = std::max(coarse_nmax, (int)bp.coarse_n);
+    if (coarse_nmax > CG_THREADS) coarse_ok = false;
+    const size_t coarse_bytes =
+        coarse_ok ? 16 + 16 * (size_t)CG_THREADS + sizeof(float) * (7 * (size_t)coarse_nmax + 8) : 0;
     size_t dyn_bytes = 0;
     int cache_slots = 0, cache_cols = 0;
-    if (cg_smem_plan(H.precision, max_slots, max_cols, &cache_slots, &cache_cols, &dyn_bytes) != 0)
+    if (cg_smem_plan(H.precision, max_slots, max_cols, coarse_bytes, &cache_slots, &cache_cols, &dyn_bytes) != 0)
         return fail("cannot size the shared memory of the CG kernel");
     const int reg_grid = cg_max_grid(H.precision, 1, dyn_bytes);
     if (reg_grid <= 0) return fail("cannot size the persistent CG kernel on this device");
     const int reg_cap = std::min(reg_grid, cap);
-    const int32_t n_segs = plan_cg_segments(H);
     const char *force_mem = std::getenv("FFEA_GPU_CG_MEMORY_STATE");
     d.n_segs = n_segs;
     d.cg_reg = n_segs <= reg_cap && !(force_mem && force_mem[0] == '1');
@@ -239,6 +271,10 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     const char *force_last = std::getenv("FFEA_GPU_CG_LAST_ARRIVER");
     d.cg_local = H.num_blobs <= CG_LOCAL_MAX_BLOBS && n_segs <= CG_LOCAL_MAX_SEGS &&
                  !(force_last && force_last[0] == '1');
+    d.coarse = coarse_ok && d.cg_reg && d.cg_local;
+    d.coarse_nmax = d.coarse ? coarse_nmax : 0;
+    d.part_stride = d.coarse ? 32 : 8;
+    h->precond = d.coarse ? want : FFEA_GPU_PRECOND_JACOBI;
     d.num_blobs = H.num_blobs;
     d.nl_pad = H.nl_pad;
     d.ne_pad = H.ne_pad;
@@ -299,7 +335,18 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(A.alloc_bytes(d.sell_val, H.any_nomass ? 9 * (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.sell_mval, H.any_mass ? (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.mass_diag, H.any_mass ? (size_t)H.nl_pad * ts : 16));
-    CK(A.alloc(d.partials, std::max(4 * (size_t)H.n_tiles, 8 * (size_t)n_segs)));
+    CK(A.alloc(d.partials, std::max(4 * (size_t)H.n_tiles, (size_t)d.part_stride * n_segs)));
+    if (d.coarse) {
+        CK(upload(A, d.seg_of_row, H.seg_of_row));
+        CK(upload(A, d.seg_nbr_ptr, H.seg_nbr_ptr));
+        CK(upload(A, d.seg_nbr, H.seg_nbr));
+        CK(A.alloc(d.phi, (size_t)H.nl_pad));
+        CK(cudaMemcpy(d.phi, H.phi.data(), H.phi.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CK(A.alloc(d.coarse_A, (size_t)coarse_total));
+        CK(A.alloc(d.coarse_X, (size_t)coarse_total));
+        CK(A.alloc(d.coarse_T, (size_t)coarse_nmax * coarse_nmax));
+        CK(A.alloc(d.coarse_Xn, (size_t)coarse_nmax * coarse_nmax));
+    }
     CK(A.alloc(d.epartials, 2 * (size_t)H.n_etiles));
     CK(A.alloc(d.cg, (size_t)H.num_blobs));
     CK(A.alloc(d.counters, (size_t)CNT_COUNT));
@@ -322,6 +369,18 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     }
     launch_rest_state(d, h->stream);
     if (d.any_mass) launch_mass_matrix(d, h->stream);
+    if (d.coarse) {
+        // X ~ A_c^-1 of the rest mesh, Newton-Schulz from a scaled identity;
+        // every step then refines it for the current mesh
+        if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS) return fail("cublasCreate failed");
+        void *ws = nullptr;
+        CK(A.alloc_bytes(ws, kCublasWorkspace));
+        if (cublasSetWorkspace(h->cublas, ws, kCublasWorkspace) != CUBLAS_STATUS_SUCCESS)
+            return fail("cublasSetWorkspace failed");
+        launch_elements(d, h->stream, ELEM_MATRIX_ONLY);
+        launch_assemble(d, h->stream);
+        if (refresh_coarse(h.get(), h->stream, kCoarseInitIterations, true)) return FFEA_GPU_ERROR;
+    }
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
     *out = h.release();
@@ -363,6 +422,29 @@ int ffea_gpu_phase_times(ffea_gpu_t *h, double out_ms[5])
     return FFEA_GPU_OK;
 }
 
+int ffea_gpu_preconditioner(ffea_gpu_t *h) { return h ? h->precond : -1; }
+
+int ffea_gpu_set_smoother_weights(ffea_gpu_t *h, int32_t blob, const float *omega)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    if (!omega) return fail("null weights");
+    if (!h->dev.coarse) return fail("smoother weights need the two-level preconditioner, which this handle does not use");
+    const BlobMap &map = h->host.maps[blob];
+    std::vector<float> &phi = h->host.phi;
+    for (int32_t n = 0; n < map.num_nodes_total; n++) {
+        const int32_t g = map.lin_of_orig[n];
+        if (g < 0) continue;
+        const float w = omega[n];
+        if (!(w > 0.f && w <= 2.f)) return fail("smoother weight of node %d is %g, outside (0, 2]", n, (double)w);
+        phi[4 * (size_t)g + 3] = w;
+    }
+    const BlobParams &bp = h->host.bp[blob];
+    CK(cudaMemcpyAsync(h->dev.phi + bp.node_off, phi.data() + 4 * (size_t)bp.node_off,
+                       4 * sizeof(float) * (size_t)bp.node_cnt, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FFEA_GPU_OK;
+}
+
 int ffea_gpu_sizes(ffea_gpu_t *h, int64_t *linear_nodes, int64_t *elements, int64_t *edges)
 {
     if (!h) return fail("null handle");
@@ -397,6 +479,7 @@ int enqueue_steps(ffea_gpu *h, int32_t nsteps, bool allow_direct)
         launch_elements(d, h->stream, ELEM_STEP);
         if (h->timing) CK(cudaEventRecord(h->ev[1], h->stream));
         if (d.any_nomass) launch_assemble(d, h->stream);
+        if (refresh_coarse(h, h->stream, 1, false)) return FFEA_GPU_ERROR;
         if (h->timing) CK(cudaEventRecord(h->ev[2], h->stream));
         launch_nodes(d, h->stream, 0);
         if (h->timing) CK(cudaEventRecord(h->ev[3], h->stream));
@@ -634,6 +717,7 @@ int ffea_gpu_solver_solve(ffea_gpu_t *h, int32_t blob, const double *pos, double
     CK(cudaMemcpyAsync(d.rhs, rhs.data(), rhs.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     launch_elements(d, h->stream, ELEM_MATRIX_ONLY);
     if (d.any_nomass) launch_assemble(d, h->stream);
+    if (refresh_coarse(h, h->stream, 1, false)) return FFEA_GPU_ERROR;
     launch_nodes(d, h->stream, 1);
     CK(launch_cg(d, h->stream));
     CK(cudaStreamSynchronize(h->stream));

@@ -1,0 +1,244 @@
+// coarse.cu -- the coarse space of the two-level CG preconditioner.
+//
+// Every CG segment (a compact block of one blob's rows, one per CTA of the
+// persistent solve) is an aggregate with six rigid modes: the translations
+// e_i and the rotations e_i x d_p, d_p = (x_p - c_s) / R_s the rest offset of
+// row p from the segment centroid.  Phi_p (3 x 6) holds them, so that
+// Phi_p^T v = (v, d_p x v) and Phi_p c = c_t + c_r x d_p.  The preconditioner
+// is M = diag(omega) D^-1 + P A_c^-1 P^T with A_c = P^T A P, the coarse
+// matrix of each blob (6 x segments square, dense).
+//
+//   k_coarse_assemble  A_c blocks (s, t) for the segments t coupled to s,
+//                      once per step (the matrix changes with the mesh)
+//   coarse_refresh     X ~ A_c^-1 by Newton-Schulz, X <- 2X - X A_c X (two
+//                      plain FP32 GEMMs through cuBLAS) from the previous
+//                      step's X; `init` starts from X = I / ||A_c||_inf and
+//                      iterates to convergence
+//
+// The matrix enters in the same difference form as the solver's SpMV:
+// (A v)_p = sum_q K_pq (v_q - v_p) + zeta_p v_p over the free rows.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "kernels.h"
+
+namespace ffea {
+
+namespace {
+
+constexpr int kAsmThreads = 256;
+constexpr int kAsmRows = CG_SEG_MAX_ROWS / kAsmThreads;  // rows per thread
+
+// C (6 x 6, row-major) += Phi_p^T K Phi_q for rest offsets dp, dq.
+__device__ __forceinline__ void add_block(float C[36], const float dp[3], const float K[9], const float dq[3])
+{
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+        // column m of Phi_q
+        float c0, c1, c2;
+        if (m < 3) {
+            c0 = m == 0;
+            c1 = m == 1;
+            c2 = m == 2;
+        } else if (m == 3) {  // e_x x d
+            c0 = 0.f;
+            c1 = -dq[2];
+            c2 = dq[1];
+        } else if (m == 4) {  // e_y x d
+            c0 = dq[2];
+            c1 = 0.f;
+            c2 = -dq[0];
+        } else {  // e_z x d
+            c0 = -dq[1];
+            c1 = dq[0];
+            c2 = 0.f;
+        }
+        const float v0 = K[0] * c0 + K[1] * c1 + K[2] * c2;
+        const float v1 = K[3] * c0 + K[4] * c1 + K[5] * c2;
+        const float v2 = K[6] * c0 + K[7] * c1 + K[8] * c2;
+        C[0 * 6 + m] += v0;
+        C[1 * 6 + m] += v1;
+        C[2 * 6 + m] += v2;
+        C[3 * 6 + m] += dp[1] * v2 - dp[2] * v1;
+        C[4 * 6 + m] += dp[2] * v0 - dp[0] * v2;
+        C[5 * 6 + m] += dp[0] * v1 - dp[1] * v0;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void load_K(const DeviceBatch &d, int base, int j, int lane, float K[9])
+{
+    const T *val = static_cast<const T *>(d.sell_val);
+    const size_t vb = (size_t)(base + 32 * j) * 9 + lane;
+#pragma unroll
+    for (int k = 0; k < 9; k++) K[k] = (float)val[vb + 32 * k];
+}
+
+// One CTA per segment s of a NoMass blob.  A row's slots are sorted by
+// column and segments are contiguous row ranges, so the slots of each coupled
+// segment t form one run: a cursor per row walks them once over the targets.
+// Each (s, t) block is a fixed-order block reduction (deterministic).
+template <typename T>
+__global__ void __launch_bounds__(kAsmThreads) k_coarse_assemble(DeviceBatch d)
+{
+    const int s = blockIdx.x;
+    const int b = d.seg_blob[s];
+    const BlobParams &bp = d.bp[b];
+    if (bp.solver != SOLVER_NOMASS) return;  // CTA-uniform
+    const int r0 = d.seg_row0[s], nrows = d.seg_rows[s];
+    const int nc = bp.coarse_n, ls = s - bp.seg_off;
+    float *Ac = d.coarse_A + bp.coarse_xoff;
+    const int lane32 = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ float red[36][kAsmThreads / 32];
+
+    int cursor[kAsmRows];
+#pragma unroll
+    for (int i = 0; i < kAsmRows; i++) cursor[i] = 0;
+    for (int k = d.seg_nbr_ptr[s]; k < d.seg_nbr_ptr[s + 1]; k++) {
+        const int t = d.seg_nbr[k];
+        float C[36];
+#pragma unroll
+        for (int i = 0; i < 36; i++) C[i] = 0.f;
+#pragma unroll
+        for (int i = 0; i < kAsmRows; i++) {
+            const int rr = threadIdx.x + i * kAsmThreads;
+            if (rr >= nrows) continue;
+            const int p = r0 + rr;
+            if (d.flags[p] & NODE_PINNED) continue;
+            const float4 fp = d.phi[p];
+            const float dp[3] = {fp.x, fp.y, fp.z};
+            const int sl = p >> 5, lane = p & 31;
+            const int L = d.slice_len[sl], base = d.slice_ptr[sl];
+            float K[9];
+            if (t == s) {
+                // diagonal of A in difference form: zeta_p I - sum_q K_pq
+                float S[9];
+#pragma unroll
+                for (int m = 0; m < 9; m++) S[m] = 0.f;
+                for (int j = 0; j < L; j++) {
+                    load_K<T>(d, base, j, lane, K);
+#pragma unroll
+                    for (int m = 0; m < 9; m++) S[m] -= K[m];
+                }
+                const float z = bp.calc_stokes == 1 ? (float)d.drag[p] : 0.f;
+                S[0] += z;
+                S[4] += z;
+                S[8] += z;
+                add_block(C, dp, S, dp);
+            }
+            int j = cursor[i];
+            while (j < L) {
+                const int q = d.sell_col[base + 32 * j + lane];
+                const int tq = d.seg_of_row[q];
+                if (tq > t) break;
+                if (tq == t && q != p && !(d.flags[q] & NODE_PINNED)) {
+                    load_K<T>(d, base, j, lane, K);
+                    const float4 fq = d.phi[q];
+                    const float dq[3] = {fq.x, fq.y, fq.z};
+                    add_block(C, dp, K, dq);
+                }
+                j++;
+            }
+            cursor[i] = j;
+        }
+        // fixed-order block reduction of the 36 entries
+#pragma unroll
+        for (int i = 0; i < 36; i++) {
+            float v = C[i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane32 == 0) red[i][warp] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < 36) {
+            float v = 0.f;
+            for (int w = 0; w < kAsmThreads / 32; w++) v += red[threadIdx.x][w];
+            const int li = threadIdx.x / 6, mi = threadIdx.x % 6, lt = t - bp.seg_off;
+            Ac[(size_t)(6 * ls + li) * nc + (6 * lt + mi)] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// X <- (X + X^T) / 2 over one blob's n x n matrix (src may alias nothing).
+__global__ void k_symmetrize(const float *__restrict__ src, float *__restrict__ dst, int n)
+{
+    const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || j >= n) return;
+    dst[(size_t)i * n + j] = 0.5f * (src[(size_t)i * n + j] + src[(size_t)j * n + i]);
+}
+
+// X = I / ||A||_inf (the Newton-Schulz start, convergent for an SPD A).
+__global__ void k_scaled_identity(const float *__restrict__ A, float *__restrict__ X, int n)
+{
+    __shared__ float red[32];
+    float m = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        float r = 0.f;
+        for (int j = 0; j < n; j++) r += fabsf(A[(size_t)i * n + j]);
+        m = fmaxf(m, r);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float mm = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) mm = fmaxf(mm, red[w]);
+        red[0] = mm > 0.f ? 1.f / mm : 1.f;
+    }
+    __syncthreads();
+    const float a = red[0];
+    for (size_t k = threadIdx.x; k < (size_t)n * n; k += blockDim.x) X[k] = (k / n == k % n) ? a : 0.f;
+}
+
+}  // namespace
+
+void launch_coarse_assemble(const DeviceBatch &d, cudaStream_t s)
+{
+    if (!d.coarse || d.n_segs == 0) return;
+    if (d.precision == PREC_FP64)
+        k_coarse_assemble<double><<<d.n_segs, kAsmThreads, 0, s>>>(d);
+    else
+        k_coarse_assemble<float><<<d.n_segs, kAsmThreads, 0, s>>>(d);
+    count_launches(1);
+}
+
+int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cublasHandle_t cb, cudaStream_t s,
+                   int iterations, bool init)
+{
+    if (!d.coarse) return 0;
+    if (cublasSetStream(cb, s) != CUBLAS_STATUS_SUCCESS) return -1;
+    const float one = 1.f, zero = 0.f, minus_one = -1.f, two = 2.f;
+    for (const BlobParams &bp : bps) {
+        const int n = bp.coarse_n;
+        if (bp.solver != SOLVER_NOMASS || n == 0) continue;
+        float *A = d.coarse_A + bp.coarse_xoff, *X = d.coarse_X + bp.coarse_xoff;
+        float *Tm = d.coarse_T, *Xn = d.coarse_Xn;
+        if (init) {
+            k_scaled_identity<<<1, 1024, 0, s>>>(A, X, n);
+            count_launches(1);
+        }
+        for (int it = 0; it < iterations; it++) {
+            // T = A X; Xn = 2 X - X T; X = sym(Xn).  The matrices are
+            // symmetric, so row- and column-major readings agree.
+            if (cublasSgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A, n, X, n, &zero, Tm, n) !=
+                CUBLAS_STATUS_SUCCESS)
+                return -1;
+            if (cudaMemcpyAsync(Xn, X, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+                return -1;
+            if (cublasSgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &minus_one, X, n, Tm, n, &two, Xn, n) !=
+                CUBLAS_STATUS_SUCCESS)
+                return -1;
+            dim3 grid((n + 255) / 256, n);
+            k_symmetrize<<<grid, 256, 0, s>>>(Xn, X, n);
+            count_launches(1);
+        }
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace ffea

@@ -159,6 +159,63 @@ int32_t plan_cg_segments(HostBatch &H)
     return (int32_t)H.seg_row0.size();
 }
 
+int64_t build_coarse(HostBatch &H)
+{
+    const int32_t nseg = (int32_t)H.seg_row0.size();
+    H.seg_of_row.assign(H.nl_pad, -1);
+    H.phi.assign(4 * (size_t)H.nl_pad, 0.f);
+    for (int32_t s = 0; s < nseg; s++) {
+        const int32_t r0 = H.seg_row0[s], n = H.seg_rows[s];
+        double c[3] = {0, 0, 0};
+        for (int32_t r = r0; r < r0 + n; r++)
+            for (int k = 0; k < 3; k++) c[k] += H.pos[3 * (size_t)r + k];
+        for (int k = 0; k < 3; k++) c[k] /= std::max(1, n);
+        double r2 = 0.0;
+        for (int32_t r = r0; r < r0 + n; r++)
+            for (int k = 0; k < 3; k++) {
+                const double dx = H.pos[3 * (size_t)r + k] - c[k];
+                r2 += dx * dx;
+            }
+        const double R = n > 0 && r2 > 0 ? std::sqrt(r2 / n) : 1.0;
+        for (int32_t r = r0; r < r0 + n; r++) {
+            H.seg_of_row[r] = s;
+            for (int k = 0; k < 3; k++) H.phi[4 * (size_t)r + k] = (float)((H.pos[3 * (size_t)r + k] - c[k]) / R);
+            H.phi[4 * (size_t)r + 3] = 1.f;
+        }
+    }
+    // couplings through the matrix pattern
+    H.seg_nbr_ptr.assign(nseg + 1, 0);
+    H.seg_nbr.clear();
+    const int32_t nslices = (int32_t)H.slice_len.size();
+    for (int32_t s = 0; s < nseg; s++) {
+        std::vector<int32_t> nb{s};
+        const int32_t r0 = H.seg_row0[s], n = H.seg_rows[s];
+        for (int32_t r = r0; r < r0 + n; r++) {
+            const int32_t sl = r / 32, lane = r % 32;
+            if (sl >= nslices) continue;
+            for (int32_t j = 0; j < H.slice_len[sl]; j++) {
+                const int32_t q = H.sell_col[H.slice_ptr[sl] + 32 * j + lane];
+                const int32_t t = H.seg_of_row[q];
+                if (t >= 0) nb.push_back(t);
+            }
+        }
+        std::sort(nb.begin(), nb.end());
+        nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+        H.seg_nbr.insert(H.seg_nbr.end(), nb.begin(), nb.end());
+        H.seg_nbr_ptr[s + 1] = (int32_t)H.seg_nbr.size();
+    }
+    int64_t coff = 0, xoff = 0;
+    for (int b = 0; b < H.num_blobs; b++) {
+        BlobParams &bp = H.bp[b];
+        bp.coarse_off = (int32_t)coff;
+        bp.coarse_n = 6 * bp.seg_cnt;
+        bp.coarse_xoff = (int32_t)xoff;
+        coff += bp.coarse_n;
+        xoff += (int64_t)bp.coarse_n * bp.coarse_n;
+    }
+    return xoff;
+}
+
 void ffea_seed_words(int32_t rng_seed, uint64_t out[6])
 {
     // sixseed[i] = (rand() + rand()) % twoMax[i/3] with a wrapping int sum

@@ -48,6 +48,12 @@ struct HostBatch {
     // per CTA of the persistent CG kernel (or several per CTA)
     std::vector<int32_t> seg_row0, seg_rows, seg_blob;
     std::vector<int32_t> parts;                            // CG segments per blob
+    // two-level preconditioner: segment of each padded row (-1 padding);
+    // per row (x - c_s) / R_s of its segment at rest and the smoother weight;
+    // per segment the sorted segments it couples to (itself included)
+    std::vector<int32_t> seg_of_row;
+    std::vector<float> phi;                                // 4 per padded row
+    std::vector<int32_t> seg_nbr_ptr, seg_nbr;
     int32_t num_streams = 0;
     std::vector<uint32_t> stream_state;                   // 6 per stream
     std::vector<mrg::JumpMat> stream_step;                // per stream: A^(draws per step)
@@ -71,6 +77,13 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
 // The CG segments of the batch (H.parts per blob, 32-row aligned row ranges):
 // fills H.seg_* and H.bp[b].seg_off / seg_cnt; returns the number of segments.
 int32_t plan_cg_segments(HostBatch &H);
+
+// Coarse-space data of the two-level preconditioner for the planned
+// segments (call after plan_cg_segments): seg_of_row, phi (smoother weight
+// 1), seg_nbr_*, and per blob coarse_off / coarse_n / coarse_xoff (6 rigid
+// modes per segment).  Returns the total size of the per-blob dense coarse
+// matrices (sum of coarse_n^2).
+int64_t build_coarse(HostBatch &H);
 
 // World::init's six seed words (src/World.cpp:299-305).
 void ffea_seed_words(int32_t rng_seed, uint64_t out[6]);

@@ -877,43 +877,52 @@ __device__ __forceinline__ DF df_warp_sum(DF v)
     return v;
 }
 
-// Partial sums of a CG segment: three quantities, each a (hi, lo) float pair,
-// in the 32 bytes of the segment's partials slot.  Per thread and per warp the
-// sums run in W; warp 0 adds the warp sums in FP64 (a butterfly over the
-// CTA's warps) and lane 0 splits the results.
-template <typename W>
-__device__ __forceinline__ void seg_partials(double *part, int seg, const W (&in)[3], int mask, double *smem_raw)
+// Partial sums of a CG segment, written to its slot P of the partials
+// buffer: three dot-product terms, each a (hi, lo) float pair in P[0..5]
+// (mask selects which), and NX plain FP32 sums in P[ex_off ..] (the
+// segment's coarse-space restrictions).  Per thread and per warp the dot
+// terms run in W; then warp k of the CTA combines quantity k over the warps,
+// the dot terms in double-float (FP32 pipes) or FP64, in parallel.
+template <typename W, int NX>
+__device__ __forceinline__ void seg_partials(float *P, const W (&in)[3], int mask, const float *ex, int ex_off,
+                                             double *smem_raw)
 {
+    static_assert(CG_THREADS / 32 >= 3 + NX, "one warp per combined quantity");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    W *smem = reinterpret_cast<W *>(smem_raw);
+    W *sw = reinterpret_cast<W *>(smem_raw);
+    float *sxs = reinterpret_cast<float *>(smem_raw + 3 * 32);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const W s = warp_sum<W>(in[k]);
-        if (lane == 0) smem[k * 32 + warp] = s;
+        if (lane == 0) sw[k * 32 + warp] = s;
+    }
+#pragma unroll
+    for (int k = 0; k < NX; k++) {
+        const float s = warp_sum<float>(ex[k]);
+        if (lane == 0) sxs[k * 32 + warp] = s;
     }
     __syncthreads();
-    if (warp == 0) {
-        float *P = reinterpret_cast<float *>(part) + 8 * (size_t)seg;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            if (!(mask & (1 << k))) continue;
+    if (warp < 3) {
+        if (mask & (1 << warp)) {
             float hi, lo;
             if (sizeof(W) == 4) {
-                // FP32 warp sums added in double-float on the FP32 pipes (an
-                // FP64 butterfly or conversion here costs ~0.5 us per phase)
-                const DF v = df_warp_sum(DF{lane < nw ? (float)smem[k * 32 + lane] : 0.f, 0.f});
+                const DF v = df_warp_sum(DF{lane < nw ? (float)sw[warp * 32 + lane] : 0.f, 0.f});
                 hi = v.hi;
                 lo = v.lo;
             } else {
-                const double a = warp_sum<double>(lane < nw ? (double)smem[k * 32 + lane] : 0.0);
+                const double a = warp_sum<double>(lane < nw ? (double)sw[warp * 32 + lane] : 0.0);
                 hi = (float)a;
                 lo = (float)(a - (double)hi);
             }
             if (lane == 0) {
-                P[2 * k] = hi;
-                P[2 * k + 1] = lo;
+                P[2 * warp] = hi;
+                P[2 * warp + 1] = lo;
             }
         }
+    } else if (warp < 3 + NX) {
+        const int k = warp - 3;
+        const float v = warp_sum<float>(lane < nw ? sxs[k * 32 + lane] : 0.f);
+        if (lane == 0) P[ex_off + k] = v;
     }
     __syncthreads();
 }
@@ -923,7 +932,8 @@ constexpr int kSumUnroll = 4;
 
 // Adds the partials of segments s0 + first, s0 + first + stride, ... (< cnt)
 // to a[0..2] in that order; kSumUnroll loads are issued before the adds.
-__device__ __forceinline__ void add_seg_partials(const double *part, int s0, int cnt, int first, int stride, DF a[3])
+__device__ __forceinline__ void add_seg_partials(const double *part, int slot4, int s0, int cnt, int first, int stride,
+                                                 DF a[3])
 {
     for (int t = first; t < cnt; t += kSumUnroll * stride) {
         float4 v01[kSumUnroll];
@@ -932,8 +942,8 @@ __device__ __forceinline__ void add_seg_partials(const double *part, int s0, int
         for (int u = 0; u < kSumUnroll; u++) {
             const int tt = t + u * stride;
             if (tt < cnt) {
-                v01[u] = __ldcg(reinterpret_cast<const float4 *>(part) + 2 * (size_t)(s0 + tt));
-                v2[u] = __ldcg(reinterpret_cast<const float2 *>(part) + 4 * (size_t)(s0 + tt) + 2);
+                v01[u] = __ldcg(reinterpret_cast<const float4 *>(part) + (size_t)slot4 * (s0 + tt));
+                v2[u] = __ldcg(reinterpret_cast<const float2 *>(part) + 2 * (size_t)slot4 * (s0 + tt) + 2);
             } else {
                 v01[u] = make_float4(0.f, 0.f, 0.f, 0.f);
                 v2[u] = make_float2(0.f, 0.f);
@@ -953,7 +963,7 @@ __device__ __forceinline__ void add_seg_partials(const double *part, int s0, int
 __device__ __forceinline__ void warp_blob_sums(const DeviceBatch &d, const double *part, int b, DF out[3])
 {
     DF a[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    add_seg_partials(part, d.bp[b].seg_off, d.bp[b].seg_cnt, threadIdx.x & 31, 32, a);
+    add_seg_partials(part, d.part_stride / 4, d.bp[b].seg_off, d.bp[b].seg_cnt, threadIdx.x & 31, 32, a);
 #pragma unroll
     for (int k = 0; k < 3; k++) out[k] = df_warp_sum(a[k]);
 }
@@ -967,7 +977,7 @@ __device__ __forceinline__ void block_blob_sums(const DeviceBatch &d, const doub
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     DF a[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    add_seg_partials(part, d.bp[b].seg_off, d.bp[b].seg_cnt, threadIdx.x, blockDim.x, a);
+    add_seg_partials(part, d.part_stride / 4, d.bp[b].seg_off, d.bp[b].seg_cnt, threadIdx.x, blockDim.x, a);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const DF s = df_warp_sum(a[k]);
@@ -989,7 +999,7 @@ __device__ __forceinline__ void block_blob_sums(const DeviceBatch &d, const doub
 // One CG transition of a blob from its three sums:
 //   ACTIVE   sums r.u, w.u, r.r: stop test, then alpha / beta of the next update
 //   VERIFY   sums r.u, -, |b - A x|^2: converged, or restart from that residual
-//   RESTART  sums -, w.u, -: alpha of the first restarted update, beta = 0
+//   RESTART  sums r.u, w.u, -: alpha of the first restarted update, beta = 0
 // Returns true when the blob stops (cg.state is then CONVERGED or FAILED) and
 // sets *fail_bits to the failure bits (0 if none).
 //
@@ -1068,15 +1078,19 @@ __device__ __forceinline__ bool transition_core(CgScalars &cg, const BlobParams 
             cg.state = CG_RESTART;
         }
     } else if (cg.state == CG_RESTART) {
+        // r.u of the restarted u (phase B of the restart step recomputes it,
+        // with the coarse correction where there is one)
         cg.state = CG_ACTIVE;
         cg.iters += 1;
         bool nan;
         if (fast) {
+            cg.gamma_f = sums[0].hi + sums[0].lo;
             cg.beta_f = 0.f;
             cg.pap_f = sums[1].hi + sums[1].lo;
             cg.alpha_f = cg.gamma_f / cg.pap_f;
             nan = !(cg.alpha_f == cg.alpha_f);
         } else {
+            cg.gamma = (double)sums[0].hi + (double)sums[0].lo;
             cg.beta = 0.0;
             cg.alpha = cg.gamma / ((double)sums[1].hi + (double)sums[1].lo);
             nan = !(cg.alpha == cg.alpha);
@@ -1203,13 +1217,34 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, i
 // all CTAs reach bit-identical states.  CTA 0 alone records failure bits.
 // Also refreshes the CTA's view (state, alpha, beta of its nb blobs) and
 // returns the number of blobs still iterating.
+//
+// With the coarse space (gv != nullptr; one blob per CTA) it also forms the
+// coarse residual of the CTA's blob for the next update, from the segment
+// restrictions of this iteration (slot floats 8.., 14.., 20..: P^T r_k,
+// P^T s_(k-1), P^T w_k): g = P^T r_(k+1) = P^T r_k - alpha (P^T w_k + beta
+// P^T s_(k-1)) with the new alpha and beta; after a failed true-residual
+// check (RESTART) g = P^T r of the true residual.
 template <typename T>
 __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const double *part, CgScalars *s_cg,
                                                      float *sm, unsigned int *s_run, int nb, const int *s_blob,
-                                                     int *s_state, T *s_alpha, T *s_beta)
+                                                     int *s_state, T *s_alpha, T *s_beta, float *gv)
 {
     const int nbl = d.num_blobs, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr bool fast = sizeof(T) == 4;
+    // coarse restrictions, loaded first so that they travel with the sums
+    float ptr = 0.f, pts = 0.f, ptw = 0.f;
+    int cb = -1;
+    if (gv) {
+        cb = s_blob[0];
+        const BlobParams &bp = d.bp[cb];
+        const int j = threadIdx.x;
+        if (j < bp.coarse_n) {
+            const float *slot = reinterpret_cast<const float *>(part) + (size_t)d.part_stride * (bp.seg_off + j / 6);
+            ptr = __ldcg(slot + 8 + j % 6);
+            pts = __ldcg(slot + 14 + j % 6);
+            ptw = __ldcg(slot + 20 + j % 6);
+        }
+    }
     if (nbl < 8) {
         // one blob after the other with the whole CTA; thread 0 (in warp 0,
         // which holds the sums) runs every transition
@@ -1250,6 +1285,13 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
         }
     }
     __syncthreads();
+    if (gv) {
+        const CgScalars &cg = s_cg[cb];
+        const int j = threadIdx.x;
+        if (j < d.bp[cb].coarse_n)
+            gv[j] = cg.state == CG_RESTART ? ptr : ptr - cg.alpha_f * (ptw + cg.beta_f * pts);
+        __syncthreads();
+    }
     return *s_run;
 }
 
@@ -1276,7 +1318,7 @@ template <typename T, bool REG>
 __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
 {
     using W = T;
-    __shared__ double red[3 * 32];
+    __shared__ double red[3 * 32 + 9 * 32];  // 3 dot terms (W) and up to 18 FP32 sums per warp
     __shared__ float sm_df[2 * 3 * 32];
     __shared__ int s_nt, s_nb, s_err, s_last[2];
     __shared__ unsigned int s_pub;
@@ -1329,9 +1371,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         }
         __syncthreads();
     };
-    // partials buffer of the current iteration
+    // partials buffer of the current iteration, and a segment's slot in it
     int parity = 0;
-    auto part = [&]() { return d.partials + (size_t)parity * 4 * d.n_segs; };
+    auto part = [&]() { return d.partials + (size_t)parity * (d.part_stride / 2) * d.n_segs; };
+    auto slot = [&](int seg) { return reinterpret_cast<float *>(part()) + (size_t)d.part_stride * seg; };
     refresh();
     using V4 = typename Vec4T<T>::type;
     using T2 = typename CgCache<T>::T2;
@@ -1403,6 +1446,58 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
         }
     }
+    // two-level preconditioner (REG and local only): per row the rest offset
+    // d_p and smoother weight, the CTA's 6 rows of X ~ A_c^-1, the blob's
+    // coarse residual g and this segment's coarse correction c
+    const bool coarse = REG && local && d.coarse;
+    float4 *phi_s = nullptr;
+    float *xrow = nullptr, *gv = nullptr, *cvec = nullptr;
+    int nc = 0;
+    if (coarse) {
+        size_t off = 6 * (size_t)CG_THREADS * sizeof(T) + (size_t)cc.JC * CG_THREADS * sizeof(int) +
+                     (size_t)cc.J * CG_THREADS * (4 * sizeof(T2) + sizeof(T));
+        off = (off + 15) & ~(size_t)15;
+        phi_s = reinterpret_cast<float4 *>(cg_dyn + off);
+        xrow = reinterpret_cast<float *>(phi_s + CG_THREADS);
+        gv = xrow + 6 * (size_t)d.coarse_nmax;
+        cvec = gv + d.coarse_nmax;
+        const BlobParams &bp = d.bp[s_blob[0]];
+        nc = bp.coarse_n;
+        phi_s[tid] = reg_valid ? d.phi[s_row0[0] + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float *Xg = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (S0 - bp.seg_off)) * nc;
+        for (int k = tid; k < 6 * nc; k += CG_THREADS) xrow[k] = Xg[k];
+    }
+    // c = the CTA's rows of X times g (after g is complete)
+    auto coarse_solve = [&]() {
+        const int lane = tid & 31, warp = tid >> 5;
+        if (warp < 6) {
+            float a = 0.f;
+            for (int k = lane; k < nc; k += 32) a = fmaf(xrow[warp * nc + k], gv[k], a);
+            a = warp_sum<float>(a);
+            if (lane == 0) cvec[warp] = a;
+        }
+        __syncthreads();
+    };
+    // u = omega D^-1 r + Phi_p c of the thread's row (REG, coarse)
+    auto coarse_u = [&](RowState<T> &S) {
+        const float4 f = phi_s[tid];
+        const float cx = cvec[3], cy = cvec[4], cz = cvec[5];
+        const T pc[3] = {(T)(cvec[0] + cy * f.z - cz * f.y), (T)(cvec[1] + cz * f.x - cx * f.z),
+                         (T)(cvec[2] + cx * f.y - cy * f.x)};
+#pragma unroll
+        for (int k = 0; k < 3; k++) S.u[k] = (T)f.w * sdinv[k * CG_THREADS + tid] * S.r[k] + pc[k];
+    };
+    // Phi_p^T v = (v, d_p x v) into ex[0..5]
+    auto restrict6 = [&](const T v[3], float *ex) {
+        const float4 f = phi_s[tid];
+        const float v0 = (float)v[0], v1 = (float)v[1], v2 = (float)v[2];
+        ex[0] = v0;
+        ex[1] = v1;
+        ex[2] = v2;
+        ex[3] = f.y * v2 - f.z * v1;
+        ex[4] = f.z * v0 - f.x * v2;
+        ex[5] = f.x * v1 - f.y * v0;
+    };
     auto row_info = [&](int j, int &row, bool &valid, T &diag, bool &nomass) {
         if (REG) {
             row = s_row0[0] + tid;
@@ -1430,6 +1525,14 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     // r -= alpha s; u = D^-1 r.  Partials: slot 0 r.u, slot 2 r.r.
     auto phase_a = [&](int j) {
         const int k = s_tslot[j];
+        if (coarse && s_state[k] == CG_RESTART) {
+            // restart from the true residual: u = M r, published for phase B
+            if (reg_valid) {
+                coarse_u(reg);
+                U4[s_row0[0] + tid] = V4{reg.u[0], reg.u[1], reg.u[2], (T)0};
+            }
+            return;
+        }
         if (s_state[k] != CG_ACTIVE) return;  // CTA-uniform
         int row;
         bool valid, nomass = true;
@@ -1449,6 +1552,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                 xref(S, cc2) += a * S.p[cc2];
                 S.r[cc2] -= a * S.s[cc2];
                 S.u[cc2] = dinv_of(S, cc2) * S.r[cc2];
+            }
+            if (coarse) coarse_u(S);
+#pragma unroll
+            for (int cc2 = 0; cc2 < 3; cc2++) {
                 pg += S.r[cc2] * S.u[cc2];
                 pr += S.r[cc2] * S.r[cc2];
             }
@@ -1456,7 +1563,17 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         }
         if (!REG && valid) store_row<T>(d, row, loc);
         const W in[3] = {pg, (W)0, pr};
-        seg_partials<W>(part(), S0 + j, in, 5, red);
+        if (coarse) {
+            // restrictions of the new r and s: slot floats 8.. and 14..
+            float ex[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+            if (valid) {
+                restrict6(S.r, ex);
+                restrict6(S.s, ex + 6);
+            }
+            seg_partials<W, 12>(slot(S0 + j), in, 5, ex, 8, red);
+        } else {
+            seg_partials<W, 0>(slot(S0 + j), in, 5, nullptr, 0, red);
+        }
     };
     // phase B of segment j: ACTIVE / RESTART and the prologue: w = A u, slot 1
     // w.u (the prologue and RESTART also fill slots 0 and 2); VERIFY: the
@@ -1498,12 +1615,33 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
         }
         if (!REG && valid) store_row<T>(d, row, loc);
-        if (state == CG_VERIFY) {
+        if (coarse) {
+            // restrictions: ACTIVE P^T w (slot floats 20..); the prologue,
+            // RESTART and VERIFY restart the coarse recurrence: P^T r, 0, P^T w
+            float ex[18];
+#pragma unroll
+            for (int m = 0; m < 18; m++) ex[m] = 0.f;
+            const bool full = prologue || state != CG_ACTIVE;
+            if (valid) {
+                if (full) restrict6(S.r, ex);
+                if (state != CG_VERIFY) restrict6(S.w, ex + 12);
+            }
+            if (state == CG_VERIFY) {
+                const double in[3] = {vg, 0.0, vr};
+                seg_partials<double, 18>(slot(S0 + j), in, 5, ex, 8, red);
+            } else if (full) {
+                const W in[3] = {pg, pd, pr};
+                seg_partials<W, 18>(slot(S0 + j), in, 7, ex, 8, red);
+            } else {
+                const W in[3] = {pg, pd, pr};
+                seg_partials<W, 6>(slot(S0 + j), in, 2, ex + 12, 20, red);
+            }
+        } else if (state == CG_VERIFY) {
             const double in[3] = {vg, 0.0, vr};
-            seg_partials<double>(part(), S0 + j, in, 5, red);
+            seg_partials<double, 0>(slot(S0 + j), in, 5, nullptr, 0, red);
         } else {
             const W in[3] = {pg, pd, pr};
-            seg_partials<W>(part(), S0 + j, in, (prologue || state == CG_RESTART) ? 7 : 2, red);
+            seg_partials<W, 0>(slot(S0 + j), in, (prologue || state == CG_RESTART) ? 7 : 2, nullptr, 0, red);
         }
     };
 
@@ -1513,21 +1651,48 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         if (!local) return reducing_barrier(d, &s_err, &s_pub, s_last, sm_df);
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) return 0u;
-        return local_reduce<T>(d, part(), s_cg, sm_df, &s_run, nb, s_blob, s_state, s_alpha, s_beta);
+        return local_reduce<T>(d, part(), s_cg, sm_df, &s_run, nb, s_blob, s_state, s_alpha, s_beta,
+                               coarse ? gv : nullptr);
     };
-    // publish u of the own rows for the neighbours (the k_nodes start value;
-    // zero on pinned rows) before the first product
+    if (coarse) {
+        // u_0 = M r_0 needs P^T r_0 of every segment of the blob: restrict
+        // into the second partials buffer, sum after a barrier, solve
+        parity = 1;
+        {
+            float ex[6] = {0, 0, 0, 0, 0, 0};
+            if (reg_valid) restrict6(reg.r, ex);
+            const W none[3] = {(W)0, (W)0, (W)0};
+            seg_partials<W, 6>(slot(S0), none, 0, ex, 8, red);
+        }
+        counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
+        if (!s_err) {
+            const BlobParams &bp = d.bp[s_blob[0]];
+            if (tid < nc) gv[tid] = __ldcg(slot(bp.seg_off + tid / 6) + 8 + tid % 6);
+            __syncthreads();
+            coarse_solve();
+            if (reg_valid) coarse_u(reg);
+        }
+        parity = 0;
+    }
+    // publish u of the own rows for the neighbours (the k_nodes start value,
+    // zero on pinned rows; with the coarse space u_0 = M r_0) before the
+    // first product
     for (int j = 0; j < nt; j++) {
         const int row = s_row0[j] + tid;
         if (tid < s_rows[j]) {
-            const T *u = static_cast<const T *>(d.u) + 3 * (size_t)row;
-            U4[row] = V4{u[0], u[1], u[2], (T)0};
+            if (coarse) {
+                U4[row] = reg_valid ? V4{reg.u[0], reg.u[1], reg.u[2], (T)0} : V4{(T)0, (T)0, (T)0, (T)0};
+            } else {
+                const T *u = static_cast<const T *>(d.u) + 3 * (size_t)row;
+                U4[row] = V4{u[0], u[1], u[2], (T)0};
+            }
         }
     }
     counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
     if (!s_err)
         for (int j = 0; j < nt; j++) phase_b(j, true);
     unsigned int running = s_err ? 0u : reduce();
+    if (coarse && running) coarse_solve();
     long long loops = 0;
     while (!s_err && running > 0) {
         if (local) parity ^= 1;
@@ -1539,6 +1704,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         for (int j = 0; j < nt; j++) phase_b(j, false);
         loops++;
         running = reduce();
+        if (coarse && running) coarse_solve();
     }
     publish_x();
     if (local && c == 0)
@@ -1761,7 +1927,7 @@ void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs)
 }
 
 template <typename T>
-static int cg_smem_plan_t(int max_slots, int max_cols, int *J, int *JC, size_t *dyn_bytes)
+static int cg_smem_plan_t(int max_slots, int max_cols, size_t extra_bytes, int *J, int *JC, size_t *dyn_bytes)
 {
     int dev = 0, optin = 0;
     *J = *JC = 0;
@@ -1772,24 +1938,24 @@ static int cg_smem_plan_t(int max_slots, int max_cols, int *J, int *JC, size_t *
     if (cudaFuncGetAttributes(&fa, k_cg<T, true>) != cudaSuccess) return -1;
     const size_t reserve = 1024;  // per-CTA system use
     const size_t state = 6 * (size_t)CG_THREADS * sizeof(T);  // x and D^-1
-    const size_t fixed = fa.sharedSizeBytes + reserve + state;
+    const size_t fixed = fa.sharedSizeBytes + reserve + state + extra_bytes;
     if ((size_t)optin < fixed) return -1;
     size_t room = optin - fixed;
     const size_t per_col = (size_t)CG_THREADS * sizeof(int), per_slot = (size_t)CG_THREADS * 9 * sizeof(T);
     *JC = (int)std::min<size_t>(room / per_col, (size_t)std::max(0, max_cols));
     room -= (size_t)*JC * per_col;
     *J = (int)std::min<size_t>(room / per_slot, (size_t)std::max(0, std::min(max_slots, *JC)));
-    *dyn_bytes = state + (size_t)*JC * per_col + (size_t)*J * per_slot;
+    *dyn_bytes = state + (size_t)*JC * per_col + (size_t)*J * per_slot + extra_bytes;
     if (cudaFuncSetAttribute(k_cg<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*dyn_bytes) !=
         cudaSuccess)
         return -1;
     return 0;
 }
 
-int cg_smem_plan(int precision, int max_slots, int max_cols, int *J, int *JC, size_t *dyn_bytes)
+int cg_smem_plan(int precision, int max_slots, int max_cols, size_t extra_bytes, int *J, int *JC, size_t *dyn_bytes)
 {
-    return precision == PREC_FP64 ? cg_smem_plan_t<double>(max_slots, max_cols, J, JC, dyn_bytes)
-                                  : cg_smem_plan_t<float>(max_slots, max_cols, J, JC, dyn_bytes);
+    return precision == PREC_FP64 ? cg_smem_plan_t<double>(max_slots, max_cols, extra_bytes, J, JC, dyn_bytes)
+                                  : cg_smem_plan_t<float>(max_slots, max_cols, extra_bytes, J, JC, dyn_bytes);
 }
 
 int cg_max_grid(int precision, int reg, size_t dyn_bytes)

@@ -3,7 +3,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "layout.h"
+
+struct cublasContext;  // cublas_v2.h: cublasHandle_t is a cublasContext *
 
 namespace ffea {
 
@@ -20,6 +24,15 @@ struct DeviceBatch {
     int32_t cg_local = 0;         // 1: every CTA reduces the dot products itself (few segments and blobs)
     int32_t cg_cache_slots = 0;   // REG: matrix slots per row whose values are copied to shared memory
     int32_t cg_cache_cols = 0;    // REG: matrix slots per row whose column indices are copied
+    int32_t part_stride = 8;      // floats per segment slot of the CG partials (32 with the coarse space)
+    // two-level preconditioner (REG and local reduction, NoMass, mixed precision)
+    int32_t coarse = 0;           // 1: u = diag(omega) D^-1 r + P A_c^-1 P^T r
+    int32_t coarse_nmax = 0;      // largest coarse dimension of a blob
+    float4 *phi = nullptr;        // per padded row: rest offset from the segment centroid / R, smoother weight
+    int32_t *seg_of_row = nullptr;
+    int32_t *seg_nbr_ptr = nullptr, *seg_nbr = nullptr;   // segments coupled to each segment (itself included)
+    float *coarse_A = nullptr, *coarse_X = nullptr;       // per blob: A_c and X ~ A_c^-1 (coarse_xoff)
+    float *coarse_T = nullptr, *coarse_Xn = nullptr;      // Newton-Schulz scratch (coarse_nmax^2)
     int32_t cg_dyn_smem = 0;      // REG: dynamic shared memory bytes of that copy
     // blobs
     BlobParams *bp = nullptr;
@@ -54,7 +67,7 @@ struct DeviceBatch {
     void *sell_mval = nullptr;    // mass matrix: 1 T per entry
     void *mass_diag = nullptr;    // T per node
     // reductions / status
-    double *partials = nullptr;     // 4 per node tile (node kernel); CG: two buffers of 4 per segment
+    double *partials = nullptr;     // 4 per node tile (node kernel); CG: two buffers of part_stride floats per segment
     CgScalars *cg = nullptr;        // per blob
     unsigned int *counters = nullptr;  // one per reduction site
     unsigned int *bar = nullptr;    // grid barrier: arrival count, generation
@@ -92,9 +105,16 @@ void launch_rng_draws(const mrg::JumpMat *table, const uint32_t *state, uint64_t
                       cudaStream_t s);
 // Shared-memory plan of the register-resident CG kernel on the current
 // device: column indices of JC slots per row (at most max_cols) and values of
-// J slots (at most max_slots), plus x and D^-1; dyn_bytes is the dynamic
-// shared memory that takes (also set as the kernel's limit).  -1 on error.
-int cg_smem_plan(int precision, int max_slots, int max_cols, int *J, int *JC, size_t *dyn_bytes);
+// J slots (at most max_slots), plus x and D^-1 and extra_bytes (the coarse
+// space); dyn_bytes is the dynamic shared memory that takes (also set as the
+// kernel's limit).  -1 on error.
+int cg_smem_plan(int precision, int max_slots, int max_cols, size_t extra_bytes, int *J, int *JC, size_t *dyn_bytes);
+// Two-level preconditioner (coarse.cu): the coarse matrices of the current
+// mesh, and `iterations` Newton-Schulz updates of X ~ A_c^-1 per blob
+// (`init`: from I / ||A_c||_inf).  0 on success.
+void launch_coarse_assemble(const DeviceBatch &d, cudaStream_t s);
+int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, ::cublasContext *cb, cudaStream_t s,
+                   int iterations, bool init);
 // CTAs of the persistent CG kernel (register-resident variant with dyn_bytes
 // of dynamic shared memory, or not) that fit co-resident on the current
 // device, 0 on error

@@ -44,6 +44,8 @@ struct BlobParams {
     int32_t elem_off, elem_cnt, elem_pad;   // padded element range
     int32_t tile_off, tile_cnt;             // node tiles (CTAs) of this blob
     int32_t seg_off, seg_cnt;               // CG segments of this blob
+    int32_t coarse_off, coarse_n;           // two-level: first coarse dof, number of coarse dofs (6 per segment)
+    int32_t coarse_xoff;                    // offset of the blob's dense coarse matrices (coarse_n^2 floats)
     int32_t num_nodes_total;                // N_t of the reference (linear + secondary)
     int32_t true_residual;
 };

@@ -53,9 +53,12 @@ def _mesh_struct(keep: _Keep, pos, topology, material, drag=None, pinned=None, v
                   len(pins), L.ptr(pins, L._ip))
 
 
-def _params_struct(p: SimulationParams, true_residual: int = 0) -> L.Params:
+PRECOND_JACOBI, PRECOND_TWO_LEVEL, PRECOND_LEARNED = 0, 1, 2
+
+
+def _params_struct(p: SimulationParams, true_residual: int = 0, preconditioner: int = PRECOND_JACOBI) -> L.Params:
     return L.Params(p.dt, p.kT, p.epsilon2, p.max_iterations_cg, p.calc_noise, p.calc_stokes, p.solver, p.precision,
-                    p.rng_seed, true_residual)
+                    p.rng_seed, true_residual, preconditioner)
 
 
 class World:
@@ -67,7 +70,7 @@ class World:
     """
 
     def __init__(self, blobs: Sequence, rng_mode: int = RNG_PER_BLOB, true_residual: bool = False,
-                 graph: bool = True, velocities: Sequence | None = None):
+                 graph: bool = True, velocities: Sequence | None = None, preconditioner: int = PRECOND_JACOBI):
         keep = _Keep()
         meshes, params = [], []
         self.num_nodes = []
@@ -81,7 +84,7 @@ class World:
             vel = None if velocities is None else velocities[i]
             meshes.append(_mesh_struct(keep, pos, topo, get("material"), get("drag"), get("pinned"), vel))
             p = get("params")
-            params.append(_params_struct(p, int(true_residual)))
+            params.append(_params_struct(p, int(true_residual), int(preconditioner)))
             self.num_nodes.append(len(np.asarray(pos).reshape(-1, 3)))
             self.num_elements.append(len(np.asarray(topo).reshape(-1, 10)))
             self.solvers.append(p.solver)
@@ -154,6 +157,16 @@ class World:
 
     def stream(self) -> int:
         return L.lib().ffea_gpu_stream(self._h) or 0
+
+    def preconditioner(self) -> int:
+        """The preconditioner the solves use (PRECOND_*), after fall-backs."""
+        return int(L.lib().ffea_gpu_preconditioner(self._h))
+
+    def set_smoother_weights(self, blob: int, omega) -> None:
+        """Per-node Jacobi weights of the learned preconditioner (blob node order)."""
+        w = np.ascontiguousarray(omega, dtype=np.float32)
+        L.check(L.lib().ffea_gpu_set_smoother_weights(self._h, int(blob), w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+                "ffea_gpu_set_smoother_weights")
 
     def blob(self, i: int) -> "Blob":
         return Blob(self, i)

@@ -43,6 +43,17 @@ extern "C" {
 
 #define FFEA_GPU_PRECISION_FP64 0  /* every kernel in FP64 */
 #define FFEA_GPU_PRECISION_MIXED 1 /* FP32 element forces and SpMV; FP64 positions, dots, residuals */
+/* Preconditioner of the NoMass CG solve.  JACOBI is NoMassCGSolver's
+ * (src/NoMassCGSolver.cpp:278-291).  TWO_LEVEL adds a coarse correction
+ * P A_c^-1 P^T r over six rigid modes per CG segment (a compact block of
+ * about a thousand nodes), LEARNED also weights the Jacobi term per node by
+ * ffea_gpu_set_smoother_weights.  Both stop on the same residual test; they
+ * apply to NoMass blobs in mixed precision on the register-resident solve
+ * path and fall back to JACOBI elsewhere (ffea_gpu_preconditioner reports
+ * which). */
+#define FFEA_GPU_PRECOND_JACOBI 0
+#define FFEA_GPU_PRECOND_TWO_LEVEL 1
+#define FFEA_GPU_PRECOND_LEARNED 2
 
 #define FFEA_GPU_RNG_PER_BLOB 0    /* each blob draws from its own stream, seeded from its rng_seed */
 #define FFEA_GPU_RNG_SHARED 1      /* all blobs share stream 0 in FFEA's single-thread draw order */
@@ -74,6 +85,7 @@ typedef struct {
     int32_t precision;          /* FFEA_GPU_PRECISION_* */
     int32_t rng_seed;           /* SimulationParams::rng_seed, seeded as World::init does */
     int32_t true_residual;      /* 1: confirm every solve with an FP64 true residual */
+    int32_t preconditioner;     /* FFEA_GPU_PRECOND_*; the same for every blob of a batch */
 } ffea_gpu_params;
 
 /* --- handle lifetime ----------------------------------------------------- */
@@ -194,6 +206,16 @@ int64_t ffea_gpu_kernel_launches(void);
 
 /* Sizes of a handle: total linear nodes, elements and edges across blobs. */
 int ffea_gpu_sizes(ffea_gpu_t *h, int64_t *linear_nodes, int64_t *elements, int64_t *edges);
+
+/* The preconditioner the handle's solves use (FFEA_GPU_PRECOND_*), after the
+ * fall-back rules above; -1 on a null handle.  No reference counterpart. */
+int ffea_gpu_preconditioner(ffea_gpu_t *h);
+
+/* Per-node weights of the Jacobi term of the LEARNED preconditioner for one
+ * blob: omega[num_nodes] in the blob's node order (secondary nodes ignored),
+ * each in (0, 2].  Takes effect from the next solve.  No reference
+ * counterpart. */
+int ffea_gpu_set_smoother_weights(ffea_gpu_t *h, int32_t blob, const float *omega);
 
 /* Per-phase timing of the last ffea_gpu_step call, measured with CUDA events
  * on the handle's stream (milliseconds): elements, assembly, node gather,
