@@ -102,6 +102,10 @@ struct ffea_gpu {
     DeviceArena arena;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t step_exec = nullptr;
+    cudaGraphExec_t step_exec_coarse = nullptr;  // the step with the coarse-space refresh
+    int64_t fixed_per_step_coarse = 0;
+    int coarse_every = 10;                       // steps between coarse-space refreshes
+    int64_t steps_done = 0;
     int graph_mode = 1;
     int timing = 0;
     double phase_ms[5] = {0, 0, 0, 0, 0};
@@ -115,6 +119,7 @@ struct ffea_gpu {
     {
         if (cublas) cublasDestroy(cublas);
         if (step_exec) cudaGraphExecDestroy(step_exec);
+        if (step_exec_coarse) cudaGraphExecDestroy(step_exec_coarse);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
@@ -137,7 +142,13 @@ int refresh_coarse(ffea_gpu *h, cudaStream_t s, int iterations, bool init)
     return FFEA_GPU_OK;
 }
 
-int build_step_graph(ffea_gpu *h)
+// Whether this step refreshes the coarse space (the first of every
+// coarse_every steps; the matrix moves little from step to step and the
+// refresh keeps X an inverse of a recent coarse matrix, which is what the
+// preconditioner needs).
+bool coarse_step(const ffea_gpu *h) { return h->dev.coarse && h->steps_done % h->coarse_every == 0; }
+
+int capture_step_graph(ffea_gpu *h, bool with_coarse, cudaGraphExec_t *out, int64_t *fixed)
 {
     DeviceBatch &d = h->dev;
     cudaStream_t s = h->stream;
@@ -145,7 +156,7 @@ int build_step_graph(ffea_gpu *h)
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     launch_elements(d, s, ELEM_STEP);
     if (d.any_nomass) launch_assemble(d, s);
-    int rc = refresh_coarse(h, s, 1, false);
+    int rc = with_coarse ? refresh_coarse(h, s, 1, false) : FFEA_GPU_OK;
     launch_nodes(d, s, 0);
     cudaError_t le = launch_cg(d, s);
     launch_euler(d, s);
@@ -155,10 +166,18 @@ int build_step_graph(ffea_gpu *h)
         cudaGetLastError();
         return fail("capturing the step graph failed: %s / %s", cudaGetErrorString(le), cudaGetErrorString(ce));
     }
-    h->fixed_per_step = 4 + (d.any_nomass ? 1 : 0) + (d.coarse ? 2 : 0);
-    cudaError_t e = cudaGraphInstantiate(&h->step_exec, graph, 0);
+    *fixed = 4 + (d.any_nomass ? 1 : 0) + (with_coarse ? 2 : 0);
+    cudaError_t e = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail("cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+    return FFEA_GPU_OK;
+}
+
+int build_step_graph(ffea_gpu *h)
+{
+    if (capture_step_graph(h, false, &h->step_exec, &h->fixed_per_step)) return FFEA_GPU_ERROR;
+    if (h->dev.coarse && capture_step_graph(h, true, &h->step_exec_coarse, &h->fixed_per_step_coarse))
+        return FFEA_GPU_ERROR;
     return FFEA_GPU_OK;
 }
 
@@ -248,8 +267,9 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     bool coarse_ok = want != FFEA_GPU_PRECOND_JACOBI && H.precision == PREC_MIXED && !H.any_mass;
     for (const BlobParams &bp : H.bp) coarse_nmax = std::max(coarse_nmax, (int)bp.coarse_n);
     if (coarse_nmax > CG_THREADS) coarse_ok = false;
+    // phi per row, the CTA's six rows of X, c, and 6 x 32 reduction floats
     const size_t coarse_bytes =
-        coarse_ok ? 16 + 16 * (size_t)CG_THREADS + sizeof(float) * (7 * (size_t)coarse_nmax + 8) : 0;
+        coarse_ok ? 16 + 16 * (size_t)CG_THREADS + sizeof(float) * (6 * (size_t)coarse_nmax + 8 + 6 * 32) : 0;
     size_t dyn_bytes = 0;
     int cache_slots = 0, cache_cols = 0;
     if (cg_smem_plan(H.precision, max_slots, max_cols, coarse_bytes, &cache_slots, &cache_cols, &dyn_bytes) != 0)
@@ -273,7 +293,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
                  !(force_last && force_last[0] == '1');
     d.coarse = coarse_ok && d.cg_reg && d.cg_local;
     d.coarse_nmax = d.coarse ? coarse_nmax : 0;
-    d.part_stride = d.coarse ? 32 : 8;
+    d.part_stride = d.coarse ? 20 : 8;  // floats: DF dot terms 0..5; coarse P^T r 8..13, P^T w 14..19
     h->precond = d.coarse ? want : FFEA_GPU_PRECOND_JACOBI;
     d.num_blobs = H.num_blobs;
     d.nl_pad = H.nl_pad;
@@ -380,6 +400,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
         launch_elements(d, h->stream, ELEM_MATRIX_ONLY);
         launch_assemble(d, h->stream);
         if (refresh_coarse(h.get(), h->stream, kCoarseInitIterations, true)) return FFEA_GPU_ERROR;
+        if (const char *e = std::getenv("FFEA_GPU_COARSE_REFRESH")) h->coarse_every = std::max(1, std::atoi(e));
     }
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
@@ -469,8 +490,10 @@ int enqueue_steps(ffea_gpu *h, int32_t nsteps, bool allow_direct)
                 // fall back to direct launches when the graph cannot be built
                 h->graph_mode = 0;
             } else {
-                CK(cudaGraphLaunch(h->step_exec, h->stream));
-                count_launches(h->fixed_per_step);
+                const bool cs = coarse_step(h);
+                CK(cudaGraphLaunch(cs ? h->step_exec_coarse : h->step_exec, h->stream));
+                count_launches(cs ? h->fixed_per_step_coarse : h->fixed_per_step);
+                h->steps_done++;
                 continue;
             }
         }
@@ -479,7 +502,8 @@ int enqueue_steps(ffea_gpu *h, int32_t nsteps, bool allow_direct)
         launch_elements(d, h->stream, ELEM_STEP);
         if (h->timing) CK(cudaEventRecord(h->ev[1], h->stream));
         if (d.any_nomass) launch_assemble(d, h->stream);
-        if (refresh_coarse(h, h->stream, 1, false)) return FFEA_GPU_ERROR;
+        if (coarse_step(h) && refresh_coarse(h, h->stream, 1, false)) return FFEA_GPU_ERROR;
+        h->steps_done++;
         if (h->timing) CK(cudaEventRecord(h->ev[2], h->stream));
         launch_nodes(d, h->stream, 0);
         if (h->timing) CK(cudaEventRecord(h->ev[3], h->stream));
@@ -590,6 +614,7 @@ int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const dou
 {
     if (check_blob(h, blob)) return FFEA_GPU_ERROR;
     CK(cudaStreamSynchronize(h->stream));
+    if (pos) h->steps_done = 0;  // new positions: refresh the coarse space on the next step
     const BlobParams &bp = h->host.bp[blob];
     const BlobMap &map = h->host.maps[blob];
     const size_t n3 = 3 * (size_t)bp.node_cnt, off = 3 * (size_t)bp.node_off;

@@ -1218,31 +1218,58 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, i
 // Also refreshes the CTA's view (state, alpha, beta of its nb blobs) and
 // returns the number of blobs still iterating.
 //
-// With the coarse space (gv != nullptr; one blob per CTA) it also forms the
-// coarse residual of the CTA's blob for the next update, from the segment
-// restrictions of this iteration (slot floats 8.., 14.., 20..: P^T r_k,
-// P^T s_(k-1), P^T w_k): g = P^T r_(k+1) = P^T r_k - alpha (P^T w_k + beta
-// P^T s_(k-1)) with the new alpha and beta; after a failed true-residual
-// check (RESTART) g = P^T r of the true residual.
+// With the coarse space (cz.n > 0; one blob per CTA) it also forms the
+// CTA's coarse correction for the next update: thread j holds coarse dof j
+// of the blob, with h_j = (P^T s)_j carried from iteration to iteration, and
+// from the segment restrictions of this iteration (slot floats 8..: P^T r_k,
+// 14..: P^T w_k) computes h = P^T w_k + beta h, g = P^T r_(k+1) = P^T r_k -
+// alpha h with the new alpha and beta (after a failed true-residual check,
+// RESTART: g = P^T r of the true residual), then c = X g over the CTA's six
+// rows of X ~ A_c^-1 in one block reduction.
+struct CoarseCtx {
+    const float *xrow;  // the CTA's 6 rows of X, n floats each
+    float *cvec;        // c (6 floats)
+    float *red6;        // 6 x 32 floats of reduction scratch
+    int n;              // coarse dofs of the blob (0: no coarse space)
+};
+
+// c = X g, g_j held by thread j (zero beyond n): a 6-value block reduction.
+__device__ __forceinline__ void coarse_apply(const CoarseCtx &cz, float g)
+{
+    const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
+#pragma unroll
+    for (int l = 0; l < 6; l++) {
+        float v = j < cz.n ? cz.xrow[l * cz.n + j] * g : 0.f;
+        v = warp_sum<float>(v);
+        if (lane == 0) cz.red6[l * 32 + warp] = v;
+    }
+    __syncthreads();
+    if (warp < 6) {
+        const float v = warp_sum<float>(lane < (int)(blockDim.x >> 5) ? cz.red6[warp * 32 + lane] : 0.f);
+        if (lane == 0) cz.cvec[warp] = v;
+    }
+    __syncthreads();
+}
+
 template <typename T>
 __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const double *part, CgScalars *s_cg,
                                                      float *sm, unsigned int *s_run, int nb, const int *s_blob,
-                                                     int *s_state, T *s_alpha, T *s_beta, float *gv)
+                                                     int *s_state, T *s_alpha, T *s_beta, const CoarseCtx &cz,
+                                                     float &h)
 {
     const int nbl = d.num_blobs, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr bool fast = sizeof(T) == 4;
     // coarse restrictions, loaded first so that they travel with the sums
-    float ptr = 0.f, pts = 0.f, ptw = 0.f;
+    float ptr = 0.f, ptw = 0.f;
     int cb = -1;
-    if (gv) {
+    if (cz.n) {
         cb = s_blob[0];
         const BlobParams &bp = d.bp[cb];
         const int j = threadIdx.x;
         if (j < bp.coarse_n) {
             const float *slot = reinterpret_cast<const float *>(part) + (size_t)d.part_stride * (bp.seg_off + j / 6);
             ptr = __ldcg(slot + 8 + j % 6);
-            pts = __ldcg(slot + 14 + j % 6);
-            ptw = __ldcg(slot + 20 + j % 6);
+            ptw = __ldcg(slot + 14 + j % 6);
         }
     }
     if (nbl < 8) {
@@ -1285,12 +1312,19 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
         }
     }
     __syncthreads();
-    if (gv) {
+    if (cz.n) {
         const CgScalars &cg = s_cg[cb];
-        const int j = threadIdx.x;
-        if (j < d.bp[cb].coarse_n)
-            gv[j] = cg.state == CG_RESTART ? ptr : ptr - cg.alpha_f * (ptw + cg.beta_f * pts);
-        __syncthreads();
+        float g = 0.f;
+        if (threadIdx.x < cz.n) {
+            if (cg.state == CG_RESTART) {
+                h = 0.f;
+                g = ptr;
+            } else {
+                h = ptw + cg.beta_f * h;
+                g = ptr - cg.alpha_f * h;
+            }
+        }
+        coarse_apply(cz, g);
     }
     return *s_run;
 }
@@ -1451,33 +1485,22 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     // coarse residual g and this segment's coarse correction c
     const bool coarse = REG && local && d.coarse;
     float4 *phi_s = nullptr;
-    float *xrow = nullptr, *gv = nullptr, *cvec = nullptr;
-    int nc = 0;
+    float *cvec = nullptr;
+    float h_coarse = 0.f;  // (P^T s)_tid of the blob's coarse dof tid
+    CoarseCtx cz{};
     if (coarse) {
         size_t off = 6 * (size_t)CG_THREADS * sizeof(T) + (size_t)cc.JC * CG_THREADS * sizeof(int) +
                      (size_t)cc.J * CG_THREADS * (4 * sizeof(T2) + sizeof(T));
         off = (off + 15) & ~(size_t)15;
         phi_s = reinterpret_cast<float4 *>(cg_dyn + off);
-        xrow = reinterpret_cast<float *>(phi_s + CG_THREADS);
-        gv = xrow + 6 * (size_t)d.coarse_nmax;
-        cvec = gv + d.coarse_nmax;
+        float *xrow = reinterpret_cast<float *>(phi_s + CG_THREADS);
+        cvec = xrow + 6 * (size_t)d.coarse_nmax;
         const BlobParams &bp = d.bp[s_blob[0]];
-        nc = bp.coarse_n;
+        cz = CoarseCtx{xrow, cvec, cvec + 8, bp.coarse_n};
         phi_s[tid] = reg_valid ? d.phi[s_row0[0] + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float *Xg = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (S0 - bp.seg_off)) * nc;
-        for (int k = tid; k < 6 * nc; k += CG_THREADS) xrow[k] = Xg[k];
+        const float *Xg = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (S0 - bp.seg_off)) * bp.coarse_n;
+        for (int k = tid; k < 6 * bp.coarse_n; k += CG_THREADS) xrow[k] = Xg[k];
     }
-    // c = the CTA's rows of X times g (after g is complete)
-    auto coarse_solve = [&]() {
-        const int lane = tid & 31, warp = tid >> 5;
-        if (warp < 6) {
-            float a = 0.f;
-            for (int k = lane; k < nc; k += 32) a = fmaf(xrow[warp * nc + k], gv[k], a);
-            a = warp_sum<float>(a);
-            if (lane == 0) cvec[warp] = a;
-        }
-        __syncthreads();
-    };
     // u = omega D^-1 r + Phi_p c of the thread's row (REG, coarse)
     auto coarse_u = [&](RowState<T> &S) {
         const float4 f = phi_s[tid];
@@ -1564,13 +1587,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         if (!REG && valid) store_row<T>(d, row, loc);
         const W in[3] = {pg, (W)0, pr};
         if (coarse) {
-            // restrictions of the new r and s: slot floats 8.. and 14..
-            float ex[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-            if (valid) {
-                restrict6(S.r, ex);
-                restrict6(S.s, ex + 6);
-            }
-            seg_partials<W, 12>(slot(S0 + j), in, 5, ex, 8, red);
+            // restriction of the new r: slot floats 8..
+            float ex[6] = {0, 0, 0, 0, 0, 0};
+            if (valid) restrict6(S.r, ex);
+            seg_partials<W, 6>(slot(S0 + j), in, 5, ex, 8, red);
         } else {
             seg_partials<W, 0>(slot(S0 + j), in, 5, nullptr, 0, red);
         }
@@ -1616,25 +1636,26 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         }
         if (!REG && valid) store_row<T>(d, row, loc);
         if (coarse) {
-            // restrictions: ACTIVE P^T w (slot floats 20..); the prologue,
-            // RESTART and VERIFY restart the coarse recurrence: P^T r, 0, P^T w
-            float ex[18];
+            // restrictions: ACTIVE P^T w (slot floats 14..); the prologue,
+            // RESTART and VERIFY restart the coarse recurrence: P^T r (8..)
+            // and P^T w (14.., zero for VERIFY)
+            float ex[12];
 #pragma unroll
-            for (int m = 0; m < 18; m++) ex[m] = 0.f;
+            for (int m = 0; m < 12; m++) ex[m] = 0.f;
             const bool full = prologue || state != CG_ACTIVE;
             if (valid) {
                 if (full) restrict6(S.r, ex);
-                if (state != CG_VERIFY) restrict6(S.w, ex + 12);
+                if (state != CG_VERIFY) restrict6(S.w, ex + 6);
             }
             if (state == CG_VERIFY) {
                 const double in[3] = {vg, 0.0, vr};
-                seg_partials<double, 18>(slot(S0 + j), in, 5, ex, 8, red);
+                seg_partials<double, 12>(slot(S0 + j), in, 5, ex, 8, red);
             } else if (full) {
                 const W in[3] = {pg, pd, pr};
-                seg_partials<W, 18>(slot(S0 + j), in, 7, ex, 8, red);
+                seg_partials<W, 12>(slot(S0 + j), in, 7, ex, 8, red);
             } else {
                 const W in[3] = {pg, pd, pr};
-                seg_partials<W, 6>(slot(S0 + j), in, 2, ex + 12, 20, red);
+                seg_partials<W, 6>(slot(S0 + j), in, 2, ex + 6, 14, red);
             }
         } else if (state == CG_VERIFY) {
             const double in[3] = {vg, 0.0, vr};
@@ -1652,7 +1673,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) return 0u;
         return local_reduce<T>(d, part(), s_cg, sm_df, &s_run, nb, s_blob, s_state, s_alpha, s_beta,
-                               coarse ? gv : nullptr);
+                               cz, h_coarse);
     };
     if (coarse) {
         // u_0 = M r_0 needs P^T r_0 of every segment of the blob: restrict
@@ -1667,9 +1688,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (!s_err) {
             const BlobParams &bp = d.bp[s_blob[0]];
-            if (tid < nc) gv[tid] = __ldcg(slot(bp.seg_off + tid / 6) + 8 + tid % 6);
-            __syncthreads();
-            coarse_solve();
+            coarse_apply(cz, tid < cz.n ? __ldcg(slot(bp.seg_off + tid / 6) + 8 + tid % 6) : 0.f);
             if (reg_valid) coarse_u(reg);
         }
         parity = 0;
@@ -1692,7 +1711,6 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     if (!s_err)
         for (int j = 0; j < nt; j++) phase_b(j, true);
     unsigned int running = s_err ? 0u : reduce();
-    if (coarse && running) coarse_solve();
     long long loops = 0;
     while (!s_err && running > 0) {
         if (local) parity ^= 1;
@@ -1704,7 +1722,6 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         for (int j = 0; j < nt; j++) phase_b(j, false);
         loops++;
         running = reduce();
-        if (coarse && running) coarse_solve();
     }
     publish_x();
     if (local && c == 0)
