@@ -85,6 +85,11 @@ SIGNATURES = {
     "ffea_gpu_preconditioner": (ctypes.c_int, [ctypes.c_void_p]),
     "ffea_gpu_set_smoother_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32,
                                                      ctypes.POINTER(ctypes.c_float)]),
+    "ffea_gpu_mpnn_num_params": (ctypes.c_int, []),
+    "ffea_gpu_mpnn_apply": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "ffea_gpu_mpnn_loss_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), _dp,
+                                               ctypes.POINTER(ctypes.c_float)]),
+    "ffea_gpu_mpnn_probe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32] + [ctypes.POINTER(ctypes.c_float)] * 5),
     "ffea_gpu_energies_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 5 + [ctypes.c_int32, ctypes.c_int32,
                                                                           ctypes.c_void_p, ctypes.c_void_p]),
 }

@@ -114,6 +114,8 @@ struct ffea_gpu {
     size_t tsize = 4;
     std::vector<std::vector<double>> sec_vel;  // per blob: initial velocities of secondary nodes
     int precond = FFEA_GPU_PRECOND_JACOBI;     // in use, after fall-backs
+    MpnnBuffers mpnn;                          // learned smoother weights (allocated on first use)
+    bool mpnn_ready = false;
     cublasHandle_t cublas = nullptr;           // coarse-space GEMMs
     ~ffea_gpu()
     {
@@ -463,6 +465,107 @@ int ffea_gpu_set_smoother_weights(ffea_gpu_t *h, int32_t blob, const float *omeg
     CK(cudaMemcpyAsync(h->dev.phi + bp.node_off, phi.data() + 4 * (size_t)bp.node_off,
                        4 * sizeof(float) * (size_t)bp.node_cnt, cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    return FFEA_GPU_OK;
+}
+
+namespace {
+
+int mpnn_alloc(ffea_gpu *h)
+{
+    if (h->mpnn_ready) return FFEA_GPU_OK;
+    if (h->precond != FFEA_GPU_PRECOND_LEARNED) return fail("the network needs a handle with the LEARNED preconditioner");
+    DeviceBatch &d = h->dev;
+    DeviceArena &A = h->arena;
+    MpnnBuffers &B = h->mpnn;
+    const size_t n = d.nl_pad;
+    int coarse_total = 0;
+    for (const BlobParams &bp : h->host.bp) coarse_total += bp.coarse_n;
+    CK(A.alloc(B.x0, n * MPNN_FEATURES));
+    for (auto &hb : B.h) CK(A.alloc(hb, n * MPNN_HIDDEN));
+    CK(A.alloc(B.omega, n));
+    CK(A.alloc(B.v, n));
+    CK(A.alloc(B.e, n));
+    CK(A.alloc(B.gw, n));
+    CK(A.alloc(B.gvec, (size_t)coarse_total));
+    CK(A.alloc(B.cvec, (size_t)coarse_total));
+    CK(A.alloc(B.cta_sums, 3 * ((n + 127) / 128)));
+    CK(A.alloc(B.scal, 3));
+    for (float **p : {&B.dh, &B.dh2, &B.dself, &B.tbuf}) CK(A.alloc(*p, n * MPNN_HIDDEN));
+    CK(A.alloc(B.partial, ((n + 63) / 64) * (size_t)MPNN_NUM_PARAMS));
+    CK(A.alloc(B.theta, (size_t)MPNN_NUM_PARAMS));
+    CK(A.alloc(B.grad, (size_t)MPNN_NUM_PARAMS));
+    h->mpnn_ready = true;
+    return FFEA_GPU_OK;
+}
+
+int mpnn_upload(ffea_gpu *h, const float *theta)
+{
+    if (!theta) return fail("null network parameters");
+    if (mpnn_alloc(h)) return FFEA_GPU_ERROR;
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpyAsync(h->mpnn.theta, theta, sizeof(float) * MPNN_NUM_PARAMS, cudaMemcpyHostToDevice, h->stream));
+    return FFEA_GPU_OK;
+}
+
+}  // namespace
+
+int ffea_gpu_mpnn_num_params(void) { return MPNN_NUM_PARAMS; }
+
+int ffea_gpu_mpnn_apply(ffea_gpu_t *h, const float *theta)
+{
+    if (!h) return fail("null handle");
+    if (mpnn_upload(h, theta)) return FFEA_GPU_ERROR;
+    if (mpnn_forward(h->dev, h->mpnn, h->mpnn.theta, true, h->stream)) return fail("network forward pass failed");
+    CK(cudaStreamSynchronize(h->stream));
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_mpnn_loss_grad(ffea_gpu_t *h, const float *theta, double *loss, float *grad)
+{
+    if (!h) return fail("null handle");
+    if (mpnn_upload(h, theta)) return FFEA_GPU_ERROR;
+    MpnnBuffers &B = h->mpnn;
+    if (mpnn_forward(h->dev, B, B.theta, false, h->stream)) return fail("network forward pass failed");
+    if (mpnn_loss(h->dev, B, h->stream)) return fail("network loss failed");
+    if (grad && mpnn_backward(h->dev, B, B.theta, B.grad, h->stream)) return fail("network backward pass failed");
+    double sc[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(sc, B.scal, sizeof(sc), cudaMemcpyDeviceToHost, h->stream));
+    if (grad) CK(cudaMemcpyAsync(grad, B.grad, sizeof(float) * MPNN_NUM_PARAMS, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (loss) *loss = sc[0];
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_mpnn_probe(ffea_gpu_t *h, int32_t blob, const float *theta, const float *domega, float *features,
+                        float *omega, float *grad)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    if (mpnn_upload(h, theta)) return FFEA_GPU_ERROR;
+    DeviceBatch &d = h->dev;
+    MpnnBuffers &B = h->mpnn;
+    const BlobMap &map = h->host.maps[blob];
+    if (mpnn_forward(d, B, B.theta, false, h->stream)) return fail("network forward pass failed");
+    if (domega && grad) {
+        // dL/d omega = k1 * gw.x - k2 * gw.y with k1 = 1, k2 = 0: gw.x = domega
+        std::vector<float2> gw(d.nl_pad, make_float2(0.f, 0.f));
+        for (int32_t n = 0; n < map.num_nodes_total; n++)
+            if (map.lin_of_orig[n] >= 0) gw[map.lin_of_orig[n]].x = domega[n];
+        const double sc[3] = {0.0, 1.0, 0.0};
+        CK(cudaMemcpyAsync(B.gw, gw.data(), sizeof(float2) * gw.size(), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(B.scal, sc, sizeof(sc), cudaMemcpyHostToDevice, h->stream));
+        if (mpnn_backward(d, B, B.theta, B.grad, h->stream)) return fail("network backward pass failed");
+        CK(cudaMemcpyAsync(grad, B.grad, sizeof(float) * MPNN_NUM_PARAMS, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    std::vector<float> x0((size_t)d.nl_pad * MPNN_FEATURES), om(d.nl_pad);
+    CK(cudaMemcpy(x0.data(), B.x0, sizeof(float) * x0.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(om.data(), B.omega, sizeof(float) * om.size(), cudaMemcpyDeviceToHost));
+    for (int32_t n = 0; n < map.num_nodes_total; n++) {
+        const int32_t g = map.lin_of_orig[n];
+        for (int k = 0; k < MPNN_FEATURES; k++)
+            if (features) features[(size_t)n * MPNN_FEATURES + k] = g >= 0 ? x0[(size_t)g * MPNN_FEATURES + k] : 0.f;
+        if (omega) omega[n] = g >= 0 ? om[g] : 1.f;
+    }
     return FFEA_GPU_OK;
 }
 

@@ -1,5 +1,6 @@
 // kernels.h -- device buffers of a batch and the host-side launchers of its kernels.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -109,6 +110,31 @@ void launch_rng_draws(const mrg::JumpMat *table, const uint32_t *state, uint64_t
 // space); dyn_bytes is the dynamic shared memory that takes (also set as the
 // kernel's limit).  -1 on error.
 int cg_smem_plan(int precision, int max_slots, int max_cols, size_t extra_bytes, int *J, int *JC, size_t *dyn_bytes);
+// Learned smoother weights (learned.cu): a 3-layer mesh message-passing
+// network, hidden width 32, 8 input features per node.
+constexpr int MPNN_FEATURES = 8;
+constexpr int MPNN_HIDDEN = 32;
+constexpr int MPNN_NUM_PARAMS = 2 * MPNN_HIDDEN * MPNN_FEATURES + MPNN_HIDDEN +
+                                2 * (2 * MPNN_HIDDEN * MPNN_HIDDEN + MPNN_HIDDEN) + MPNN_HIDDEN + 1;
+struct MpnnBuffers {
+    float *x0 = nullptr;                    // features, 8 per padded row
+    __nv_bfloat16 *h[3] = {nullptr, nullptr, nullptr};  // activations, 32 per padded row
+    float *omega = nullptr;                 // per padded row
+    float4 *v = nullptr, *e = nullptr;      // D^-1 f and z = M f
+    float2 *gw = nullptr;                   // per row (Az.v, f.v): dL/d omega = k1 x - k2 y
+    float *gvec = nullptr, *cvec = nullptr; // coarse P^T f and X P^T f
+    double *cta_sums = nullptr, *scal = nullptr;   // 3 per forward CTA; loss, k1, k2
+    float *dh = nullptr, *dh2 = nullptr, *dself = nullptr, *tbuf = nullptr;  // 32 per padded row
+    float *partial = nullptr;               // per backward CTA: MPNN_NUM_PARAMS
+    float *theta = nullptr, *grad = nullptr;
+};
+// forward pass (omega; write_phi: also the smoother weights of the solve),
+// the loss of the last solve's (rhs, solution) pair, and the backward pass
+// into grad_dev.  0 on success.
+int mpnn_forward(const DeviceBatch &d, MpnnBuffers &B, const float *theta_dev, bool write_phi, cudaStream_t s);
+int mpnn_loss(const DeviceBatch &d, MpnnBuffers &B, cudaStream_t s);
+int mpnn_backward(const DeviceBatch &d, MpnnBuffers &B, const float *theta_dev, float *grad_dev, cudaStream_t s);
+
 // Two-level preconditioner (coarse.cu): the coarse matrices of the current
 // mesh, and `iterations` Newton-Schulz updates of X ~ A_c^-1 per blob
 // (`init`: from I / ||A_c||_inf).  0 on success.

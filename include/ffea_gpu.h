@@ -217,6 +217,33 @@ int ffea_gpu_preconditioner(ffea_gpu_t *h);
  * counterpart. */
 int ffea_gpu_set_smoother_weights(ffea_gpu_t *h, int32_t blob, const float *omega);
 
+/* --- learned smoother weights (no reference counterpart) --------------------
+ * A mesh message-passing network sets omega for every free node of every
+ * NoMass blob: 8 features per node from the current matrix and coarse
+ * layout, three layers h' = ReLU(Ws h + Wn mean(h over edge neighbours) + b)
+ * of width 32 (BF16 activations, FP32 weights and sums), omega = 2
+ * sigmoid(wo . h + bo).  theta holds ffea_gpu_mpnn_num_params() floats:
+ * per layer Ws (32 x din, row-major), Wn (32 x din), b (32) with din = 8, 32,
+ * 32; then wo (32), bo.  The handle must use the LEARNED preconditioner. */
+int ffea_gpu_mpnn_num_params(void);
+
+/* Evaluate the network on the current mesh and use its omega from the next
+ * solve on. */
+int ffea_gpu_mpnn_apply(ffea_gpu_t *h, const float *theta);
+
+/* Training signal from the last solve's (rhs f, solution x) pair, on that
+ * solve's matrix A and coarse inverse: loss = e^T A e / x^T f with
+ * e = x - M f, M the preconditioner with the network's omega; grad (may be
+ * NULL) = dloss/dtheta. */
+int ffea_gpu_mpnn_loss_grad(ffea_gpu_t *h, const float *theta, double *loss, float *grad);
+
+/* For testing the network against a CPU restatement: for blob `blob`, the
+ * features (8 per node) and omega (1 per node) of theta, in the blob's node
+ * order (zero / 1 on secondary and pinned nodes), and the gradient of
+ * sum_n domega[n] omega[n] with respect to theta (domega per node). */
+int ffea_gpu_mpnn_probe(ffea_gpu_t *h, int32_t blob, const float *theta, const float *domega, float *features,
+                        float *omega, float *grad);
+
 /* Per-phase timing of the last ffea_gpu_step call, measured with CUDA events
  * on the handle's stream (milliseconds): elements, assembly, node gather,
  * CG solve, update.  Only filled when timing was enabled. */
