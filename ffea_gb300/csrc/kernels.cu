@@ -1963,8 +1963,10 @@ static int cg_smem_plan_t(int max_slots, int max_cols, size_t extra_bytes, int *
     room -= (size_t)*JC * per_col;
     *J = (int)std::min<size_t>(room / per_slot, (size_t)std::max(0, std::min(max_slots, *JC)));
     *dyn_bytes = state + (size_t)*JC * per_col + (size_t)*J * per_slot + extra_bytes;
-    if (cudaFuncSetAttribute(k_cg<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*dyn_bytes) !=
-        cudaSuccess)
+    // the limit is a property of the kernel, shared by every handle: set it
+    // to the device maximum so that no handle's plan lowers another's
+    if (cudaFuncSetAttribute(k_cg<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin - (int)fa.sharedSizeBytes) != cudaSuccess)
         return -1;
     return 0;
 }

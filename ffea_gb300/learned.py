@@ -5,9 +5,12 @@ The network and its gradient run on the GPU inside the library
 maps 8 per-node features of the current matrix to a weight omega_p in (0, 2)
 of the Jacobi term of M = diag(omega) D^-1 + P A_c^-1 P^T.  Training pairs
 (rhs f, solution x) come from the NoMass solves of ordinary time steps, one
-pair per step, and the loss of a pair is the energy-norm error of one
-application of M: e^T A e / x^T f with e = x - M f.  The solve itself does
-not change: it stops on the same residual test with any omega.
+pair per step, and the loss of a pair is the energy-norm error of the best
+multiple of one application of M, relative to |x|_A:
+1 - (f.z)^2 / ((z.Az)(x.f)) with z = M f -- invariant to the scale of M, as
+CG is.  The solve itself does not change: it stops on the same residual
+test with any omega.  data/mpnn_weights.npz holds the weights trained by
+running this module (20,000 pairs over training_meshes()).
 
 This module holds the parameter layout (the same as the library's), the
 initialisation, Adam, the training loop and the weight file.
@@ -166,3 +169,35 @@ def load(path: str = WEIGHTS_FILE) -> np.ndarray:
     if theta.size != NUM_PARAMS:
         raise ValueError(f"{path}: {theta.size} parameters, expected {NUM_PARAMS}")
     return theta
+
+
+def training_meshes(count: int = 8, seed: int = 0):
+    """The training family: spheres of radius log-uniform in [5, 25] nm at the
+    1.25 nm cell, moduli scaled uniformly by [0.5, 2] around 3.7e8 / 1.1e9
+    Pa, NoMass CG to epsilon 1e-6 in mixed precision, one RNG seed each."""
+    from . import params as P
+    from .mesh import make_blob, sphere_mesh
+    rng = np.random.default_rng(seed)
+    radii = np.exp(rng.uniform(np.log(5.0), np.log(25.0), size=count))
+    out = []
+    for i, r in enumerate(radii):
+        g = float(rng.uniform(0.5, 2.0))
+        prm = P.SimulationParams.from_si(dt=1e-14, kT=P.kT_at(300.0) * P.MESO_ENERGY, epsilon=1e-6,
+                                         max_iterations_cg=10000, rng_seed=200 + i, solver=P.SOLVER_NOMASS,
+                                         precision=P.PRECISION_MIXED)
+        out.append(make_blob(sphere_mesh(float(r), seed=i), prm, shear_mod=3.7e8 * g, bulk_mod=1.1e9 * g))
+    return out
+
+
+if __name__ == "__main__":
+    # Regenerates data/mpnn_weights.npz: 20,000 (rhs, solution) pairs, one per
+    # time step, round-robin over the training family (needs a GPU).
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--pairs", type=int, default=20000)
+    ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--out", default=WEIGHTS_FILE)
+    a = ap.parse_args()
+    theta, losses = train(training_meshes(), pairs=a.pairs, lr=a.lr, log=print)
+    save(theta, a.out, pairs=a.pairs, losses=losses)
+    print(f"saved {a.out}: loss {losses[:100].mean():.5f} -> {losses[-100:].mean():.5f}")

@@ -108,3 +108,16 @@ def test_falls_back_to_jacobi(gpulib, case):
         assert w.preconditioner() == JACOBI
         w.run(2)
         assert w.blob(0).status()["fail_bits"] == 0
+
+
+def test_handles_with_different_plans_coexist(gpulib):
+    """The CG kernel's shared-memory plan depends on the mesh; handles with
+    different plans must be able to step in any order."""
+    a = spec(radius_nm=5.0, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    b = spec(radius_nm=9.0, seed=2, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    with _world([a], preconditioner=TWO_LEVEL) as wa, _world([b], preconditioner=JACOBI) as wb:
+        for _ in range(2):
+            wa.run(1)
+            wb.run(1)
+        assert wa.blob(0).status()["fail_bits"] == 0
+        assert wb.blob(0).status()["fail_bits"] == 0
