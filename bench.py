@@ -2,18 +2,22 @@
 """Throughput of FFEA's per-timestep blob update on GB300.
 
 Metric: node-steps/s (linear nodes advanced one timestep per second) with
-every CG solve run to relative residual 1e-6.
+every CG solve run to relative residual 1e-6 (confirmed by an FP64 true
+residual), for the learned two-level preconditioner (the headline `value`)
+and for plain Jacobi-PCG (`plain`), measured in the same run, with their
+ratios in `learned_vs_plain`.
 
 Workload (default): a 64^3-cell grid split into 6 tetrahedra per cell and
 cut to a 40 nm-radius sphere (146,737 linear nodes, 823,968 elements,
 1,135,891 nodes with the edge midpoints), node positions jittered by
 N(0, 0.05 cell) from a seed; density 1.5e3 kg/m^3, shear/bulk modulus
 3.7e8/1.1e9 Pa, shear/bulk viscosity 1e-3 Pa s, kT at 300 K, dt 1e-14 s,
-thermal noise on, Stokes drag on, CG_nomass solver with Jacobi-PCG to
-epsilon 1e-6, FP32 element forces and SpMV with FP64 dot products.
+thermal noise on, Stokes drag on, CG_nomass solver to epsilon 1e-6, FP32
+element forces and SpMV with double-float / FP64 reductions.
 Synthetic, seeded inputs stand in for a real protein mesh.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--precond learned|two-level|jacobi] [--no-plain]
 
 N > 1 runs under torchrun, one replica blob per GPU with its own RNG stream
 (the path does not shard a single blob: replicas only, weak scaling).
@@ -56,7 +60,9 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the cpu_baseline sample")
-    ap.add_argument("--precond", choices=sorted(PRECONDS), default="jacobi")
+    ap.add_argument("--precond", choices=sorted(PRECONDS), default="learned",
+                    help="preconditioner of the headline arm (plain Jacobi-PCG is measured beside it)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain Jacobi-PCG arm")
     return ap.parse_args()
 
 
@@ -78,7 +84,7 @@ def config_of(args, spec, world_size):
         "linear_nodes": int(m.num_linear),
         "elements": int(m.num_elements),
         "total_nodes": int(m.num_nodes),
-        "solver": "CG_nomass Jacobi-PCG, epsilon 1e-6, convergence confirmed by an FP64 true residual",
+        "solver": "CG_nomass, epsilon 1e-6, convergence confirmed by an FP64 true residual",
         "precision": "FP32 element forces + SpMV, FP64 positions/dots" if args.precision == "mixed" else "FP64",
         "noise": "on (MRG32k3a, RngStream-exact)",
         "replicas": world_size,
@@ -244,18 +250,18 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def run_gb300(args):
+def measure_arm(args, spec, precond: str, world: int, local: int):
+    """One arm on this rank: warm-up, K timed steps (device events on the
+    handle's stream, L2 flushed between steps), the end-to-end loop through
+    the C ABI with host buffers, and a profile pass with per-phase events."""
     import torch
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from ffea_gb300 import learned
     from ffea_gb300.world import World, kernel_launches
 
-    spec = build_spec(args.workload, rank, args.precision)
     N = spec.mesh.num_linear
-    w = World([spec], graph=True, true_residual=True, preconditioner=PRECONDS[args.precond])
+    w = World([spec], graph=True, true_residual=True, preconditioner=PRECONDS[precond])
+    if precond == "learned" and w.preconditioner() == PRECONDS["learned"]:
+        learned.apply(w, learned.load())
     nl, ne, nedges = w.sizes()
     stream = torch.cuda.ExternalStream(w.stream())
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -264,7 +270,7 @@ def run_gb300(args):
         if world > 1:
             torch.distributed.barrier()
 
-    w.run(max(args.warmup, 3) if args.warmup >= 0 else 3)
+    w.run(max(args.warmup, 3))
     K = args.steps
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
@@ -284,8 +290,7 @@ def run_gb300(args):
     torch.cuda.synchronize()
     barrier()
     clocks = sampler.stop()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(sum(step_ms))
+    total_ms = float(sum(s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)))
     loops = w.cg_loop_count() - loops0
     launches = kernel_launches() - launches0
     total_ms = max_over_ranks(total_ms, world)
@@ -302,12 +307,11 @@ def run_gb300(args):
         blob.set_nodes(pos, vel)
         w.run(1)
         pos, vel, _ = blob.get_nodes()
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(e2e_s, world)
-    e2e = {"value": aggregate_throughput(N, Ke, world, e2e_s), "unit": "node-steps/s", "h2d_bytes_per_step": 2 * 3 * 8 * N,
-           "d2h_bytes_per_step": 3 * 3 * 8 * N, "steps": Ke}
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": aggregate_throughput(N, Ke, world, e2e_s), "unit": "node-steps/s",
+           "h2d_bytes_per_step": 2 * 3 * 8 * N, "d2h_bytes_per_step": 3 * 3 * 8 * N, "steps": Ke}
 
-    # profile pass: direct launches with CUDA events around each kernel of a step
+    # profile pass: direct launches with CUDA events around each phase of a step
     prof_steps = 3
     loops_p0 = w.cg_loop_count()
     w.set_timing(True)
@@ -315,7 +319,39 @@ def run_gb300(args):
     phases = w.phase_times() / prof_steps
     w.set_timing(False)
     iters_p = (w.cg_loop_count() - loops_p0) / prof_steps
+    pc_used = {v: k for k, v in PRECONDS.items()}[w.preconditioner()]
+    w.close()
     cg_ms = float(phases[3])
+    return {
+        "value": value, "ms_per_step": total_ms / K, "e2e": e2e, "gpu_launches": int(launches),
+        "cg_iters_per_step": loops / K, "clocks": clocks, "preconditioner": pc_used,
+        "phase_ms_per_step": {"elements": float(phases[0]), "assemble": float(phases[1]),
+                              "nodes": float(phases[2]), "cg": cg_ms, "euler": float(phases[4])},
+        "cg_us_per_iteration": 1e3 * cg_ms / max(iters_p, 1), "cg_iters_profiled": iters_p,
+        "sizes": (nl, ne, nedges),
+    }
+
+
+def run_gb300(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    spec = build_spec(args.workload, rank, args.precision)
+    main_arm = measure_arm(args, spec, args.precond, world, local)
+    plain = None
+    if args.precond != "jacobi" and not args.no_plain:
+        plain = measure_arm(args, spec, "jacobi", world, local)
+    if rank != 0:
+        return
+    nl, ne, nedges = main_arm["sizes"]
+    # roofline of the dominant kernel (k_cg): the algorithmic bytes of its
+    # iterations over its measured duration
+    iters_p = main_arm["cg_iters_profiled"]
+    cg_ms = main_arm["phase_ms_per_step"]["cg"]
     alg = int(iters_p * cg_iteration_bytes(nl, nedges))
     peak, peak_kind = measured_peak()
     achieved = alg / (cg_ms / 1e3) / 1e9
@@ -324,25 +360,29 @@ def run_gb300(args):
                 "traffic": ncu_traffic(), "algorithmic_bytes_per_launch": alg,
                 "avg_launch_us": round(cg_ms * 1e3, 1), "cg_iters_per_launch": iters_p,
                 "bytes_per_iteration": cg_iteration_bytes(nl, nedges)}
-    if rank != 0:
-        w.close()
-        return
     line = {
-        "metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": K,
-        "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": main_arm["value"], "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": main_arm["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": config_of(args, spec, world), "e2e": e2e, "gpu_launches": int(launches),
-        "cg_iters_per_step": loops / K, "roofline": roofline, "clocks": clocks,
-        "phase_ms_per_step": {"elements": float(phases[0]), "assemble": float(phases[1]),
-                              "nodes": float(phases[2]), "cg": float(phases[3]), "euler": float(phases[4])},
-        "cg_us_per_iteration": 1e3 * cg_ms / max(iters_p, 1),
-        "preconditioner": {v: k for k, v in PRECONDS.items()}[w.preconditioner()],
+        "config": config_of(args, spec, world), "e2e": main_arm["e2e"], "gpu_launches": main_arm["gpu_launches"],
+        "preconditioner": main_arm["preconditioner"], "cg_iters_per_step": main_arm["cg_iters_per_step"],
+        "roofline": roofline, "clocks": main_arm["clocks"], "phase_ms_per_step": main_arm["phase_ms_per_step"],
+        "cg_us_per_iteration": main_arm["cg_us_per_iteration"],
     }
     line["config"]["edges"] = int(nedges)
+    line["config"]["solver"] = (f"CG_nomass, {main_arm['preconditioner']} preconditioner, epsilon 1e-6, "
+                                "convergence confirmed by an FP64 true residual")
+    if plain is not None:
+        line["plain"] = {k: plain[k] for k in ("value", "ms_per_step", "cg_iters_per_step", "cg_us_per_iteration",
+                                               "e2e", "clocks", "preconditioner")}
+        line["learned_vs_plain"] = {
+            "node_steps_ratio": main_arm["value"] / plain["value"],
+            "e2e_ratio": main_arm["e2e"]["value"] / plain["e2e"]["value"],
+            "iteration_ratio": plain["cg_iters_per_step"] / max(main_arm["cg_iters_per_step"], 1e-9),
+        }
     if world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(spec, args.cpu_seconds)
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
-    w.close()
     print(json.dumps(line), flush=True)
 
 
