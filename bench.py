@@ -296,9 +296,13 @@ def measure_arm(args, spec, precond: str, world: int, local: int):
     total_ms = max_over_ranks(total_ms, world)
     value = aggregate_throughput(N, K, world, total_ms / 1e3)
 
-    # end to end through the C ABI with host buffers: set_nodes (H2D) + step + get_nodes (D2H)
+    # end to end through the C ABI with the caller's host buffers (all N_t
+    # nodes in the reference's order): set_nodes (positions and velocities,
+    # H2D) + step + get_nodes (positions, velocities, forces, D2H)
     blob = w.blob(0)
-    pos, vel, _ = blob.get_nodes()
+    Nt = spec.mesh.num_nodes
+    bufs = tuple(np.empty((Nt, 3)) for _ in range(3))
+    pos, vel, _ = blob.get_nodes(out=bufs)
     Ke = args.e2e_steps or max(3, K // 2)
     barrier()
     torch.cuda.synchronize()
@@ -306,10 +310,10 @@ def measure_arm(args, spec, precond: str, world: int, local: int):
     for _ in range(Ke):
         blob.set_nodes(pos, vel)
         w.run(1)
-        pos, vel, _ = blob.get_nodes()
+        pos, vel, _ = blob.get_nodes(out=bufs)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = {"value": aggregate_throughput(N, Ke, world, e2e_s), "unit": "node-steps/s",
-           "h2d_bytes_per_step": 2 * 3 * 8 * N, "d2h_bytes_per_step": 3 * 3 * 8 * N, "steps": Ke}
+           "h2d_bytes_per_step": 2 * 3 * 8 * Nt, "d2h_bytes_per_step": 3 * 3 * 8 * Nt, "steps": Ke}
 
     # profile pass: direct launches with CUDA events around each phase of a step
     prof_steps = 3

@@ -112,7 +112,15 @@ struct ffea_gpu {
     cudaEvent_t ev[6] = {};
     int64_t fixed_per_step = 0;  // kernels of a step graph outside the CG loop
     size_t tsize = 4;
-    std::vector<std::vector<double>> sec_vel;  // per blob: initial velocities of secondary nodes
+    // node I/O in the reference's node order, reconstructed on the device:
+    // per original node (row, -1) for a corner node, (row_a, row_b) for an
+    // edge midpoint (its edge in the last element that lists it), (-1, -1)
+    // for a node of no element; per blob the offset into these arrays
+    std::vector<int64_t> io_off;
+    int2 *io_src = nullptr;
+    double *io_secvel = nullptr;  // secondary-node velocities (mass blobs keep them; NoMass report 0)
+    double *io_stage = nullptr;   // 9 doubles per node of the largest blob (pos, vel, force)
+    int32_t io_max_nodes = 0;
     int precond = FFEA_GPU_PRECOND_JACOBI;     // in use, after fall-backs
     MpnnBuffers mpnn;                          // learned smoother weights (allocated on first use)
     bool mpnn_ready = false;
@@ -129,6 +137,51 @@ struct ffea_gpu {
 };
 
 namespace {
+
+// One blob's nodes in the reference's order from the device state: corner
+// nodes copy their row (velocity, and the solve's x as the force), edge
+// midpoints average their edge's end rows (src/Blob.cpp:759-761), with the
+// stored secondary velocity for the mass solver and zero for NoMass.
+template <typename T>
+__global__ void k_nodes_out(DeviceBatch d, const int2 *src, int n, const double *secvel, int nomass, double *pos,
+                            double *vel, double *force)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 s = src[i];
+    const T *x = static_cast<const T *>(d.x);
+    for (int c = 0; c < 3; c++) {
+        double p = 0.0, v = nomass ? 0.0 : secvel[3 * (size_t)i + c], f = 0.0;
+        if (s.x >= 0 && s.y < 0) {
+            p = d.pos[3 * (size_t)s.x + c];
+            v = d.vel[3 * (size_t)s.x + c];
+            f = (double)x[3 * (size_t)s.x + c];
+        } else if (s.x >= 0) {
+            p = .5 * (d.pos[3 * (size_t)s.x + c] + d.pos[3 * (size_t)s.y + c]);
+        }
+        pos[3 * (size_t)i + c] = p;
+        vel[3 * (size_t)i + c] = v;
+        force[3 * (size_t)i + c] = f;
+    }
+}
+
+// The inverse for positions and velocities: corner nodes set their row;
+// secondary velocities are kept for the mass solver.
+__global__ void k_nodes_in(DeviceBatch d, const int2 *src, int n, const double *pos, const double *vel,
+                           double *secvel, int mass)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 s = src[i];
+    for (int c = 0; c < 3; c++) {
+        if (s.x >= 0 && s.y < 0) {
+            if (pos) d.pos[3 * (size_t)s.x + c] = pos[3 * (size_t)i + c];
+            if (vel) d.vel[3 * (size_t)s.x + c] = vel[3 * (size_t)i + c];
+        } else if (vel && mass) {
+            secvel[3 * (size_t)i + c] = vel[3 * (size_t)i + c];
+        }
+    }
+}
 
 constexpr size_t kCublasWorkspace = 4u << 20;  // a fixed workspace makes the GEMMs capturable
 constexpr int kCoarseInitIterations = 40;      // Newton-Schulz from I / ||A_c||: log2(cond) + a few
@@ -380,14 +433,34 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     for (auto &e : h->ev) CK(cudaEventCreate(&e));
     // secondary-node initial velocities (they never change: their rows are identity)
-    h->sec_vel.resize(num_blobs);
-    for (int b = 0; b < num_blobs; b++) {
-        const ffea_gpu_mesh &m = meshes[b];
-        h->sec_vel[b].assign(3 * (size_t)m.num_nodes, 0.0);
-        if (m.vel && params[b].solver == SOLVER_MASS)
+    {
+        static const int mid[6][3] = {{4, 0, 1}, {5, 0, 2}, {6, 0, 3}, {7, 1, 2}, {8, 1, 3}, {9, 2, 3}};
+        std::vector<int2> src;
+        std::vector<double> secvel;
+        for (int b = 0; b < num_blobs; b++) {
+            const ffea_gpu_mesh &m = meshes[b];
+            const BlobMap &map = H.maps[b];
+            h->io_off.push_back((int64_t)src.size());
+            h->io_max_nodes = std::max(h->io_max_nodes, m.num_nodes);
+            const size_t base = src.size();
+            src.resize(base + m.num_nodes, make_int2(-1, -1));
+            secvel.resize(3 * src.size(), 0.0);
             for (int32_t n = 0; n < m.num_nodes; n++)
-                if (H.maps[b].lin_of_orig[n] < 0)
-                    for (int c = 0; c < 3; c++) h->sec_vel[b][3 * (size_t)n + c] = m.vel[3 * (size_t)n + c];
+                if (map.lin_of_orig[n] >= 0) src[base + n] = make_int2(map.lin_of_orig[n], -1);
+            for (int32_t e = 0; e < map.num_elements; e++) {  // last element wins (src/Blob.cpp:759-761)
+                const int32_t *t = &map.topology[10 * (size_t)e];
+                for (int k = 0; k < 6; k++)
+                    src[base + t[mid[k][0]]] =
+                        make_int2(map.lin_of_orig[t[mid[k][1]]], map.lin_of_orig[t[mid[k][2]]]);
+            }
+            if (m.vel && params[b].solver == SOLVER_MASS)
+                for (int32_t n = 0; n < m.num_nodes; n++)
+                    if (map.lin_of_orig[n] < 0)
+                        for (int c = 0; c < 3; c++) secvel[3 * (base + n) + c] = m.vel[3 * (size_t)n + c];
+        }
+        CK(upload(A, h->io_src, src));
+        CK(upload(A, h->io_secvel, secvel));
+        CK(A.alloc(h->io_stage, 9 * (size_t)h->io_max_nodes));
     }
     launch_rest_state(d, h->stream);
     if (d.any_mass) launch_mass_matrix(d, h->stream);
@@ -674,72 +747,50 @@ int64_t ffea_gpu_cg_loop_count(ffea_gpu_t *h)
 int ffea_gpu_get_nodes(ffea_gpu_t *h, int32_t blob, double *pos, double *vel, double *force)
 {
     if (check_blob(h, blob)) return FFEA_GPU_ERROR;
-    CK(cudaStreamSynchronize(h->stream));
     const BlobParams &bp = h->host.bp[blob];
-    const BlobMap &map = h->host.maps[blob];
-    const size_t n3 = 3 * (size_t)bp.node_cnt, off = 3 * (size_t)bp.node_off;
-    std::vector<double> p(n3), v(n3), x;
-    CK(cudaMemcpy(p.data(), h->dev.pos + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(v.data(), h->dev.vel + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
-    if (copy_typed_to_double(h, h->dev.x, off, n3, x)) return FFEA_GPU_ERROR;
-    const int32_t N = map.num_nodes_total;
-    std::vector<double> P(3 * (size_t)N, 0.0);
-    for (int32_t n = 0; n < N; n++) {
-        const int32_t g = map.lin_of_orig[n];
-        if (g < 0) continue;
-        const size_t l = 3 * (size_t)(g - bp.node_off);
-        for (int c = 0; c < 3; c++) {
-            P[3 * (size_t)n + c] = p[l + c];
-            if (vel) vel[3 * (size_t)n + c] = v[l + c];
-            if (force) force[3 * (size_t)n + c] = x[l + c];
-        }
+    const int32_t N = h->host.maps[blob].num_nodes_total;
+    const int64_t o = h->io_off[blob];
+    double *st = h->io_stage;
+    if (N > 0) {
+        const int blocks = (N + 255) / 256;
+        if (h->dev.precision == PREC_FP64)
+            k_nodes_out<double><<<blocks, 256, 0, h->stream>>>(h->dev, h->io_src + o, N, h->io_secvel + 3 * o,
+                                                               bp.solver == SOLVER_NOMASS, st, st + 3 * (size_t)N,
+                                                               st + 6 * (size_t)N);
+        else
+            k_nodes_out<float><<<blocks, 256, 0, h->stream>>>(h->dev, h->io_src + o, N, h->io_secvel + 3 * o,
+                                                              bp.solver == SOLVER_NOMASS, st, st + 3 * (size_t)N,
+                                                              st + 6 * (size_t)N);
+        count_launches(1);
+        const size_t bytes = 3 * sizeof(double) * (size_t)N;
+        if (pos) CK(cudaMemcpyAsync(pos, st, bytes, cudaMemcpyDeviceToHost, h->stream));
+        if (vel) CK(cudaMemcpyAsync(vel, st + 3 * (size_t)N, bytes, cudaMemcpyDeviceToHost, h->stream));
+        if (force) CK(cudaMemcpyAsync(force, st + 6 * (size_t)N, bytes, cudaMemcpyDeviceToHost, h->stream));
     }
-    // midpoints in element order, last element wins (Blob::update_positions, src/Blob.cpp:759-761)
-    static const int mid[6][3] = {{4, 0, 1}, {5, 0, 2}, {6, 0, 3}, {7, 1, 2}, {8, 1, 3}, {9, 2, 3}};
-    for (int32_t e = 0; e < map.num_elements; e++) {
-        const int32_t *t = &map.topology[10 * (size_t)e];
-        for (int m = 0; m < 6; m++)
-            for (int c = 0; c < 3; c++)
-                P[3 * (size_t)t[mid[m][0]] + c] = .5 * (P[3 * (size_t)t[mid[m][1]] + c] + P[3 * (size_t)t[mid[m][2]] + c]);
-    }
-    for (int32_t n = 0; n < N; n++) {
-        if (map.lin_of_orig[n] >= 0) continue;
-        for (int c = 0; c < 3; c++) {
-            if (vel) vel[3 * (size_t)n + c] = (bp.solver == SOLVER_NOMASS) ? 0.0 : h->sec_vel[blob][3 * (size_t)n + c];
-            if (force) force[3 * (size_t)n + c] = 0.0;
-        }
-    }
-    if (pos) std::memcpy(pos, P.data(), P.size() * sizeof(double));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
     return FFEA_GPU_OK;
 }
 
 int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const double *vel)
 {
     if (check_blob(h, blob)) return FFEA_GPU_ERROR;
-    CK(cudaStreamSynchronize(h->stream));
     if (pos) h->steps_done = 0;  // new positions: refresh the coarse space on the next step
     const BlobParams &bp = h->host.bp[blob];
-    const BlobMap &map = h->host.maps[blob];
-    const size_t n3 = 3 * (size_t)bp.node_cnt, off = 3 * (size_t)bp.node_off;
-    std::vector<double> p(n3), v(n3);
-    // every linear entry is overwritten when both arrays are given: no read-back then
-    if (!pos) CK(cudaMemcpy(p.data(), h->dev.pos + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
-    if (!vel) CK(cudaMemcpy(v.data(), h->dev.vel + off, n3 * sizeof(double), cudaMemcpyDeviceToHost));
-    for (int32_t n = 0; n < map.num_nodes_total; n++) {
-        const int32_t g = map.lin_of_orig[n];
-        if (g < 0) {
-            if (vel && bp.solver == SOLVER_MASS)
-                for (int c = 0; c < 3; c++) h->sec_vel[blob][3 * (size_t)n + c] = vel[3 * (size_t)n + c];
-            continue;
-        }
-        const size_t l = 3 * (size_t)(g - bp.node_off);
-        for (int c = 0; c < 3; c++) {
-            if (pos) p[l + c] = pos[3 * (size_t)n + c];
-            if (vel) v[l + c] = vel[3 * (size_t)n + c];
-        }
+    const int32_t N = h->host.maps[blob].num_nodes_total;
+    const int64_t o = h->io_off[blob];
+    double *st = h->io_stage;
+    const size_t bytes = 3 * sizeof(double) * (size_t)N;
+    if (N > 0 && (pos || vel)) {
+        if (pos) CK(cudaMemcpyAsync(st, pos, bytes, cudaMemcpyHostToDevice, h->stream));
+        if (vel) CK(cudaMemcpyAsync(st + 3 * (size_t)N, vel, bytes, cudaMemcpyHostToDevice, h->stream));
+        k_nodes_in<<<(N + 255) / 256, 256, 0, h->stream>>>(h->dev, h->io_src + o, N, pos ? st : nullptr,
+                                                          vel ? st + 3 * (size_t)N : nullptr, h->io_secvel + 3 * o,
+                                                          bp.solver == SOLVER_MASS);
+        count_launches(1);
     }
-    CK(cudaMemcpy(h->dev.pos + off, p.data(), n3 * sizeof(double), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->dev.vel + off, v.data(), n3 * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
     return FFEA_GPU_OK;
 }
 

@@ -183,8 +183,15 @@ class Blob:
         self.n = world.num_nodes[index]
         self.e = world.num_elements[index]
 
-    def get_nodes(self):
-        pos = np.zeros((self.n, 3)); vel = np.zeros((self.n, 3)); force = np.zeros((self.n, 3))
+    def get_nodes(self, out=None):
+        """(pos, vel, force), each (num_nodes, 3) float64 in the blob's node
+        order; `out` = three such C-contiguous arrays to fill instead."""
+        if out is None:
+            out = (np.empty((self.n, 3)), np.empty((self.n, 3)), np.empty((self.n, 3)))
+        for a in out:
+            if a.dtype != np.float64 or a.shape != (self.n, 3) or not a.flags.c_contiguous:
+                raise ValueError("get_nodes: out arrays must be C-contiguous float64 of shape (num_nodes, 3)")
+        pos, vel, force = out
         L.check(L.lib().ffea_gpu_get_nodes(self.world.handle, self.index, L.ptr(pos), L.ptr(vel), L.ptr(force)))
         return pos, vel, force
 
