@@ -520,6 +520,28 @@ int ffea_gpu_phase_times(ffea_gpu_t *h, double out_ms[5])
 
 int ffea_gpu_preconditioner(ffea_gpu_t *h) { return h ? h->precond : -1; }
 
+int ffea_gpu_selftest_barrier_timeout(int32_t ctas, int32_t spin_limit, int32_t *timed_out)
+{
+    if (!timed_out) return fail("null result");
+    if (ctas < 1 || ctas > 64 || spin_limit < 1 || spin_limit > (1 << 20))
+        return fail("selftest: ctas must be in [1, 64] and spin_limit in [1, 2^20]");
+    unsigned int *bar = nullptr;
+    int *out = nullptr;
+    CK(cudaMalloc(&bar, 8 * sizeof(unsigned int)));
+    cudaError_t e = cudaMalloc(&out, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(bar, 0, 8 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(out, 0, sizeof(int));
+    if (e == cudaSuccess) e = launch_barrier_timeout_selftest(bar, (unsigned)spin_limit, out, ctas, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    int r = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&r, out, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(bar);
+    cudaFree(out);
+    if (e != cudaSuccess) return fail("selftest: %s", cudaGetErrorString(e));
+    *timed_out = r;
+    return FFEA_GPU_OK;
+}
+
 int ffea_gpu_set_smoother_weights(ffea_gpu_t *h, int32_t blob, const float *omega)
 {
     if (check_blob(h, blob)) return FFEA_GPU_ERROR;

@@ -529,7 +529,8 @@ constexpr int kMaxRestarts = 4;
 // last arrival directly, one L2 round trip sooner than with a separate
 // release word.  The CTAs are co-resident (cooperative launch); a wait that
 // exceeds the spin limit raises the time-out flag instead of hanging.
-__device__ __forceinline__ void counting_barrier(unsigned int *bar, unsigned int target, int *s_err)
+__device__ __forceinline__ void counting_barrier(unsigned int *bar, unsigned int target, int *s_err,
+                                                 unsigned int spin_limit = kSpinLimit)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -538,7 +539,7 @@ __device__ __forceinline__ void counting_barrier(unsigned int *bar, unsigned int
         volatile unsigned int *vb = bar;
         unsigned int spins = 0;
         while ((int)(vb[5] - target) < 0) {
-            if (++spins > kSpinLimit || vb[4]) {
+            if (++spins > spin_limit || vb[4]) {
                 *s_err = 1;
                 atomicExch(&bar[4], 1u);
                 break;
@@ -1733,6 +1734,18 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     }
 }
 
+// Self-test of the grid barrier's time-out: every CTA arrives, but the target
+// is one arrival more than the grid, so no wait can end; each waiter gives up
+// after spin_limit sleeps, raises the time-out flag and returns.  out[0] =
+// number of CTAs that reported the time-out.
+__global__ void k_barrier_timeout_selftest(unsigned int *bar, unsigned int spin_limit, int *out)
+{
+    __shared__ int s_err;
+    if (threadIdx.x == 0) s_err = 0;
+    counting_barrier(bar, gridDim.x + 1, &s_err, spin_limit);
+    if (threadIdx.x == 0 && s_err) atomicAdd(out, 1);
+}
+
 // Euler update (src/Blob.cpp:3937-3969) and the RNG advance to the next step.
 template <typename T>
 __global__ void __launch_bounds__(NODE_TILE) k_euler(DeviceBatch d)
@@ -1991,6 +2004,22 @@ int cg_max_grid(int precision, int reg, size_t dyn_bytes)
                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float, false>, CG_THREADS, 0);
     if (e != cudaSuccess) return 0;
     return sms * per_sm;
+}
+
+cudaError_t launch_barrier_timeout_selftest(unsigned int *bar, unsigned int spin_limit, int *out, int ctas,
+                                            cudaStream_t s)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)ctas);
+    cfg.blockDim = dim3(32);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FFEA_LAUNCHED();
+    return cudaLaunchKernelEx(&cfg, k_barrier_timeout_selftest, bar, spin_limit, out);
 }
 
 cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s)

@@ -97,6 +97,11 @@ void launch_elements(const DeviceBatch &d, cudaStream_t s, int mode);
 void launch_assemble(const DeviceBatch &d, cudaStream_t s);
 void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs);
 cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s);
+// The CG kernel's grid barrier with a target that no arrival reaches and the
+// given spin limit, on `ctas` co-resident CTAs; *out counts the CTAs that
+// reported the time-out (bar: 8 zeroed words, out: one zeroed int).
+cudaError_t launch_barrier_timeout_selftest(unsigned int *bar, unsigned int spin_limit, int *out, int ctas,
+                                            cudaStream_t s);
 void launch_euler(const DeviceBatch &d, cudaStream_t s);
 void launch_energies(const DeviceBatch &d, cudaStream_t s);
 void launch_apply(const DeviceBatch &d, cudaStream_t s, const double *in, double *out);

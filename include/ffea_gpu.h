@@ -130,8 +130,11 @@ int ffea_gpu_energies(ffea_gpu_t *h, int32_t blob, double *strain, double *kinet
 
 /* Status of the last step: inverted-element count, CG iterations of the last
  * solve, FP64 true relative residual ||b - A x|| / ||b|| of the last solve
- * (NaN when the check is off), and the failure bits (1 inversion, 2 CG did
- * not converge, 4 non-finite values). */
+ * (NaN when the check is off), and the failure bits (FFEA_GPU_FAIL_*). */
+#define FFEA_GPU_FAIL_INVERSION 1  /* an element inverted (Blob::update_internal_forces' check) */
+#define FFEA_GPU_FAIL_CG 2         /* the solve did not converge in max_iterations_cg */
+#define FFEA_GPU_FAIL_NAN 4        /* non-finite values in the solve */
+#define FFEA_GPU_FAIL_TIMEOUT 8    /* a grid barrier of the solve gave up waiting */
 int ffea_gpu_status(ffea_gpu_t *h, int32_t blob, int32_t *inverted, int32_t *cg_iters, double *true_relres,
                     int32_t *fail_bits);
 
@@ -210,6 +213,13 @@ int ffea_gpu_sizes(ffea_gpu_t *h, int64_t *linear_nodes, int64_t *elements, int6
 /* The preconditioner the handle's solves use (FFEA_GPU_PRECOND_*), after the
  * fall-back rules above; -1 on a null handle.  No reference counterpart. */
 int ffea_gpu_preconditioner(ffea_gpu_t *h);
+
+/* Failure-detection self-test of the solve's grid barrier: `ctas` CTAs wait
+ * for one arrival more than there are, each gives up after `spin_limit`
+ * sleeps of ~32 ns and raises the barrier's time-out flag, which the solve
+ * reports as FFEA_GPU_FAIL_TIMEOUT.  *timed_out = number of CTAs that
+ * reported it (ctas when the time-out works).  No reference counterpart. */
+int ffea_gpu_selftest_barrier_timeout(int32_t ctas, int32_t spin_limit, int32_t *timed_out);
 
 /* Per-node weights of the Jacobi term of the LEARNED preconditioner for one
  * blob: omega[num_nodes] in the blob's node order (secondary nodes ignored),
