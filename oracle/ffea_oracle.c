@@ -12,7 +12,7 @@
  * to the FFEA source tree).  Operation order inside each function follows the
  * reference statement by statement so that, compiled with -ffp-contract=off,
  * the FP64 results match the reference objects bit for bit (pinned by
- * tests/test_oracle_vs_reference.py and the committed golden vectors).
+ * tests/test_oracle.py and the committed golden vectors).
  *
  * Units: everything is in FFEA meso units (include/dimensions.h:30-41); the
  * caller converts SI inputs (see ffea_gb300/params.py).
