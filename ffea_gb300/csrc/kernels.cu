@@ -878,6 +878,35 @@ __device__ __forceinline__ DF df_warp_sum(DF v)
     return v;
 }
 
+// Sum of N values per lane over a warp (N a power of two, 2..32) by a
+// transposed butterfly: at offsets 16, 8, ... each lane keeps half of its
+// values and adds its partner's copy of that half (N/2 + N/4 + ... shuffles),
+// then the remaining offsets add whole values.  Returns this lane's total of
+// value index idx; every lane holding the same idx holds the same bits.
+template <int N>
+__device__ __forceinline__ float warp_sum_multi(float (&v)[N], int &idx)
+{
+    static_assert(N >= 2 && N <= 32 && (N & (N - 1)) == 0, "N must be a power of two in [2, 32]");
+    const int lane = threadIdx.x & 31;
+    idx = 0;
+    int o = 16;
+#pragma unroll
+    for (int h = N / 2; h >= 1; h /= 2, o /= 2) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < h; k++) {
+            const float send = upper ? v[k] : v[k + h];
+            const float keep = upper ? v[k + h] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+        if (upper) idx += h;
+    }
+    float x = v[0];
+#pragma unroll
+    for (; o > 0; o /= 2) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
 // Partial sums of a CG segment, written to its slot P of the partials
 // buffer: three dot-product terms, each a (hi, lo) float pair in P[0..5]
 // (mask selects which), and NX plain FP32 sums in P[ex_off ..] (the
@@ -892,15 +921,29 @@ __device__ __forceinline__ void seg_partials(float *P, const W (&in)[3], int mas
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     W *sw = reinterpret_cast<W *>(smem_raw);
     float *sxs = reinterpret_cast<float *>(smem_raw + 3 * 32);
+    if (sizeof(W) == 4) {
+        // all 3 + NX values in one transposed butterfly
+        constexpr int NV = (3 + NX) <= 4 ? 4 : (3 + NX) <= 8 ? 8 : 16;
+        float v[NV];
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const W s = warp_sum<W>(in[k]);
-        if (lane == 0) sw[k * 32 + warp] = s;
-    }
+        for (int k = 0; k < NV; k++) v[k] = k < 3 ? (float)in[k] : k < 3 + NX ? ex[k - 3] : 0.f;
+        int idx;
+        const float t = warp_sum_multi<NV>(v, idx);
+        if ((lane & (32 / NV - 1)) == 0) {
+            if (idx < 3) sw[idx * 32 + warp] = (W)t;
+            else if (idx < 3 + NX) sxs[(idx - 3) * 32 + warp] = t;
+        }
+    } else {
 #pragma unroll
-    for (int k = 0; k < NX; k++) {
-        const float s = warp_sum<float>(ex[k]);
-        if (lane == 0) sxs[k * 32 + warp] = s;
+        for (int k = 0; k < 3; k++) {
+            const W s = warp_sum<W>(in[k]);
+            if (lane == 0) sw[k * 32 + warp] = s;
+        }
+#pragma unroll
+        for (int k = 0; k < NX; k++) {
+            const float s = warp_sum<float>(ex[k]);
+            if (lane == 0) sxs[k * 32 + warp] = s;
+        }
     }
     __syncthreads();
     if (warp < 3) {
@@ -1238,12 +1281,12 @@ struct CoarseCtx {
 __device__ __forceinline__ void coarse_apply(const CoarseCtx &cz, float g)
 {
     const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
+    float v[8];
 #pragma unroll
-    for (int l = 0; l < 6; l++) {
-        float v = j < cz.n ? cz.xrow[l * cz.n + j] * g : 0.f;
-        v = warp_sum<float>(v);
-        if (lane == 0) cz.red6[l * 32 + warp] = v;
-    }
+    for (int l = 0; l < 8; l++) v[l] = (l < 6 && j < cz.n) ? cz.xrow[l * cz.n + j] * g : 0.f;
+    int idx;
+    const float t = warp_sum_multi<8>(v, idx);
+    if ((lane & 3) == 0 && idx < 6) cz.red6[idx * 32 + warp] = t;
     __syncthreads();
     if (warp < 6) {
         const float v = warp_sum<float>(lane < (int)(blockDim.x >> 5) ? cz.red6[warp * 32 + lane] : 0.f);
