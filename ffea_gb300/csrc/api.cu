@@ -322,9 +322,12 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     bool coarse_ok = want != FFEA_GPU_PRECOND_JACOBI && H.precision == PREC_MIXED && !H.any_mass;
     for (const BlobParams &bp : H.bp) coarse_nmax = std::max(coarse_nmax, (int)bp.coarse_n);
     if (coarse_nmax > CG_THREADS) coarse_ok = false;
-    // phi per row, the CTA's six rows of X, c, and 6 x 32 reduction floats
+    // phi per row, the CTA's six rows of X, c, 6 x 32 reduction floats and
+    // the carried P^T s per coarse dof
     const size_t coarse_bytes =
-        coarse_ok ? 16 + 16 * (size_t)CG_THREADS + sizeof(float) * (6 * (size_t)coarse_nmax + 8 + 6 * 32) : 0;
+        coarse_ok ? 16 + 16 * (size_t)CG_THREADS +
+                        sizeof(float) * (6 * (size_t)coarse_nmax + 8 + 6 * 32 + (size_t)CG_THREADS)
+                  : 0;
     size_t dyn_bytes = 0;
     int cache_slots = 0, cache_cols = 0;
     if (cg_smem_plan(H.precision, max_slots, max_cols, coarse_bytes, &cache_slots, &cache_cols, &dyn_bytes) != 0)

@@ -1274,8 +1274,18 @@ struct CoarseCtx {
     const float *xrow;  // the CTA's 6 rows of X, n floats each
     float *cvec;        // c (6 floats)
     float *red6;        // 6 x 32 floats of reduction scratch
+    float *h;           // (P^T s)_j for coarse dof j, carried across iterations (CG_THREADS floats)
     int n;              // coarse dofs of the blob (0: no coarse space)
 };
+
+// L2 load issued where it stands (volatile asm keeps it ahead of the
+// barriers that follow, so its latency overlaps the reduction's own loads)
+__device__ __forceinline__ float ld_early(const float *p)
+{
+    float v;
+    asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
 
 // c = X g, g_j held by thread j (zero beyond n): a 6-value block reduction.
 __device__ __forceinline__ void coarse_apply(const CoarseCtx &cz, float g)
@@ -1298,8 +1308,7 @@ __device__ __forceinline__ void coarse_apply(const CoarseCtx &cz, float g)
 template <typename T>
 __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const double *part, CgScalars *s_cg,
                                                      float *sm, unsigned int *s_run, int nb, const int *s_blob,
-                                                     int *s_state, T *s_alpha, T *s_beta, const CoarseCtx &cz,
-                                                     float &h)
+                                                     int *s_state, T *s_alpha, T *s_beta, const CoarseCtx &cz)
 {
     const int nbl = d.num_blobs, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr bool fast = sizeof(T) == 4;
@@ -1312,8 +1321,8 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
         const int j = threadIdx.x;
         if (j < bp.coarse_n) {
             const float *slot = reinterpret_cast<const float *>(part) + (size_t)d.part_stride * (bp.seg_off + j / 6);
-            ptr = __ldcg(slot + 8 + j % 6);
-            ptw = __ldcg(slot + 14 + j % 6);
+            ptr = ld_early(slot + 8 + j % 6);
+            ptw = ld_early(slot + 14 + j % 6);
         }
     }
     if (nbl < 8) {
@@ -1360,6 +1369,7 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
         const CgScalars &cg = s_cg[cb];
         float g = 0.f;
         if (threadIdx.x < cz.n) {
+            float &h = cz.h[threadIdx.x];
             if (cg.state == CG_RESTART) {
                 h = 0.f;
                 g = ptr;
@@ -1530,7 +1540,6 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     const bool coarse = REG && local && d.coarse;
     float4 *phi_s = nullptr;
     float *cvec = nullptr;
-    float h_coarse = 0.f;  // (P^T s)_tid of the blob's coarse dof tid
     CoarseCtx cz{};
     if (coarse) {
         size_t off = 6 * (size_t)CG_THREADS * sizeof(T) + (size_t)cc.JC * CG_THREADS * sizeof(int) +
@@ -1540,7 +1549,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         float *xrow = reinterpret_cast<float *>(phi_s + CG_THREADS);
         cvec = xrow + 6 * (size_t)d.coarse_nmax;
         const BlobParams &bp = d.bp[s_blob[0]];
-        cz = CoarseCtx{xrow, cvec, cvec + 8, bp.coarse_n};
+        cz = CoarseCtx{xrow, cvec, cvec + 8, cvec + 8 + 6 * 32, bp.coarse_n};
+        cz.h[tid] = 0.f;
         phi_s[tid] = reg_valid ? d.phi[s_row0[0] + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float *Xg = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (S0 - bp.seg_off)) * bp.coarse_n;
         for (int k = tid; k < 6 * bp.coarse_n; k += CG_THREADS) xrow[k] = Xg[k];
@@ -1717,7 +1727,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) return 0u;
         return local_reduce<T>(d, part(), s_cg, sm_df, &s_run, nb, s_blob, s_state, s_alpha, s_beta,
-                               cz, h_coarse);
+                               cz);
     };
     if (coarse) {
         // u_0 = M r_0 needs P^T r_0 of every segment of the blob: restrict
