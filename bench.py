@@ -43,6 +43,9 @@ WORKLOADS = {
     "sphere40": dict(radius_nm=40.0, cell_nm=1.25, desc="64^3-cell Freudenthal grid cut to a 40 nm sphere"),
     "sphere20": dict(radius_nm=20.0, cell_nm=1.25, desc="32^3-cell Freudenthal grid cut to a 20 nm sphere"),
     "sphere10": dict(radius_nm=10.0, cell_nm=1.25, desc="16^3-cell Freudenthal grid cut to a 10 nm sphere"),
+    "ensemble64": dict(radius_nm=None, cell_nm=1.25,
+                       desc="64 independent blobs in one batch: radii log-uniform 5-40 nm at a 1.25 nm cell, "
+                            "moduli x U[0.5, 2], one RNG stream each"),
 }
 METRIC = "node-steps/s at CG rel-res 1e-6"
 PRECONDS = {"jacobi": 0, "two-level": 1, "learned": 2}
@@ -66,24 +69,39 @@ def parse_args():
     return ap.parse_args()
 
 
-def build_spec(workload: str, rank: int, precision: str):
+def build_specs(workload: str, rank: int, precision: str):
+    """The blobs of one rank's replica of the workload."""
     from ffea_gb300 import params as P
     from ffea_gb300.mesh import make_blob, sphere_mesh
     w = WORKLOADS[workload]
-    mesh = sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0)
-    prm = P.SimulationParams.from_si(dt=1e-14, kT=P.kT_at(300.0) * P.MESO_ENERGY, epsilon=1e-6,
-                                     max_iterations_cg=10000, rng_seed=replica_seed(rank), solver=P.SOLVER_NOMASS,
-                                     precision=P.PRECISION_MIXED if precision == "mixed" else P.PRECISION_FP64)
-    return make_blob(mesh, prm)
+    prec = P.PRECISION_MIXED if precision == "mixed" else P.PRECISION_FP64
+
+    def prm(seed):
+        return P.SimulationParams.from_si(dt=1e-14, kT=P.kT_at(300.0) * P.MESO_ENERGY, epsilon=1e-6,
+                                          max_iterations_cg=10000, rng_seed=seed, solver=P.SOLVER_NOMASS,
+                                          precision=prec)
+    if w["radius_nm"] is not None:
+        return [make_blob(sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0), prm(replica_seed(rank)))]
+    rng = np.random.default_rng(2)
+    radii = np.exp(rng.uniform(np.log(5.0), np.log(40.0), size=64))
+    scale = rng.uniform(0.5, 2.0, size=64)
+    return [make_blob(sphere_mesh(float(r), cell_nm=w["cell_nm"], seed=i),
+                      prm(1000 * (rank + 1) + i), shear_mod=3.7e8 * g, bulk_mod=1.1e9 * g)
+            for i, (r, g) in enumerate(zip(radii, scale))]
 
 
-def config_of(args, spec, world_size):
-    m = spec.mesh
+def build_spec(workload: str, rank: int, precision: str):
+    return build_specs(workload, rank, precision)[0]
+
+
+def config_of(args, specs, world_size):
+    specs = specs if isinstance(specs, (list, tuple)) else [specs]
     return {
         "workload": f"{args.workload}: {WORKLOADS[args.workload]['desc']}",
-        "linear_nodes": int(m.num_linear),
-        "elements": int(m.num_elements),
-        "total_nodes": int(m.num_nodes),
+        "blobs": len(specs),
+        "linear_nodes": int(sum(s.mesh.num_linear for s in specs)),
+        "elements": int(sum(s.mesh.num_elements for s in specs)),
+        "total_nodes": int(sum(s.mesh.num_nodes for s in specs)),
         "solver": "CG_nomass, epsilon 1e-6, convergence confirmed by an FP64 true residual",
         "precision": "FP32 element forces + SpMV, FP64 positions/dots" if args.precision == "mixed" else "FP64",
         "noise": "on (MRG32k3a, RngStream-exact)",
@@ -179,26 +197,42 @@ def ncu_traffic(kernel="k_cg", workload="sphere40"):
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_baseline(spec, budget_s: float):
-    """Oracle (C restatement of FFEA's path) on all host cores, bounded sample."""
+def cpu_baseline(specs, budget_s: float):
+    """Oracle (C restatement of FFEA's path) on all host cores, bounded sample:
+    whole timesteps of the workload's blobs in order (OpenMP within each blob)
+    until the budget is spent; node-steps/s over what was stepped."""
     from oracle import oracle as O
     O.build(ref=False)
+    specs = specs if isinstance(specs, (list, tuple)) else [specs]
     threads = os.cpu_count() or 1
-    b = O.blob_from_spec(spec, num_threads=threads)
-    t0 = time.perf_counter()
-    rc = b.step(1)
-    first = time.perf_counter() - t0
-    steps, total = 1, first
-    while rc == 0 and total + first < budget_s:
-        t = time.perf_counter()
+    done_nodes, total, steps, blobs_used = 0, 0.0, 0, set()
+    k = 0
+    while total < budget_s and (k == 0 or len(specs) > 1 or total < budget_s):
+        i = k % len(specs)
+        b = O.blob_from_spec(specs[i], num_threads=threads)
+        t0 = time.perf_counter()
         rc = b.step(1)
-        total += time.perf_counter() - t
-        steps += 1
-    if rc != 0:
-        raise RuntimeError("oracle step failed in the CPU baseline")
-    v = spec.mesh.num_linear * steps / total
+        first = time.perf_counter() - t0
+        n_steps, t_blob = 1, first
+        while rc == 0 and len(specs) == 1 and total + t_blob + first < budget_s:
+            t = time.perf_counter()
+            rc = b.step(1)
+            t_blob += time.perf_counter() - t
+            n_steps += 1
+        if rc != 0:
+            raise RuntimeError("oracle step failed in the CPU baseline")
+        done_nodes += specs[i].mesh.num_linear * n_steps
+        total += t_blob
+        steps += n_steps
+        blobs_used.add(i)
+        k += 1
+        if len(specs) == 1:
+            break
+    v = done_nodes / total
+    what = ("the full workload" if len(specs) == 1 else
+            f"{len(blobs_used)} of the workload's {len(specs)} blobs, one step each")
     return {"value": v, "unit": "node-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} timestep(s) of the full workload after set-up, {total:.1f} s, OpenMP "
+            "sample": f"{steps} timestep(s) of {what} after set-up, {total:.1f} s, OpenMP "
                       f"{threads} threads, per-thread RNG streams as FFEA_PARALLEL_WITHIN_BLOB",
             "steps": steps, "seconds": total}
 
@@ -235,8 +269,9 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    spec = build_spec(args.workload, 0, args.precision)
-    base = cpu_baseline(spec, budget_s=max(args.cpu_seconds, 30.0))
+    specs = build_specs(args.workload, 0, args.precision)
+    spec = specs
+    base = cpu_baseline(specs, budget_s=max(args.cpu_seconds, 30.0))
     line = {
         "metric": METRIC, "value": base["value"], "unit": "node-steps/s", "n_gpus": args.gpus,
         "steps": base["steps"], "warmup": 0, "ms_per_step": 1e3 * base["seconds"] / base["steps"],
@@ -250,7 +285,7 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def measure_arm(args, spec, precond: str, world: int, local: int):
+def measure_arm(args, specs, precond: str, world: int, local: int):
     """One arm on this rank: warm-up, K timed steps (device events on the
     handle's stream, L2 flushed between steps), the end-to-end loop through
     the C ABI with host buffers, and a profile pass with per-phase events."""
@@ -258,8 +293,8 @@ def measure_arm(args, spec, precond: str, world: int, local: int):
     from ffea_gb300 import learned
     from ffea_gb300.world import World, kernel_launches
 
-    N = spec.mesh.num_linear
-    w = World([spec], graph=True, true_residual=True, preconditioner=PRECONDS[precond])
+    N = sum(s_.mesh.num_linear for s_ in specs)
+    w = World(list(specs), graph=True, true_residual=True, preconditioner=PRECONDS[precond])
     if precond == "learned" and w.preconditioner() == PRECONDS["learned"]:
         learned.apply(w, learned.load())
     nl, ne, nedges = w.sizes()
@@ -299,18 +334,21 @@ def measure_arm(args, spec, precond: str, world: int, local: int):
     # end to end through the C ABI with the caller's host buffers (all N_t
     # nodes in the reference's order): set_nodes (positions and velocities,
     # H2D) + step + get_nodes (positions, velocities, forces, D2H)
-    blob = w.blob(0)
-    Nt = spec.mesh.num_nodes
-    bufs = tuple(np.empty((Nt, 3)) for _ in range(3))
-    pos, vel, _ = blob.get_nodes(out=bufs)
+    blobs = [w.blob(i) for i in range(len(specs))]
+    Nt = sum(s_.mesh.num_nodes for s_ in specs)
+    bufs = [tuple(np.empty((s_.mesh.num_nodes, 3)) for _ in range(3)) for s_ in specs]
+    for b_, buf in zip(blobs, bufs):
+        b_.get_nodes(out=buf)
     Ke = args.e2e_steps or max(3, K // 2)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(Ke):
-        blob.set_nodes(pos, vel)
+        for b_, buf in zip(blobs, bufs):
+            b_.set_nodes(buf[0], buf[1])
         w.run(1)
-        pos, vel, _ = blob.get_nodes(out=bufs)
+        for b_, buf in zip(blobs, bufs):
+            b_.get_nodes(out=buf)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = {"value": aggregate_throughput(N, Ke, world, e2e_s), "unit": "node-steps/s",
            "h2d_bytes_per_step": 2 * 3 * 8 * Nt, "d2h_bytes_per_step": 3 * 3 * 8 * Nt, "steps": Ke}
@@ -344,11 +382,11 @@ def run_gb300(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    spec = build_spec(args.workload, rank, args.precision)
-    main_arm = measure_arm(args, spec, args.precond, world, local)
+    specs = build_specs(args.workload, rank, args.precision)
+    main_arm = measure_arm(args, specs, args.precond, world, local)
     plain = None
-    if args.precond != "jacobi" and not args.no_plain:
-        plain = measure_arm(args, spec, "jacobi", world, local)
+    if main_arm["preconditioner"] != "jacobi" and not args.no_plain:
+        plain = measure_arm(args, specs, "jacobi", world, local)
     if rank != 0:
         return
     nl, ne, nedges = main_arm["sizes"]
@@ -368,7 +406,7 @@ def run_gb300(args):
         "metric": METRIC, "value": main_arm["value"], "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": main_arm["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": config_of(args, spec, world), "e2e": main_arm["e2e"], "gpu_launches": main_arm["gpu_launches"],
+        "config": config_of(args, specs, world), "e2e": main_arm["e2e"], "gpu_launches": main_arm["gpu_launches"],
         "preconditioner": main_arm["preconditioner"], "cg_iters_per_step": main_arm["cg_iters_per_step"],
         "roofline": roofline, "clocks": main_arm["clocks"], "phase_ms_per_step": main_arm["phase_ms_per_step"],
         "cg_us_per_iteration": main_arm["cg_us_per_iteration"],
@@ -385,7 +423,7 @@ def run_gb300(args):
             "iteration_ratio": plain["cg_iters_per_step"] / max(main_arm["cg_iters_per_step"], 1e-9),
         }
     if world == 1 and not args.no_cpu_baseline:
-        base = cpu_baseline(spec, args.cpu_seconds)
+        base = cpu_baseline(specs, args.cpu_seconds)
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line), flush=True)
 

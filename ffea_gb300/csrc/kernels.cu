@@ -820,6 +820,41 @@ struct RowState {
     T x[3], r[3], u[3], w[3], s[3], p[3], dinv[3];
 };
 
+// Fields of the row state (memory-resident variant: each phase moves only
+// the fields it reads or writes).
+enum RowField : int { RF_X = 1, RF_R = 2, RF_U = 4, RF_W = 8, RF_S = 16, RF_P = 32, RF_DINV = 64 };
+
+template <typename T>
+__device__ __forceinline__ void load_fields(const DeviceBatch &d, int row, RowState<T> &S, int m)
+{
+    const size_t o = 3 * (size_t)row;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (m & RF_X) S.x[c] = static_cast<const T *>(d.x)[o + c];
+        if (m & RF_R) S.r[c] = static_cast<const T *>(d.r)[o + c];
+        if (m & RF_U) S.u[c] = static_cast<const T *>(d.u)[o + c];
+        if (m & RF_W) S.w[c] = static_cast<const T *>(d.w)[o + c];
+        if (m & RF_S) S.s[c] = static_cast<const T *>(d.s)[o + c];
+        if (m & RF_P) S.p[c] = static_cast<const T *>(d.p)[o + c];
+        if (m & RF_DINV) S.dinv[c] = static_cast<const T *>(d.dinv)[o + c];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void store_fields(const DeviceBatch &d, int row, const RowState<T> &S, int m)
+{
+    const size_t o = 3 * (size_t)row;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (m & RF_X) static_cast<T *>(d.x)[o + c] = S.x[c];
+        if (m & RF_R) static_cast<T *>(d.r)[o + c] = S.r[c];
+        if (m & RF_U) static_cast<T *>(d.u)[o + c] = S.u[c];
+        if (m & RF_W) static_cast<T *>(d.w)[o + c] = S.w[c];
+        if (m & RF_S) static_cast<T *>(d.s)[o + c] = S.s[c];
+        if (m & RF_P) static_cast<T *>(d.p)[o + c] = S.p[c];
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void load_row(const DeviceBatch &d, int row, RowState<T> &S)
 {
@@ -1618,7 +1653,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         W pg = 0, pr = 0;
         RowState<T> loc;
         RowState<T> &S = REG ? reg : loc;
-        if (!REG && valid) load_row<T>(d, row, loc);
+        if (!REG && valid) load_fields<T>(d, row, loc, RF_X | RF_R | RF_U | RF_W | RF_S | RF_P | RF_DINV);
         if (valid) {
             const T a = s_alpha[k], b = s_beta[k];
             const bool first = b == (T)0;
@@ -1638,7 +1673,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
             U4[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
         }
-        if (!REG && valid) store_row<T>(d, row, loc);
+        if (!REG && valid) store_fields<T>(d, row, loc, RF_X | RF_R | RF_U | RF_S | RF_P);
         const W in[3] = {pg, (W)0, pr};
         if (coarse) {
             // restriction of the new r: slot floats 8..
@@ -1663,7 +1698,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         double vr = 0.0, vg = 0.0;
         RowState<T> loc;
         RowState<T> &S = REG ? reg : loc;
-        if (!REG && valid) load_row<T>(d, row, loc);
+        if (!REG && valid) load_fields<T>(d, row, loc, RF_R | RF_U | (state == CG_VERIFY ? RF_DINV : 0));
         if (valid) {
             if (state != CG_VERIFY) {
                 T au[3];
@@ -1688,7 +1723,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                 U4[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
             }
         }
-        if (!REG && valid) store_row<T>(d, row, loc);
+        if (!REG && valid) store_fields<T>(d, row, loc, state == CG_VERIFY ? (RF_R | RF_U) : RF_W);
         if (coarse) {
             // restrictions: ACTIVE P^T w (slot floats 14..); the prologue,
             // RESTART and VERIFY restart the coarse recurrence: P^T r (8..)
