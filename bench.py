@@ -66,6 +66,8 @@ def parse_args():
     ap.add_argument("--precond", choices=sorted(PRECONDS), default="learned",
                     help="preconditioner of the headline arm (plain Jacobi-PCG is measured beside it)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain Jacobi-PCG arm")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick each arm's launch shape with ffea_gb300.autotune on this batch first")
     return ap.parse_args()
 
 
@@ -294,7 +296,19 @@ def measure_arm(args, specs, precond: str, world: int, local: int):
     from ffea_gb300.world import World, kernel_launches
 
     N = sum(s_.mesh.num_linear for s_ in specs)
-    w = World(list(specs), graph=True, true_residual=True, preconditioner=PRECONDS[precond])
+    tuned = None
+    if args.autotune:
+        from ffea_gb300 import autotune
+        space = [{"FFEA_GPU_CG_SMEM_SLOTS": sl, "FFEA_GPU_CG_MAX_CTAS": ct, "FFEA_GPU_COARSE_REFRESH": rf}
+                 for sl in (0, 2, 64) for ct in (torch.cuda.get_device_properties(local).multi_processor_count,
+                                                 (3 * torch.cuda.get_device_properties(local).multi_processor_count) // 4)
+                 for rf in ((10, 25) if precond != "jacobi" else (10,))]
+        tuned = autotune.tune(specs, PRECONDS[precond], space=space, cache=None,
+                              weights=learned.load() if precond == "learned" else None)
+        with autotune.applied(tuned["config"]):
+            w = World(list(specs), graph=True, true_residual=True, preconditioner=PRECONDS[precond])
+    else:
+        w = World(list(specs), graph=True, true_residual=True, preconditioner=PRECONDS[precond])
     if precond == "learned" and w.preconditioner() == PRECONDS["learned"]:
         learned.apply(w, learned.load())
     nl, ne, nedges = w.sizes()
@@ -370,7 +384,7 @@ def measure_arm(args, specs, precond: str, world: int, local: int):
         "phase_ms_per_step": {"elements": float(phases[0]), "assemble": float(phases[1]),
                               "nodes": float(phases[2]), "cg": cg_ms, "euler": float(phases[4])},
         "cg_us_per_iteration": 1e3 * cg_ms / max(iters_p, 1), "cg_iters_profiled": iters_p,
-        "sizes": (nl, ne, nedges),
+        "sizes": (nl, ne, nedges), "autotune": tuned,
     }
 
 
@@ -411,6 +425,8 @@ def run_gb300(args):
         "roofline": roofline, "clocks": main_arm["clocks"], "phase_ms_per_step": main_arm["phase_ms_per_step"],
         "cg_us_per_iteration": main_arm["cg_us_per_iteration"],
     }
+    if main_arm["autotune"]:
+        line["autotune"] = main_arm["autotune"]
     line["config"]["edges"] = int(nedges)
     line["config"]["solver"] = (f"CG_nomass, {main_arm['preconditioner']} preconditioner, epsilon 1e-6, "
                                 "convergence confirmed by an FP64 true residual")
