@@ -1297,7 +1297,7 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, i
 // Also refreshes the CTA's view (state, alpha, beta of its nb blobs) and
 // returns the number of blobs still iterating.
 //
-// With the coarse space (cz.n > 0; one blob per CTA) it also forms the
+// With the coarse space (coarse_n > 0; one blob per CTA) it also forms the
 // CTA's coarse correction for the next update: thread j holds coarse dof j
 // of the blob, with h_j = (P^T s)_j carried from iteration to iteration, and
 // from the segment restrictions of this iteration (slot floats 8..: P^T r_k,
@@ -1305,13 +1305,54 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, i
 // alpha h with the new alpha and beta (after a failed true-residual check,
 // RESTART: g = P^T r of the true residual), then c = X g over the CTA's six
 // rows of X ~ A_c^-1 in one block reduction.
-struct CoarseCtx {
-    const float *xrow;  // the CTA's 6 rows of X, n floats each
-    float *cvec;        // c (6 floats)
-    float *red6;        // 6 x 32 floats of reduction scratch
-    float *h;           // (P^T s)_j for coarse dof j, carried across iterations (CG_THREADS floats)
-    int n;              // coarse dofs of the blob (0: no coarse space)
+// Dynamic shared memory of the CG kernel (layout in k_cg).
+extern __shared__ __align__(16) unsigned char cg_dyn[];
+
+// The coarse-space region of the dynamic shared memory: per thread the rest
+// offset and smoother weight (phi), the CTA's 6 rows of X, c (8 floats),
+// 6 x 32 reduction floats, and (P^T s)_j per coarse dof j.  The addresses are
+// recomputed from kernel parameters wherever they are used, so that they
+// need no registers across the iteration.
+struct CoarseView {
+    float4 *phi;
+    float *xrow, *cvec, *red6, *h;
 };
+
+template <typename T>
+__device__ __forceinline__ CoarseView coarse_view(const DeviceBatch &d)
+{
+    using T2 = typename CgCache<T>::T2;
+    size_t off = 6 * (size_t)CG_THREADS * sizeof(T) + (size_t)d.cg_cache_cols * CG_THREADS * sizeof(int) +
+                 (size_t)d.cg_cache_slots * CG_THREADS * (4 * sizeof(T2) + sizeof(T));
+    off = (off + 15) & ~(size_t)15;
+    CoarseView v;
+    v.phi = reinterpret_cast<float4 *>(cg_dyn + off);
+    v.xrow = reinterpret_cast<float *>(v.phi + CG_THREADS);
+    v.cvec = v.xrow + 6 * (size_t)d.coarse_nmax;
+    v.red6 = v.cvec + 8;
+    v.h = v.red6 + 6 * 32;
+    return v;
+}
+
+// c = X g, g_j held by thread j (zero beyond n): a 6-value block reduction.
+template <typename T>
+__device__ __forceinline__ void coarse_apply(const DeviceBatch &d, int n, float g)
+{
+    const CoarseView cv = coarse_view<T>(d);
+    const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
+    float v[8];
+#pragma unroll
+    for (int l = 0; l < 8; l++) v[l] = (l < 6 && j < n) ? cv.xrow[l * n + j] * g : 0.f;
+    int idx;
+    const float t = warp_sum_multi<8>(v, idx);
+    if ((lane & 3) == 0 && idx < 6) cv.red6[idx * 32 + warp] = t;
+    __syncthreads();
+    if (warp < 6) {
+        const float u = warp_sum<float>(lane < (int)(blockDim.x >> 5) ? cv.red6[warp * 32 + lane] : 0.f);
+        if (lane == 0) cv.cvec[warp] = u;
+    }
+    __syncthreads();
+}
 
 // L2 load issued where it stands (volatile asm keeps it ahead of the
 // barriers that follow, so its latency overlaps the reduction's own loads)
@@ -1322,35 +1363,17 @@ __device__ __forceinline__ float ld_early(const float *p)
     return v;
 }
 
-// c = X g, g_j held by thread j (zero beyond n): a 6-value block reduction.
-__device__ __forceinline__ void coarse_apply(const CoarseCtx &cz, float g)
-{
-    const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
-    float v[8];
-#pragma unroll
-    for (int l = 0; l < 8; l++) v[l] = (l < 6 && j < cz.n) ? cz.xrow[l * cz.n + j] * g : 0.f;
-    int idx;
-    const float t = warp_sum_multi<8>(v, idx);
-    if ((lane & 3) == 0 && idx < 6) cz.red6[idx * 32 + warp] = t;
-    __syncthreads();
-    if (warp < 6) {
-        const float v = warp_sum<float>(lane < (int)(blockDim.x >> 5) ? cz.red6[warp * 32 + lane] : 0.f);
-        if (lane == 0) cz.cvec[warp] = v;
-    }
-    __syncthreads();
-}
-
 template <typename T>
 __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const double *part, CgScalars *s_cg,
                                                      float *sm, unsigned int *s_run, int nb, const int *s_blob,
-                                                     int *s_state, T *s_alpha, T *s_beta, const CoarseCtx &cz)
+                                                     int *s_state, T *s_alpha, T *s_beta, int coarse_n)
 {
     const int nbl = d.num_blobs, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr bool fast = sizeof(T) == 4;
     // coarse restrictions, loaded first so that they travel with the sums
     float ptr = 0.f, ptw = 0.f;
     int cb = -1;
-    if (cz.n) {
+    if (coarse_n) {
         cb = s_blob[0];
         const BlobParams &bp = d.bp[cb];
         const int j = threadIdx.x;
@@ -1400,11 +1423,11 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
         }
     }
     __syncthreads();
-    if (cz.n) {
+    if (coarse_n) {
         const CgScalars &cg = s_cg[cb];
         float g = 0.f;
-        if (threadIdx.x < cz.n) {
-            float &h = cz.h[threadIdx.x];
+        if (threadIdx.x < coarse_n) {
+            float &h = coarse_view<T>(d).h[threadIdx.x];
             if (cg.state == CG_RESTART) {
                 h = 0.f;
                 g = ptr;
@@ -1413,7 +1436,7 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
                 g = ptr - cg.alpha_f * h;
             }
         }
-        coarse_apply(cz, g);
+        coarse_apply<T>(d, coarse_n, g);
     }
     return *s_run;
 }
@@ -1451,7 +1474,6 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     __shared__ CgScalars s_cg[CG_LOCAL_MAX_BLOBS];
     __shared__ unsigned int s_run;
 
-    extern __shared__ __align__(16) unsigned char cg_dyn[];
     const int G = gridDim.x, c = blockIdx.x, tid = threadIdx.x;
     const bool local = d.cg_local;
     const int S0 = (int)(((long long)d.n_segs * c) / G), S1 = (int)(((long long)d.n_segs * (c + 1)) / G);
@@ -1573,26 +1595,21 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     // d_p and smoother weight, the CTA's 6 rows of X ~ A_c^-1, the blob's
     // coarse residual g and this segment's coarse correction c
     const bool coarse = REG && local && d.coarse;
-    float4 *phi_s = nullptr;
-    float *cvec = nullptr;
-    CoarseCtx cz{};
+    int coarse_n = 0;  // coarse dofs of the CTA's blob (0: no coarse space)
     if (coarse) {
-        size_t off = 6 * (size_t)CG_THREADS * sizeof(T) + (size_t)cc.JC * CG_THREADS * sizeof(int) +
-                     (size_t)cc.J * CG_THREADS * (4 * sizeof(T2) + sizeof(T));
-        off = (off + 15) & ~(size_t)15;
-        phi_s = reinterpret_cast<float4 *>(cg_dyn + off);
-        float *xrow = reinterpret_cast<float *>(phi_s + CG_THREADS);
-        cvec = xrow + 6 * (size_t)d.coarse_nmax;
+        const CoarseView cv = coarse_view<T>(d);
         const BlobParams &bp = d.bp[s_blob[0]];
-        cz = CoarseCtx{xrow, cvec, cvec + 8, cvec + 8 + 6 * 32, bp.coarse_n};
-        cz.h[tid] = 0.f;
-        phi_s[tid] = reg_valid ? d.phi[s_row0[0] + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
+        coarse_n = bp.coarse_n;
+        cv.h[tid] = 0.f;
+        cv.phi[tid] = reg_valid ? d.phi[s_row0[0] + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float *Xg = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (S0 - bp.seg_off)) * bp.coarse_n;
-        for (int k = tid; k < 6 * bp.coarse_n; k += CG_THREADS) xrow[k] = Xg[k];
+        for (int k = tid; k < 6 * bp.coarse_n; k += CG_THREADS) cv.xrow[k] = Xg[k];
     }
     // u = omega D^-1 r + Phi_p c of the thread's row (REG, coarse)
     auto coarse_u = [&](RowState<T> &S) {
-        const float4 f = phi_s[tid];
+        const CoarseView cv = coarse_view<T>(d);
+        const float4 f = cv.phi[tid];
+        const float *cvec = cv.cvec;
         const float cx = cvec[3], cy = cvec[4], cz = cvec[5];
         const T pc[3] = {(T)(cvec[0] + cy * f.z - cz * f.y), (T)(cvec[1] + cz * f.x - cx * f.z),
                          (T)(cvec[2] + cx * f.y - cy * f.x)};
@@ -1601,7 +1618,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     };
     // Phi_p^T v = (v, d_p x v) into ex[0..5]
     auto restrict6 = [&](const T v[3], float *ex) {
-        const float4 f = phi_s[tid];
+        const float4 f = coarse_view<T>(d).phi[tid];
         const float v0 = (float)v[0], v1 = (float)v[1], v2 = (float)v[2];
         ex[0] = v0;
         ex[1] = v1;
@@ -1762,7 +1779,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) return 0u;
         return local_reduce<T>(d, part(), s_cg, sm_df, &s_run, nb, s_blob, s_state, s_alpha, s_beta,
-                               cz);
+                               coarse_n);
     };
     if (coarse) {
         // u_0 = M r_0 needs P^T r_0 of every segment of the blob: restrict
@@ -1777,7 +1794,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (!s_err) {
             const BlobParams &bp = d.bp[s_blob[0]];
-            coarse_apply(cz, tid < cz.n ? __ldcg(slot(bp.seg_off + tid / 6) + 8 + tid % 6) : 0.f);
+            coarse_apply<T>(d, coarse_n, tid < coarse_n ? __ldcg(slot(bp.seg_off + tid / 6) + 8 + tid % 6) : 0.f);
             if (reg_valid) coarse_u(reg);
         }
         parity = 0;
