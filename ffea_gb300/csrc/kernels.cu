@@ -1334,6 +1334,21 @@ __device__ __forceinline__ CoarseView coarse_view(const DeviceBatch &d)
     return v;
 }
 
+// The on-chip matrix copy of the register-resident CG kernel (layout in
+// k_cg), recomputed from kernel parameters where it is used.
+template <typename T>
+__device__ __forceinline__ CgCache<T> cg_cache_view(const DeviceBatch &d)
+{
+    using T2 = typename CgCache<T>::T2;
+    CgCache<T> cc;
+    cc.J = d.cg_cache_slots;
+    cc.JC = d.cg_cache_cols;
+    cc.col = reinterpret_cast<const int *>(cg_dyn + 6 * (size_t)CG_THREADS * sizeof(T));
+    cc.kv2 = reinterpret_cast<const T2 *>(cc.col + (size_t)cc.JC * CG_THREADS);
+    cc.kv1 = reinterpret_cast<const T *>(cc.kv2 + 4 * (size_t)cc.J * CG_THREADS);
+    return cc;
+}
+
 // c = X g, g_j held by thread j (zero beyond n): a 6-value block reduction.
 template <typename T>
 __device__ __forceinline__ void coarse_apply(const DeviceBatch &d, int n, float g)
@@ -1523,8 +1538,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     refresh();
     using V4 = typename Vec4T<T>::type;
     using T2 = typename CgCache<T>::T2;
-    T *X = static_cast<T *>(d.x);
-    V4 *U4 = static_cast<V4 *>(d.u4);
+    // x and the published u in global memory: addresses from the kernel
+    // parameters at each use (no registers held across the iteration)
+    auto X = [&]() { return static_cast<T *>(d.x); };
+    auto U4 = [&]() { return static_cast<V4 *>(d.u4); };
 
     // row of this thread in segment j, and whether it is a free (unpinned) row
     auto row_of = [&](int j, bool &valid) {
@@ -1546,13 +1563,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     T reg_diag = 0;
     T *sx = reinterpret_cast<T *>(cg_dyn);
     T *sdinv = sx + 3 * CG_THREADS;
-    CgCache<T> cc;
     if (REG) {
-        cc.J = d.cg_cache_slots;
-        cc.JC = d.cg_cache_cols;
-        cc.col = reinterpret_cast<const int *>(sdinv + 3 * CG_THREADS);
-        cc.kv2 = reinterpret_cast<const T2 *>(cc.col + (size_t)cc.JC * CG_THREADS);
-        cc.kv1 = reinterpret_cast<const T *>(cc.kv2 + 4 * (size_t)cc.J * CG_THREADS);
+        const CgCache<T> cc = cg_cache_view<T>(d);
         const int row = row_of(0, reg_valid);
         const size_t o = 3 * (size_t)row;
         if (tid < s_rows[0]) {
@@ -1647,7 +1659,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         if (REG && reg_valid) {
             const size_t o = 3 * (size_t)(s_row0[0] + tid);
 #pragma unroll
-            for (int k = 0; k < 3; k++) X[o + k] = sx[k * CG_THREADS + tid];
+            for (int k = 0; k < 3; k++) X()[o + k] = sx[k * CG_THREADS + tid];
         }
     };
     // phase A of segment j: p = u + beta p; s = w + beta s; x += alpha p;
@@ -1658,7 +1670,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             // restart from the true residual: u = M r, published for phase B
             if (reg_valid) {
                 coarse_u(reg);
-                U4[s_row0[0] + tid] = V4{reg.u[0], reg.u[1], reg.u[2], (T)0};
+                U4()[s_row0[0] + tid] = V4{reg.u[0], reg.u[1], reg.u[2], (T)0};
             }
             return;
         }
@@ -1688,7 +1700,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                 pg += S.r[cc2] * S.u[cc2];
                 pr += S.r[cc2] * S.r[cc2];
             }
-            U4[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
+            U4()[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
         }
         if (!REG && valid) store_fields<T>(d, row, loc, RF_X | RF_R | RF_U | RF_S | RF_P);
         const W in[3] = {pg, (W)0, pr};
@@ -1719,7 +1731,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         if (valid) {
             if (state != CG_VERIFY) {
                 T au[3];
-                sell_row_cg<T>(d, row, nomass, diag, U4, au, cc);
+                sell_row_cg<T>(d, row, nomass, diag, static_cast<const V4 *>(d.u4), au,
+                               REG ? cg_cache_view<T>(d) : CgCache<T>{});
 #pragma unroll
                 for (int cc2 = 0; cc2 < 3; cc2++) {
                     S.w[cc2] = au[cc2];
@@ -1729,7 +1742,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                 }
             } else {
                 double rt[3];
-                true_residual_row<T>(d, row, nomass, (double)diag, X, rt);
+                true_residual_row<T>(d, row, nomass, (double)diag, X(), rt);
 #pragma unroll
                 for (int cc2 = 0; cc2 < 3; cc2++) {
                     S.r[cc2] = (T)rt[cc2];
@@ -1737,7 +1750,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                     vr += rt[cc2] * rt[cc2];
                     vg += (double)S.r[cc2] * (double)S.u[cc2];
                 }
-                U4[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
+                U4()[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
             }
         }
         if (!REG && valid) store_fields<T>(d, row, loc, state == CG_VERIFY ? (RF_R | RF_U) : RF_W);
@@ -1806,10 +1819,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         const int row = s_row0[j] + tid;
         if (tid < s_rows[j]) {
             if (coarse) {
-                U4[row] = reg_valid ? V4{reg.u[0], reg.u[1], reg.u[2], (T)0} : V4{(T)0, (T)0, (T)0, (T)0};
+                U4()[row] = reg_valid ? V4{reg.u[0], reg.u[1], reg.u[2], (T)0} : V4{(T)0, (T)0, (T)0, (T)0};
             } else {
                 const T *u = static_cast<const T *>(d.u) + 3 * (size_t)row;
-                U4[row] = V4{u[0], u[1], u[2], (T)0};
+                U4()[row] = V4{u[0], u[1], u[2], (T)0};
             }
         }
     }
