@@ -1322,7 +1322,7 @@ template <typename T>
 __device__ __forceinline__ CoarseView coarse_view(const DeviceBatch &d)
 {
     using T2 = typename CgCache<T>::T2;
-    size_t off = 6 * (size_t)CG_THREADS * sizeof(T) + (size_t)d.cg_cache_cols * CG_THREADS * sizeof(int) +
+    size_t off = 12 * (size_t)CG_THREADS * sizeof(T) + (size_t)d.cg_cache_cols * CG_THREADS * sizeof(int) +
                  (size_t)d.cg_cache_slots * CG_THREADS * (4 * sizeof(T2) + sizeof(T));
     off = (off + 15) & ~(size_t)15;
     CoarseView v;
@@ -1343,7 +1343,7 @@ __device__ __forceinline__ CgCache<T> cg_cache_view(const DeviceBatch &d)
     CgCache<T> cc;
     cc.J = d.cg_cache_slots;
     cc.JC = d.cg_cache_cols;
-    cc.col = reinterpret_cast<const int *>(cg_dyn + 6 * (size_t)CG_THREADS * sizeof(T));
+    cc.col = reinterpret_cast<const int *>(cg_dyn + 12 * (size_t)CG_THREADS * sizeof(T));
     cc.kv2 = reinterpret_cast<const T2 *>(cc.col + (size_t)cc.JC * CG_THREADS);
     cc.kv1 = reinterpret_cast<const T *>(cc.kv2 + 4 * (size_t)cc.J * CG_THREADS);
     return cc;
@@ -1554,10 +1554,12 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         nomass = bp.solver == SOLVER_NOMASS;
         return nomass ? (T)(bp.calc_stokes == 1 ? d.drag[row] : 0.0) : static_cast<const T *>(d.mass_diag)[row];
     };
-    // REG: r, u, w, s, p of the CTA's only segment in registers; x, D^-1 and
-    // the on-chip matrix copy in dynamic shared memory:
-    //   sx[3 CG_THREADS] T | sdinv[3 CG_THREADS] T | col[JC CG_THREADS] int |
-    //   kv2[4 J CG_THREADS] T2 | kv1[J CG_THREADS] T
+    // REG: r, u, w of the CTA's only segment in registers; x, D^-1, p, s and
+    // the on-chip matrix copy in dynamic shared memory (p and s are used in
+    // phase A only; in registers they would be spilled around the SpMV):
+    //   x[3 CG_THREADS] T | dinv[3 CG_THREADS] T | p[3 CG_THREADS] T |
+    //   s[3 CG_THREADS] T | col[JC CG_THREADS] int | kv2[4 J CG_THREADS] T2 |
+    //   kv1[J CG_THREADS] T | coarse region (coarse_view)
     RowState<T> reg;
     bool reg_valid = false, reg_nomass = true;
     T reg_diag = 0;
@@ -1574,8 +1576,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                 reg.r[k] = static_cast<const T *>(d.r)[o + k];
                 reg.u[k] = static_cast<const T *>(d.u)[o + k];
                 reg.w[k] = static_cast<const T *>(d.w)[o + k];
-                reg.s[k] = static_cast<const T *>(d.s)[o + k];
-                reg.p[k] = static_cast<const T *>(d.p)[o + k];
+                sx[(9 + k) * CG_THREADS + tid] = static_cast<const T *>(d.s)[o + k];
+                sx[(6 + k) * CG_THREADS + tid] = static_cast<const T *>(d.p)[o + k];
                 sx[k * CG_THREADS + tid] = static_cast<const T *>(d.x)[o + k];
                 sdinv[k * CG_THREADS + tid] = static_cast<const T *>(d.dinv)[o + k];
             }
@@ -1652,6 +1654,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     };
     // x and D^-1 of the thread's row (component k)
     auto xref = [&](RowState<T> &S, int k) -> T & { return REG ? sx[k * CG_THREADS + tid] : S.x[k]; };
+    auto pref = [&](RowState<T> &S, int k) -> T & { return REG ? sx[(6 + k) * CG_THREADS + tid] : S.p[k]; };
+    auto sref = [&](RowState<T> &S, int k) -> T & { return REG ? sx[(9 + k) * CG_THREADS + tid] : S.s[k]; };
     auto dinv_of = [&](const RowState<T> &S, int k) -> T { return REG ? sdinv[k * CG_THREADS + tid] : S.dinv[k]; };
     // REG: x of the own rows to global memory (for the FP64 true residual and
     // the Euler update; the memory-resident variant keeps it there)
@@ -1688,10 +1692,12 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             const bool first = b == (T)0;
 #pragma unroll
             for (int cc2 = 0; cc2 < 3; cc2++) {
-                S.p[cc2] = first ? S.u[cc2] : S.u[cc2] + b * S.p[cc2];
-                S.s[cc2] = first ? S.w[cc2] : S.w[cc2] + b * S.s[cc2];
-                xref(S, cc2) += a * S.p[cc2];
-                S.r[cc2] -= a * S.s[cc2];
+                const T pn = first ? S.u[cc2] : S.u[cc2] + b * pref(S, cc2);
+                const T sn = first ? S.w[cc2] : S.w[cc2] + b * sref(S, cc2);
+                pref(S, cc2) = pn;
+                sref(S, cc2) = sn;
+                xref(S, cc2) += a * pn;
+                S.r[cc2] -= a * sn;
                 S.u[cc2] = dinv_of(S, cc2) * S.r[cc2];
             }
             if (coarse) coarse_u(S);
@@ -1830,7 +1836,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     if (!s_err)
         for (int j = 0; j < nt; j++) phase_b(j, true);
     unsigned int running = s_err ? 0u : reduce();
-    long long loops = 0;
+    int loops = 0;
     while (!s_err && running > 0) {
         if (local) parity ^= 1;
         else refresh();  // the local reduction refreshed already
@@ -2085,7 +2091,7 @@ static int cg_smem_plan_t(int max_slots, int max_cols, size_t extra_bytes, int *
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, k_cg<T, true>) != cudaSuccess) return -1;
     const size_t reserve = 1024;  // per-CTA system use
-    const size_t state = 6 * (size_t)CG_THREADS * sizeof(T);  // x and D^-1
+    const size_t state = 12 * (size_t)CG_THREADS * sizeof(T);  // x, D^-1, p and s
     const size_t fixed = fa.sharedSizeBytes + reserve + state + extra_bytes;
     if ((size_t)optin < fixed) return -1;
     size_t room = optin - fixed;
