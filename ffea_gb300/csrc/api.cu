@@ -85,6 +85,22 @@ cudaError_t upload(DeviceArena &A, T *&dst, const std::vector<T> &src)
     return cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
+// FP64 host values as T of the batch's precision (float in PREC_MIXED)
+cudaError_t upload_t(DeviceArena &A, void *&dst, const std::vector<double> &src, int precision)
+{
+    if (precision == PREC_FP64) {
+        double *p = nullptr;
+        cudaError_t e = upload(A, p, src);
+        dst = p;
+        return e;
+    }
+    std::vector<float> f(src.begin(), src.end());
+    float *p = nullptr;
+    cudaError_t e = upload(A, p, f);
+    dst = p;
+    return e;
+}
+
 // process-wide jump table per device (for ffea_gpu_rng_draws)
 std::mutex g_table_mu;
 std::vector<mrg::JumpMat *> g_tables;
@@ -209,6 +225,7 @@ int capture_step_graph(ffea_gpu *h, bool with_coarse, cudaGraphExec_t *out, int6
     cudaStream_t s = h->stream;
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    launch_noise(d, s);
     launch_elements(d, s, ELEM_STEP);
     if (d.any_nomass) launch_assemble(d, s);
     int rc = with_coarse ? refresh_coarse(h, s, 1, false) : FFEA_GPU_OK;
@@ -221,7 +238,7 @@ int capture_step_graph(ffea_gpu *h, bool with_coarse, cudaGraphExec_t *out, int6
         cudaGetLastError();
         return fail("capturing the step graph failed: %s / %s", cudaGetErrorString(le), cudaGetErrorString(ce));
     }
-    *fixed = 4 + (d.any_nomass ? 1 : 0) + (with_coarse ? 2 : 0);
+    *fixed = 4 + (d.noise_runs ? 1 : 0) + (d.any_nomass ? 1 : 0) + (with_coarse ? 2 : 0);
     cudaError_t e = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail("cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
@@ -377,6 +394,8 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(upload(A, d.jump_table, table));
     CK(upload(A, d.stream_state, H.stream_state));
     CK(upload(A, d.stream_step, H.stream_step));
+    CK(upload(A, d.noise_run_off, H.noise_run_off));
+    d.noise_runs = H.noise_run_off.back();
     CK(upload(A, d.pos, H.pos));
     CK(upload(A, d.vel, H.vel));
     CK(upload(A, d.drag, H.drag));
@@ -386,7 +405,21 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(upload(A, d.gather_idx, H.gather_idx));
     CK(upload(A, d.fold_ptr, H.fold_ptr));
     CK(upload(A, d.fold_sec, H.fold_sec));
-    CK(upload(A, d.fold_drag, H.fold_drag));
+    CK(upload_t(A, d.fold_amp, H.fold_amp, H.precision));
+    CK(upload_t(A, d.node_amp, H.node_amp, H.precision));
+    {
+        std::vector<double> mt(MAT_T_STRIDE * std::max<size_t>(H.materials.size(), 1), 0.0);
+        for (size_t i = 0; i < H.materials.size(); i++) {
+            const Material &m = H.materials[i];
+            double *o = &mt[MAT_T_STRIDE * i];
+            o[MAT_T_RHO] = m.rho;
+            o[MAT_T_A] = m.A;
+            o[MAT_T_B] = m.B;
+            o[MAT_T_G] = m.G;
+            o[MAT_T_E] = m.E;
+        }
+        CK(upload_t(A, d.mat_t, mt, H.precision));
+    }
     CK(upload(A, d.conn, H.conn));
     CK(upload(A, d.mat_id, H.mat_id));
     CK(upload(A, d.edge_p, H.edge_p));
@@ -409,6 +442,8 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(A.alloc_bytes(d.jinv0, 9 * (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.vol0, (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.efrc, 12 * (size_t)H.ne_pad * ts));
+    CK(A.alloc_bytes(d.elem_noise, 7 * (size_t)H.ne_pad * ts));
+    CK(A.alloc_bytes(d.node_noise, std::max<size_t>(3 * (size_t)H.noise_nodes, 2) * ts));
     CK(A.alloc_bytes(d.g, H.any_nomass ? 9 * (size_t)H.ne_pad * ts : 16));
     CK(A.alloc_bytes(d.sell_val, H.any_nomass ? 9 * (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.sell_mval, H.any_mass ? (size_t)d.n_entries * ts : 16));
@@ -700,6 +735,7 @@ int enqueue_steps(ffea_gpu *h, int32_t nsteps, bool allow_direct)
         }
         if (!allow_direct) return fail("asynchronous stepping needs graph mode without timing");
         if (h->timing) CK(cudaEventRecord(h->ev[0], h->stream));
+        launch_noise(d, h->stream);
         launch_elements(d, h->stream, ELEM_STEP);
         if (h->timing) CK(cudaEventRecord(h->ev[1], h->stream));
         if (d.any_nomass) launch_assemble(d, h->stream);

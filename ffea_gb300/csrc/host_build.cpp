@@ -492,7 +492,10 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
                     if (m.stokes_drag[s] == 0.0) continue;
                     for (int k = 0; k < 2; k++) {
                         int32_t corner = m.topology[10 * e + kMid[j - 4][k]];
-                        fold[H.maps[b].lin_of_orig[corner]].push_back({s, m.stokes_drag[s]});
+                        // noise amplitude of the secondary node, the expression of
+                        // src/Blob.cpp:3896 evaluated once here instead of every step
+                        fold[H.maps[b].lin_of_orig[corner]].push_back(
+                            {s, std::sqrt((24 * p.kT * m.stokes_drag[s]) / (p.dt))});
                     }
                 }
         }
@@ -501,8 +504,17 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
         for (int32_t g = 0; g < H.nl_pad; g++)
             for (auto &pr : fold[g]) {
                 H.fold_sec.push_back(pr.first);
-                H.fold_drag.push_back(pr.second);
+                H.fold_amp.push_back(pr.second);
             }
+        // the same amplitude for the linear nodes' own draws
+        H.node_amp.assign(H.nl_pad, 0.0);
+        for (int b = 0; b < num_blobs; b++) {
+            const ffea_gpu_params &p = params[b];
+            if (p.calc_stokes != 1 || p.calc_noise != 1) continue;
+            const BlobParams &bp = H.bp[b];
+            for (int32_t g = bp.node_off; g < bp.node_off + bp.node_cnt; g++)
+                if (H.drag[g] != 0.0) H.node_amp[g] = std::sqrt((24 * p.kT * H.drag[g]) / (p.dt));
+        }
     }
 
     // ---- edges and their (elem, a, b) terms -------------------------------------
@@ -624,6 +636,27 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
             }
             per_stream_draws[0] = acc;
         }
+        // runs of the noise kernel: each generates NOISE_RUN consecutive
+        // draws of one blob's element or node range after one jump
+        H.noise_run_off.assign(2 * (size_t)num_blobs + 1, 0);
+        int64_t runs = 0, nodes = 0;
+        for (int b = 0; b < num_blobs; b++) {
+            const ffea_gpu_params &p = params[b];
+            const int64_t ed = (p.calc_noise == 1) ? 7ll * meshes[b].num_elements : 0;
+            const int64_t nd = (p.calc_noise == 1 && p.calc_stokes == 1) ? 3ll * meshes[b].num_nodes : 0;
+            H.noise_run_off[2 * b] = (int32_t)runs;
+            runs += (ed + NOISE_RUN - 1) / NOISE_RUN;
+            H.noise_run_off[2 * b + 1] = (int32_t)runs;
+            runs += (nd + NOISE_RUN - 1) / NOISE_RUN;
+            H.bp[b].noise_node_off = (int32_t)nodes;
+            if (nd) nodes += meshes[b].num_nodes;
+        }
+        if (runs >= (1ll << 31) || nodes >= (1ll << 31)) {
+            err = "too many random draws per step";
+            return false;
+        }
+        H.noise_run_off[2 * (size_t)num_blobs] = (int32_t)runs;
+        H.noise_nodes = nodes;
         H.stream_step.resize(H.num_streams);
         for (int s = 0; s < H.num_streams; s++) {
             uint64_t six[6];

@@ -36,7 +36,8 @@ struct HostBatch {
     std::vector<int32_t> orig;           // per padded node: original index in its blob, -1 padding
     std::vector<int32_t> gather_ptr, gather_idx;          // node -> (elem*4 + corner), element order
     std::vector<int32_t> fold_ptr, fold_sec;              // node -> secondary nodes folded onto it
-    std::vector<double> fold_drag;
+    std::vector<double> fold_amp;                         // noise amplitude of each folded secondary node
+    std::vector<double> node_amp;                         // per padded node: amplitude of its own noise
     std::vector<int32_t> edge_p, edge_q;                  // edges (p < q), sorted by (p, q)
     std::vector<int32_t> edge_cptr, edge_cidx;            // edge -> (elem*16 + a*4 + b), element order
     // SELL-32 layout of the node-node matrix: slices of 32 consecutive rows,
@@ -57,6 +58,10 @@ struct HostBatch {
     int32_t num_streams = 0;
     std::vector<uint32_t> stream_state;                   // 6 per stream
     std::vector<mrg::JumpMat> stream_step;                // per stream: A^(draws per step)
+    // the noise kernel's runs of NOISE_RUN draws: prefix over (blob, kind)
+    // pairs, kind 0 = element draws, 1 = node draws (2 * num_blobs + 1)
+    std::vector<int32_t> noise_run_off;
+    int64_t noise_nodes = 0;                              // nodes with node draws (all blobs)
     std::vector<BlobMap> maps;
 };
 

@@ -135,6 +135,43 @@ __device__ __forceinline__ void jacobian(const double *pos, int4 c, T J[3][3])
     }
 }
 
+// Double-float accumulation (Knuth's TwoSum, error-free in FP32): sums with
+// ~48-bit precision on the FP32 pipes, which on GB300 run many times faster
+// than FP64.
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF df_add(DF a, DF b)
+{
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float err = (a.hi - (s - bb)) + (b.hi - bb);
+    err += a.lo + b.lo;
+    const float hi = s + err;
+    return DF{hi, err - (hi - s)};
+}
+
+// Force sum of the node kernel: FP64 in FP64 mode; in mixed precision a
+// double-float sum of the FP32 element forces, which keeps the FP64 pipes
+// (1/64 of the FP32 rate on GB300) out of the per-corner loop.
+template <typename T> struct ForceSum {
+    double v = 0.0;
+    __device__ __forceinline__ void add(T x) { v += (double)x; }
+    __device__ __forceinline__ void add_d(double x) { v += x; }
+    __device__ __forceinline__ double value() const { return v; }
+};
+template <> struct ForceSum<float> {
+    DF v{0.f, 0.f};
+    __device__ __forceinline__ void add(float x) { v = df_add(v, DF{x, 0.f}); }
+    __device__ __forceinline__ void add_d(double x)
+    {
+        const float h = (float)x;
+        v = df_add(v, DF{h, (float)(x - (double)h)});
+    }
+    __device__ __forceinline__ double value() const { return (double)v.hi + (double)v.lo; }
+};
+
 template <typename T>
 __device__ __forceinline__ void load_g(const T *g, int el, int a, T out[3])
 {
@@ -186,6 +223,52 @@ __global__ void k_rest_state(DeviceBatch d)
     d.det_sign[e] = det > 0 ? 1 : (det < 0 ? -1 : 0);
 }
 
+// The step's random draws, ahead of the element and node kernels.  Each
+// thread jumps once to the start of its run (mrg::jump, four table products)
+// and draws NOISE_RUN consecutive values from there, so the jump is paid once
+// per 32 draws rather than once per element or node; every secondary node's
+// draws, which two linear nodes fold in, are made once.  The values are the
+// same centred draws the consumers took from their own jumps: element e of a
+// blob uses draws elem_draw_base + 7 le .. +6 (src/tetra_element_linear.cpp:417-436),
+// node n uses node_draw_base + 3 n .. +2 in original numbering (src/Blob.cpp:3867-3899).
+// One centred draw: FP64 as the reference computes it (FP64 mode); in mixed
+// precision the FP32 value from the same integer state (mrg::centred_f),
+// within 2 ulp of rounding the FP64 value, with no FP64 instruction.
+template <typename T> __device__ __forceinline__ T draw(uint32_t *st);
+template <> __device__ __forceinline__ double draw<double>(uint32_t *st) { return mrg::centred(st); }
+template <> __device__ __forceinline__ float draw<float>(uint32_t *st) { return mrg::centred_f(st); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_noise(DeviceBatch d)
+{
+    const int run = blockIdx.x * blockDim.x + threadIdx.x;
+    if (run >= d.noise_runs) return;
+    // the (blob, kind) pair holding this run: the last prefix entry <= run
+    int lo = 0, hi = 2 * d.num_blobs;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (d.noise_run_off[mid] <= run) lo = mid;
+        else hi = mid;
+    }
+    const int b = lo >> 1, kind = lo & 1;
+    if (d.status[b]) return;  // a failed blob takes no further step
+    const BlobParams &bp = d.bp[b];
+    const uint32_t first = (uint32_t)(run - d.noise_run_off[lo]) * NOISE_RUN;
+    const uint32_t total = kind == 0 ? 7u * (uint32_t)bp.elem_cnt : 3u * (uint32_t)bp.num_nodes_total;
+    const int cnt = (int)min((uint32_t)NOISE_RUN, total - first);
+    uint32_t st[6];
+#pragma unroll
+    for (int i = 0; i < 6; i++) st[i] = d.stream_state[6 * bp.stream + i];
+    mrg::jump(d.jump_table, (kind == 0 ? bp.elem_draw_base : bp.node_draw_base) + first, st);
+    if (kind == 0) {
+        T *o = static_cast<T *>(d.elem_noise) + 7 * (size_t)bp.elem_off + first;
+        for (int i = 0; i < cnt; i++) o[i] = draw<T>(st);
+    } else {
+        T *o = static_cast<T *>(d.node_noise) + 3 * (size_t)bp.noise_node_off + first;
+        for (int i = 0; i < cnt; i++) o[i] = draw<T>(st);
+    }
+}
+
 // The per-step element kernel.
 template <typename T>
 __global__ void __launch_bounds__(ELEM_TILE) k_elements(DeviceBatch d, int mode)
@@ -211,8 +294,8 @@ __global__ void __launch_bounds__(ELEM_TILE) k_elements(DeviceBatch d, int mode)
         }
         if (geo.det != (T)0) d.det_sign[e] = geo.det > (T)0 ? 1 : -1;
     }
-    const Material m = d.mats[d.mat_id[e]];
-    const T A = (T)m.A, B = (T)m.B, G = (T)m.G, Eb = (T)m.E;
+    const T *m = static_cast<const T *>(d.mat_t) + MAT_T_STRIDE * (size_t)d.mat_id[e];
+    const T A = m[MAT_T_A], B = m[MAT_T_B], G = m[MAT_T_G], Eb = m[MAT_T_E];
     const T vol = geo.vol;
     const T *dpsi = geo.dpsi;
 
@@ -255,13 +338,10 @@ __global__ void __launch_bounds__(ELEM_TILE) k_elements(DeviceBatch d, int mode)
     S[2][2] += cb;
     // fluctuating stress: 7 draws at offset 7*element (src/tetra_element_linear.cpp:417-436)
     if (bp.calc_noise == 1) {
-        uint32_t st[6];
-#pragma unroll
-        for (int i = 0; i < 6; i++) st[i] = d.stream_state[6 * bp.stream + i];
-        mrg::jump(d.jump_table, bp.elem_draw_base + 7u * (uint32_t)le, st);
+        const T *nz = static_cast<const T *>(d.elem_noise) + 7 * (size_t)e;  // k_noise
         T u[7];
 #pragma unroll
-        for (int k = 0; k < 7; k++) u[k] = (T)mrg::centred(st);
+        for (int k = 0; k < 7; k++) u[k] = nz[k];
         const T cf = sqrt(((T)24 * (T)bp.kT) / (vol * (T)bp.dt));
         const T bf = sqrt(B) * u[0];
         const T s2a = sqrt((T)2 * A), sa = sqrt(A);
@@ -326,8 +406,8 @@ __global__ void __launch_bounds__(EDGE_TILE) k_assemble(DeviceBatch d)
         T ga[3], gb[3];
         load_g<T>(g, el, a, ga);
         load_g<T>(g, el, bb, gb);
-        const Material m = d.mats[d.mat_id[el]];
-        const T A = (T)m.A, B = (T)m.B;
+        const T *m = static_cast<const T *>(d.mat_t) + MAT_T_STRIDE * (size_t)d.mat_id[el];
+        const T A = m[MAT_T_A], B = m[MAT_T_B];
         const T gab = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
 #pragma unroll
         for (int i = 0; i < 3; i++)
@@ -389,58 +469,58 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
     const bool failed = d.status[b] != 0;
     const bool valid = local < bp.node_cnt && !(d.flags[row] & NODE_PINNED) && !failed;
     const bool nomass = bp.solver == SOLVER_NOMASS;
-    double f[3] = {0.0, 0.0, 0.0};
-    double D[3] = {0.0, 0.0, 0.0};
+    ForceSum<T> fs[3];
+    T D[3] = {(T)0, (T)0, (T)0};
     const double drag = bp.calc_stokes == 1 ? d.drag[row] : 0.0;
     if (valid) {
         const T *ef = static_cast<const T *>(d.efrc);
         const T *g = static_cast<const T *>(d.g);
+        const T *mt = static_cast<const T *>(d.mat_t);
         for (int k = d.gather_ptr[row]; k < d.gather_ptr[row + 1]; k++) {
             const int gi = d.gather_idx[k];
             const int el = gi >> 2, a = gi & 3;
             if (!use_given_rhs) {
-                f[0] += (double)ef[12 * (size_t)el + 3 * a];
-                f[1] += (double)ef[12 * (size_t)el + 3 * a + 1];
-                f[2] += (double)ef[12 * (size_t)el + 3 * a + 2];
+#pragma unroll
+                for (int i = 0; i < 3; i++) fs[i].add(ef[12 * (size_t)el + 3 * a + i]);
             }
             if (nomass) {
                 T ga[3];
                 load_g<T>(g, el, a, ga);
-                const Material m = d.mats[d.mat_id[el]];
+                const T *m = mt + MAT_T_STRIDE * (size_t)d.mat_id[el];
+                const T mA = m[MAT_T_A], mB = m[MAT_T_B];
                 const T gg = ga[0] * ga[0] + ga[1] * ga[1] + ga[2] * ga[2];
 #pragma unroll
-                for (int i = 0; i < 3; i++) D[i] += (double)((T)m.A * (gg + ga[i] * ga[i]) + (T)m.B * ga[i] * ga[i]);
+                for (int i = 0; i < 3; i++) D[i] += mA * (gg + ga[i] * ga[i]) + mB * ga[i] * ga[i];
             }
         }
         if (!use_given_rhs) {
             if (!nomass && bp.calc_stokes == 1) {
 #pragma unroll
-                for (int i = 0; i < 3; i++) f[i] -= d.vel[3 * (size_t)row + i] * drag;
+                for (int i = 0; i < 3; i++) fs[i].add_d(-(d.vel[3 * (size_t)row + i] * drag));
             }
             if (bp.calc_noise == 1 && bp.calc_stokes == 1) {
-                const uint32_t *s0 = d.stream_state + 6 * bp.stream;
+                // draws from k_noise, amplitudes sqrt((24 kT drag) / dt) set up once
+                const T *nz = static_cast<const T *>(d.node_noise) + 3 * (size_t)bp.noise_node_off;
+                const T *na = static_cast<const T *>(d.node_amp), *fa = static_cast<const T *>(d.fold_amp);
                 if (drag != 0.0) {
-                    uint32_t st[6];
+                    const T *z = nz + 3 * (size_t)d.orig[row];
+                    const T amp = na[row];
 #pragma unroll
-                    for (int i = 0; i < 6; i++) st[i] = s0[i];
-                    mrg::jump(d.jump_table, bp.node_draw_base + 3u * (uint32_t)d.orig[row], st);
-                    const double amp = sqrt((24 * bp.kT * drag) / (bp.dt));
-#pragma unroll
-                    for (int i = 0; i < 3; i++) f[i] -= mrg::centred(st) * amp;
+                    for (int i = 0; i < 3; i++) fs[i].add(-(z[i] * amp));
                 }
                 // secondary nodes with a drag: half of their force lands here
                 for (int k = d.fold_ptr[row]; k < d.fold_ptr[row + 1]; k++) {
-                    uint32_t st[6];
+                    const T *z = nz + 3 * (size_t)d.fold_sec[k];
+                    const T amp = fa[k];
 #pragma unroll
-                    for (int i = 0; i < 6; i++) st[i] = s0[i];
-                    mrg::jump(d.jump_table, bp.node_draw_base + 3u * (uint32_t)d.fold_sec[k], st);
-                    const double amp = sqrt((24 * bp.kT * d.fold_drag[k]) / (bp.dt));
-#pragma unroll
-                    for (int i = 0; i < 3; i++) f[i] += 0.5 * (-(mrg::centred(st) * amp));
+                    for (int i = 0; i < 3; i++) fs[i].add((T)0.5 * (-(z[i] * amp)));
                 }
             }
         }
     }
+    double f[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[i] = fs[i].value();
     if (use_given_rhs && valid) {
 #pragma unroll
         for (int i = 0; i < 3; i++) f[i] = d.rhs[3 * (size_t)row + i];
@@ -448,7 +528,7 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
     T *dinv = static_cast<T *>(d.dinv);
     if (nomass) {
 #pragma unroll
-        for (int i = 0; i < 3; i++) dinv[3 * (size_t)row + i] = valid ? (T)(1.0 / (D[i] + drag)) : (T)1;
+        for (int i = 0; i < 3; i++) dinv[3 * (size_t)row + i] = valid ? (T)1 / (D[i] + (T)drag) : (T)1;
     }
     // CG start: x = 0, r = f, u = D^-1 r, w = s = p = 0
     T *x = static_cast<T *>(d.x), *r = static_cast<T *>(d.r), *u = static_cast<T *>(d.u);
@@ -884,23 +964,6 @@ __device__ __forceinline__ void store_row(const DeviceBatch &d, int row, const R
         static_cast<T *>(d.s)[o + c] = S.s[c];
         static_cast<T *>(d.p)[o + c] = S.p[c];
     }
-}
-
-// Double-float accumulation (Knuth's TwoSum, error-free in FP32): sums with
-// ~48-bit precision on the FP32 pipes, which on GB300 run many times faster
-// than FP64.
-struct DF {
-    float hi, lo;
-};
-
-__device__ __forceinline__ DF df_add(DF a, DF b)
-{
-    const float s = a.hi + b.hi;
-    const float bb = s - a.hi;
-    float err = (a.hi - (s - bb)) + (b.hi - bb);
-    err += a.lo + b.lo;
-    const float hi = s + err;
-    return DF{hi, err - (hi - s)};
 }
 
 __device__ __forceinline__ DF df_warp_sum(DF v)
@@ -2073,6 +2136,12 @@ void launch_assemble(const DeviceBatch &d, cudaStream_t s)
 {
     if (d.n_edges == 0) return;
     PREC_DISPATCH(d, k_assemble, blocks_for(d.n_edges, EDGE_TILE), EDGE_TILE, s, d);
+}
+
+void launch_noise(const DeviceBatch &d, cudaStream_t s)
+{
+    if (d.noise_runs == 0) return;
+    PREC_DISPATCH(d, k_noise, blocks_for(d.noise_runs, 256), 256, s, d);
 }
 
 void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs)

@@ -38,19 +38,28 @@ struct DeviceBatch {
     // blobs
     BlobParams *bp = nullptr;
     Material *mats = nullptr;
+    void *mat_t = nullptr;        // the material table in T (MAT_T_STRIDE per material)
     int32_t *tile_blob = nullptr, *etile_blob = nullptr;
     int32_t *seg_row0 = nullptr, *seg_rows = nullptr, *seg_blob = nullptr;   // CG segments
     // RNG
     mrg::JumpMat *jump_table = nullptr;
     uint32_t *stream_state = nullptr;
     mrg::JumpMat *stream_step = nullptr;
+    // the step's draws, generated up front (k_noise): element draws 7 T per
+    // padded element, node draws 3 T per node in original numbering
+    // (from bp.noise_node_off); runs of NOISE_RUN draws, prefix per (blob, kind)
+    int32_t noise_runs = 0;
+    int32_t *noise_run_off = nullptr;
+    void *elem_noise = nullptr;
+    void *node_noise = nullptr;
     // nodes (FP64 state and rhs)
     double *pos = nullptr, *vel = nullptr, *drag = nullptr, *rhs = nullptr;
     uint8_t *flags = nullptr;
     int32_t *orig = nullptr;
     int32_t *gather_ptr = nullptr, *gather_idx = nullptr;
     int32_t *fold_ptr = nullptr, *fold_sec = nullptr;
-    double *fold_drag = nullptr;
+    void *fold_amp = nullptr;     // T: noise amplitude sqrt(24 kT drag / dt) of each folded secondary node
+    void *node_amp = nullptr;     // T per padded node: the amplitude of its own draws
     // CG vectors, T-typed, 3 per padded node: solution x, residual r,
     // u = D^-1 r, w = A u, the recurrences s, p; Jacobi dinv
     void *x = nullptr, *r = nullptr, *u = nullptr, *w = nullptr, *p = nullptr, *s = nullptr, *dinv = nullptr;
@@ -79,6 +88,9 @@ struct DeviceBatch {
     unsigned long long *loop_count = nullptr;  // CG iterations executed by the persistent kernel (max over blobs)
 };
 
+// material table in the working precision T: no FP64 conversion per use
+enum MatT { MAT_T_RHO = 0, MAT_T_A = 1, MAT_T_B = 2, MAT_T_G = 3, MAT_T_E = 4, MAT_T_STRIDE = 8 };
+
 // reduction counter slots
 enum CounterSlot { CNT_NODES = 0, CNT_ENERGY = 1, CNT_COUNT = 4 };
 
@@ -95,6 +107,8 @@ void launch_rest_state(const DeviceBatch &d, cudaStream_t s);
 void launch_mass_matrix(const DeviceBatch &d, cudaStream_t s);
 void launch_elements(const DeviceBatch &d, cudaStream_t s, int mode);
 void launch_assemble(const DeviceBatch &d, cudaStream_t s);
+// the step's random draws (nothing when no blob draws)
+void launch_noise(const DeviceBatch &d, cudaStream_t s);
 void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs);
 cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s);
 // The CG kernel's grid barrier with a target that no arrival reaches and the

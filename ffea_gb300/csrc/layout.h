@@ -19,6 +19,7 @@ constexpr int ELEM_TILE = 128;   // elements per CTA of the element kernel
 constexpr int EDGE_TILE = 256;
 constexpr int MAX_BLOBS = 1 << 20;
 constexpr int CG_SEG_MAX_ROWS = 1024;  // rows of a CG segment (one per thread of a CG CTA)
+constexpr int NOISE_RUN = 32;          // consecutive draws per thread of the noise kernel (one jump each)
 
 enum SolverKind : int32_t { SOLVER_NOMASS = 0, SOLVER_MASS = 1 };
 enum Precision : int32_t { PREC_FP64 = 0, PREC_MIXED = 1 };
@@ -47,6 +48,7 @@ struct BlobParams {
     int32_t coarse_off, coarse_n;           // two-level: first coarse dof, number of coarse dofs (6 per segment)
     int32_t coarse_xoff;                    // offset of the blob's dense coarse matrices (coarse_n^2 floats)
     int32_t num_nodes_total;                // N_t of the reference (linear + secondary)
+    int32_t noise_node_off;                 // first node of the blob's node draws in the node-noise buffer
     int32_t true_residual;
 };
 

@@ -84,9 +84,10 @@ MRG_HD void jump(const JumpMat *table, uint32_t off, uint32_t *s)
     }
 }
 
-// One draw: the recurrences of src/RngStream.cpp:270-283 on int64, then the
-// combination of :286 in double.  Returns u in (0, 1).
-MRG_HD double u01(uint32_t *s)
+// One step of both components (the recurrences of src/RngStream.cpp:270-283
+// on int64); returns n = (p1 - p2) mod m1 in [1, m1] (m1 when p1 == p2),
+// the integer that :286 scales by 1 / (m1 + 1).
+MRG_HD int64_t next_n(uint32_t *s)
 {
     int64_t p1 = 1403580ll * (int64_t)s[1] - 810728ll * (int64_t)s[0];
     p1 %= (int64_t)M1;
@@ -96,14 +97,32 @@ MRG_HD double u01(uint32_t *s)
     p2 %= (int64_t)M2;
     if (p2 < 0) p2 += M2;
     s[3] = s[4]; s[4] = s[5]; s[5] = (uint32_t)p2;
+    return (p1 > p2) ? p1 - p2 : p1 - p2 + (int64_t)M1;
+}
+
+// One draw: the combination of src/RngStream.cpp:286 in double.  Returns u
+// in (0, 1).
+MRG_HD double u01(uint32_t *s)
+{
     const double norm = 1.0 / (4294967087.0 + 1.0);
-    return (p1 > p2) ? (double)(p1 - p2) * norm : (double)(p1 - p2 + (int64_t)M1) * norm;
+    return (double)next_n(s) * norm;
 }
 
 // RAND(-.5, .5) of include/tetra_element_linear.h:118: -0.5 + 1.0 * u.
 MRG_HD double centred(uint32_t *s)
 {
     return -0.5 + u01(s);
+}
+
+// The same draw in FP32 with no FP64 arithmetic: -0.5 + n / (m1 + 1) is
+// (n - (m1 + 1) / 2) / (m1 + 1) exactly, an int32 numerator times one
+// constant; two FP32 roundings (numerator, product) put it within 2 ulp of
+// the FP64 value rounded to FP32.  The stream's integer state is the same.
+MRG_HD float centred_f(uint32_t *s)
+{
+    constexpr float norm = (float)(1.0 / (4294967087.0 + 1.0));
+    const int32_t q = (int32_t)(next_n(s) - 2147483544ll);  // (m1 + 1) / 2
+    return (float)q * norm;
 }
 
 // ---- host-side helpers (table construction) --------------------------------
