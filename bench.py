@@ -345,12 +345,14 @@ def measure_arm(args, specs, precond: str, world: int, local: int):
     total_ms = max_over_ranks(total_ms, world)
     value = aggregate_throughput(N, K, world, total_ms / 1e3)
 
-    # end to end through the C ABI with the caller's host buffers (all N_t
-    # nodes in the reference's order): set_nodes (positions and velocities,
-    # H2D) + step + get_nodes (positions, velocities, forces, D2H)
+    # end to end through the C ABI with the caller's pinned host buffers (all
+    # N_t nodes in the reference's order): set_nodes (positions and
+    # velocities, H2D) + step + get_nodes (positions, velocities, forces, D2H)
     blobs = [w.blob(i) for i in range(len(specs))]
     Nt = sum(s_.mesh.num_nodes for s_ in specs)
-    bufs = [tuple(np.empty((s_.mesh.num_nodes, 3)) for _ in range(3)) for s_ in specs]
+    # pinned (page-locked) host arrays, as a caller that streams state would hold
+    bufs = [tuple(torch.empty((s_.mesh.num_nodes, 3), dtype=torch.float64, pin_memory=True).numpy()
+                  for _ in range(3)) for s_ in specs]
     for b_, buf in zip(blobs, bufs):
         b_.get_nodes(out=buf)
     Ke = args.e2e_steps or max(3, K // 2)

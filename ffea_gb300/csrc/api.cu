@@ -136,6 +136,7 @@ struct ffea_gpu {
     int2 *io_src = nullptr;
     double *io_secvel = nullptr;  // secondary-node velocities (mass blobs keep them; NoMass report 0)
     double *io_stage = nullptr;   // 9 doubles per node of the largest blob (pos, vel, force)
+    int *io_moved = nullptr;      // set_nodes: 1 when a position changed
     int32_t io_max_nodes = 0;
     int precond = FFEA_GPU_PRECOND_JACOBI;     // in use, after fall-backs
     MpnnBuffers mpnn;                          // learned smoother weights (allocated on first use)
@@ -184,14 +185,20 @@ __global__ void k_nodes_out(DeviceBatch d, const int2 *src, int n, const double 
 // The inverse for positions and velocities: corner nodes set their row;
 // secondary velocities are kept for the mass solver.
 __global__ void k_nodes_in(DeviceBatch d, const int2 *src, int n, const double *pos, const double *vel,
-                           double *secvel, int mass)
+                           double *secvel, int mass, int *moved)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int2 s = src[i];
     for (int c = 0; c < 3; c++) {
         if (s.x >= 0 && s.y < 0) {
-            if (pos) d.pos[3 * (size_t)s.x + c] = pos[3 * (size_t)i + c];
+            if (pos) {
+                double &dst = d.pos[3 * (size_t)s.x + c];
+                const double v = pos[3 * (size_t)i + c];
+                if (__double_as_longlong(dst) != __double_as_longlong(v)) *moved = 1;
+                dst = v;
+                if (d.pos_df) d.pos_df[3 * (size_t)s.x + c] = split_pos(v);
+            }
             if (vel) d.vel[3 * (size_t)s.x + c] = vel[3 * (size_t)i + c];
         } else if (vel && mass) {
             secvel[3 * (size_t)i + c] = vel[3 * (size_t)i + c];
@@ -397,6 +404,11 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(upload(A, d.noise_run_off, H.noise_run_off));
     d.noise_runs = H.noise_run_off.back();
     CK(upload(A, d.pos, H.pos));
+    if (H.precision == PREC_MIXED) {
+        std::vector<float2> pdf(H.pos.size());
+        for (size_t i = 0; i < H.pos.size(); i++) pdf[i] = split_pos(H.pos[i]);
+        CK(upload(A, d.pos_df, pdf));
+    }
     CK(upload(A, d.vel, H.vel));
     CK(upload(A, d.drag, H.drag));
     CK(upload(A, d.flags, H.flags));
@@ -499,6 +511,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
         CK(upload(A, h->io_src, src));
         CK(upload(A, h->io_secvel, secvel));
         CK(A.alloc(h->io_stage, 9 * (size_t)h->io_max_nodes));
+        CK(A.alloc(h->io_moved, 1));
     }
     launch_rest_state(d, h->stream);
     if (d.any_mass) launch_mass_matrix(d, h->stream);
@@ -836,7 +849,6 @@ int ffea_gpu_get_nodes(ffea_gpu_t *h, int32_t blob, double *pos, double *vel, do
 int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const double *vel)
 {
     if (check_blob(h, blob)) return FFEA_GPU_ERROR;
-    if (pos) h->steps_done = 0;  // new positions: refresh the coarse space on the next step
     const BlobParams &bp = h->host.bp[blob];
     const int32_t N = h->host.maps[blob].num_nodes_total;
     const int64_t o = h->io_off[blob];
@@ -845,10 +857,19 @@ int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const dou
     if (N > 0 && (pos || vel)) {
         if (pos) CK(cudaMemcpyAsync(st, pos, bytes, cudaMemcpyHostToDevice, h->stream));
         if (vel) CK(cudaMemcpyAsync(st + 3 * (size_t)N, vel, bytes, cudaMemcpyHostToDevice, h->stream));
+        if (pos) CK(cudaMemsetAsync(h->io_moved, 0, sizeof(int), h->stream));
         k_nodes_in<<<(N + 255) / 256, 256, 0, h->stream>>>(h->dev, h->io_src + o, N, pos ? st : nullptr,
                                                           vel ? st + 3 * (size_t)N : nullptr, h->io_secvel + 3 * o,
-                                                          bp.solver == SOLVER_MASS);
+                                                          bp.solver == SOLVER_MASS, h->io_moved);
         count_launches(1);
+        if (pos) {
+            // positions that differ from the current ones: refresh the
+            // coarse space on the next step (the same positions need none)
+            int moved = 0;
+            CK(cudaMemcpyAsync(&moved, h->io_moved, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            if (moved) h->steps_done = 0;
+        }
     }
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());

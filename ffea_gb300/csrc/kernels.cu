@@ -135,6 +135,29 @@ __device__ __forceinline__ void jacobian(const double *pos, int4 c, T J[3][3])
     }
 }
 
+// Edge vectors of the element from the double-float copy of the positions
+// (mixed precision): (hi_n - hi_0) + (lo_n - lo_0), within an FP32 rounding
+// of the FP64 difference, with no FP64 instruction.  FP64 mode reads the
+// FP64 positions.
+template <typename T>
+__device__ __forceinline__ void jacobian_t(const DeviceBatch &d, int4 c, T J[3][3])
+{
+    if constexpr (sizeof(T) == sizeof(double)) {
+        jacobian<T>(d.pos, c, J);
+    } else {
+        const float2 *p = d.pos_df;
+        const float2 a[3] = {p[3 * (size_t)c.x], p[3 * (size_t)c.x + 1], p[3 * (size_t)c.x + 2]};
+        const int n[3] = {c.y, c.z, c.w};
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const float2 q = p[3 * (size_t)n[r] + k];
+                J[r][k] = (q.x - a[k].x) + (q.y - a[k].y);
+            }
+    }
+}
+
 // Double-float accumulation (Knuth's TwoSum, error-free in FP32): sums with
 // ~48-bit precision on the FP32 pipes, which on GB300 run many times faster
 // than FP64.
@@ -239,33 +262,46 @@ template <> __device__ __forceinline__ double draw<double>(uint32_t *st) { retur
 template <> __device__ __forceinline__ float draw<float>(uint32_t *st) { return mrg::centred_f(st); }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_noise(DeviceBatch d)
+__global__ void __launch_bounds__(NOISE_THREADS) k_noise(DeviceBatch d)
 {
+    // each warp stages its 32 runs in shared memory (row per run, padded to
+    // 33 so that both the per-run writes and the per-draw reads are
+    // conflict-free for FP32), then stores run by run, one coalesced line
+    // per run, instead of 32 scattered words per store instruction
+    static_assert(NOISE_RUN == 32 && NOISE_THREADS % 32 == 0, "one lane per draw of a run");
+    __shared__ T stage[NOISE_THREADS / 32][32][NOISE_RUN + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int run = blockIdx.x * blockDim.x + threadIdx.x;
-    if (run >= d.noise_runs) return;
-    // the (blob, kind) pair holding this run: the last prefix entry <= run
-    int lo = 0, hi = 2 * d.num_blobs;
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (d.noise_run_off[mid] <= run) lo = mid;
-        else hi = mid;
-    }
-    const int b = lo >> 1, kind = lo & 1;
-    if (d.status[b]) return;  // a failed blob takes no further step
-    const BlobParams &bp = d.bp[b];
-    const uint32_t first = (uint32_t)(run - d.noise_run_off[lo]) * NOISE_RUN;
-    const uint32_t total = kind == 0 ? 7u * (uint32_t)bp.elem_cnt : 3u * (uint32_t)bp.num_nodes_total;
-    const int cnt = (int)min((uint32_t)NOISE_RUN, total - first);
-    uint32_t st[6];
+    int cnt = 0;
+    T *dst = nullptr;
+    if (run < d.noise_runs) {
+        // the (blob, kind) pair holding this run: the last prefix entry <= run
+        int lo = 0, hi = 2 * d.num_blobs;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (d.noise_run_off[mid] <= run) lo = mid;
+            else hi = mid;
+        }
+        const int b = lo >> 1, kind = lo & 1;
+        if (d.status[b] == 0) {  // a failed blob takes no further step
+            const BlobParams &bp = d.bp[b];
+            const uint32_t first = (uint32_t)(run - d.noise_run_off[lo]) * NOISE_RUN;
+            const uint32_t total = kind == 0 ? 7u * (uint32_t)bp.elem_cnt : 3u * (uint32_t)bp.num_nodes_total;
+            cnt = (int)min((uint32_t)NOISE_RUN, total - first);
+            dst = kind == 0 ? static_cast<T *>(d.elem_noise) + 7 * (size_t)bp.elem_off + first
+                            : static_cast<T *>(d.node_noise) + 3 * (size_t)bp.noise_node_off + first;
+            uint32_t st[6];
 #pragma unroll
-    for (int i = 0; i < 6; i++) st[i] = d.stream_state[6 * bp.stream + i];
-    mrg::jump(d.jump_table, (kind == 0 ? bp.elem_draw_base : bp.node_draw_base) + first, st);
-    if (kind == 0) {
-        T *o = static_cast<T *>(d.elem_noise) + 7 * (size_t)bp.elem_off + first;
-        for (int i = 0; i < cnt; i++) o[i] = draw<T>(st);
-    } else {
-        T *o = static_cast<T *>(d.node_noise) + 3 * (size_t)bp.noise_node_off + first;
-        for (int i = 0; i < cnt; i++) o[i] = draw<T>(st);
+            for (int i = 0; i < 6; i++) st[i] = d.stream_state[6 * bp.stream + i];
+            mrg::jump(d.jump_table, (kind == 0 ? bp.elem_draw_base : bp.node_draw_base) + first, st);
+            for (int i = 0; i < cnt; i++) stage[warp][lane][i] = draw<T>(st);
+        }
+    }
+    __syncwarp();
+    for (int i = 0; i < 32; i++) {
+        const int c = __shfl_sync(0xffffffffu, cnt, i);
+        T *o = reinterpret_cast<T *>(__shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(dst), i));
+        if (lane < c) o[lane] = stage[warp][i][lane];
     }
 }
 
@@ -282,7 +318,7 @@ __global__ void __launch_bounds__(ELEM_TILE) k_elements(DeviceBatch d, int mode)
     const int e = bp.elem_off + le;
     const int4 c = reinterpret_cast<const int4 *>(d.conn)[e];
     T J[3][3];
-    jacobian<T>(d.pos, c, J);
+    jacobian_t<T>(d, c, J);
     ElemGeom<T> geo;
     shape_functions<T>(J, geo);
     if (mode == ELEM_STEP) {
@@ -1961,14 +1997,17 @@ __global__ void __launch_bounds__(NODE_TILE) k_euler(DeviceBatch d)
     for (int i = 0; i < 3; i++) {
         const size_t k = 3 * (size_t)row + i;
         const double xi = (double)x[k];
+        double p;
         if (bp.solver == SOLVER_NOMASS) {
             d.vel[k] = xi;
-            d.pos[k] += xi * dt;
+            p = d.pos[k] + xi * dt;
         } else {
             const double v = d.vel[k] + xi * dt;
             d.vel[k] = v;
-            d.pos[k] += v * dt;
+            p = d.pos[k] + v * dt;
         }
+        d.pos[k] = p;
+        if (d.pos_df) d.pos_df[k] = split_pos(p);
     }
 }
 
@@ -2141,7 +2180,7 @@ void launch_assemble(const DeviceBatch &d, cudaStream_t s)
 void launch_noise(const DeviceBatch &d, cudaStream_t s)
 {
     if (d.noise_runs == 0) return;
-    PREC_DISPATCH(d, k_noise, blocks_for(d.noise_runs, 256), 256, s, d);
+    PREC_DISPATCH(d, k_noise, blocks_for(d.noise_runs, NOISE_THREADS), NOISE_THREADS, s, d);
 }
 
 void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs)

@@ -54,6 +54,7 @@ struct DeviceBatch {
     void *node_noise = nullptr;
     // nodes (FP64 state and rhs)
     double *pos = nullptr, *vel = nullptr, *drag = nullptr, *rhs = nullptr;
+    float2 *pos_df = nullptr;     // mixed precision: positions as (hi, lo) FP32 pairs, kept with pos
     uint8_t *flags = nullptr;
     int32_t *orig = nullptr;
     int32_t *gather_ptr = nullptr, *gather_idx = nullptr;
@@ -87,6 +88,14 @@ struct DeviceBatch {
     double *epartials = nullptr;    // 2 per element tile
     unsigned long long *loop_count = nullptr;  // CG iterations executed by the persistent kernel (max over blobs)
 };
+
+// A position as a double-float pair (DeviceBatch::pos_df): hi = (float)p,
+// lo = (float)(p - hi); the same bits on the host and the device.
+__host__ __device__ inline float2 split_pos(double p)
+{
+    const float h = (float)p;
+    return make_float2(h, (float)(p - (double)h));
+}
 
 // material table in the working precision T: no FP64 conversion per use
 enum MatT { MAT_T_RHO = 0, MAT_T_A = 1, MAT_T_B = 2, MAT_T_G = 3, MAT_T_E = 4, MAT_T_STRIDE = 8 };

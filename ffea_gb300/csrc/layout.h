@@ -20,6 +20,7 @@ constexpr int EDGE_TILE = 256;
 constexpr int MAX_BLOBS = 1 << 20;
 constexpr int CG_SEG_MAX_ROWS = 1024;  // rows of a CG segment (one per thread of a CG CTA)
 constexpr int NOISE_RUN = 32;          // consecutive draws per thread of the noise kernel (one jump each)
+constexpr int NOISE_THREADS = 128;     // threads per CTA of the noise kernel
 
 enum SolverKind : int32_t { SOLVER_NOMASS = 0, SOLVER_MASS = 1 };
 enum Precision : int32_t { PREC_FP64 = 0, PREC_MIXED = 1 };
