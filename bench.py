@@ -43,6 +43,10 @@ WORKLOADS = {
     "sphere40": dict(radius_nm=40.0, cell_nm=1.25, desc="64^3-cell Freudenthal grid cut to a 40 nm sphere"),
     "sphere20": dict(radius_nm=20.0, cell_nm=1.25, desc="32^3-cell Freudenthal grid cut to a 20 nm sphere"),
     "sphere10": dict(radius_nm=10.0, cell_nm=1.25, desc="16^3-cell Freudenthal grid cut to a 10 nm sphere"),
+    "sphere61": dict(radius_nm=61.25, cell_nm=1.25,
+                     desc="98^3-cell Freudenthal grid cut to a 61.25 nm sphere (the ~500k-node single blob)"),
+    "replicas256": dict(radius_nm=20.0, cell_nm=1.25, replicas=256,
+                        desc="256 replicas of the 20 nm sphere in one batch, one RNG stream each"),
     "ensemble64": dict(radius_nm=None, cell_nm=1.25,
                        desc="64 independent blobs in one batch: radii log-uniform 5-40 nm at a 1.25 nm cell, "
                             "moduli x U[0.5, 2], one RNG stream each"),
@@ -82,6 +86,9 @@ def build_specs(workload: str, rank: int, precision: str):
         return P.SimulationParams.from_si(dt=1e-14, kT=P.kT_at(300.0) * P.MESO_ENERGY, epsilon=1e-6,
                                           max_iterations_cg=10000, rng_seed=seed, solver=P.SOLVER_NOMASS,
                                           precision=prec)
+    if w.get("replicas"):
+        mesh = sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0)
+        return [make_blob(mesh, prm(100000 * (rank + 1) + i)) for i in range(w["replicas"])]
     if w["radius_nm"] is not None:
         return [make_blob(sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0), prm(replica_seed(rank)))]
     rng = np.random.default_rng(2)
@@ -185,6 +192,19 @@ def cg_iteration_bytes(num_linear: int, num_edges: int) -> int:
     40 B + 148 N."""
     B = num_linear + 2 * num_edges
     return 40 * B + 148 * num_linear
+
+
+def step_kernel_bytes(num_linear: int, num_elements: int, num_edges: int, num_total: int) -> dict:
+    """Algorithmic bytes per launch of the per-step kernels in the same model:
+    element forces 12 N + 168 E (positions, connectivity, rest state,
+    material and sign in; nodal forces, scaled gradients and sign out);
+    the draws 4 (7 E + 3 N_t) (one FP32 value written per draw); the
+    viscosity assembly 40 E + 64 E + 36 B (element coefficients and source
+    indices in, block values out); the node gather 64 E + 16 N; the update
+    48 N."""
+    N, E, B = num_linear, num_elements, num_linear + 2 * num_edges
+    return {"noise": 4 * (7 * E + 3 * num_total), "elements": 12 * N + 168 * E,
+            "assemble": 40 * E + 64 * E + 36 * B, "nodes": 64 * E + 16 * N, "euler": 48 * N}
 
 
 def ncu_traffic(kernel="k_cg", workload="sphere40"):
@@ -375,6 +395,7 @@ def measure_arm(args, specs, precond: str, world: int, local: int):
     w.set_timing(True)
     w.run(prof_steps)
     phases = w.phase_times() / prof_steps
+    kernel_ms = {k: v / prof_steps for k, v in w.kernel_times().items()}
     w.set_timing(False)
     iters_p = (w.cg_loop_count() - loops_p0) / prof_steps
     pc_used = {v: k for k, v in PRECONDS.items()}[w.preconditioner()]
@@ -386,7 +407,8 @@ def measure_arm(args, specs, precond: str, world: int, local: int):
         "phase_ms_per_step": {"elements": float(phases[0]), "assemble": float(phases[1]),
                               "nodes": float(phases[2]), "cg": cg_ms, "euler": float(phases[4])},
         "cg_us_per_iteration": 1e3 * cg_ms / max(iters_p, 1), "cg_iters_profiled": iters_p,
-        "sizes": (nl, ne, nedges), "autotune": tuned,
+        "sizes": (nl, ne, nedges), "autotune": tuned, "kernel_ms": kernel_ms,
+        "total_nodes": sum(s_.mesh.num_nodes for s_ in specs),
     }
 
 
@@ -418,6 +440,20 @@ def run_gb300(args):
                 "traffic": ncu_traffic(), "algorithmic_bytes_per_launch": alg,
                 "avg_launch_us": round(cg_ms * 1e3, 1), "cg_iters_per_launch": iters_p,
                 "bytes_per_iteration": cg_iteration_bytes(nl, nedges)}
+    # every other kernel of the step against the same peak: algorithmic bytes
+    # over its event-timed duration in the profile pass (direct launches)
+    kernels = {}
+    for name, b in step_kernel_bytes(nl, ne, nedges, main_arm["total_nodes"]).items():
+        ms = main_arm["kernel_ms"].get(name, 0.0)
+        if ms > 0:
+            gbs = b / (ms / 1e3) / 1e9
+            kernels[name] = {"us": round(ms * 1e3, 1), "algorithmic_bytes": b, "achieved_gbs": round(gbs, 1),
+                             "frac": round(gbs / peak, 4)}
+    kernels["cg"] = {"us": round(cg_ms * 1e3, 1), "algorithmic_bytes": alg, "achieved_gbs": round(achieved, 1),
+                     "frac": round(achieved / peak, 4)}
+    if main_arm["kernel_ms"].get("coarse", 0.0) > 0:
+        kernels["coarse"] = {"us": round(main_arm["kernel_ms"]["coarse"] * 1e3, 1),
+                             "note": "coarse-space refresh, every tenth step (averaged per step)"}
     line = {
         "metric": METRIC, "value": main_arm["value"], "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": main_arm["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -425,7 +461,7 @@ def run_gb300(args):
         "config": config_of(args, specs, world), "e2e": main_arm["e2e"], "gpu_launches": main_arm["gpu_launches"],
         "preconditioner": main_arm["preconditioner"], "cg_iters_per_step": main_arm["cg_iters_per_step"],
         "roofline": roofline, "clocks": main_arm["clocks"], "phase_ms_per_step": main_arm["phase_ms_per_step"],
-        "cg_us_per_iteration": main_arm["cg_us_per_iteration"],
+        "cg_us_per_iteration": main_arm["cg_us_per_iteration"], "kernel_roofline": kernels,
     }
     if main_arm["autotune"]:
         line["autotune"] = main_arm["autotune"]

@@ -76,6 +76,7 @@ SIGNATURES = {
                                       ctypes.POINTER(ctypes.c_int64)]),
     "ffea_gpu_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ffea_gpu_phase_times": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "ffea_gpu_kernel_times": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "ffea_gpu_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "ffea_gpu_set_graph_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ffea_gpu_step_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),

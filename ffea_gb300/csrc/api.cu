@@ -125,7 +125,8 @@ struct ffea_gpu {
     int graph_mode = 1;
     int timing = 0;
     double phase_ms[5] = {0, 0, 0, 0, 0};
-    cudaEvent_t ev[6] = {};
+    double kernel_ms[FFEA_GPU_NUM_KERNEL_TIMES] = {};  // noise, elements, assembly, coarse, nodes, CG, update
+    cudaEvent_t ev[FFEA_GPU_NUM_KERNEL_TIMES + 1] = {};
     int64_t fixed_per_step = 0;  // kernels of a step graph outside the CG loop
     size_t tsize = 4;
     // node I/O in the reference's node order, reconstructed on the device:
@@ -569,6 +570,13 @@ int ffea_gpu_phase_times(ffea_gpu_t *h, double out_ms[5])
     return FFEA_GPU_OK;
 }
 
+int ffea_gpu_kernel_times(ffea_gpu_t *h, double out_ms[FFEA_GPU_NUM_KERNEL_TIMES])
+{
+    if (!h || !out_ms) return fail("null argument");
+    for (int i = 0; i < FFEA_GPU_NUM_KERNEL_TIMES; i++) out_ms[i] = h->kernel_ms[i];
+    return FFEA_GPU_OK;
+}
+
 int ffea_gpu_preconditioner(ffea_gpu_t *h) { return h ? h->precond : -1; }
 
 int ffea_gpu_selftest_barrier_timeout(int32_t ctas, int32_t spin_limit, int32_t *timed_out)
@@ -747,27 +755,38 @@ int enqueue_steps(ffea_gpu *h, int32_t nsteps, bool allow_direct)
             }
         }
         if (!allow_direct) return fail("asynchronous stepping needs graph mode without timing");
-        if (h->timing) CK(cudaEventRecord(h->ev[0], h->stream));
+        // with timing on, an event after each kernel (or group) of the step
+        auto mark = [&](int i) { return h->timing ? cudaEventRecord(h->ev[i], h->stream) : cudaSuccess; };
+        CK(mark(0));
         launch_noise(d, h->stream);
+        CK(mark(1));
         launch_elements(d, h->stream, ELEM_STEP);
-        if (h->timing) CK(cudaEventRecord(h->ev[1], h->stream));
+        CK(mark(2));
         if (d.any_nomass) launch_assemble(d, h->stream);
+        CK(mark(3));
         if (coarse_step(h) && refresh_coarse(h, h->stream, 1, false)) return FFEA_GPU_ERROR;
         h->steps_done++;
-        if (h->timing) CK(cudaEventRecord(h->ev[2], h->stream));
+        CK(mark(4));
         launch_nodes(d, h->stream, 0);
-        if (h->timing) CK(cudaEventRecord(h->ev[3], h->stream));
+        CK(mark(5));
         CK(launch_cg(d, h->stream));
-        if (h->timing) CK(cudaEventRecord(h->ev[4], h->stream));
+        CK(mark(6));
         launch_euler(d, h->stream);
+        CK(mark(7));
         if (h->timing) {
-            CK(cudaEventRecord(h->ev[5], h->stream));
-            CK(cudaEventSynchronize(h->ev[5]));
-            for (int i = 0; i < 5; i++) {
+            CK(cudaEventSynchronize(h->ev[FFEA_GPU_NUM_KERNEL_TIMES]));
+            for (int i = 0; i < FFEA_GPU_NUM_KERNEL_TIMES; i++) {
                 float ms = 0;
                 CK(cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]));
-                h->phase_ms[i] += ms;
+                h->kernel_ms[i] += ms;
             }
+            // the coarser phases: elements (noise + elements), assembly (with
+            // the coarse refresh), nodes, CG, update
+            h->phase_ms[0] = h->kernel_ms[0] + h->kernel_ms[1];
+            h->phase_ms[1] = h->kernel_ms[2] + h->kernel_ms[3];
+            h->phase_ms[2] = h->kernel_ms[4];
+            h->phase_ms[3] = h->kernel_ms[5];
+            h->phase_ms[4] = h->kernel_ms[6];
         }
     }
     return FFEA_GPU_OK;
@@ -793,6 +812,7 @@ int ffea_gpu_step(ffea_gpu_t *h, int32_t nsteps)
     if (!h) return fail("null handle");
     if (nsteps < 0) return fail("nsteps must be >= 0");
     for (int i = 0; i < 5; i++) h->phase_ms[i] = 0;
+    for (int i = 0; i < FFEA_GPU_NUM_KERNEL_TIMES; i++) h->kernel_ms[i] = 0;
     if (enqueue_steps(h, nsteps, true) != FFEA_GPU_OK) return FFEA_GPU_ERROR;
     return sync_and_check(h);
 }

@@ -150,6 +150,14 @@ class World:
         L.check(L.lib().ffea_gpu_phase_times(self._h, L.ptr(out)))
         return out
 
+    KERNEL_TIMES = ("noise", "elements", "assemble", "coarse", "nodes", "cg", "euler")
+
+    def kernel_times(self) -> dict:
+        """Milliseconds per kernel over the last timed run() (set_timing(True))."""
+        out = np.zeros(len(self.KERNEL_TIMES))
+        L.check(L.lib().ffea_gpu_kernel_times(self._h, L.ptr(out)))
+        return dict(zip(self.KERNEL_TIMES, out.tolist()))
+
     def sizes(self):
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         L.check(L.lib().ffea_gpu_sizes(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))

@@ -260,6 +260,15 @@ int ffea_gpu_mpnn_probe(ffea_gpu_t *h, int32_t blob, const float *theta, const f
 int ffea_gpu_set_timing(ffea_gpu_t *h, int32_t enable);
 int ffea_gpu_phase_times(ffea_gpu_t *h, double out_ms[5]);
 
+/* The same timing per kernel (milliseconds, summed over the steps of the
+ * last ffea_gpu_step call): random draws (k_noise), element forces
+ * (k_elements), viscosity assembly (k_assemble), coarse-space refresh (every
+ * tenth step with the two-level preconditioner, else 0), node gather
+ * (k_nodes), CG solve (k_cg), update (k_euler).  No reference counterpart:
+ * it exists for the per-kernel roofline. */
+#define FFEA_GPU_NUM_KERNEL_TIMES 7
+int ffea_gpu_kernel_times(ffea_gpu_t *h, double out_ms[FFEA_GPU_NUM_KERNEL_TIMES]);
+
 /* The handle's CUDA stream (cudaStream_t), for callers that order their own
  * work after a step. */
 void *ffea_gpu_stream(ffea_gpu_t *h);
