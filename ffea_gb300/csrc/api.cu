@@ -336,8 +336,10 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     int max_cols = 0;
     for (int32_t L : H.slice_len) max_cols = std::max(max_cols, (int)L);
     const int32_t n_segs = plan_cg_segments(H);
-    // two-level preconditioner: NoMass blobs, mixed precision, one segment
-    // per CTA with local reductions, at most CG_THREADS coarse dofs per blob
+    // two-level preconditioner: NoMass blobs, mixed precision.  The
+    // register-resident kernel carries it with one segment per CTA, local
+    // reductions and at most CG_THREADS coarse dofs per blob; every other
+    // batch runs it in the memory-resident kernel
     const int want = params[0].preconditioner;
     for (int b = 1; b < num_blobs; b++)
         if (params[b].preconditioner != want) return fail("all blobs of a batch must use the same preconditioner");
@@ -346,11 +348,11 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     int coarse_nmax = 0;
     bool coarse_ok = want != FFEA_GPU_PRECOND_JACOBI && H.precision == PREC_MIXED && !H.any_mass;
     for (const BlobParams &bp : H.bp) coarse_nmax = std::max(coarse_nmax, (int)bp.coarse_n);
-    if (coarse_nmax > CG_THREADS) coarse_ok = false;
+    const bool coarse_reg_ok = coarse_ok && coarse_nmax <= CG_THREADS;
     // phi per row, the CTA's six rows of X, c, 6 x 32 reduction floats and
     // the carried P^T s per coarse dof
     const size_t coarse_bytes =
-        coarse_ok ? 16 + 16 * (size_t)CG_THREADS +
+        coarse_reg_ok ? 16 + 16 * (size_t)CG_THREADS +
                         sizeof(float) * (6 * (size_t)coarse_nmax + 8 + 6 * 32 + (size_t)CG_THREADS)
                   : 0;
     size_t dyn_bytes = 0;
@@ -374,7 +376,33 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     const char *force_last = std::getenv("FFEA_GPU_CG_LAST_ARRIVER");
     d.cg_local = H.num_blobs <= CG_LOCAL_MAX_BLOBS && n_segs <= CG_LOCAL_MAX_SEGS &&
                  !(force_last && force_last[0] == '1');
-    d.coarse = coarse_ok && d.cg_reg && d.cg_local;
+    d.coarse = coarse_reg_ok && d.cg_reg && d.cg_local;
+    if (coarse_ok && !d.coarse) {
+        // the memory-resident kernel with the coarse space: its shared memory
+        // holds g of one blob and P^T s of every blob a CTA touches
+        const int G = std::min(mem_cap, n_segs);
+        int hmax = 0;
+        for (int c = 0; c < G; c++) {
+            const int S0 = (int)(((int64_t)n_segs * c) / G), S1 = (int)(((int64_t)n_segs * (c + 1)) / G);
+            int sum = 0, last = -1;
+            for (int sg = S0; sg < S1; sg++)
+                if (H.seg_blob[sg] != last) {
+                    last = H.seg_blob[sg];
+                    sum += H.bp[last].coarse_n;
+                }
+            hmax = std::max(hmax, sum);
+        }
+        const size_t mem_bytes = cg_mem_coarse_bytes(coarse_nmax, hmax);
+        if ((int64_t)G * CG_MAX_SEGS >= n_segs && cg_mem_smem_allow(H.precision, mem_bytes) == 0 &&
+            cg_max_grid(H.precision, 0, mem_bytes) >= G) {
+            d.coarse = 1;
+            d.cg_reg = 0;
+            d.cg_grid = G;
+            d.cg_cache_slots = d.cg_cache_cols = 0;
+            d.cg_dyn_smem = (int32_t)mem_bytes;
+            d.coarse_hmax = hmax;
+        }
+    }
     d.coarse_nmax = d.coarse ? coarse_nmax : 0;
     d.part_stride = d.coarse ? 20 : 8;  // floats: DF dot terms 0..5; coarse P^T r 8..13, P^T w 14..19
     h->precond = d.coarse ? want : FFEA_GPU_PRECOND_JACOBI;
@@ -470,8 +498,9 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
         CK(cudaMemcpy(d.phi, H.phi.data(), H.phi.size() * sizeof(float), cudaMemcpyHostToDevice));
         CK(A.alloc(d.coarse_A, (size_t)coarse_total));
         CK(A.alloc(d.coarse_X, (size_t)coarse_total));
-        CK(A.alloc(d.coarse_T, (size_t)coarse_nmax * coarse_nmax));
-        CK(A.alloc(d.coarse_Xn, (size_t)coarse_nmax * coarse_nmax));
+        // Newton-Schulz scratch for a run of equal-size blobs at once
+        CK(A.alloc(d.coarse_T, std::max((size_t)coarse_nmax * coarse_nmax, (size_t)coarse_total)));
+        CK(A.alloc(d.coarse_Xn, std::max((size_t)coarse_nmax * coarse_nmax, (size_t)coarse_total)));
     }
     CK(A.alloc(d.epartials, 2 * (size_t)H.n_etiles));
     CK(A.alloc(d.cg, (size_t)H.num_blobs));

@@ -163,17 +163,22 @@ __global__ void __launch_bounds__(kAsmThreads) k_coarse_assemble(DeviceBatch d)
     }
 }
 
-// X <- (X + X^T) / 2 over one blob's n x n matrix (src may alias nothing).
+// X <- (X + X^T) / 2 over n x n matrices, one per blockIdx.z, n^2 apart
+// (src may alias nothing).
 __global__ void k_symmetrize(const float *__restrict__ src, float *__restrict__ dst, int n)
 {
     const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || j >= n) return;
-    dst[(size_t)i * n + j] = 0.5f * (src[(size_t)i * n + j] + src[(size_t)j * n + i]);
+    const size_t o = (size_t)blockIdx.z * n * n;
+    dst[o + (size_t)i * n + j] = 0.5f * (src[o + (size_t)i * n + j] + src[o + (size_t)j * n + i]);
 }
 
-// X = I / ||A||_inf (the Newton-Schulz start, convergent for an SPD A).
+// X = I / ||A||_inf (the Newton-Schulz start, convergent for an SPD A), one
+// n x n matrix per CTA, n^2 apart.
 __global__ void k_scaled_identity(const float *__restrict__ A, float *__restrict__ X, int n)
 {
+    A += (size_t)blockIdx.x * n * n;
+    X += (size_t)blockIdx.x * n * n;
     __shared__ float red[32];
     float m = 0.f;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -213,30 +218,45 @@ int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cub
     if (!d.coarse) return 0;
     if (cublasSetStream(cb, s) != CUBLAS_STATUS_SUCCESS) return -1;
     const float one = 1.f, zero = 0.f, minus_one = -1.f, two = 2.f;
-    for (const BlobParams &bp : bps) {
+    // runs of consecutive NoMass blobs with the same coarse dimension (their
+    // matrices lie n^2 apart) are updated together by strided-batched GEMMs:
+    // one launch sequence for a whole ensemble of replicas
+    for (size_t b0 = 0; b0 < bps.size();) {
+        const BlobParams &bp = bps[b0];
         const int n = bp.coarse_n;
-        if (bp.solver != SOLVER_NOMASS || n == 0) continue;
+        size_t b1 = b0 + 1;
+        if (bp.solver != SOLVER_NOMASS || n == 0) {
+            b0 = b1;
+            continue;
+        }
+        while (b1 < bps.size() && b1 - b0 < 65535 && bps[b1].solver == SOLVER_NOMASS && bps[b1].coarse_n == n &&
+               (int64_t)bps[b1].coarse_xoff == (int64_t)bp.coarse_xoff + (int64_t)(b1 - b0) * n * n)
+            b1++;
+        const int batch = (int)(b1 - b0);
+        const long long stride = (long long)n * n;
         float *A = d.coarse_A + bp.coarse_xoff, *X = d.coarse_X + bp.coarse_xoff;
         float *Tm = d.coarse_T, *Xn = d.coarse_Xn;
         if (init) {
-            k_scaled_identity<<<1, 1024, 0, s>>>(A, X, n);
+            k_scaled_identity<<<batch, 1024, 0, s>>>(A, X, n);
             count_launches(1);
         }
         for (int it = 0; it < iterations; it++) {
             // T = A X; Xn = 2 X - X T; X = sym(Xn).  The matrices are
             // symmetric, so row- and column-major readings agree.
-            if (cublasSgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A, n, X, n, &zero, Tm, n) !=
-                CUBLAS_STATUS_SUCCESS)
+            if (cublasSgemmStridedBatched(cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A, n, stride, X, n, stride,
+                                          &zero, Tm, n, stride, batch) != CUBLAS_STATUS_SUCCESS)
                 return -1;
-            if (cudaMemcpyAsync(Xn, X, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            if (cudaMemcpyAsync(Xn, X, sizeof(float) * (size_t)stride * batch, cudaMemcpyDeviceToDevice, s) !=
+                cudaSuccess)
                 return -1;
-            if (cublasSgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &minus_one, X, n, Tm, n, &two, Xn, n) !=
-                CUBLAS_STATUS_SUCCESS)
+            if (cublasSgemmStridedBatched(cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &minus_one, X, n, stride, Tm, n,
+                                          stride, &two, Xn, n, stride, batch) != CUBLAS_STATUS_SUCCESS)
                 return -1;
-            dim3 grid((n + 255) / 256, n);
+            dim3 grid((n + 255) / 256, n, batch);
             k_symmetrize<<<grid, 256, 0, s>>>(Xn, X, n);
             count_launches(1);
         }
+        b0 = b1;
     }
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -1324,8 +1324,8 @@ __device__ __forceinline__ void cg_transition(const DeviceBatch &d, int b, const
 // every busy blob and runs its CG transition, then publishes the count of
 // blobs still iterating and releases the others.  Bounded waits as in
 // counting_barrier.
-__device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, int *s_err, unsigned int *s_pub,
-                                                         int *s_last, float *sm)
+__device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, const double *part, int *s_err,
+                                                         unsigned int *s_pub, int *s_last, float *sm)
 {
     unsigned int *bar = d.bar;
     __threadfence();
@@ -1346,7 +1346,7 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, i
                 const int st = __ldcg(&d.cg[b].state);
                 if (st == CG_CONVERGED || st == CG_FAILED) continue;
                 DF sums[3];
-                block_blob_sums(d, d.partials, b, sums, sm);
+                block_blob_sums(d, part, b, sums, sm);
                 if (threadIdx.x == 0) cg_transition(d, b, sums);
                 __syncthreads();  // sm reused by the next blob
             }
@@ -1355,7 +1355,7 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, i
                 const int st = __ldcg(&d.cg[b].state);
                 if (st == CG_CONVERGED || st == CG_FAILED) continue;
                 DF sums[3];
-                warp_blob_sums(d, d.partials, b, sums);
+                warp_blob_sums(d, part, b, sums);
                 if (lane == 0) cg_transition(d, b, sums);
             }
             __syncthreads();
@@ -1466,6 +1466,131 @@ __device__ __forceinline__ void coarse_apply(const DeviceBatch &d, int n, float 
         if (lane == 0) cv.cvec[warp] = u;
     }
     __syncthreads();
+}
+
+// Coarse space of the memory-resident CG kernel (several segments per CTA,
+// any number of coarse dofs per blob).  Dynamic shared memory: c of each of
+// the CTA's segments (8 floats), 32 x 8 reduction floats, g of the blob being
+// corrected (coarse_nmax floats), and (P^T s)_j for every coarse dof of every
+// blob the CTA touches (coarse_hmax floats, blob after blob).  Every CTA that
+// touches a blob carries its own copy of that blob's P^T s; all copies follow
+// the same arithmetic on the same partial sums, so they hold the same bits.
+struct CoarseMemView {
+    float *cvec, *red, *g, *h;
+};
+
+__device__ __forceinline__ CoarseMemView coarse_mem_view(const DeviceBatch &d)
+{
+    CoarseMemView v;
+    v.cvec = reinterpret_cast<float *>(cg_dyn);
+    v.red = v.cvec + 8 * CG_MAX_SEGS;
+    v.g = v.red + 8 * 32;
+    v.h = v.g + d.coarse_nmax;
+    return v;
+}
+
+// Phi_p^T v = (v, d_p x v) into ex[0..5] for the rest offset f.xyz of row p
+template <typename T>
+__device__ __forceinline__ void restrict6_of(const float4 f, const T v[3], float *ex)
+{
+    const float v0 = (float)v[0], v1 = (float)v[1], v2 = (float)v[2];
+    ex[0] = v0;
+    ex[1] = v1;
+    ex[2] = v2;
+    ex[3] = f.y * v2 - f.z * v1;
+    ex[4] = f.z * v0 - f.x * v2;
+    ex[5] = f.x * v1 - f.y * v0;
+}
+
+// u = omega D^-1 r + Phi_p c for row p (f = rest offset and omega, c = its
+// segment's coarse correction)
+template <typename T>
+__device__ __forceinline__ void coarse_u_of(const float4 f, const float *c, const T dinv[3], const T r[3], T u[3])
+{
+    const float cx = c[3], cy = c[4], cz = c[5];
+    const T pc[3] = {(T)(c[0] + cy * f.z - cz * f.y), (T)(c[1] + cz * f.x - cx * f.z), (T)(c[2] + cx * f.y - cy * f.x)};
+#pragma unroll
+    for (int k = 0; k < 3; k++) u[k] = (T)f.w * dinv[k] * r[k] + pc[k];
+}
+
+// The coarse corrections of the CTA's segments for the next update
+// (memory-resident kernel), after the iteration's partial sums and the CG
+// transitions: per blob k of the CTA (state ACTIVE or RESTART, or every blob
+// in the prologue), from the restrictions in the partial slots (P^T r at
+// float 8, P^T w at float 14),
+//   restart / prologue: h = 0, g = P^T r
+//   else:               h = P^T w + beta h, g = P^T r - alpha h  (= P^T r_(k+1))
+// then c_j = X_j g for each of the CTA's segments j of the blob, X_j the
+// segment's six rows of X ~ A_c^-1 (global memory, read once per iteration).
+// wps warps share a segment (lane-strided over the n coarse dofs, 6 sums per
+// lane, a transposed butterfly per warp), then one thread per (segment, row)
+// adds the wps warp sums in order: fixed order, so deterministic.
+template <typename T>
+__device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const float *part, int S0, int nt, int nb,
+                                                const int *s_blob, const int *s_tslot, const int *s_state,
+                                                const T *s_alpha, const T *s_beta, bool prologue)
+{
+    const CoarseMemView cv = coarse_mem_view(d);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int j0 = 0, hoff = 0;
+    for (int k = 0; k < nb; k++) {
+        int j1 = j0;
+        while (j1 < nt && s_tslot[j1] == k) j1++;
+        const BlobParams &bp = d.bp[s_blob[k]];
+        const int n = bp.coarse_n, st = s_state[k];
+        float *h = cv.h + hoff;
+        hoff += n;
+        if (n > 0 && (prologue || st == CG_ACTIVE || st == CG_RESTART)) {  // CTA-uniform
+            const bool restart = prologue || st == CG_RESTART;
+            const float a = (float)s_alpha[k], be = (float)s_beta[k];
+            for (int i = tid; i < n; i += blockDim.x) {
+                const float *sl = part + (size_t)d.part_stride * (bp.seg_off + i / 6);
+                const float pr = __ldcg(sl + 8 + i % 6);
+                if (restart) {
+                    h[i] = 0.f;
+                    cv.g[i] = pr;
+                } else {
+                    const float hn = __ldcg(sl + 14 + i % 6) + be * h[i];
+                    h[i] = hn;
+                    cv.g[i] = pr - a * hn;
+                }
+            }
+            __syncthreads();
+            const int m = j1 - j0;
+            int wps = 1;
+            while (wps * 2 * m <= 32) wps *= 2;
+            const int per_round = 32 / wps;
+            for (int q0 = 0; q0 < m; q0 += per_round) {
+                const int jl = q0 + warp / wps, sub = warp % wps;
+                float v[8];
+#pragma unroll
+                for (int l = 0; l < 8; l++) v[l] = 0.f;
+                if (jl < m) {
+                    const float *Xr = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (S0 + j0 + jl - bp.seg_off)) * n;
+#pragma unroll 4
+                    for (int i = sub * 32 + lane; i < n; i += wps * 32) {
+                        const float gi = cv.g[i];
+#pragma unroll
+                        for (int l = 0; l < 6; l++) v[l] = fmaf(__ldcg(Xr + (size_t)l * n + i), gi, v[l]);
+                    }
+                }
+                int idx;
+                const float t = warp_sum_multi<8>(v, idx);
+                if ((lane & 3) == 0) cv.red[warp * 8 + idx] = t;
+                __syncthreads();
+                if (tid < 6 * per_round) {
+                    const int jj = tid / 6, l = tid % 6;
+                    if (q0 + jj < m) {
+                        float s = 0.f;
+                        for (int w = 0; w < wps; w++) s += cv.red[(jj * wps + w) * 8 + l];
+                        cv.cvec[8 * (j0 + q0 + jj) + l] = s;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        j0 = j1;
+    }
 }
 
 // L2 load issued where it stands (volatile asm keeps it ahead of the
@@ -1708,6 +1833,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     // d_p and smoother weight, the CTA's 6 rows of X ~ A_c^-1, the blob's
     // coarse residual g and this segment's coarse correction c
     const bool coarse = REG && local && d.coarse;
+    // the same preconditioner in the memory-resident kernel (coarse_mem_step)
+    const bool mcoarse = !REG && d.coarse;
     int coarse_n = 0;  // coarse dofs of the CTA's blob (0: no coarse space)
     if (coarse) {
         const CoarseView cv = coarse_view<T>(d);
@@ -1777,6 +1904,21 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
             return;
         }
+        if (mcoarse && s_state[k] == CG_RESTART) {
+            // the same from the row state in memory
+            int row;
+            bool valid, nomass = true;
+            T diag = 0;
+            row_info(j, row, valid, diag, nomass);
+            if (valid) {
+                RowState<T> loc;
+                load_fields<T>(d, row, loc, RF_R | RF_DINV);
+                coarse_u_of<T>(d.phi[row], coarse_mem_view(d).cvec + 8 * j, loc.dinv, loc.r, loc.u);
+                store_fields<T>(d, row, loc, RF_U);
+                U4()[row] = V4{loc.u[0], loc.u[1], loc.u[2], (T)0};
+            }
+            return;
+        }
         if (s_state[k] != CG_ACTIVE) return;  // CTA-uniform
         int row;
         bool valid, nomass = true;
@@ -1786,6 +1928,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         RowState<T> loc;
         RowState<T> &S = REG ? reg : loc;
         if (!REG && valid) load_fields<T>(d, row, loc, RF_X | RF_R | RF_U | RF_W | RF_S | RF_P | RF_DINV);
+        float4 fm = make_float4(0.f, 0.f, 0.f, 0.f);  // mcoarse: the row's rest offset and omega
+        if (mcoarse && valid) fm = d.phi[row];
         if (valid) {
             const T a = s_alpha[k], b = s_beta[k];
             const bool first = b == (T)0;
@@ -1800,6 +1944,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                 S.u[cc2] = dinv_of(S, cc2) * S.r[cc2];
             }
             if (coarse) coarse_u(S);
+            else if (mcoarse) coarse_u_of<T>(fm, coarse_mem_view(d).cvec + 8 * j, S.dinv, S.r, S.u);
 #pragma unroll
             for (int cc2 = 0; cc2 < 3; cc2++) {
                 pg += S.r[cc2] * S.u[cc2];
@@ -1813,6 +1958,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             // restriction of the new r: slot floats 8..
             float ex[6] = {0, 0, 0, 0, 0, 0};
             if (valid) restrict6(S.r, ex);
+            seg_partials<W, 6>(slot(S0 + j), in, 5, ex, 8, red);
+        } else if (mcoarse) {
+            float ex[6] = {0, 0, 0, 0, 0, 0};
+            if (valid) restrict6_of<T>(fm, S.r, ex);
             seg_partials<W, 6>(slot(S0 + j), in, 5, ex, 8, red);
         } else {
             seg_partials<W, 0>(slot(S0 + j), in, 5, nullptr, 0, red);
@@ -1859,7 +2008,29 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
         }
         if (!REG && valid) store_fields<T>(d, row, loc, state == CG_VERIFY ? (RF_R | RF_U) : RF_W);
-        if (coarse) {
+        if (mcoarse) {
+            // the restrictions of the register-resident branch below, with
+            // the rest offset from memory
+            const float4 fm = valid ? d.phi[row] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float ex[12];
+#pragma unroll
+            for (int m = 0; m < 12; m++) ex[m] = 0.f;
+            const bool full = prologue || state != CG_ACTIVE;
+            if (valid) {
+                if (full) restrict6_of<T>(fm, S.r, ex);
+                if (state != CG_VERIFY) restrict6_of<T>(fm, S.w, ex + 6);
+            }
+            if (state == CG_VERIFY) {
+                const double in[3] = {vg, 0.0, vr};
+                seg_partials<double, 12>(slot(S0 + j), in, 5, ex, 8, red);
+            } else if (full) {
+                const W in[3] = {pg, pd, pr};
+                seg_partials<W, 12>(slot(S0 + j), in, 7, ex, 8, red);
+            } else {
+                const W in[3] = {pg, pd, pr};
+                seg_partials<W, 6>(slot(S0 + j), in, 2, ex + 6, 14, red);
+            }
+        } else if (coarse) {
             // restrictions: ACTIVE P^T w (slot floats 14..); the prologue,
             // RESTART and VERIFY restart the coarse recurrence: P^T r (8..)
             // and P^T w (14.., zero for VERIFY)
@@ -1893,7 +2064,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     unsigned int n_bar = 0;  // counting barriers passed
     // sums of the iteration's partials and the transitions; the running-blob count
     auto reduce = [&]() -> unsigned int {
-        if (!local) return reducing_barrier(d, &s_err, &s_pub, s_last, sm_df);
+        if (!local) return reducing_barrier(d, mcoarse ? part() : d.partials, &s_err, &s_pub, s_last, sm_df);
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) return 0u;
         return local_reduce<T>(d, part(), s_cg, sm_df, &s_run, nb, s_blob, s_state, s_alpha, s_beta,
@@ -1917,6 +2088,43 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         }
         parity = 0;
     }
+    if (mcoarse) {
+        // the same with the row state in memory: P^T r_0 of every segment,
+        // then c per segment and u_0 = M r_0 stored for the publication below
+        parity = 1;
+        for (int j = 0; j < nt; j++) {
+            int row;
+            bool valid, nomass = true;
+            T diag = 0;
+            row_info(j, row, valid, diag, nomass);
+            float ex[6] = {0, 0, 0, 0, 0, 0};
+            if (valid) {
+                RowState<T> loc;
+                load_fields<T>(d, row, loc, RF_R);
+                restrict6_of<T>(d.phi[row], loc.r, ex);
+            }
+            const W none[3] = {(W)0, (W)0, (W)0};
+            seg_partials<W, 6>(slot(S0 + j), none, 0, ex, 8, red);
+        }
+        counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
+        if (!s_err) {
+            coarse_mem_step<T>(d, reinterpret_cast<const float *>(part()), S0, nt, nb, s_blob, s_tslot, s_state,
+                               s_alpha, s_beta, true);
+            for (int j = 0; j < nt; j++) {
+                int row;
+                bool valid, nomass = true;
+                T diag = 0;
+                row_info(j, row, valid, diag, nomass);
+                if (valid) {
+                    RowState<T> loc;
+                    load_fields<T>(d, row, loc, RF_R | RF_DINV);
+                    coarse_u_of<T>(d.phi[row], coarse_mem_view(d).cvec + 8 * j, loc.dinv, loc.r, loc.u);
+                    store_fields<T>(d, row, loc, RF_U);
+                }
+            }
+        }
+        parity = 0;
+    }
     // publish u of the own rows for the neighbours (the k_nodes start value,
     // zero on pinned rows; with the coarse space u_0 = M r_0) before the
     // first product
@@ -1937,8 +2145,13 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     unsigned int running = s_err ? 0u : reduce();
     int loops = 0;
     while (!s_err && running > 0) {
-        if (local) parity ^= 1;
-        else refresh();  // the local reduction refreshed already
+        if (!local) refresh();  // the local reduction refreshed already
+        // memory-resident coarse space: the corrections for this update, from
+        // the partials just reduced (before the buffers swap)
+        if (mcoarse)
+            coarse_mem_step<T>(d, reinterpret_cast<const float *>(part()), S0, nt, nb, s_blob, s_tslot, s_state,
+                               s_alpha, s_beta, false);
+        if (local || mcoarse) parity ^= 1;
         if (REG && s_state[0] == CG_VERIFY) publish_x();
         for (int j = 0; j < nt; j++) phase_a(j);
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
@@ -2222,6 +2435,31 @@ int cg_smem_plan(int precision, int max_slots, int max_cols, size_t extra_bytes,
                                   : cg_smem_plan_t<float>(max_slots, max_cols, extra_bytes, J, JC, dyn_bytes);
 }
 
+// Dynamic shared memory of the memory-resident CG kernel with the coarse
+// space (coarse_mem_view): its size for the given coarse dimensions, and
+// whether the device allows it (the kernel's limit is raised to the device
+// maximum, as for the register-resident kernel).
+size_t cg_mem_coarse_bytes(int coarse_nmax, int coarse_hmax)
+{
+    return sizeof(float) * (8 * (size_t)CG_MAX_SEGS + 8 * 32 + (size_t)coarse_nmax + (size_t)coarse_hmax);
+}
+
+int cg_mem_smem_allow(int precision, size_t dyn_bytes)
+{
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
+    cudaFuncAttributes fa;
+    const void *fn = precision == PREC_FP64 ? (const void *)k_cg<double, false> : (const void *)k_cg<float, false>;
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) return -1;
+    const size_t reserve = 1024;
+    if (fa.sharedSizeBytes + reserve + dyn_bytes > (size_t)optin) return -1;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes) !=
+        cudaSuccess)
+        return -1;
+    return 0;
+}
+
 int cg_max_grid(int precision, int reg, size_t dyn_bytes)
 {
     int dev = 0, sms = 0, per_sm = 0;
@@ -2230,10 +2468,10 @@ int cg_max_grid(int precision, int reg, size_t dyn_bytes)
     cudaError_t e;
     if (precision == PREC_FP64)
         e = reg ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double, true>, CG_THREADS, dyn_bytes)
-                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double, false>, CG_THREADS, 0);
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<double, false>, CG_THREADS, dyn_bytes);
     else
         e = reg ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float, true>, CG_THREADS, dyn_bytes)
-                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float, false>, CG_THREADS, 0);
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<float, false>, CG_THREADS, dyn_bytes);
     if (e != cudaSuccess) return 0;
     return sms * per_sm;
 }
@@ -2259,7 +2497,7 @@ cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s)
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)d.cg_grid);
     cfg.blockDim = dim3(CG_THREADS);
-    cfg.dynamicSmemBytes = d.cg_reg ? (size_t)d.cg_dyn_smem : 0;
+    cfg.dynamicSmemBytes = (size_t)d.cg_dyn_smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

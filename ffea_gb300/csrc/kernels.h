@@ -29,6 +29,7 @@ struct DeviceBatch {
     // two-level preconditioner (REG and local reduction, NoMass, mixed precision)
     int32_t coarse = 0;           // 1: u = diag(omega) D^-1 r + P A_c^-1 P^T r
     int32_t coarse_nmax = 0;      // largest coarse dimension of a blob
+    int32_t coarse_hmax = 0;      // memory-resident CG kernel: most coarse dofs of the blobs one CTA touches
     float4 *phi = nullptr;        // per padded row: rest offset from the segment centroid / R, smoother weight
     int32_t *seg_of_row = nullptr;
     int32_t *seg_nbr_ptr = nullptr, *seg_nbr = nullptr;   // segments coupled to each segment (itself included)
@@ -173,6 +174,8 @@ int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, ::c
 // of dynamic shared memory, or not) that fit co-resident on the current
 // device, 0 on error
 int cg_max_grid(int precision, int reg, size_t dyn_bytes);
+size_t cg_mem_coarse_bytes(int coarse_nmax, int coarse_hmax);
+int cg_mem_smem_allow(int precision, size_t dyn_bytes);
 
 int64_t kernel_launch_count();
 void count_launches(int64_t n);

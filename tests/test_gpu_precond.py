@@ -121,3 +121,91 @@ def test_handles_with_different_plans_coexist(gpulib):
             wb.run(1)
         assert wa.blob(0).status()["fail_bits"] == 0
         assert wb.blob(0).status()["fail_bits"] == 0
+
+
+# ---------------------------------------------------------------- memory-resident solve
+# Batches with more CG segments than SMs (large blobs, ensembles), with more
+# than CG_THREADS coarse dofs per blob, or reduced by the last-arriving CTA
+# (many blobs) run the two-level preconditioner in the memory-resident CG
+# kernel.  FFEA_GPU_CG_MAX_CTAS caps the grid to put several segments on one
+# CTA at test sizes; FFEA_GPU_CG_MEMORY_STATE forces that kernel.
+
+
+@pytest.mark.parametrize("max_ctas", ["1", "2"])
+def test_memory_resident_two_level_matches_oracle(gpulib, oracle, monkeypatch, max_ctas):
+    """Two segments on one CTA, or one each, with the row state in memory."""
+    monkeypatch.setenv("FFEA_GPU_CG_MEMORY_STATE", "1")
+    monkeypatch.setenv("FFEA_GPU_CG_MAX_CTAS", max_ctas)
+    s = spec(radius_nm=9.0, precision=P.PRECISION_MIXED)
+    ref = oracle.blob_from_spec(s)
+    worst_v = worst_f = 0.0
+    with _world([s], preconditioner=TWO_LEVEL) as w:
+        assert w.preconditioner() == TWO_LEVEL
+        b = w.blob(0)
+        for _ in range(30):
+            w.run(1)
+            assert ref.step(1) == 0
+            _, vel, _ = b.get_nodes()
+            _, rvel, _ = ref.nodes()
+            worst_v = max(worst_v, rel(vel, rvel))
+            worst_f = max(worst_f, rel(b.rhs(), ref.rhs()))
+            assert b.status()["fail_bits"] == 0
+    assert worst_v <= 1e-5, worst_v
+    assert worst_f <= 1e-5, worst_f
+
+
+def test_memory_resident_two_level_needs_fewer_iterations(gpulib, monkeypatch):
+    monkeypatch.setenv("FFEA_GPU_CG_MEMORY_STATE", "1")
+    monkeypatch.setenv("FFEA_GPU_CG_MAX_CTAS", "2")
+    s = spec(radius_nm=12.0, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    iters = {}
+    for pc in (JACOBI, TWO_LEVEL):
+        with _world([s], true_residual=True, preconditioner=pc) as w:
+            assert w.preconditioner() == pc
+            w.run(2)
+            st = w.blob(0).status()
+            assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (pc, st)
+            iters[pc] = st["cg_iters"]
+    # four aggregates only: a small gain, as in the register-resident test
+    assert iters[TWO_LEVEL] < 0.8 * iters[JACOBI], iters
+
+
+@pytest.mark.parametrize("num_blobs", [3, 9])
+def test_memory_resident_two_level_local_and_last_arriver_agree(gpulib, monkeypatch, num_blobs):
+    """Uneven blobs in one batch, several segments per CTA: the redundant
+    per-CTA reduction and the last-arriver reduction sum the same partials in
+    the same order and apply the same coarse corrections, so the iterates are
+    bit-identical, and every solve meets the true residual."""
+    monkeypatch.setenv("FFEA_GPU_CG_MEMORY_STATE", "1")
+    monkeypatch.setenv("FFEA_GPU_CG_MAX_CTAS", "2")
+    specs = [spec(radius_nm=3.0 + 0.75 * i, seed=i, rng_seed=70 + i, precision=P.PRECISION_MIXED, epsilon=1e-6)
+             for i in range(num_blobs)]
+    outs = []
+    for last in ("0", "1"):
+        monkeypatch.setenv("FFEA_GPU_CG_LAST_ARRIVER", last)
+        with _world(specs, true_residual=True, preconditioner=TWO_LEVEL) as w:
+            assert w.preconditioner() == TWO_LEVEL
+            w.run(3)
+            outs.append([w.blob(i).get_nodes() for i in range(num_blobs)])
+            for i in range(num_blobs):
+                st = w.blob(i).status()
+                assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (i, st)
+    for i in range(num_blobs):
+        for a, c in zip(outs[0][i], outs[1][i]):
+            assert np.array_equal(a, c), i
+
+
+def test_two_level_beyond_one_cta_per_segment(gpulib):
+    """A blob with more CG segments than SMs (over 1024 coarse dofs): the
+    memory-resident kernel carries the coarse space, every solve meets the
+    true residual, and the iterations drop against Jacobi."""
+    s = spec(radius_nm=46.0, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    iters = {}
+    for pc in (JACOBI, TWO_LEVEL):
+        with _world([s], true_residual=True, preconditioner=pc) as w:
+            assert w.preconditioner() == pc
+            w.run(2)
+            st = w.blob(0).status()
+            assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (pc, st)
+            iters[pc] = st["cg_iters"]
+    assert iters[TWO_LEVEL] < 0.6 * iters[JACOBI], iters
