@@ -60,6 +60,7 @@ SIGNATURES = {
     "ffea_gpu_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ffea_gpu_get_nodes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp, _dp]),
     "ffea_gpu_set_nodes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp]),
+    "ffea_gpu_set_external_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _ip, _dp]),
     "ffea_gpu_get_rng_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _u64p]),
     "ffea_gpu_set_rng_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _u64p]),
     "ffea_gpu_energies": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp]),

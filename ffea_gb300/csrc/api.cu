@@ -135,6 +135,8 @@ struct ffea_gpu {
     // for a node of no element; per blob the offset into these arrays
     std::vector<int64_t> io_off;
     int2 *io_src = nullptr;
+    std::vector<int2> io_src_host;  // the same map on the host (external-force folding)
+    std::vector<double> ext_host;   // external forces per row (3 per row, folded), mirror of dev.ext
     double *io_secvel = nullptr;  // secondary-node velocities (mass blobs keep them; NoMass report 0)
     double *io_stage = nullptr;   // 9 doubles per node of the largest blob (pos, vel, force)
     int *io_moved = nullptr;      // set_nodes: 1 when a position changed
@@ -317,7 +319,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     if (num_blobs <= 0) return fail("num_blobs must be >= 1");
     const int prec = params[0].precision;
     const int reg_grid0 = cg_max_grid(prec, 1, 0);
-    const int max_grid = cg_max_grid(prec, 0, 0);
+    const int max_grid = cg_max_grid(prec, 0, cg_mem_defer_bytes(prec));
     const bool sized = reg_grid0 > 0 && max_grid > 0;
     int cap = std::numeric_limits<int>::max();
     if (const char *e = std::getenv("FFEA_GPU_CG_MAX_CTAS")) cap = std::max(1, std::atoi(e));
@@ -346,7 +348,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     if (want < FFEA_GPU_PRECOND_JACOBI || want > FFEA_GPU_PRECOND_LEARNED) return fail("unknown preconditioner");
     const int64_t coarse_total = build_coarse(H);
     int coarse_nmax = 0;
-    bool coarse_ok = want != FFEA_GPU_PRECOND_JACOBI && H.precision == PREC_MIXED && !H.any_mass;
+    bool coarse_ok = want != FFEA_GPU_PRECOND_JACOBI && H.precision == PREC_MIXED && !H.any_mass && !H.any_lumped;
     for (const BlobParams &bp : H.bp) coarse_nmax = std::max(coarse_nmax, (int)bp.coarse_n);
     const bool coarse_reg_ok = coarse_ok && coarse_nmax <= CG_THREADS;
     // phi per row, the CTA's six rows of X, c, 6 x 32 reduction floats and
@@ -368,7 +370,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     d.cg_grid = n_segs <= reg_cap ? n_segs : std::min(mem_cap, n_segs);
     d.cg_cache_slots = d.cg_reg ? cache_slots : 0;
     d.cg_cache_cols = d.cg_reg ? cache_cols : 0;
-    d.cg_dyn_smem = d.cg_reg ? (int32_t)dyn_bytes : 0;
+    d.cg_dyn_smem = d.cg_reg ? (int32_t)dyn_bytes : (int32_t)cg_mem_defer_bytes(H.precision);
     if ((int64_t)d.cg_grid * CG_MAX_SEGS < n_segs)
         return fail("batch too large: %d CG segments need more than %d co-resident CTAs", n_segs, mem_cap);
     // local reduction (every CTA sums all partials, no serial last-arriver
@@ -392,7 +394,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
                 }
             hmax = std::max(hmax, sum);
         }
-        const size_t mem_bytes = cg_mem_coarse_bytes(coarse_nmax, hmax);
+        const size_t mem_bytes = cg_mem_defer_bytes(H.precision) + cg_mem_coarse_bytes(coarse_nmax, hmax);
         if ((int64_t)G * CG_MAX_SEGS >= n_segs && cg_mem_smem_allow(H.precision, mem_bytes) == 0 &&
             cg_max_grid(H.precision, 0, mem_bytes) >= G) {
             d.coarse = 1;
@@ -416,6 +418,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     d.precision = H.precision;
     d.any_mass = H.any_mass;
     d.any_nomass = H.any_nomass;
+    d.any_lumped = H.any_lumped;
     const size_t ts = H.precision == PREC_FP64 ? sizeof(double) : sizeof(float);
     h->tsize = ts;
     CK(upload(A, d.bp, H.bp));
@@ -489,6 +492,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(A.alloc_bytes(d.sell_val, H.any_nomass ? 9 * (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.sell_mval, H.any_mass ? (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.mass_diag, H.any_mass ? (size_t)H.nl_pad * ts : 16));
+    if (H.any_lumped) CK(A.alloc(d.lumped_inv, (size_t)H.nl_pad));
     CK(A.alloc(d.partials, std::max(4 * (size_t)H.n_tiles, (size_t)d.part_stride * n_segs)));
     if (d.coarse) {
         CK(upload(A, d.seg_of_row, H.seg_of_row));
@@ -533,18 +537,20 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
                     src[base + t[mid[k][0]]] =
                         make_int2(map.lin_of_orig[t[mid[k][1]]], map.lin_of_orig[t[mid[k][2]]]);
             }
-            if (m.vel && params[b].solver == SOLVER_MASS)
+            if (m.vel && params[b].solver != SOLVER_NOMASS)
                 for (int32_t n = 0; n < m.num_nodes; n++)
                     if (map.lin_of_orig[n] < 0)
                         for (int c = 0; c < 3; c++) secvel[3 * (base + n) + c] = m.vel[3 * (size_t)n + c];
         }
         CK(upload(A, h->io_src, src));
+        h->io_src_host = src;
         CK(upload(A, h->io_secvel, secvel));
         CK(A.alloc(h->io_stage, 9 * (size_t)h->io_max_nodes));
         CK(A.alloc(h->io_moved, 1));
     }
     launch_rest_state(d, h->stream);
     if (d.any_mass) launch_mass_matrix(d, h->stream);
+    if (d.any_lumped) launch_lumped_mass(d, h->stream);
     if (d.coarse) {
         // X ~ A_c^-1 of the rest mesh, Newton-Schulz from a scaled identity;
         // every step then refines it for the current mesh
@@ -909,7 +915,7 @@ int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const dou
         if (pos) CK(cudaMemsetAsync(h->io_moved, 0, sizeof(int), h->stream));
         k_nodes_in<<<(N + 255) / 256, 256, 0, h->stream>>>(h->dev, h->io_src + o, N, pos ? st : nullptr,
                                                           vel ? st + 3 * (size_t)N : nullptr, h->io_secvel + 3 * o,
-                                                          bp.solver == SOLVER_MASS, h->io_moved);
+                                                          bp.solver != SOLVER_NOMASS, h->io_moved);
         count_launches(1);
         if (pos) {
             // positions that differ from the current ones: refresh the
@@ -922,6 +928,50 @@ int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const dou
     }
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_set_external_forces(ffea_gpu_t *h, int32_t blob, int32_t count, const int32_t *nodes,
+                                 const double *forces)
+{
+    if (check_blob(h, blob)) return FFEA_GPU_ERROR;
+    const int32_t N = h->host.maps[blob].num_nodes_total;
+    if (count < 0) return fail("count must be >= 0");
+    if (count > 0 && (!nodes || !forces)) return fail("null nodes or forces");
+    for (int32_t i = 0; i < count; i++)
+        if (nodes[i] < 0 || nodes[i] >= N) return fail("node index %d out of range [0, %d)", nodes[i], N);
+    DeviceBatch &d = h->dev;
+    if (!d.ext) {
+        if (count == 0) return FFEA_GPU_OK;  // nothing set, nothing to clear
+        CK(cudaStreamSynchronize(h->stream));
+        CK(h->arena.alloc(d.ext, 3 * (size_t)h->host.nl_pad));  // zeroed
+        h->ext_host.assign(3 * (size_t)h->host.nl_pad, 0.0);
+        // the step graphs hold the batch by value: capture them again
+        if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
+        if (h->step_exec_coarse) cudaGraphExecDestroy(h->step_exec_coarse);
+        h->step_exec = h->step_exec_coarse = nullptr;
+    }
+    // fold onto the blob's corner rows in the given order: a corner node
+    // keeps its force, an edge midpoint gives half to each end
+    const BlobParams &bp = h->host.bp[blob];
+    const int2 *src = h->io_src_host.data() + h->io_off[blob];
+    double *e = h->ext_host.data() + 3 * (size_t)bp.node_off;
+    std::fill(e, e + 3 * (size_t)bp.node_cnt, 0.0);
+    for (int32_t i = 0; i < count; i++) {
+        const int2 s = src[nodes[i]];
+        const double *f = forces + 3 * (size_t)i;
+        if (s.x >= 0 && s.y < 0) {
+            for (int c = 0; c < 3; c++) e[3 * (size_t)(s.x - bp.node_off) + c] += f[c];
+        } else if (s.x >= 0) {
+            for (int c = 0; c < 3; c++) {
+                e[3 * (size_t)(s.x - bp.node_off) + c] += 0.5 * f[c];
+                e[3 * (size_t)(s.y - bp.node_off) + c] += 0.5 * f[c];
+            }
+        }  // a node of no element takes no part in the update
+    }
+    CK(cudaMemcpyAsync(d.ext + 3 * (size_t)bp.node_off, e, sizeof(double) * 3 * (size_t)bp.node_cnt,
+                       cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
     return FFEA_GPU_OK;
 }
 

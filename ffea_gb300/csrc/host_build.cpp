@@ -260,7 +260,7 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
             err = "blob " + std::to_string(b) + ": empty mesh or missing pos/topology/material";
             return false;
         }
-        if (p.solver != SOLVER_NOMASS && p.solver != SOLVER_MASS) {
+        if (p.solver != SOLVER_NOMASS && p.solver != SOLVER_MASS && p.solver != SOLVER_LUMPED) {
             err = "unknown solver kind";
             return false;
         }
@@ -328,6 +328,7 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
         elem_off += bp.elem_pad;
         tile_off += bp.tile_cnt;
         if (p.solver == SOLVER_MASS) H.any_mass = 1;
+        else if (p.solver == SOLVER_LUMPED) H.any_lumped = 1;
         else H.any_nomass = 1;
         if ((int64_t)node_off >= (1ll << 30) || (int64_t)elem_off >= (1ll << 28)) {
             err = "batch too large";

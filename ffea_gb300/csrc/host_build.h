@@ -25,7 +25,7 @@ struct HostBatch {
     int32_t precision = PREC_MIXED;
     int32_t rng_mode = 0;
     int32_t nl_pad = 0, ne_pad = 0, n_edges = 0, n_tiles = 0, n_etiles = 0;
-    int32_t any_mass = 0, any_nomass = 0;
+    int32_t any_mass = 0, any_nomass = 0, any_lumped = 0;
     std::vector<BlobParams> bp;
     std::vector<Material> materials;
     std::vector<uint16_t> mat_id;        // per padded element

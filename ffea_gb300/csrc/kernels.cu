@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(ELEM_TILE) k_elements(DeviceBatch d, int mode)
         S[2][0] = S[0][2];
         S[2][1] = S[1][2];
     }
-    if (bp.solver == SOLVER_MASS) {
+    if (bp.solver != SOLVER_NOMASS) {
         // viscous stress A (L + L^T) + B tr(L) I from the velocity gradient
         // L_ij = sum_b v_b,i dpsi_b,j; equal to viscosity_matrix * v
         // (src/tetra_element_linear.cpp:299-328, src/Blob.cpp:703-706)
@@ -492,7 +492,27 @@ __global__ void k_mass_matrix(DeviceBatch d)
     }
 }
 
-// Node kernel: rhs and the CG start.
+// Lumped masses (MassLumpedSolver::init, src/MassLumpedSolver.cpp:40-78):
+// per corner row a quarter of rho vol_0 of every element holding it, summed
+// in element order (the gather list's order), inverted; 1 on pinned rows.
+template <typename T>
+__global__ void k_lumped_mass(DeviceBatch d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nl_pad) return;
+    const BlobParams &bp = d.bp[d.tile_blob[i / NODE_TILE]];
+    if (bp.solver != SOLVER_LUMPED) return;
+    double s = 0.0;
+    for (int k = d.gather_ptr[i]; k < d.gather_ptr[i + 1]; k++) {
+        const int el = d.gather_idx[k] >> 2;
+        s += .25 * d.mats[d.mat_id[el]].rho * (double)static_cast<const T *>(d.vol0)[el];
+    }
+    if ((d.flags[i] & NODE_PINNED) || s == 0.0) s = 1.0;
+    d.lumped_inv[i] = 1.0 / s;
+}
+
+// Node kernel: rhs and the CG start (for a lumped-mass blob the solve
+// itself, x = M_lumped^-1 f, MassLumpedSolver::solve src/MassLumpedSolver.cpp:81-89).
 template <typename T>
 __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_given_rhs)
 {
@@ -509,9 +529,18 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
     T D[3] = {(T)0, (T)0, (T)0};
     const double drag = bp.calc_stokes == 1 ? d.drag[row] : 0.0;
     if (valid) {
+        // external forces first, as FFEA adds them to Blob::force before the
+        // element contributions (src/World.cpp:1907, src/Blob.cpp:647)
+        if (d.ext && !use_given_rhs) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) fs[i].add_d(d.ext[3 * (size_t)row + i]);
+        }
         const T *ef = static_cast<const T *>(d.efrc);
         const T *g = static_cast<const T *>(d.g);
         const T *mt = static_cast<const T *>(d.mat_t);
+        // unrolled so that the loads of several (element, corner) entries
+        // are in flight together; the sums keep their order
+#pragma unroll 4
         for (int k = d.gather_ptr[row]; k < d.gather_ptr[row + 1]; k++) {
             const int gi = d.gather_idx[k];
             const int el = gi >> 2, a = gi & 3;
@@ -570,6 +599,7 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
     T *x = static_cast<T *>(d.x), *r = static_cast<T *>(d.r), *u = static_cast<T *>(d.u);
     T *p = static_cast<T *>(d.p), *sv = static_cast<T *>(d.s), *w = static_cast<T *>(d.w);
     double gam = 0.0, ff = 0.0;
+    const bool lumped = bp.solver == SOLVER_LUMPED;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const size_t k = 3 * (size_t)row + i;
@@ -577,7 +607,7 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
         if (!use_given_rhs) d.rhs[k] = fi;
         const T ri = (T)fi;
         const T ui = dinv[k] * ri;
-        x[k] = (T)0;
+        x[k] = lumped ? (T)(fi * d.lumped_inv[row]) : (T)0;
         r[k] = ri;
         u[k] = ui;
         p[k] = (T)0;
@@ -618,7 +648,8 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
                 cg.iters = 0;
                 cg.restarts = 0;
                 cg.true_relres2 = -1.0;
-                const bool done = (d.status[bb] != 0) || s1 == 0.0;
+                // a lumped-mass blob has its solution already (no CG)
+                const bool done = (d.status[bb] != 0) || s1 == 0.0 || d.bp[bb].solver == SOLVER_LUMPED;
                 cg.state = done ? CG_CONVERGED : CG_ACTIVE;
                 if (!done) atomicAdd(&running, 1u);
             }
@@ -1105,6 +1136,74 @@ __device__ __forceinline__ void seg_partials(float *P, const W (&in)[3], int mas
     __syncthreads();
 }
 
+// Dynamic shared memory of the CG kernel (layout in k_cg).
+extern __shared__ __align__(16) unsigned char cg_dyn[];
+
+// Deferred segment partials of the memory-resident CG kernel (FP32 sums).
+// seg_partials ends every segment with two CTA barriers, so every warp waits
+// for the slowest one before it starts on the next segment's rows.  Here the
+// per-warp stage of seg_partials goes to shared memory with no barrier, the
+// warps run on into the next segments, and flush_partials runs the
+// cross-warp stage for up to kDeferSegs segments after one barrier.  The
+// arithmetic and its order are those of seg_partials: the same bits.
+// Region (start of the dynamic shared memory): kDeferSegs x kDeferQ x 32
+// floats, then per deferred segment (slot, dot-term mask, NX, ex_off).
+struct DeferView {
+    float *buf;
+    int4 *meta;
+};
+
+__device__ __forceinline__ DeferView defer_view()
+{
+    DeferView v;
+    v.buf = reinterpret_cast<float *>(cg_dyn);
+    v.meta = reinterpret_cast<int4 *>(v.buf + kDeferSegs * kDeferQ * 32);
+    return v;
+}
+
+template <int NX>
+__device__ __forceinline__ void seg_partials_defer(const DeferView &dv, int c, int seg, int mask, int ex_off,
+                                                   const float (&in)[3], const float *ex)
+{
+    static_assert(3 + NX <= kDeferQ, "values per warp and segment");
+    constexpr int NV = (3 + NX) <= 4 ? 4 : (3 + NX) <= 8 ? 8 : 16;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float v[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) v[k] = k < 3 ? in[k] : k < 3 + NX ? ex[k - 3] : 0.f;
+    int idx;
+    const float t = warp_sum_multi<NV>(v, idx);
+    if ((lane & (32 / NV - 1)) == 0 && idx < 3 + NX) dv.buf[(c * kDeferQ + idx) * 32 + warp] = t;
+    if (threadIdx.x == 0) dv.meta[c] = make_int4(seg, mask, NX, ex_off);
+}
+
+// The cross-warp stage of seg_partials for the cnt deferred segments, into
+// the partials buffer part (floats, stride floats per segment slot).
+__device__ __forceinline__ void flush_partials(const DeferView &dv, int cnt, float *part, int stride)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    for (int p = warp; p < cnt * kDeferQ; p += nw) {
+        const int c = p / kDeferQ, q = p % kDeferQ;
+        const int4 m = dv.meta[c];
+        float *P = part + (size_t)stride * m.x;
+        const float *src = dv.buf + (c * kDeferQ + q) * 32;
+        if (q < 3) {
+            if (m.y & (1 << q)) {
+                const DF v = df_warp_sum(DF{lane < nw ? src[lane] : 0.f, 0.f});
+                if (lane == 0) {
+                    P[2 * q] = v.hi;
+                    P[2 * q + 1] = v.lo;
+                }
+            }
+        } else if (q - 3 < m.z) {
+            const float v = warp_sum<float>(lane < nw ? src[lane] : 0.f);
+            if (lane == 0) P[m.w + q - 3] = v;
+        }
+    }
+    __syncthreads();
+}
+
 // Loads of segment partials in flight per thread before they are added.
 constexpr int kSumUnroll = 4;
 
@@ -1404,9 +1503,6 @@ __device__ __forceinline__ unsigned int reducing_barrier(const DeviceBatch &d, c
 // alpha h with the new alpha and beta (after a failed true-residual check,
 // RESTART: g = P^T r of the true residual), then c = X g over the CTA's six
 // rows of X ~ A_c^-1 in one block reduction.
-// Dynamic shared memory of the CG kernel (layout in k_cg).
-extern __shared__ __align__(16) unsigned char cg_dyn[];
-
 // The coarse-space region of the dynamic shared memory: per thread the rest
 // offset and smoother weight (phi), the CTA's 6 rows of X, c (8 floats),
 // 6 x 32 reduction floats, and (P^T s)_j per coarse dof j.  The addresses are
@@ -1469,7 +1565,8 @@ __device__ __forceinline__ void coarse_apply(const DeviceBatch &d, int n, float 
 }
 
 // Coarse space of the memory-resident CG kernel (several segments per CTA,
-// any number of coarse dofs per blob).  Dynamic shared memory: c of each of
+// any number of coarse dofs per blob).  Dynamic shared memory, after the
+// deferred-partials region: c of each of
 // the CTA's segments (8 floats), 32 x 8 reduction floats, g of the blob being
 // corrected (coarse_nmax floats), and (P^T s)_j for every coarse dof of every
 // blob the CTA touches (coarse_hmax floats, blob after blob).  Every CTA that
@@ -1482,7 +1579,7 @@ struct CoarseMemView {
 __device__ __forceinline__ CoarseMemView coarse_mem_view(const DeviceBatch &d)
 {
     CoarseMemView v;
-    v.cvec = reinterpret_cast<float *>(cg_dyn);
+    v.cvec = reinterpret_cast<float *>(cg_dyn + kDeferBytes);
     v.red = v.cvec + 8 * CG_MAX_SEGS;
     v.g = v.red + 8 * 32;
     v.h = v.g + d.coarse_nmax;
@@ -1835,6 +1932,17 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     const bool coarse = REG && local && d.coarse;
     // the same preconditioner in the memory-resident kernel (coarse_mem_step)
     const bool mcoarse = !REG && d.coarse;
+    // memory-resident kernel in FP32: segment partials deferred (flush_partials)
+    constexpr bool kDefer = !REG && sizeof(T) == 4;
+    int dcnt = 0;  // deferred segments not yet flushed (CTA-uniform)
+    auto defer_flush = [&]() {
+        if constexpr (kDefer) {
+            if (dcnt) {
+                flush_partials(defer_view(), dcnt, reinterpret_cast<float *>(part()), d.part_stride);
+                dcnt = 0;
+            }
+        }
+    };
     int coarse_n = 0;  // coarse dofs of the CTA's blob (0: no coarse space)
     if (coarse) {
         const CoarseView cv = coarse_view<T>(d);
@@ -1953,6 +2061,18 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             U4()[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
         }
         if (!REG && valid) store_fields<T>(d, row, loc, RF_X | RF_R | RF_U | RF_S | RF_P);
+        if constexpr (kDefer) {
+            const float inf[3] = {(float)pg, 0.f, (float)pr};
+            if (mcoarse) {
+                float ex[6] = {0, 0, 0, 0, 0, 0};
+                if (valid) restrict6_of<T>(fm, S.r, ex);
+                seg_partials_defer<6>(defer_view(), dcnt, S0 + j, 5, 8, inf, ex);
+            } else {
+                seg_partials_defer<0>(defer_view(), dcnt, S0 + j, 5, 0, inf, nullptr);
+            }
+            if (++dcnt == kDeferSegs) defer_flush();
+            return;
+        }
         const W in[3] = {pg, (W)0, pr};
         if (coarse) {
             // restriction of the new r: slot floats 8..
@@ -2008,6 +2128,20 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
         }
         if (!REG && valid) store_fields<T>(d, row, loc, state == CG_VERIFY ? (RF_R | RF_U) : RF_W);
+        if constexpr (kDefer) {
+            if (!prologue && state == CG_ACTIVE) {
+                const float inf[3] = {(float)pg, (float)pd, (float)pr};
+                if (mcoarse) {
+                    float ex[6] = {0, 0, 0, 0, 0, 0};
+                    if (valid) restrict6_of<T>(d.phi[row], S.w, ex);
+                    seg_partials_defer<6>(defer_view(), dcnt, S0 + j, 2, 14, inf, ex);
+                } else {
+                    seg_partials_defer<0>(defer_view(), dcnt, S0 + j, 2, 0, inf, nullptr);
+                }
+                if (++dcnt == kDeferSegs) defer_flush();
+                return;
+            }
+        }
         if (mcoarse) {
             // the restrictions of the register-resident branch below, with
             // the rest offset from memory
@@ -2142,6 +2276,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
     if (!s_err)
         for (int j = 0; j < nt; j++) phase_b(j, true);
+    defer_flush();  // (the prologue defers nothing: a no-op)
     unsigned int running = s_err ? 0u : reduce();
     int loops = 0;
     while (!s_err && running > 0) {
@@ -2154,9 +2289,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         if (local || mcoarse) parity ^= 1;
         if (REG && s_state[0] == CG_VERIFY) publish_x();
         for (int j = 0; j < nt; j++) phase_a(j);
+        defer_flush();
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) break;
         for (int j = 0; j < nt; j++) phase_b(j, false);
+        defer_flush();
         loops++;
         running = reduce();
     }
@@ -2234,7 +2371,12 @@ __global__ void __launch_bounds__(NODE_TILE) k_apply(DeviceBatch d, const double
     const int row = tile * NODE_TILE + threadIdx.x;
     const bool valid = (row - bp.node_off) < bp.node_cnt && !(d.flags[row] & NODE_PINNED);
     double acc[3] = {0.0, 0.0, 0.0};
-    if (valid) {
+    if (valid && bp.solver == SOLVER_LUMPED) {
+        // M in with the lumped masses (MassLumpedSolver::apply_matrix,
+        // src/MassLumpedSolver.cpp:93-97, scales its result array in place by
+        // the masses; this is the product it stands for)
+        for (int i = 0; i < 3; i++) acc[i] = in[3 * (size_t)row + i] / d.lumped_inv[row];
+    } else if (valid) {
         const bool nomass = bp.solver == SOLVER_NOMASS;
         const double diag = nomass ? (bp.calc_stokes == 1 ? d.drag[row] : 0.0)
                                    : (double)static_cast<const T *>(d.mass_diag)[row];
@@ -2297,7 +2439,7 @@ __global__ void __launch_bounds__(ELEM_TILE) k_energies(DeviceBatch d)
         const double C = m.E - (2.0 / 3.0) * m.G;
         const double t1 = geo.vol / vol0;
         se = vol0 * (m.G * (ff - 3) + 0.5 * C * (t1 * t1 - 1) - (C + 2 * m.G) * log(t1));
-        if (bp.solver == SOLVER_MASS) {
+        if (bp.solver != SOLVER_NOMASS) {
             const int cn[4] = {c.x, c.y, c.z, c.w};
             for (int i = 0; i < 3; i++)
                 for (int a = 0; a < 4; a++) {
@@ -2373,6 +2515,11 @@ void launch_rest_state(const DeviceBatch &d, cudaStream_t s)
     PREC_DISPATCH(d, k_rest_state, d.n_etiles, ELEM_TILE, s, d);
 }
 
+void launch_lumped_mass(const DeviceBatch &d, cudaStream_t s)
+{
+    PREC_DISPATCH(d, k_lumped_mass, blocks_for(d.nl_pad, 256), 256, s, d);
+}
+
 void launch_mass_matrix(const DeviceBatch &d, cudaStream_t s)
 {
     const int64_t n = d.n_edges > d.nl_pad ? d.n_edges : d.nl_pad;
@@ -2439,6 +2586,8 @@ int cg_smem_plan(int precision, int max_slots, int max_cols, size_t extra_bytes,
 // space (coarse_mem_view): its size for the given coarse dimensions, and
 // whether the device allows it (the kernel's limit is raised to the device
 // maximum, as for the register-resident kernel).
+size_t cg_mem_defer_bytes(int precision) { return precision == PREC_FP64 ? 0 : kDeferBytes; }
+
 size_t cg_mem_coarse_bytes(int coarse_nmax, int coarse_hmax)
 {
     return sizeof(float) * (8 * (size_t)CG_MAX_SEGS + 8 * 32 + (size_t)coarse_nmax + (size_t)coarse_hmax);

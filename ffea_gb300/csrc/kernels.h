@@ -19,7 +19,7 @@ struct DeviceBatch {
     int32_t n_slices = 0, n_entries = 0;
     int32_t n_segs = 0;           // CG segments
     int32_t precision = PREC_MIXED;
-    int32_t any_mass = 0, any_nomass = 0;
+    int32_t any_mass = 0, any_nomass = 0, any_lumped = 0;
     int32_t cg_grid = 0;          // CTAs of the persistent CG kernel
     int32_t cg_reg = 0;           // 1: one CG segment per CTA, row state kept in registers
     int32_t cg_local = 0;         // 1: every CTA reduces the dot products itself (few segments and blobs)
@@ -55,6 +55,8 @@ struct DeviceBatch {
     void *node_noise = nullptr;
     // nodes (FP64 state and rhs)
     double *pos = nullptr, *vel = nullptr, *drag = nullptr, *rhs = nullptr;
+    double *ext = nullptr;        // external forces per row (folded; NULL until first set)
+    double *lumped_inv = nullptr; // lumped-mass solver: inverse lumped mass per row
     float2 *pos_df = nullptr;     // mixed precision: positions as (hi, lo) FP32 pairs, kept with pos
     uint8_t *flags = nullptr;
     int32_t *orig = nullptr;
@@ -111,10 +113,15 @@ constexpr int CG_THREADS = CG_SEG_MAX_ROWS;  // threads per CTA of the CG kernel
 constexpr int CG_MAX_SEGS = 64;         // segments per CTA of the persistent kernel
 constexpr int CG_LOCAL_MAX_BLOBS = 64;  // local reduction: blob records kept in shared memory
 constexpr int CG_LOCAL_MAX_SEGS = 2048; // local reduction: partial sums every CTA reads per iteration
+// memory-resident CG kernel (FP32): segment partials deferred in shared memory
+constexpr int kDeferSegs = 16;  // segments per flush
+constexpr int kDeferQ = 9;      // values per warp and segment: 3 dot terms + up to 6 restrictions
+constexpr size_t kDeferBytes = sizeof(float) * kDeferSegs * kDeferQ * 32 + 16 * kDeferSegs;
 
 // Launchers (all asynchronous on `s`).
 void launch_rest_state(const DeviceBatch &d, cudaStream_t s);
 void launch_mass_matrix(const DeviceBatch &d, cudaStream_t s);
+void launch_lumped_mass(const DeviceBatch &d, cudaStream_t s);
 void launch_elements(const DeviceBatch &d, cudaStream_t s, int mode);
 void launch_assemble(const DeviceBatch &d, cudaStream_t s);
 // the step's random draws (nothing when no blob draws)
@@ -174,6 +181,7 @@ int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, ::c
 // of dynamic shared memory, or not) that fit co-resident on the current
 // device, 0 on error
 int cg_max_grid(int precision, int reg, size_t dyn_bytes);
+size_t cg_mem_defer_bytes(int precision);
 size_t cg_mem_coarse_bytes(int coarse_nmax, int coarse_hmax);
 int cg_mem_smem_allow(int precision, size_t dyn_bytes);
 

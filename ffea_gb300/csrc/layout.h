@@ -22,7 +22,7 @@ constexpr int CG_SEG_MAX_ROWS = 1024;  // rows of a CG segment (one per thread o
 constexpr int NOISE_RUN = 32;          // consecutive draws per thread of the noise kernel (one jump each)
 constexpr int NOISE_THREADS = 128;     // threads per CTA of the noise kernel
 
-enum SolverKind : int32_t { SOLVER_NOMASS = 0, SOLVER_MASS = 1 };
+enum SolverKind : int32_t { SOLVER_NOMASS = 0, SOLVER_MASS = 1, SOLVER_LUMPED = 2 };
 enum Precision : int32_t { PREC_FP64 = 0, PREC_MIXED = 1 };
 
 // node flag bits

@@ -87,17 +87,17 @@ MRG_HD void jump(const JumpMat *table, uint32_t off, uint32_t *s)
 // One step of both components (the recurrences of src/RngStream.cpp:270-283
 // on int64); returns n = (p1 - p2) mod m1 in [1, m1] (m1 when p1 == p2),
 // the integer that :286 scales by 1 / (m1 + 1).
+// Each difference a s_i - b s_j is taken as a s_i + b (m - s_j), the same
+// residue, with both products below 2^53 (a, b < 2^21; states below m), and
+// reduced by folding (reduce64) rather than by a 64-bit division, which the
+// GPU runs as a long instruction sequence.
 MRG_HD int64_t next_n(uint32_t *s)
 {
-    int64_t p1 = 1403580ll * (int64_t)s[1] - 810728ll * (int64_t)s[0];
-    p1 %= (int64_t)M1;
-    if (p1 < 0) p1 += M1;
-    s[0] = s[1]; s[1] = s[2]; s[2] = (uint32_t)p1;
-    int64_t p2 = 527612ll * (int64_t)s[5] - 1370589ll * (int64_t)s[3];
-    p2 %= (int64_t)M2;
-    if (p2 < 0) p2 += M2;
-    s[3] = s[4]; s[4] = s[5]; s[5] = (uint32_t)p2;
-    return (p1 > p2) ? p1 - p2 : p1 - p2 + (int64_t)M1;
+    const uint32_t p1 = reduce64<M1, C1>(1403580ull * s[1] + 810728ull * (uint64_t)(M1 - s[0]));
+    s[0] = s[1]; s[1] = s[2]; s[2] = p1;
+    const uint32_t p2 = reduce64<M2, C2>(527612ull * s[5] + 1370589ull * (uint64_t)(M2 - s[3]));
+    s[3] = s[4]; s[4] = s[5]; s[5] = p2;
+    return (p1 > p2) ? (int64_t)p1 - (int64_t)p2 : (int64_t)p1 - (int64_t)p2 + (int64_t)M1;
 }
 
 // One draw: the combination of src/RngStream.cpp:286 in double.  Returns u

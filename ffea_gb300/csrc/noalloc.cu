@@ -189,7 +189,7 @@ extern "C" int ffea_gpu_energies_noalloc(const double *pos, const double *vel, c
     if (e != cudaSuccess) return fail("cudaMemsetAsync: %s", cudaGetErrorString(e));
     const int tiles = (num_elements + kTile - 1) / kTile;
     k_energies_noalloc<<<tiles, kTile, 0, s>>>(pos, vel, topology, rest_pos, material, num_elements,
-                                               solver == FFEA_GPU_SOLVER_MASS ? 1 : 0, scratch, out);
+                                               solver != FFEA_GPU_SOLVER_NOMASS ? 1 : 0, scratch, out);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail("k_energies_noalloc launch: %s", cudaGetErrorString(e));
     return FFEA_GPU_OK;

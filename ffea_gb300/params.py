@@ -25,6 +25,7 @@ PI = 3.1415926535897932384626433832795028841971693993751058209749445923078164062
 
 SOLVER_NOMASS = 0   # <solver = CG_nomass>  (src/World.cpp:2545-2562)
 SOLVER_MASS = 1     # <solver = CG>
+SOLVER_LUMPED = 2   # <solver = masslumped>: MassLumpedSolver
 
 PRECISION_FP64 = 0   # every kernel in FP64 (parity mode)
 PRECISION_MIXED = 1  # FP32 element forces + SpMV, FP64 positions / dots / residuals
@@ -107,5 +108,5 @@ def nm(x_nm: float) -> float:
 __all__ = [
     "SimulationParams", "material_si_to_meso", "stokes_drag", "kT_at", "nm",
     "MESO_LENGTH", "MESO_ENERGY", "MESO_MASS", "MESO_VOLUME", "MESO_TIME", "MESO_PRESSURE",
-    "SOLVER_NOMASS", "SOLVER_MASS", "PRECISION_FP64", "PRECISION_MIXED", "PI",
+    "SOLVER_NOMASS", "SOLVER_MASS", "SOLVER_LUMPED", "PRECISION_FP64", "PRECISION_MIXED", "PI",
 ]

@@ -208,6 +208,18 @@ class Blob:
         vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
         L.check(L.lib().ffea_gpu_set_nodes(self.world.handle, self.index, L.ptr(pos), L.ptr(vel)))
 
+    def set_external_forces(self, nodes=None, forces=None):
+        """External forces (FFEA's springs / ctforces) on nodes of this blob,
+        kept for every following step; no arguments clears them."""
+        nodes = np.ascontiguousarray([] if nodes is None else nodes, dtype=np.int32).reshape(-1)
+        forces = np.ascontiguousarray(np.zeros((0, 3)) if forces is None else forces, dtype=np.float64).reshape(-1, 3)
+        if len(nodes) != len(forces):
+            raise ValueError("set_external_forces: one force (3 components) per node")
+        L.check(L.lib().ffea_gpu_set_external_forces(self.world.handle, self.index, len(nodes),
+                                                     L.ptr(nodes, L._ip) if len(nodes) else None,
+                                                     L.ptr(forces) if len(nodes) else None),
+                "ffea_gpu_set_external_forces")
+
     def rng_state(self) -> np.ndarray:
         st = np.zeros(6, np.uint64)
         L.check(L.lib().ffea_gpu_get_rng_state(self.world.handle, self.index, L.ptr(st, L._u64p)))

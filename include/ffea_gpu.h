@@ -40,6 +40,7 @@ extern "C" {
 
 #define FFEA_GPU_SOLVER_NOMASS 0   /* <solver = CG_nomass>: NoMassCGSolver */
 #define FFEA_GPU_SOLVER_MASS 1     /* <solver = CG>: ConjugateGradientSolver */
+#define FFEA_GPU_SOLVER_LUMPED 2   /* <solver = masslumped>: MassLumpedSolver */
 
 #define FFEA_GPU_PRECISION_FP64 0  /* every kernel in FP64 */
 #define FFEA_GPU_PRECISION_MIXED 1 /* FP32 element forces and SpMV; FP64 positions, dots, residuals */
@@ -119,6 +120,19 @@ int ffea_gpu_step(ffea_gpu_t *h, int32_t nsteps);
 int ffea_gpu_get_nodes(ffea_gpu_t *h, int32_t blob, double *pos, double *vel, double *force);
 int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const double *vel);
 
+/* External forces on a blob's nodes, added to the rhs of every following
+ * step until replaced: count entries of (node index in the reference's
+ * numbering, 3 force components in meso units); repeated nodes add up;
+ * count 0 clears them.  They enter where FFEA's World interactions (springs,
+ * src/World.cpp:3808-3846) and Blob::apply_ctforces (src/Blob.cpp:647,
+ * 2094-2162) add to Blob::force before the element loop, after the per-step
+ * zeroing (src/World.cpp:1907): a secondary node's force folds half onto
+ * each end of its edge (Blob::linearise_force, src/Blob.cpp:1066-1085) and
+ * pinned nodes keep none.  The first call on a handle allocates the buffer
+ * and re-captures the step graphs. */
+int ffea_gpu_set_external_forces(ffea_gpu_t *h, int32_t blob, int32_t count, const int32_t *nodes,
+                                 const double *forces);
+
 /* RngStream state words of a blob's stream (RngStream::GetState / SetSeed,
  * src/RngStream.cpp:381-399,439-443); the .fcp checkpoint holds these. */
 int ffea_gpu_get_rng_state(ffea_gpu_t *h, int32_t blob, uint64_t state[6]);
@@ -179,7 +193,8 @@ int ffea_gpu_ffea_seed(int32_t rng_seed, uint64_t out[6]);
  *   be NULL), rest_pos (positions the rest state is taken from) -- 3*N_t
  *   doubles each in the reference node numbering --, topology (10 int32 per
  *   element), material (rho, A, B, G, E per element), out (2 doubles: strain,
- *   kinetic).  solver selects whether the kinetic term is evaluated (mass path).
+ *   kinetic).  solver selects whether the kinetic term is evaluated (the
+ *   mass and lumped-mass paths).
  *   Scratch is a static device array of the library sized for at most
  *   2,097,152 elements; larger meshes are rejected with an error.  Every GPU
  *   that loads the library holds that array (256 KiB) until the process exits.

@@ -28,7 +28,7 @@
 #define ORC_OK 0
 #define ORC_ERROR -1
 
-enum { ORC_SOLVER_NOMASS = 0, ORC_SOLVER_MASS = 1 };
+enum { ORC_SOLVER_NOMASS = 0, ORC_SOLVER_MASS = 1, ORC_SOLVER_LUMPED = 2 };
 
 /* ------------------------------------------------------------------------ */
 /* MRG32k3a (L'Ecuyer 1999; L'Ecuyer, Simard, Chen, Kelton 2002).          */
@@ -448,6 +448,8 @@ typedef struct {
     int last_iters;
     int last_inversions;
     double *rhs_copy;                   /* rhs handed to the solver in the last step */
+    double *ext;                        /* external forces per node (NULL: none), added every step */
+    double *inv_m;                      /* lumped solver: inverse lumped mass per node */
 } orc_blob;
 
 static void *orc_alloc(size_t n) { void *p = calloc(n ? n : 1, 1); return p; }
@@ -987,6 +989,36 @@ static int orc_mass_init(orc_blob *b)
     return ORC_OK;
 }
 
+/* MassLumpedSolver::init (src/MassLumpedSolver.cpp:40-78): a quarter of each
+ * element's mass rho vol_0 on each corner, 1 on secondary and pinned nodes,
+ * inverted. */
+static int orc_lumped_init(orc_blob *b)
+{
+    const int Nn = b->num_nodes;
+    b->inv_m = orc_alloc(sizeof(double) * Nn);
+    for (int n = 0; n < b->num_elements; n++)
+        for (int i = 0; i < 10; i++) {
+            const int ni = b->topo[10 * n + i];
+            if (i < 4) b->inv_m[ni] += .25 * b->rho[n] * b->vol_0[n];
+            else b->inv_m[ni] = 1;
+        }
+    for (int i = 0; i < b->num_pinned; i++) b->inv_m[b->pinned[i]] = 1.0;
+    for (int i = 0; i < Nn; i++) b->inv_m[i] = 1.0 / b->inv_m[i];
+    return ORC_OK;
+}
+
+/* MassLumpedSolver::solve (src/MassLumpedSolver.cpp:81-89) */
+static int orc_lumped_solve(orc_blob *b, double *x)
+{
+    for (int i = 0; i < b->num_nodes; i++) {
+        x[3 * i] = x[3 * i] * b->inv_m[i];
+        x[3 * i + 1] = x[3 * i + 1] * b->inv_m[i];
+        x[3 * i + 2] = x[3 * i + 2] * b->inv_m[i];
+    }
+    b->last_iters = 0;
+    return ORC_OK;
+}
+
 /* ConjugateGradientSolver::solve (src/ConjugateGradientSolver.cpp:206-232,
  * helpers :249-349). */
 static int orc_mass_solve(orc_blob *b, double *x)
@@ -1083,6 +1115,7 @@ static int orc_aggregate_and_solve(orc_blob *b)
     }
     memcpy(b->rhs_copy, force, sizeof(double) * 3 * Nn);
     if (b->solver == ORC_SOLVER_NOMASS) return orc_nomass_solve(b, force);
+    if (b->solver == ORC_SOLVER_LUMPED) return orc_lumped_solve(b, force);
     return orc_mass_solve(b, force);
 }
 
@@ -1121,7 +1154,7 @@ static void orc_euler_and_linearise(orc_blob *b)
  * units, as Blob::load_material_params leaves them, src/Blob.cpp:2864-2867).
  * stokes_drag: per node (6 pi eta r, src/Blob.cpp:408-412).
  * fparams: dt, kT, epsilon2.  iparams: max_iterations_cg, calc_noise,
- * calc_stokes, solver (0 = CG_nomass, 1 = CG), num_threads. */
+ * calc_stokes, solver (0 = CG_nomass, 1 = CG, 2 = masslumped), num_threads. */
 orc_blob *orc_blob_create(int num_nodes, int num_elements, const double *pos, const int *topo,
                           const double *material, const double *stokes_drag, int num_pinned,
                           const int *pinned, const double *fparams, const int *iparams)
@@ -1196,6 +1229,7 @@ orc_blob *orc_blob_create(int num_nodes, int num_elements, const double *pos, co
     }
     /* the solver init (src/Blob.cpp:359-380) */
     if (b->solver == ORC_SOLVER_NOMASS) orc_nomass_init(b);
+    else if (b->solver == ORC_SOLVER_LUMPED) orc_lumped_init(b);
     else orc_mass_init(b);
     return b;
 }
@@ -1207,7 +1241,7 @@ void orc_blob_destroy(orc_blob *b)
                     b->is_pinned, b->pinned, b->J_inv_0, b->vol_0, b->vol, b->last_det, b->dpsi, b->visc,
                     b->node_force, b->F_ij, b->rng, b->nm_key, b->nm_col, b->nm_val, b->nm_src_ptr,
                     b->nm_src, b->pre, b->r, b->p, b->z, b->q, b->f, b->work_in, b->work_out, b->m_key,
-                    b->m_col, b->m_val, b->d, b->s, b->rhs_copy};
+                    b->m_col, b->m_val, b->d, b->s, b->rhs_copy, b->ext, b->inv_m};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
     free(b);
 }
@@ -1242,11 +1276,27 @@ int orc_blob_step(orc_blob *b, int nsteps)
     for (int s = 0; s < nsteps; s++) {
         memset(b->node_force, 0, sizeof(double) * 30 * b->num_elements);
         memset(b->force, 0, sizeof(double) * 3 * b->num_nodes);
+        /* interactions and constant forces add to Blob::force before the
+         * element loop (src/World.cpp:1907 zeroes it; springs
+         * src/World.cpp:3808-3846; Blob::apply_ctforces src/Blob.cpp:647,
+         * 2094-2162 through add_force_to_node-style sums, :2195-2199) */
+        if (b->ext)
+            for (int i = 0; i < 3 * b->num_nodes; i++) b->force[i] += b->ext[i];
         if (orc_internal_forces(b) != ORC_OK) return ORC_ERROR;
         if (orc_aggregate_and_solve(b) != ORC_OK) return ORC_ERROR;
         orc_euler_and_linearise(b);
     }
     return ORC_OK;
+}
+
+/* External forces: count (node, 3 components) entries, summed per node in
+ * the given order, applied at every following step; count 0 clears them. */
+void orc_blob_set_external_forces(orc_blob *b, int count, const int *nodes, const double *forces)
+{
+    if (!b->ext) b->ext = (double *)orc_alloc(sizeof(double) * 3 * b->num_nodes);
+    memset(b->ext, 0, sizeof(double) * 3 * b->num_nodes);
+    for (int i = 0; i < count; i++)
+        for (int c = 0; c < 3; c++) b->ext[3 * nodes[i] + c] += forces[3 * i + c];
 }
 
 void orc_blob_get_nodes(const orc_blob *b, double *pos, double *vel, double *force)

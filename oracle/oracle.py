@@ -70,6 +70,7 @@ def port_lib():
         lib.orc_blob_set_rng_state.argtypes = [ctypes.c_void_p, ctypes.c_int, _u64p]
         lib.orc_blob_get_rng_state.argtypes = [ctypes.c_void_p, ctypes.c_int, _u64p]
         lib.orc_blob_set_nodes.argtypes = [ctypes.c_void_p, _dp, _dp]
+        lib.orc_blob_set_external_forces.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp]
         lib.orc_blob_last_cg_iters.restype = ctypes.c_int
         lib.orc_blob_last_cg_iters.argtypes = [ctypes.c_void_p]
         lib.orc_blob_energies.argtypes = [ctypes.c_void_p, _dp, _dp]
@@ -204,6 +205,11 @@ class OracleBlob:
         pos = None if pos is None else np.ascontiguousarray(pos, dtype=np.float64)
         vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64)
         self.lib.orc_blob_set_nodes(self.h, _ptr(pos, _dp), _ptr(vel, _dp))
+
+    def set_external_forces(self, nodes=None, forces=None):
+        nodes = np.ascontiguousarray([] if nodes is None else nodes, dtype=np.int32).reshape(-1)
+        forces = np.ascontiguousarray(np.zeros((0, 3)) if forces is None else forces, dtype=np.float64).reshape(-1)
+        self.lib.orc_blob_set_external_forces(self.h, len(nodes), _ptr(nodes, _ip), _ptr(forces, _dp))
 
     def rhs(self):
         out = np.zeros((self.n, 3))

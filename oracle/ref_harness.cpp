@@ -20,6 +20,7 @@
 
 #include "ConjugateGradientSolver.h"
 #include "NoMassCGSolver.h"
+#include "MassLumpedSolver.h"
 #include "RngStream.h"
 #include "SimulationParams.h"
 #include "mat_vec_fns.h"
@@ -235,7 +236,9 @@ void *ref_blob_create(int num_nodes, int num_elements, const double *pos, const 
             b->node[ni].force_contributions[counter[ni]++] = &b->elem[e].node_force[j];
         }
     delete[] counter;
+    // the solver factory of Blob::init (src/Blob.cpp:359-375)
     if (b->solver_kind == 0) b->solver = new NoMassCGSolver();
+    else if (b->solver_kind == 2) b->solver = new MassLumpedSolver();
     else b->solver = new ConjugateGradientSolver();
     if (b->solver->init(num_nodes, num_elements, b->node, b->elem, &b->params, num_pinned, b->pinned, b->bsite) ==
         FFEA_ERROR) {

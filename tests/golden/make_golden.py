@@ -1,12 +1,13 @@
 """Generate the golden vectors in tests/golden/*.npz from FFEA's own objects.
 
 Runs the reference harness (oracle/_ref/libffea_ref.so: FFEA's
-tetra_element_linear, NoMassCGSolver, ConjugateGradientSolver, RngStream ...
+tetra_element_linear, NoMassCGSolver, ConjugateGradientSolver,
+MassLumpedSolver, RngStream ...
 compiled from the FFEA sources by oracle/Makefile) on small synthetic blobs and
 stores inputs and per-step outputs.  Needs the FFEA source tree (only present
 where the reference is mounted); the fixtures it writes travel with the repo.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -29,6 +30,7 @@ CASES = {
     "mass_sphere4": (lambda: sphere_mesh(4.0, seed=3), P.SOLVER_MASS, None, 11, 6),
     "nomass_cube3_pinned": (lambda: cube_mesh(3, seed=5), P.SOLVER_NOMASS, [0, 1, 2, 5], 44, 6),
     "mass_cube3_pinned": (lambda: cube_mesh(3, seed=5), P.SOLVER_MASS, [0, 7], 44, 6),
+    "lumped_cube3_pinned": (lambda: cube_mesh(3, seed=5), P.SOLVER_LUMPED, [0, 7], 9, 6),
 }
 RECORD_STEPS = (1, 2, 6)
 
@@ -64,7 +66,8 @@ def main():
     O.build(ref=True)
     if not O.ref_available():
         raise SystemExit("the reference objects could not be built (FFEA sources missing)")
-    for name in CASES:
+    names = sys.argv[1:] or list(CASES)  # e.g. make_golden.py lumped_cube3_pinned
+    for name in names:
         make(name)
         print("wrote", name)
 

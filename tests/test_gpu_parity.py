@@ -208,3 +208,27 @@ def test_true_residual_confirms_convergence(gpulib, oracle):
             st = w.blob(0).status()
             assert st["fail_bits"] == 0
             assert st["true_relres"] < 1e-6, st
+
+
+@pytest.mark.parametrize("pinned", [None, [0, 7]])
+def test_lumped_mass_solver_matches_oracle(gpulib, oracle, pinned):
+    """<solver = masslumped>: x = M_lumped^-1 f with no CG (MassLumpedSolver,
+    src/MassLumpedSolver.cpp:40-89), then the mass-path Euler update; FP64
+    tolerances as above, and no CG iterations are reported."""
+    from ffea_gb300.world import World
+    s = spec(radius_nm=4.0, solver=P.SOLVER_LUMPED, pinned=pinned)
+    ref = oracle.blob_from_spec(s)
+    with World([s]) as w:
+        b = w.blob(0)
+        for step in range(10):
+            w.run(1)
+            assert ref.step(1) == 0
+            pos, vel, _ = b.get_nodes()
+            rpos, rvel, _ = ref.nodes()
+            assert rel(b.rhs(), ref.rhs()) < 1e-9, step
+            assert rel(vel, rvel) < 1e-9, step
+            assert np.abs(pos - rpos).max() < 1e-10, step
+            assert b.status()["cg_iters"] == 0
+        ks, kk = b.energies()
+        rs, rk = ref.energies()
+        assert abs(ks - rs) <= 1e-9 * abs(rs) and abs(kk - rk) <= 1e-9 * abs(rk), (ks, rs, kk, rk)

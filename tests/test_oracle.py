@@ -93,7 +93,7 @@ REF_MESH = os.path.join(os.environ.get("FFEA_REFERENCE_SRC", "/root/reference"),
 
 
 @pytest.mark.skipif(not os.path.exists(REF_MESH + ".node"), reason="FFEA sources not present")
-@pytest.mark.parametrize("solver", [0, 1])
+@pytest.mark.parametrize("solver", [0, 1, 2])
 def test_oracle_matches_reference_objects_sphere_63_120(oracle, solver):
     oracle.build(ref=True)
     if not oracle.ref_available():
