@@ -97,6 +97,7 @@ class World:
         L.check(L.lib().ffea_gpu_create_batch(n, marr, parr, int(rng_mode), ctypes.byref(h)), "ffea_gpu_create_batch")
         self._h = h
         self.num_blobs = n
+        self.rng_mode = int(rng_mode)
         L.lib().ffea_gpu_set_graph_mode(self._h, 1 if graph else 0)
 
     # -- lifetime

@@ -41,3 +41,30 @@ def test_strain_energy_equipartition(gpulib):
     se = np.asarray(samples)
     ratio = se.mean() / expected
     assert abs(ratio - 1.0) < 0.03, (ratio, se.mean(), expected)
+
+
+def test_strain_energy_equipartition_two_level_many_replicas(gpulib):
+    """The larger-ensemble check: 96 replicas (more than 64, so the solve
+    reduces at the last-arriving CTA, in the memory-resident kernel with the
+    two-level preconditioner) to 2 % of kT (3N - 6) / 2, with every solve at
+    relative residual 1e-6 confirmed by the FP64 true residual."""
+    from ffea_gb300.world import World
+    mesh = sphere_mesh(7.5, cell_nm=2.5, seed=3)
+    kT = P.kT_at(300.0) * P.MESO_ENERGY
+    specs = [make_blob(mesh, P.SimulationParams.from_si(dt=1e-14, kT=kT, epsilon=1e-6, rng_seed=5000 + r,
+                                                        solver=P.SOLVER_NOMASS, precision=P.PRECISION_MIXED))
+             for r in range(96)]
+    n = mesh.num_linear
+    expected = specs[0].params.kT * (3 * n - 6) / 2
+    samples = []
+    with World(specs, true_residual=True, preconditioner=1) as w:
+        assert w.preconditioner() == 1
+        w.run(2000)
+        for _ in range(16):
+            w.run(400)
+            samples.append([w.blob(i).energies()[0] for i in range(len(specs))])
+            for i in range(len(specs)):
+                st = w.blob(i).status()
+                assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (i, st)
+    ratio = np.asarray(samples).mean() / expected
+    assert abs(ratio - 1.0) < 0.02, ratio
