@@ -798,7 +798,7 @@ __device__ __forceinline__ void block_fma(const T K[9], T d0, T d1, T d2, T &a0,
 // q = A u for one row of the CG kernel (sell_row's arithmetic): slots with
 // values on chip in groups of 4 (only the neighbour loads go to L2), then the
 // rest in groups of 2 (values and neighbours from L2, issued together).
-template <typename T>
+template <typename T, bool MEM = false>
 __device__ __forceinline__ void sell_row_cg(const DeviceBatch &d, int row, bool nomass, T diag,
                                             const typename Vec4T<T>::type *u4, T out[3], const CgCache<T> &cc)
 {
@@ -818,6 +818,41 @@ __device__ __forceinline__ void sell_row_cg(const DeviceBatch &d, int row, bool 
             a0 = fma(m, y.x, a0);
             a1 = fma(m, y.y, a1);
             a2 = fma(m, y.z, a2);
+        }
+        out[0] = a0;
+        out[1] = a1;
+        out[2] = a2;
+        return;
+    }
+    if constexpr (MEM) {
+        // memory-resident kernel (no on-chip copy): the column indices of the
+        // next group are loaded together with this group's values and
+        // neighbours, so a group costs one memory round trip instead of two
+        // (index, then neighbour).  Same slots, same FMA order: same bits.
+        const T *val = static_cast<const T *>(d.sell_val);
+        constexpr int G2 = 2;
+        int cn[G2];
+#pragma unroll
+        for (int g = 0; g < G2; g++) cn[g] = g < L ? __ldg(&d.sell_col[base + 32 * g + lane]) : row;
+        for (int j0 = 0; j0 < L; j0 += G2) {
+            typename Vec4T<T>::type y[G2];
+            T K[G2][9];
+            int nx[G2];
+#pragma unroll
+            for (int g = 0; g < G2; g++) {
+                const int j = j0 + g;
+                y[g] = ldcg4(&u4[cn[g]]);
+                const size_t vb = (size_t)(base + 32 * j) * 9 + lane;
+#pragma unroll
+                for (int k = 0; k < 9; k++) K[g][k] = j < L ? __ldg(&val[vb + 32 * k]) : (T)0;
+                const int jn = j + G2;
+                nx[g] = jn < L ? __ldg(&d.sell_col[base + 32 * jn + lane]) : row;
+            }
+#pragma unroll
+            for (int g = 0; g < G2; g++)
+                if (j0 + g < L) block_fma(K[g], y[g].x - me.x, y[g].y - me.y, y[g].z - me.z, a0, a1, a2);
+#pragma unroll
+            for (int g = 0; g < G2; g++) cn[g] = nx[g];
         }
         out[0] = a0;
         out[1] = a1;
@@ -2105,8 +2140,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         if (valid) {
             if (state != CG_VERIFY) {
                 T au[3];
-                sell_row_cg<T>(d, row, nomass, diag, static_cast<const V4 *>(d.u4), au,
-                               REG ? cg_cache_view<T>(d) : CgCache<T>{});
+                sell_row_cg<T, !REG>(d, row, nomass, diag, static_cast<const V4 *>(d.u4), au,
+                                     REG ? cg_cache_view<T>(d) : CgCache<T>{});
 #pragma unroll
                 for (int cc2 = 0; cc2 < 3; cc2++) {
                     S.w[cc2] = au[cc2];
