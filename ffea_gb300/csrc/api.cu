@@ -873,6 +873,25 @@ int64_t ffea_gpu_cg_loop_count(ffea_gpu_t *h)
     return (int64_t)c;
 }
 
+// A caller's array in device memory of this device (used in place by the
+// node kernels); NULL for host memory, which goes through staging and one
+// copy-engine transfer per array: on GB300 that measured faster than the
+// kernels reading or writing pinned host memory over the host link.
+static void *device_view(const void *p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // not a pointer CUDA knows: clear the error
+        return nullptr;
+    }
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    if ((a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == dev)
+        return const_cast<void *>(p);
+    return nullptr;
+}
+
 int ffea_gpu_get_nodes(ffea_gpu_t *h, int32_t blob, double *pos, double *vel, double *force)
 {
     if (check_blob(h, blob)) return FFEA_GPU_ERROR;
@@ -881,20 +900,26 @@ int ffea_gpu_get_nodes(ffea_gpu_t *h, int32_t blob, double *pos, double *vel, do
     const int64_t o = h->io_off[blob];
     double *st = h->io_stage;
     if (N > 0) {
+        // the kernel writes each array straight into the caller's device
+        // memory, else into staging, copied to the host after
+        double *const out[3] = {pos, vel, force};
+        double *dst[3];
+        for (int k = 0; k < 3; k++) {
+            double *v = static_cast<double *>(device_view(out[k]));
+            dst[k] = v ? v : st + 3 * (size_t)k * N;
+        }
         const int blocks = (N + 255) / 256;
         if (h->dev.precision == PREC_FP64)
             k_nodes_out<double><<<blocks, 256, 0, h->stream>>>(h->dev, h->io_src + o, N, h->io_secvel + 3 * o,
-                                                               bp.solver == SOLVER_NOMASS, st, st + 3 * (size_t)N,
-                                                               st + 6 * (size_t)N);
+                                                               bp.solver == SOLVER_NOMASS, dst[0], dst[1], dst[2]);
         else
             k_nodes_out<float><<<blocks, 256, 0, h->stream>>>(h->dev, h->io_src + o, N, h->io_secvel + 3 * o,
-                                                              bp.solver == SOLVER_NOMASS, st, st + 3 * (size_t)N,
-                                                              st + 6 * (size_t)N);
+                                                              bp.solver == SOLVER_NOMASS, dst[0], dst[1], dst[2]);
         count_launches(1);
         const size_t bytes = 3 * sizeof(double) * (size_t)N;
-        if (pos) CK(cudaMemcpyAsync(pos, st, bytes, cudaMemcpyDeviceToHost, h->stream));
-        if (vel) CK(cudaMemcpyAsync(vel, st + 3 * (size_t)N, bytes, cudaMemcpyDeviceToHost, h->stream));
-        if (force) CK(cudaMemcpyAsync(force, st + 6 * (size_t)N, bytes, cudaMemcpyDeviceToHost, h->stream));
+        for (int k = 0; k < 3; k++)
+            if (out[k] && dst[k] == st + 3 * (size_t)k * N)
+                CK(cudaMemcpyAsync(out[k], dst[k], bytes, cudaMemcpyDeviceToHost, h->stream));
     }
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
@@ -910,12 +935,21 @@ int ffea_gpu_set_nodes(ffea_gpu_t *h, int32_t blob, const double *pos, const dou
     double *st = h->io_stage;
     const size_t bytes = 3 * sizeof(double) * (size_t)N;
     if (N > 0 && (pos || vel)) {
-        if (pos) CK(cudaMemcpyAsync(st, pos, bytes, cudaMemcpyHostToDevice, h->stream));
-        if (vel) CK(cudaMemcpyAsync(st + 3 * (size_t)N, vel, bytes, cudaMemcpyHostToDevice, h->stream));
+        // read straight from the caller's device memory, else from staging
+        const double *src_pos = static_cast<const double *>(device_view(pos));
+        const double *src_vel = static_cast<const double *>(device_view(vel));
+        if (pos && !src_pos) {
+            CK(cudaMemcpyAsync(st, pos, bytes, cudaMemcpyHostToDevice, h->stream));
+            src_pos = st;
+        }
+        if (vel && !src_vel) {
+            CK(cudaMemcpyAsync(st + 3 * (size_t)N, vel, bytes, cudaMemcpyHostToDevice, h->stream));
+            src_vel = st + 3 * (size_t)N;
+        }
         if (pos) CK(cudaMemsetAsync(h->io_moved, 0, sizeof(int), h->stream));
-        k_nodes_in<<<(N + 255) / 256, 256, 0, h->stream>>>(h->dev, h->io_src + o, N, pos ? st : nullptr,
-                                                          vel ? st + 3 * (size_t)N : nullptr, h->io_secvel + 3 * o,
-                                                          bp.solver != SOLVER_NOMASS, h->io_moved);
+        k_nodes_in<<<(N + 255) / 256, 256, 0, h->stream>>>(h->dev, h->io_src + o, N, src_pos, src_vel,
+                                                          h->io_secvel + 3 * o, bp.solver != SOLVER_NOMASS,
+                                                          h->io_moved);
         count_launches(1);
         if (pos) {
             // positions that differ from the current ones: refresh the

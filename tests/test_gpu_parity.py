@@ -232,3 +232,46 @@ def test_lumped_mass_solver_matches_oracle(gpulib, oracle, pinned):
         ks, kk = b.energies()
         rs, rk = ref.energies()
         assert abs(ks - rs) <= 1e-9 * abs(rs) and abs(kk - rk) <= 1e-9 * abs(rk), (ks, rs, kk, rk)
+
+
+def test_node_io_pinned_and_device_buffers_agree(gpulib):
+    """get_nodes / set_nodes with pinned host arrays (staged copies) and with
+    device arrays (used in place): the values are those of the path with
+    pageable arrays, bit for bit."""
+    import ctypes
+
+    import torch
+
+    from ffea_gb300 import _lib as L
+    from ffea_gb300.world import World
+    s = spec(radius_nm=4.0, solver=P.SOLVER_MASS, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    n = s.mesh.num_nodes
+    with World([s]) as w:
+        b = w.blob(0)
+        w.run(3)
+        ref = b.get_nodes()
+        pinned = tuple(torch.empty((n, 3), dtype=torch.float64, pin_memory=True) for _ in range(3))
+        b.get_nodes(out=tuple(t.numpy() for t in pinned))
+        for a, c in zip(ref, pinned):
+            assert np.array_equal(a, c.numpy())
+        dev = tuple(torch.empty((n, 3), dtype=torch.float64, device="cuda") for _ in range(3))
+        dp = [ctypes.cast(t.data_ptr(), L._dp) for t in dev]
+        L.check(L.lib().ffea_gpu_get_nodes(w.handle, 0, *dp))
+        torch.cuda.synchronize()
+        for a, c in zip(ref, dev):
+            assert np.array_equal(a, c.cpu().numpy())
+        # set from pinned (shifted positions, scaled velocities), read back staged
+        pos2 = torch.from_numpy(ref[0] + 0.01).pin_memory()
+        vel2 = torch.from_numpy(ref[1] * 0.5).pin_memory()
+        b.set_nodes(pos2.numpy(), vel2.numpy())
+        got = b.get_nodes()
+        corner = np.zeros(n, bool)
+        corner[s.mesh.topology[:, :4]] = True
+        assert np.array_equal(got[0][corner], ref[0][corner] + 0.01)
+        assert np.array_equal(got[1][corner], ref[1][corner] * 0.5)
+        # and from device arrays
+        pos3 = torch.from_numpy(ref[0]).cuda()
+        L.check(L.lib().ffea_gpu_set_nodes(w.handle, 0, ctypes.cast(pos3.data_ptr(), L._dp), None))
+        assert np.array_equal(b.get_nodes()[0][corner], ref[0][corner])
+        w.run(2)
+        assert b.status()["fail_bits"] == 0
