@@ -437,7 +437,7 @@ def run_gb300(args):
     achieved = alg / (cg_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": "k_cg", "achieved": round(achieved, 1), "peak": peak,
                 "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": ncu_traffic(), "algorithmic_bytes_per_launch": alg,
+                "traffic": ncu_traffic(workload=args.workload), "algorithmic_bytes_per_launch": alg,
                 "avg_launch_us": round(cg_ms * 1e3, 1), "cg_iters_per_launch": iters_p,
                 "bytes_per_iteration": cg_iteration_bytes(nl, nedges)}
     # every other kernel of the step against the same peak: algorithmic bytes
