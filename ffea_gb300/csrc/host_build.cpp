@@ -72,11 +72,15 @@ std::vector<int32_t> plan_parts(const std::vector<int32_t> &counts, int32_t ctas
         k[b] = (slices[b] + max_slices - 1) / max_slices;
         total += k[b];
     }
-    if (total <= ctas) {
-        // longest segment first: (slices per segment rounded up, blob)
+    {
+        // longest segment first: (slices per segment rounded up, blob).  Up
+        // to one segment per CTA, or, with more segments than CTAs, up to a
+        // multiple of the CTA count, so that every CTA of the memory-resident
+        // solve gets the same number of (shorter) segments
+        const int64_t target = total <= ctas ? ctas : ((total + ctas - 1) / ctas) * ctas;
         std::priority_queue<std::pair<int32_t, int>> q;
         for (int b = 0; b < nb; b++) q.push({(slices[b] + k[b] - 1) / k[b], -b});
-        while (total < ctas && !q.empty()) {
+        while (total < target && !q.empty()) {
             const int b = -q.top().second;
             q.pop();
             if (k[b] >= slices[b]) continue;  // one slice per segment already
