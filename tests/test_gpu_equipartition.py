@@ -68,3 +68,33 @@ def test_strain_energy_equipartition_two_level_many_replicas(gpulib):
                 assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (i, st)
     ratio = np.asarray(samples).mean() / expected
     assert abs(ratio - 1.0) < 0.02, ratio
+
+
+def test_mass_solver_equipartition(gpulib):
+    """The reference's mass-path check (tests/physics/sphere_63_120_mass/
+    averages.py:52-57, epsilon 0.01): mean kinetic energy kT 3N / 2 within 4 %
+    and mean strain energy kT (3N - 6) / 2 within 3 %, N corner nodes.  Here
+    64 replicas of one mesh in one batch (ConjugateGradientSolver with the
+    mass matrix, mixed precision), 2,000 steps of burn-in, then 12 samples
+    400 steps apart."""
+    from ffea_gb300.world import World
+    mesh = sphere_mesh(7.5, cell_nm=2.5, seed=3)
+    kT = P.kT_at(300.0) * P.MESO_ENERGY
+    specs = [make_blob(mesh, P.SimulationParams.from_si(dt=1e-14, kT=kT, epsilon=0.01, rng_seed=7000 + r,
+                                                        solver=P.SOLVER_MASS, precision=P.PRECISION_MIXED))
+             for r in range(64)]
+    n = mesh.num_linear
+    ke_th, se_th = specs[0].params.kT * 3 * n / 2, specs[0].params.kT * (3 * n - 6) / 2
+    se, ke = [], []
+    with World(specs) as w:
+        w.run(2000)
+        for _ in range(12):
+            w.run(400)
+            e = [w.blob(i).energies() for i in range(len(specs))]
+            se.append([x[0] for x in e])
+            ke.append([x[1] for x in e])
+            for i in range(len(specs)):
+                assert w.blob(i).status()["fail_bits"] == 0
+    ke_ratio, se_ratio = np.mean(ke) / ke_th, np.mean(se) / se_th
+    assert abs(ke_ratio - 1.0) < 0.04, ke_ratio
+    assert abs(se_ratio - 1.0) < 0.03, se_ratio
