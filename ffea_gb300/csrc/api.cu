@@ -406,24 +406,6 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
         }
     }
     d.coarse_nmax = d.coarse ? coarse_nmax : 0;
-    // memory-resident kernel in FP32: a ring of bulk-copy stages per warp for
-    // the NoMass row products, 4 slots deep where the shared memory allows,
-    // else off (FFEA_GPU_CG_TMA=0 turns it off, for comparisons)
-    if (!d.cg_reg && H.precision == PREC_MIXED) {
-        const char *tma_env = std::getenv("FFEA_GPU_CG_TMA");
-        const bool tma_on = !(tma_env && tma_env[0] == '0');
-        const size_t base = (size_t)d.cg_dyn_smem;  // deferred partials (+ coarse space)
-        const size_t off = (base + 127) & ~(size_t)127;
-        for (int R = kTmaMaxStages; tma_on && R == kTmaMaxStages; R /= 2) {
-            const size_t total = off + 32 * (size_t)R * (kTmaStageBytes + sizeof(unsigned long long));
-            if (cg_mem_smem_allow(H.precision, total) == 0 && cg_max_grid(H.precision, 0, total) >= d.cg_grid) {
-                d.cg_tma_stages = R;
-                d.cg_tma_off = (int32_t)off;
-                d.cg_dyn_smem = (int32_t)total;
-                break;
-            }
-        }
-    }
     d.part_stride = d.coarse ? 20 : 8;  // floats: DF dot terms 0..5; coarse P^T r 8..13, P^T w 14..19
     h->precond = d.coarse ? want : FFEA_GPU_PRECOND_JACOBI;
     d.num_blobs = H.num_blobs;

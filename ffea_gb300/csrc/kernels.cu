@@ -1725,167 +1725,6 @@ __device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const floa
     }
 }
 
-// ---------------------------------------------------------------- staged SpMV
-// The memory-resident kernel's row product for NoMass rows in FP32, by warp:
-// the 32 lanes of a warp own the 32 rows of one SELL slice, whose slot j is
-// one contiguous 1,152-byte block of values (9 planes of 32) and one
-// 128-byte block of column indices.  Lane 0 moves slot blocks into a ring of
-// shared-memory stages with bulk copies (cp.async.bulk, completion counted
-// on one mbarrier per stage) up to R slots ahead, so the values are in
-// flight long before they are used and hold no registers meanwhile; each
-// lane then reads its values and column from the stage and gathers its 16-byte
-// neighbour entries, two slots at a time.  The FMA order is sell_row_cg's, so
-// the product has the same bits.  Every wait is bounded: past the limit the
-// kernel's time-out flag is raised (the solve then stops with an error).
-constexpr unsigned int kTmaSpinLimit = 1u << 22;
-
-struct TmaRing {
-    unsigned char *buf;      // [warp][stage][kTmaStageBytes]
-    unsigned long long *bar; // [warp][stage]
-    int R;
-};
-
-__device__ __forceinline__ TmaRing tma_ring(const DeviceBatch &d)
-{
-    TmaRing r;
-    r.R = d.cg_tma_stages;
-    r.buf = cg_dyn + d.cg_tma_off;
-    r.bar = reinterpret_cast<unsigned long long *>(r.buf + 32 * (size_t)r.R * kTmaStageBytes);
-    return r;
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-// lane 0: stage slot j of slice `base` (values, then column indices)
-__device__ __forceinline__ void tma_issue_slot(const DeviceBatch &d, const TmaRing &rg, int warp, int st, int base,
-                                               int j)
-{
-    const uint32_t bar = smem_u32(rg.bar + warp * rg.R + st);
-    const uint32_t dst = smem_u32(rg.buf + ((size_t)warp * rg.R + st) * kTmaStageBytes);
-    const float *vals = static_cast<const float *>(d.sell_val) + (size_t)(base + 32 * j) * 9;
-    const int *cols = d.sell_col + base + 32 * j;
-    // the stage was last read through the generic proxy: order those reads
-    // before the bulk copy (async proxy) overwrites it
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
-                 :: "r"(bar), "r"(kTmaStageBytes) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 :: "r"(dst), "l"(vals), "r"(9 * 32 * 4), "r"(bar) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 :: "r"(dst + 9 * 32 * 4), "l"(cols), "r"(32 * 4), "r"(bar) : "memory");
-}
-
-// bounded wait for the given phase of a stage's mbarrier; false on time-out
-__device__ __forceinline__ bool tma_wait(const TmaRing &rg, int warp, int st, uint32_t parity)
-{
-    const uint32_t bar = smem_u32(rg.bar + warp * rg.R + st);
-    for (unsigned int spins = 0; spins < kTmaSpinLimit; spins++) {
-        uint32_t ok;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
-// every lane of every warp: initialise the ring's mbarriers (one arrival
-// each: lane 0's expect_tx), before any use
-__device__ __forceinline__ void tma_ring_init(const TmaRing &rg)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane < rg.R) {
-        const uint32_t bar = smem_u32(rg.bar + warp * rg.R + lane);
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    __syncthreads();
-}
-
-// q = A u of the lane's row (valid) for the warp's slice; all 32 lanes call
-// it together.  cnt counts the slots this warp has staged so far (uniform in
-// the warp): slot j uses stage (cnt + j) % R at phase ((cnt + j) / R) & 1.
-// Returns false (all lanes) if a wait timed out.
-__device__ __forceinline__ bool sell_row_tma(const DeviceBatch &d, int row, bool valid, float diag, const float4 *u4,
-                                             float out[3], const TmaRing &rg, unsigned int &cnt)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int sl = row >> 5;
-    const int L = __ldg(&d.slice_len[sl]), base = __ldg(&d.slice_ptr[sl]);
-    const int R = rg.R;  // 4: the current group's two stages and the next group's two
-    if (lane == 0)
-        for (int j = 0; j < min(R, L); j++) tma_issue_slot(d, rg, warp, (cnt + j) % R, base, j);
-    int issued = min(R, L), consumed = 0;  // slots staged / released (uniform in the warp)
-    __syncwarp();
-    const float4 me = ldcg4(&u4[row]);
-    float a0 = diag * me.x, a1 = diag * me.y, a2 = diag * me.z;
-    bool ok = true;
-    // wait for the stages of slots j, j + 1 and read this lane's columns
-    auto cols_of = [&](int j, int c[2]) {
-#pragma unroll
-        for (int g = 0; g < 2; g++) {
-            const int jj = j + g;
-            c[g] = row;
-            if (jj < L && ok) {
-                const int st = (cnt + jj) % R;
-                ok = tma_wait(rg, warp, st, ((cnt + jj) / R) & 1u);
-                if (ok && valid)
-                    c[g] = reinterpret_cast<const int *>(rg.buf + ((size_t)warp * R + st) * kTmaStageBytes +
-                                                         9 * 32 * 4)[lane];
-            }
-        }
-    };
-    int cc[2];
-    cols_of(0, cc);
-    ok = __all_sync(0xffffffffu, ok);
-    float4 y[2] = {ldcg4(&u4[cc[0]]), ldcg4(&u4[cc[1]])};
-    for (int j0 = 0; j0 < L && ok; j0 += 2) {
-        // the next group's columns and neighbour gathers go out first and
-        // are in flight during this group's FMAs
-        int cn[2];
-        cols_of(j0 + 2, cn);
-        ok = __all_sync(0xffffffffu, ok);
-        if (!ok) break;
-        const float4 yn[2] = {ldcg4(&u4[cn[0]]), ldcg4(&u4[cn[1]])};
-        float K[2][9];
-#pragma unroll
-        for (int g = 0; g < 2; g++) {
-            const int j = j0 + g;
-            const float *v = reinterpret_cast<const float *>(rg.buf + ((size_t)warp * R + (cnt + j) % R) *
-                                                                          kTmaStageBytes);
-#pragma unroll
-            for (int k = 0; k < 9; k++) K[g][k] = j < L ? v[32 * k + lane] : 0.f;
-        }
-        __syncwarp();
-        // refill the two stages just read with the slots R further on
-        if (lane == 0)
-#pragma unroll
-            for (int g = 0; g < 2; g++) {
-                const int j = j0 + g + R;
-                if (j < L) tma_issue_slot(d, rg, warp, (cnt + j) % R, base, j);
-            }
-        issued = min(L, j0 + 2 + R);
-        consumed = min(L, j0 + 4);
-        if (j0 < L) block_fma(K[0], y[0].x - me.x, y[0].y - me.y, y[0].z - me.z, a0, a1, a2);
-        if (j0 + 1 < L) block_fma(K[1], y[1].x - me.x, y[1].y - me.y, y[1].z - me.z, a0, a1, a2);
-        y[0] = yn[0];
-        y[1] = yn[1];
-    }
-    if (!ok) {
-        // a copy never completed: let the ones still in flight land (again
-        // bounded) before the solve stops
-        for (int j = consumed; j < issued; j++) tma_wait(rg, warp, (cnt + j) % R, ((cnt + j) / R) & 1u);
-    }
-    cnt += (unsigned int)L;
-    out[0] = a0;
-    out[1] = a1;
-    out[2] = a2;
-    return ok;
-}
-
 // L2 load issued where it stands (volatile asm keeps it ahead of the
 // barriers that follow, so its latency overlaps the reduction's own loads)
 __device__ __forceinline__ float ld_early(const float *p)
@@ -2139,13 +1978,6 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
         }
     };
-    // memory-resident kernel in FP32: NoMass row products staged by bulk
-    // copies (sell_row_tma); tma_cnt counts the warp's staged slots
-    constexpr bool kTma = !REG && sizeof(T) == 4;
-    unsigned int tma_cnt = 0;
-    if constexpr (kTma) {
-        if (d.cg_tma_stages > 0) tma_ring_init(tma_ring(d));
-    }
     int coarse_n = 0;  // coarse dofs of the CTA's blob (0: no coarse space)
     if (coarse) {
         const CoarseView cv = coarse_view<T>(d);
@@ -2305,30 +2137,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         RowState<T> loc;
         RowState<T> &S = REG ? reg : loc;
         if (!REG && valid) load_fields<T>(d, row, loc, RF_R | RF_U | (state == CG_VERIFY ? RF_DINV : 0));
-        // staged product: every lane of each warp whose slice lies in the
-        // segment takes part (rows past the segment or pinned compute and
-        // discard)
-        T au[3] = {(T)0, (T)0, (T)0};
-        bool staged = false;
-        if constexpr (kTma) {
-            if (d.cg_tma_stages > 0 && state != CG_VERIFY &&
-                d.bp[s_blob[s_tslot[j]]].solver == SOLVER_NOMASS) {  // CTA-uniform
-                staged = true;
-                if ((tid & ~31) < s_rows[j]) {  // warp-uniform
-                    const int wrow = s_row0[j] + tid;
-                    if (!sell_row_tma(d, wrow, valid, valid ? (float)diag : 0.f,
-                                      static_cast<const float4 *>(d.u4), reinterpret_cast<float *>(au), tma_ring(d),
-                                      tma_cnt) &&
-                        (tid & 31) == 0)
-                        atomicExch(&d.bar[4], 1u);  // the solve's time-out flag: every CTA stops
-                }
-            }
-        }
         if (valid) {
             if (state != CG_VERIFY) {
-                if (!staged)
-                    sell_row_cg<T, !REG>(d, row, nomass, diag, static_cast<const V4 *>(d.u4), au,
-                                         REG ? cg_cache_view<T>(d) : CgCache<T>{});
+                T au[3];
+                sell_row_cg<T, !REG>(d, row, nomass, diag, static_cast<const V4 *>(d.u4), au,
+                                     REG ? cg_cache_view<T>(d) : CgCache<T>{});
 #pragma unroll
                 for (int cc2 = 0; cc2 < 3; cc2++) {
                     S.w[cc2] = au[cc2];

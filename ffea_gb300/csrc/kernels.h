@@ -30,8 +30,6 @@ struct DeviceBatch {
     int32_t coarse = 0;           // 1: u = diag(omega) D^-1 r + P A_c^-1 P^T r
     int32_t coarse_nmax = 0;      // largest coarse dimension of a blob
     int32_t coarse_hmax = 0;      // memory-resident CG kernel: most coarse dofs of the blobs one CTA touches
-    int32_t cg_tma_stages = 0;    // memory-resident CG kernel (FP32): slots per warp staged by bulk copies (0: off)
-    int32_t cg_tma_off = 0;       // byte offset of that ring in the dynamic shared memory
     float4 *phi = nullptr;        // per padded row: rest offset from the segment centroid / R, smoother weight
     int32_t *seg_of_row = nullptr;
     int32_t *seg_nbr_ptr = nullptr, *seg_nbr = nullptr;   // segments coupled to each segment (itself included)
@@ -119,10 +117,6 @@ constexpr int CG_LOCAL_MAX_SEGS = 2048; // local reduction: partial sums every C
 constexpr int kDeferSegs = 16;  // segments per flush
 constexpr int kDeferQ = 9;      // values per warp and segment: 3 dot terms + up to 6 restrictions
 constexpr size_t kDeferBytes = sizeof(float) * kDeferSegs * kDeferQ * 32 + 16 * kDeferSegs;
-// memory-resident CG kernel (FP32): per warp a ring of slot stages, each the
-// 9 x 32 values and 32 column indices of one slot of the warp's slice
-constexpr int kTmaStageBytes = 9 * 32 * 4 + 32 * 4;
-constexpr int kTmaMaxStages = 4;
 
 // Launchers (all asynchronous on `s`).
 void launch_rest_state(const DeviceBatch &d, cudaStream_t s);

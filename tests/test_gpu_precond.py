@@ -209,28 +209,3 @@ def test_two_level_beyond_one_cta_per_segment(gpulib):
             assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (pc, st)
             iters[pc] = st["cg_iters"]
     assert iters[TWO_LEVEL] < 0.6 * iters[JACOBI], iters
-
-
-@pytest.mark.parametrize("pc", [JACOBI, TWO_LEVEL])
-def test_staged_row_products_are_exact(gpulib, monkeypatch, pc):
-    """The memory-resident kernel's NoMass row products staged through
-    shared memory by bulk copies (FFEA_GPU_CG_TMA, on by default) use the same
-    values in the same order as the direct loads: the iterates are
-    bit-identical with staging on and off, several segments per CTA."""
-    monkeypatch.setenv("FFEA_GPU_CG_MEMORY_STATE", "1")
-    monkeypatch.setenv("FFEA_GPU_CG_MAX_CTAS", "2")
-    specs = [spec(radius_nm=9.0, seed=1, precision=P.PRECISION_MIXED, epsilon=1e-6),
-             spec(radius_nm=5.0, seed=2, rng_seed=45, precision=P.PRECISION_MIXED, epsilon=1e-6)]
-    outs = []
-    for tma in ("0", "1"):
-        monkeypatch.setenv("FFEA_GPU_CG_TMA", tma)
-        with _world(specs, true_residual=True, preconditioner=pc) as w:
-            assert w.preconditioner() == pc
-            w.run(4)
-            outs.append([w.blob(i).get_nodes() for i in range(len(specs))])
-            for i in range(len(specs)):
-                st = w.blob(i).status()
-                assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (tma, i, st)
-    for i in range(len(specs)):
-        for a, c in zip(outs[0][i], outs[1][i]):
-            assert np.array_equal(a, c), i
