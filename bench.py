@@ -47,6 +47,9 @@ WORKLOADS = {
                      desc="98^3-cell Freudenthal grid cut to a 61.25 nm sphere (the ~500k-node single blob)"),
     "replicas256": dict(radius_nm=20.0, cell_nm=1.25, replicas=256,
                         desc="256 replicas of the 20 nm sphere in one batch, one RNG stream each"),
+    "heldout": dict(radius_nm=None, cell_nm=1.25, radii=(10.0, 20.0, 30.0, 40.0, 50.0),
+                    desc="the learned preconditioner's held-out family in one batch: spheres of radius "
+                         "10, 20, 30, 40 and 50 nm (the network was trained on radii 5-25 nm)"),
     "ensemble64": dict(radius_nm=None, cell_nm=1.25,
                        desc="64 independent blobs in one batch: radii log-uniform 5-40 nm at a 1.25 nm cell, "
                             "moduli x U[0.5, 2], one RNG stream each"),
@@ -89,6 +92,9 @@ def build_specs(workload: str, rank: int, precision: str):
     if w.get("replicas"):
         mesh = sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0)
         return [make_blob(mesh, prm(100000 * (rank + 1) + i)) for i in range(w["replicas"])]
+    if w.get("radii"):
+        return [make_blob(sphere_mesh(r, cell_nm=w["cell_nm"], seed=10 + i), prm(2000 * (rank + 1) + i))
+                for i, r in enumerate(w["radii"])]
     if w["radius_nm"] is not None:
         return [make_blob(sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0), prm(replica_seed(rank)))]
     rng = np.random.default_rng(2)

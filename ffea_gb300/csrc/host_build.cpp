@@ -618,7 +618,10 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
             bp.stream = (rng_mode == FFEA_GPU_RNG_SHARED) ? 0 : b;
             uint64_t base = (rng_mode == FFEA_GPU_RNG_SHARED) ? acc : 0;
             bp.elem_draw_base = (uint32_t)base;
-            uint64_t ed = (p.calc_noise == 1) ? 7ull * meshes[b].num_elements : 0;
+            // a blob with every node pinned skips its element loop and with
+            // it the element draws (src/Blob.cpp:643-645)
+            bp.all_pinned = meshes[b].num_pinned == meshes[b].num_nodes ? 1 : 0;
+            uint64_t ed = (p.calc_noise == 1 && !bp.all_pinned) ? 7ull * meshes[b].num_elements : 0;
             if (rng_mode == FFEA_GPU_RNG_SHARED) acc += ed;
             else per_stream_draws[b] = ed;
         }
@@ -647,7 +650,7 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
         int64_t runs = 0, nodes = 0;
         for (int b = 0; b < num_blobs; b++) {
             const ffea_gpu_params &p = params[b];
-            const int64_t ed = (p.calc_noise == 1) ? 7ll * meshes[b].num_elements : 0;
+            const int64_t ed = (p.calc_noise == 1 && !H.bp[b].all_pinned) ? 7ll * meshes[b].num_elements : 0;
             const int64_t nd = (p.calc_noise == 1 && p.calc_stokes == 1) ? 3ll * meshes[b].num_nodes : 0;
             H.noise_run_off[2 * b] = (int32_t)runs;
             runs += (ed + NOISE_RUN - 1) / NOISE_RUN;

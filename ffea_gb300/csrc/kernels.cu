@@ -315,6 +315,8 @@ __global__ void __launch_bounds__(ELEM_TILE) k_elements(DeviceBatch d, int mode)
     const int le = tile * ELEM_TILE - bp.elem_off + threadIdx.x;
     if (le >= bp.elem_cnt) return;
     if (mode == ELEM_STEP && d.status[b]) return;  // a failed blob stays at its failing step
+    // every node pinned: no element step and no element draws (src/Blob.cpp:643-645)
+    if (mode == ELEM_STEP && bp.all_pinned) return;
     const int e = bp.elem_off + le;
     const int4 c = reinterpret_cast<const int4 *>(d.conn)[e];
     T J[3][3];

@@ -51,6 +51,7 @@ struct BlobParams {
     int32_t num_nodes_total;                // N_t of the reference (linear + secondary)
     int32_t noise_node_off;                 // first node of the blob's node draws in the node-noise buffer
     int32_t true_residual;
+    int32_t all_pinned;                     // every node pinned: no element step, no element draws (src/Blob.cpp:643-645)
 };
 
 // material table entry (meso units, tetra_element_linear fields)

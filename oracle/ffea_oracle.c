@@ -603,6 +603,12 @@ static int orc_internal_forces(orc_blob *b)
 {
     int num_inversions = 0;
     const int E = b->num_elements;
+    /* a blob with every node pinned takes no element step, so it draws no
+     * element noise (src/Blob.cpp:643-645) */
+    if (b->num_pinned == b->num_nodes) {
+        b->last_inversions = 0;
+        return ORC_OK;
+    }
 #pragma omp parallel num_threads(b->num_threads) reduction(+ : num_inversions)
     {
         int tid = 0;

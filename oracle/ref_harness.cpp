@@ -52,6 +52,10 @@ int ref_internal_forces(RefBlob *b)
     matrix3 J, stress;
     vector12 du;
     int num_inversions = 0;
+    if (b->num_pinned == b->num_nodes) {  // src/Blob.cpp:643-645
+        b->last_inversions = 0;
+        return FFEA_OK;
+    }
     for (int n = 0; n < b->num_elements; n++) {
         b->elem[n].calculate_jacobian(J);
         if (b->elem[n].calc_shape_function_derivatives_and_volume(J) == FFEA_ERROR) num_inversions++;

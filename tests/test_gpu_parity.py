@@ -275,3 +275,28 @@ def test_node_io_pinned_and_device_buffers_agree(gpulib):
         assert np.array_equal(b.get_nodes()[0][corner], ref[0][corner])
         w.run(2)
         assert b.status()["fail_bits"] == 0
+
+
+@pytest.mark.parametrize("solver", [P.SOLVER_NOMASS, P.SOLVER_MASS])
+def test_all_pinned_blob(gpulib, oracle, solver):
+    """Every node pinned: no element step and no element draws, as in the
+    reference (src/Blob.cpp:643-645); the RNG stream advances by the node
+    draws alone, bit for bit with the oracle.  Nothing moves.  (FFEA's
+    NoMassCGSolver turns the all-zero rhs into NaN positions, 0 / 0 before
+    its stopping test; the GPU solve stops on the zero rhs, as FFEA's own
+    residual2 treats sum f^2 = 0 as converged, and returns x = 0.)"""
+    from ffea_gb300.world import World
+    s0 = spec(radius_nm=3.0)
+    s = spec(radius_nm=3.0, solver=solver, pinned=list(range(s0.mesh.num_nodes)))
+    ref = oracle.blob_from_spec(s)
+    with World([s]) as w:
+        pos0, _, _ = w.blob(0).get_nodes()
+        w.run(5)
+        assert ref.step(5) == 0
+        b = w.blob(0)
+        assert np.array_equal(b.rng_state(), ref.rng_state())
+        pos, vel, _ = b.get_nodes()
+        assert np.array_equal(pos, pos0) and not vel.any()
+        if solver == P.SOLVER_MASS:
+            assert np.array_equal(pos, ref.nodes()[0])
+        assert b.status()["fail_bits"] == 0

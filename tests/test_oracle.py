@@ -112,3 +112,34 @@ def test_oracle_matches_reference_objects_sphere_63_120(oracle, solver):
         for x, y in zip(blobs[0].nodes(), blobs[1].nodes()):
             assert np.array_equal(x, y)
         assert np.array_equal(blobs[0].rng_state(), blobs[1].rng_state())
+
+
+def test_all_pinned_blob_draws_node_noise_only(oracle):
+    """A blob with every node pinned skips its element loop
+    (src/Blob.cpp:643-645), so a step draws only the 3 N_t node values of
+    aggregate_forces_and_solve.  With the mass solver nothing moves; FFEA's
+    NoMassCGSolver divides 0 by 0 on the all-zero rhs (alpha before its
+    stopping test, src/NoMassCGSolver.cpp:165-197), so its positions become
+    NaN -- the oracle restates that too.  The reference objects agree where
+    they are built."""
+    from tests.helpers import spec
+    s0 = spec(radius_nm=3.0)
+    for solver in (0, 1):
+        s = spec(radius_nm=3.0, solver=solver, pinned=list(range(s0.mesh.num_nodes)))
+        b = oracle.blob_from_spec(s)
+        st0 = b.rng_state()
+        assert b.step(3) == 0
+        assert np.array_equal(b.rng_state(), oracle.rng_jump(st0, 3 * 3 * s.mesh.num_nodes))
+        pos, vel, _ = b.nodes()
+        if solver == 1:
+            corner = np.zeros(len(pos), bool)
+            corner[s.mesh.topology[:, :4]] = True
+            assert np.array_equal(pos[corner], s.mesh.pos[corner]) and not vel.any()
+        else:
+            assert np.isnan(pos).all()
+        if oracle.ref_available():
+            r = oracle.blob_from_spec(s, impl="ref")
+            assert r.step(3) == 0
+            assert np.array_equal(r.rng_state(), b.rng_state())
+            for x, y in zip(r.nodes(), b.nodes()):
+                assert np.array_equal(x, y, equal_nan=True)
