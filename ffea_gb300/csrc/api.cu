@@ -304,6 +304,45 @@ int ffea_gpu_ffea_seed(int32_t rng_seed, uint64_t out[6])
     return FFEA_GPU_OK;
 }
 
+namespace {
+// The memory-resident solve of a batch of several blobs: every blob's
+// segments dealt over the G CTAs, largest blob first, one segment per CTA in
+// turn (CTA c keeps the count n_segs (c + 1) / G - n_segs c / G), then each
+// CTA's segments sorted, which groups them by blob.  So each CTA holds a
+// share of every large blob, and when the small blobs have converged every
+// CTA still has rows to iterate instead of most of them waiting at the grid
+// barriers.  Empty (the plain order) for one blob or one segment per CTA.
+std::vector<int32_t> deal_segments(const HostBatch &H, int G)
+{
+    const int32_t n_segs = (int32_t)H.seg_row0.size();
+    std::vector<int32_t> order;
+    if (H.num_blobs <= 1 || n_segs <= G) return order;
+    std::vector<int32_t> blobs(H.num_blobs);
+    for (int b = 0; b < H.num_blobs; b++) blobs[b] = b;
+    std::stable_sort(blobs.begin(), blobs.end(),
+                     [&](int a, int b) { return H.bp[a].node_cnt > H.bp[b].node_cnt; });
+    std::vector<int32_t> cap(G), start(G);
+    for (int c = 0; c < G; c++) {
+        start[c] = (int32_t)(((int64_t)n_segs * c) / G);
+        cap[c] = (int32_t)(((int64_t)n_segs * (c + 1)) / G) - start[c];
+    }
+    std::vector<std::vector<int32_t>> per(G);
+    int c = 0;
+    for (int b : blobs)
+        for (int32_t s = H.bp[b].seg_off; s < H.bp[b].seg_off + H.bp[b].seg_cnt; s++) {
+            while ((int32_t)per[c].size() >= cap[c]) c = (c + 1) % G;
+            per[c].push_back(s);
+            c = (c + 1) % G;
+        }
+    order.resize(n_segs);
+    for (int k = 0; k < G; k++) {
+        std::sort(per[k].begin(), per[k].end());
+        std::copy(per[k].begin(), per[k].end(), order.begin() + start[k]);
+    }
+    return order;
+}
+}  // namespace
+
 int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_params *params,
                           int32_t rng_mode, ffea_gpu_t **out)
 {
@@ -383,15 +422,18 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
         // the memory-resident kernel with the coarse space: its shared memory
         // holds g of one blob and P^T s of every blob a CTA touches
         const int G = std::min(mem_cap, n_segs);
+        const std::vector<int32_t> order = deal_segments(H, G);
         int hmax = 0;
         for (int c = 0; c < G; c++) {
             const int S0 = (int)(((int64_t)n_segs * c) / G), S1 = (int)(((int64_t)n_segs * (c + 1)) / G);
             int sum = 0, last = -1;
-            for (int sg = S0; sg < S1; sg++)
+            for (int k = S0; k < S1; k++) {
+                const int sg = order.empty() ? k : order[k];
                 if (H.seg_blob[sg] != last) {
                     last = H.seg_blob[sg];
                     sum += H.bp[last].coarse_n;
                 }
+            }
             hmax = std::max(hmax, sum);
         }
         const size_t mem_bytes = cg_mem_defer_bytes(H.precision) + cg_mem_coarse_bytes(coarse_nmax, hmax);
@@ -427,6 +469,10 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(upload(A, d.seg_row0, H.seg_row0));
     CK(upload(A, d.seg_rows, H.seg_rows));
     CK(upload(A, d.seg_blob, H.seg_blob));
+    if (!d.cg_reg) {
+        const std::vector<int32_t> order = deal_segments(H, d.cg_grid);
+        if (!order.empty()) CK(upload(A, d.seg_order, order));
+    }
     CK(upload(A, d.etile_blob, H.etile_blob));
     std::vector<mrg::JumpMat> table(mrg::JUMP_TABLE_ENTRIES);
     mrg::build_jump_table(table.data());

@@ -1660,7 +1660,8 @@ __device__ __forceinline__ void coarse_u_of(const float4 f, const float *c, cons
 // lane, a transposed butterfly per warp), then one thread per (segment, row)
 // adds the wps warp sums in order: fixed order, so deterministic.
 template <typename T>
-__device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const float *part, int S0, int nt, int nb,
+__device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const float *part, const int *s_sid, int nt,
+                                                int nb,
                                                 const int *s_blob, const int *s_tslot, const int *s_state,
                                                 const T *s_alpha, const T *s_beta, bool prologue)
 {
@@ -1700,7 +1701,7 @@ __device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const floa
 #pragma unroll
                 for (int l = 0; l < 8; l++) v[l] = 0.f;
                 if (jl < m) {
-                    const float *Xr = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (S0 + j0 + jl - bp.seg_off)) * n;
+                    const float *Xr = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (s_sid[j0 + jl] - bp.seg_off)) * n;
 #pragma unroll 4
                     for (int i = sub * 32 + lane; i < n; i += wps * 32) {
                         const float gi = cv.g[i];
@@ -1843,6 +1844,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
     __shared__ unsigned int s_pub;
     __shared__ int s_tslot[CG_MAX_SEGS], s_row0[CG_MAX_SEGS], s_rows[CG_MAX_SEGS];
     __shared__ int s_blob[CG_MAX_SEGS], s_state[CG_MAX_SEGS];
+    __shared__ int s_sid[CG_MAX_SEGS];  // global index of the CTA's segment j
     __shared__ T s_alpha[CG_MAX_SEGS], s_beta[CG_MAX_SEGS];
     __shared__ CgScalars s_cg[CG_LOCAL_MAX_BLOBS];
     __shared__ unsigned int s_run;
@@ -1854,11 +1856,16 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         s_err = 0;
         int nb = 0;
         for (int j = 0; j < S1 - S0; j++) {
-            const int b = d.seg_blob[S0 + j];
+            // the CTA's segments: a range of the blob-ordered segments, or
+            // its part of a list that deals every blob's segments over the
+            // CTAs (memory-resident batches), sorted by segment
+            const int sid = d.seg_order ? d.seg_order[S0 + j] : S0 + j;
+            s_sid[j] = sid;
+            const int b = d.seg_blob[sid];
             if (nb == 0 || s_blob[nb - 1] != b) s_blob[nb++] = b;
             s_tslot[j] = nb - 1;
-            s_row0[j] = d.seg_row0[S0 + j];
-            s_rows[j] = d.seg_rows[S0 + j];
+            s_row0[j] = d.seg_row0[sid];
+            s_rows[j] = d.seg_rows[sid];
         }
         s_nt = S1 - S0;
         s_nb = nb;
@@ -1987,7 +1994,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         coarse_n = bp.coarse_n;
         cv.h[tid] = 0.f;
         cv.phi[tid] = reg_valid ? d.phi[s_row0[0] + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float *Xg = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (S0 - bp.seg_off)) * bp.coarse_n;
+        const float *Xg = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (s_sid[0] - bp.seg_off)) * bp.coarse_n;
         for (int k = tid; k < 6 * bp.coarse_n; k += CG_THREADS) cv.xrow[k] = Xg[k];
     }
     // u = omega D^-1 r + Phi_p c of the thread's row (REG, coarse)
@@ -2103,9 +2110,9 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             if (mcoarse) {
                 float ex[6] = {0, 0, 0, 0, 0, 0};
                 if (valid) restrict6_of<T>(fm, S.r, ex);
-                seg_partials_defer<6>(defer_view(), dcnt, S0 + j, 5, 8, inf, ex);
+                seg_partials_defer<6>(defer_view(), dcnt, s_sid[j], 5, 8, inf, ex);
             } else {
-                seg_partials_defer<0>(defer_view(), dcnt, S0 + j, 5, 0, inf, nullptr);
+                seg_partials_defer<0>(defer_view(), dcnt, s_sid[j], 5, 0, inf, nullptr);
             }
             if (++dcnt == kDeferSegs) defer_flush();
             return;
@@ -2115,13 +2122,13 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             // restriction of the new r: slot floats 8..
             float ex[6] = {0, 0, 0, 0, 0, 0};
             if (valid) restrict6(S.r, ex);
-            seg_partials<W, 6>(slot(S0 + j), in, 5, ex, 8, red);
+            seg_partials<W, 6>(slot(s_sid[j]), in, 5, ex, 8, red);
         } else if (mcoarse) {
             float ex[6] = {0, 0, 0, 0, 0, 0};
             if (valid) restrict6_of<T>(fm, S.r, ex);
-            seg_partials<W, 6>(slot(S0 + j), in, 5, ex, 8, red);
+            seg_partials<W, 6>(slot(s_sid[j]), in, 5, ex, 8, red);
         } else {
-            seg_partials<W, 0>(slot(S0 + j), in, 5, nullptr, 0, red);
+            seg_partials<W, 0>(slot(s_sid[j]), in, 5, nullptr, 0, red);
         }
     };
     // phase B of segment j: ACTIVE / RESTART and the prologue: w = A u, slot 1
@@ -2171,9 +2178,9 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                 if (mcoarse) {
                     float ex[6] = {0, 0, 0, 0, 0, 0};
                     if (valid) restrict6_of<T>(d.phi[row], S.w, ex);
-                    seg_partials_defer<6>(defer_view(), dcnt, S0 + j, 2, 14, inf, ex);
+                    seg_partials_defer<6>(defer_view(), dcnt, s_sid[j], 2, 14, inf, ex);
                 } else {
-                    seg_partials_defer<0>(defer_view(), dcnt, S0 + j, 2, 0, inf, nullptr);
+                    seg_partials_defer<0>(defer_view(), dcnt, s_sid[j], 2, 0, inf, nullptr);
                 }
                 if (++dcnt == kDeferSegs) defer_flush();
                 return;
@@ -2193,13 +2200,13 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
             if (state == CG_VERIFY) {
                 const double in[3] = {vg, 0.0, vr};
-                seg_partials<double, 12>(slot(S0 + j), in, 5, ex, 8, red);
+                seg_partials<double, 12>(slot(s_sid[j]), in, 5, ex, 8, red);
             } else if (full) {
                 const W in[3] = {pg, pd, pr};
-                seg_partials<W, 12>(slot(S0 + j), in, 7, ex, 8, red);
+                seg_partials<W, 12>(slot(s_sid[j]), in, 7, ex, 8, red);
             } else {
                 const W in[3] = {pg, pd, pr};
-                seg_partials<W, 6>(slot(S0 + j), in, 2, ex + 6, 14, red);
+                seg_partials<W, 6>(slot(s_sid[j]), in, 2, ex + 6, 14, red);
             }
         } else if (coarse) {
             // restrictions: ACTIVE P^T w (slot floats 14..); the prologue,
@@ -2215,20 +2222,20 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
             if (state == CG_VERIFY) {
                 const double in[3] = {vg, 0.0, vr};
-                seg_partials<double, 12>(slot(S0 + j), in, 5, ex, 8, red);
+                seg_partials<double, 12>(slot(s_sid[j]), in, 5, ex, 8, red);
             } else if (full) {
                 const W in[3] = {pg, pd, pr};
-                seg_partials<W, 12>(slot(S0 + j), in, 7, ex, 8, red);
+                seg_partials<W, 12>(slot(s_sid[j]), in, 7, ex, 8, red);
             } else {
                 const W in[3] = {pg, pd, pr};
-                seg_partials<W, 6>(slot(S0 + j), in, 2, ex + 6, 14, red);
+                seg_partials<W, 6>(slot(s_sid[j]), in, 2, ex + 6, 14, red);
             }
         } else if (state == CG_VERIFY) {
             const double in[3] = {vg, 0.0, vr};
-            seg_partials<double, 0>(slot(S0 + j), in, 5, nullptr, 0, red);
+            seg_partials<double, 0>(slot(s_sid[j]), in, 5, nullptr, 0, red);
         } else {
             const W in[3] = {pg, pd, pr};
-            seg_partials<W, 0>(slot(S0 + j), in, (prologue || state == CG_RESTART) ? 7 : 2, nullptr, 0, red);
+            seg_partials<W, 0>(slot(s_sid[j]), in, (prologue || state == CG_RESTART) ? 7 : 2, nullptr, 0, red);
         }
     };
 
@@ -2249,7 +2256,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             float ex[6] = {0, 0, 0, 0, 0, 0};
             if (reg_valid) restrict6(reg.r, ex);
             const W none[3] = {(W)0, (W)0, (W)0};
-            seg_partials<W, 6>(slot(S0), none, 0, ex, 8, red);
+            seg_partials<W, 6>(slot(s_sid[0]), none, 0, ex, 8, red);
         }
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (!s_err) {
@@ -2275,11 +2282,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                 restrict6_of<T>(d.phi[row], loc.r, ex);
             }
             const W none[3] = {(W)0, (W)0, (W)0};
-            seg_partials<W, 6>(slot(S0 + j), none, 0, ex, 8, red);
+            seg_partials<W, 6>(slot(s_sid[j]), none, 0, ex, 8, red);
         }
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (!s_err) {
-            coarse_mem_step<T>(d, reinterpret_cast<const float *>(part()), S0, nt, nb, s_blob, s_tslot, s_state,
+            coarse_mem_step<T>(d, reinterpret_cast<const float *>(part()), s_sid, nt, nb, s_blob, s_tslot, s_state,
                                s_alpha, s_beta, true);
             for (int j = 0; j < nt; j++) {
                 int row;
@@ -2321,7 +2328,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         // memory-resident coarse space: the corrections for this update, from
         // the partials just reduced (before the buffers swap)
         if (mcoarse)
-            coarse_mem_step<T>(d, reinterpret_cast<const float *>(part()), S0, nt, nb, s_blob, s_tslot, s_state,
+            coarse_mem_step<T>(d, reinterpret_cast<const float *>(part()), s_sid, nt, nb, s_blob, s_tslot, s_state,
                                s_alpha, s_beta, false);
         if (local || mcoarse) parity ^= 1;
         if (REG && s_state[0] == CG_VERIFY) publish_x();

@@ -42,6 +42,8 @@ struct DeviceBatch {
     void *mat_t = nullptr;        // the material table in T (MAT_T_STRIDE per material)
     int32_t *tile_blob = nullptr, *etile_blob = nullptr;
     int32_t *seg_row0 = nullptr, *seg_rows = nullptr, *seg_blob = nullptr;   // CG segments
+    int32_t *seg_order = nullptr;  // memory-resident solve of several blobs: CTA c's segments are
+                                   // seg_order[n_segs c / G .. n_segs (c + 1) / G) (NULL: in order)
     // RNG
     mrg::JumpMat *jump_table = nullptr;
     uint32_t *stream_state = nullptr;
