@@ -17,7 +17,13 @@ element forces and SpMV with double-float / FP64 reductions.
 Synthetic, seeded inputs stand in for a real protein mesh.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--precond learned|two-level|jacobi] [--no-plain]
+                  [--workload sphere40|sphere61|replicas256|ensemble64|heldout|...]
+                  [--precond learned|two-level|jacobi] [--no-plain] [--autotune]
+
+Other workloads: sphere61 (98^3-cell sphere, ~515k nodes), replicas256 (256
+replicas of the 20 nm sphere), ensemble64 (64 uneven blobs), heldout (the
+learned preconditioner's held-out family, 10-50 nm).  Each line carries the
+roofline of k_cg and of every step kernel (kernel_roofline).
 
 N > 1 runs under torchrun, one replica blob per GPU with its own RNG stream
 (the path does not shard a single blob: replicas only, weak scaling).
@@ -103,10 +109,6 @@ def build_specs(workload: str, rank: int, precision: str):
     return [make_blob(sphere_mesh(float(r), cell_nm=w["cell_nm"], seed=i),
                       prm(1000 * (rank + 1) + i), shear_mod=3.7e8 * g, bulk_mod=1.1e9 * g)
             for i, (r, g) in enumerate(zip(radii, scale))]
-
-
-def build_spec(workload: str, rank: int, precision: str):
-    return build_specs(workload, rank, precision)[0]
 
 
 def config_of(args, specs, world_size):
