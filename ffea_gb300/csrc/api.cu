@@ -436,7 +436,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
             }
             hmax = std::max(hmax, sum);
         }
-        const size_t mem_bytes = cg_mem_defer_bytes(H.precision) + cg_mem_coarse_bytes(coarse_nmax, hmax);
+        const size_t mem_bytes = cg_mem_defer_bytes(H.precision) + cg_mem_coarse_bytes(hmax);
         if ((int64_t)G * CG_MAX_SEGS >= n_segs && cg_mem_smem_allow(H.precision, mem_bytes) == 0 &&
             cg_max_grid(H.precision, 0, mem_bytes) >= G) {
             d.coarse = 1;

@@ -1603,14 +1603,15 @@ __device__ __forceinline__ void coarse_apply(const DeviceBatch &d, int n, float 
 
 // Coarse space of the memory-resident CG kernel (several segments per CTA,
 // any number of coarse dofs per blob).  Dynamic shared memory, after the
-// deferred-partials region: c of each of
-// the CTA's segments (8 floats), 32 x 8 reduction floats, g of the blob being
-// corrected (coarse_nmax floats), and (P^T s)_j for every coarse dof of every
-// blob the CTA touches (coarse_hmax floats, blob after blob).  Every CTA that
+// deferred-partials region: c of each of the CTA's segments (8 floats),
+// 32 x 8 reduction floats, the first coarse dof of each of the CTA's blobs in
+// the next two arrays, then g and (P^T s)_j for every coarse dof of every
+// blob the CTA touches (coarse_hmax floats each, blob after blob).  Every CTA that
 // touches a blob carries its own copy of that blob's P^T s; all copies follow
 // the same arithmetic on the same partial sums, so they hold the same bits.
 struct CoarseMemView {
     float *cvec, *red, *g, *h;
+    int *hoff;  // per blob k of the CTA: its first coarse dof in g and h
 };
 
 __device__ __forceinline__ CoarseMemView coarse_mem_view(const DeviceBatch &d)
@@ -1618,8 +1619,9 @@ __device__ __forceinline__ CoarseMemView coarse_mem_view(const DeviceBatch &d)
     CoarseMemView v;
     v.cvec = reinterpret_cast<float *>(cg_dyn + kDeferBytes);
     v.red = v.cvec + 8 * CG_MAX_SEGS;
-    v.g = v.red + 8 * 32;
-    v.h = v.g + d.coarse_nmax;
+    v.hoff = reinterpret_cast<int *>(v.red + 8 * 32);
+    v.g = reinterpret_cast<float *>(v.hoff + CG_MAX_SEGS);
+    v.h = v.g + d.coarse_hmax;
     return v;
 }
 
@@ -1649,82 +1651,86 @@ __device__ __forceinline__ void coarse_u_of(const float4 f, const float *c, cons
 
 // The coarse corrections of the CTA's segments for the next update
 // (memory-resident kernel), after the iteration's partial sums and the CG
-// transitions: per blob k of the CTA (state ACTIVE or RESTART, or every blob
-// in the prologue), from the restrictions in the partial slots (P^T r at
-// float 8, P^T w at float 14),
+// transitions.  First, for every blob k of the CTA (state ACTIVE or RESTART,
+// or every blob in the prologue), from the restrictions in the partial slots
+// (P^T r at float 8, P^T w at float 14), each blob in its own region:
 //   restart / prologue: h = 0, g = P^T r
 //   else:               h = P^T w + beta h, g = P^T r - alpha h  (= P^T r_(k+1))
-// then c_j = X_j g for each of the CTA's segments j of the blob, X_j the
-// segment's six rows of X ~ A_c^-1 (global memory, read once per iteration).
-// wps warps share a segment (lane-strided over the n coarse dofs, 6 sums per
-// lane, a transposed butterfly per warp), then one thread per (segment, row)
-// adds the wps warp sums in order: fixed order, so deterministic.
+// then, after one barrier, c_j = X_j g for every segment j of those blobs,
+// X_j the segment's six rows of X ~ A_c^-1 (global memory, read once per
+// iteration).  wps warps share a segment (lane-strided over its blob's coarse
+// dofs, 6 sums per lane, a transposed butterfly per warp), then one thread per
+// (segment, row) adds the wps warp sums in order: fixed order, so
+// deterministic.  A CTA that holds segments of many blobs (a dealt batch)
+// pays two barriers per round of 32 / wps segments, not per blob.
 template <typename T>
 __device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const float *part, const int *s_sid, int nt,
-                                                int nb,
-                                                const int *s_blob, const int *s_tslot, const int *s_state,
+                                                int nb, const int *s_blob, const int *s_tslot, const int *s_state,
                                                 const T *s_alpha, const T *s_beta, bool prologue)
 {
     const CoarseMemView cv = coarse_mem_view(d);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    int j0 = 0, hoff = 0;
+    int hoff = 0;
     for (int k = 0; k < nb; k++) {
-        int j1 = j0;
-        while (j1 < nt && s_tslot[j1] == k) j1++;
         const BlobParams &bp = d.bp[s_blob[k]];
         const int n = bp.coarse_n, st = s_state[k];
-        float *h = cv.h + hoff;
-        hoff += n;
+        if (tid == 0) cv.hoff[k] = hoff;
         if (n > 0 && (prologue || st == CG_ACTIVE || st == CG_RESTART)) {  // CTA-uniform
             const bool restart = prologue || st == CG_RESTART;
             const float a = (float)s_alpha[k], be = (float)s_beta[k];
+            float *h = cv.h + hoff, *g = cv.g + hoff;
             for (int i = tid; i < n; i += blockDim.x) {
                 const float *sl = part + (size_t)d.part_stride * (bp.seg_off + i / 6);
                 const float pr = __ldcg(sl + 8 + i % 6);
                 if (restart) {
                     h[i] = 0.f;
-                    cv.g[i] = pr;
+                    g[i] = pr;
                 } else {
                     const float hn = __ldcg(sl + 14 + i % 6) + be * h[i];
                     h[i] = hn;
-                    cv.g[i] = pr - a * hn;
+                    g[i] = pr - a * hn;
                 }
-            }
-            __syncthreads();
-            const int m = j1 - j0;
-            int wps = 1;
-            while (wps * 2 * m <= 32) wps *= 2;
-            const int per_round = 32 / wps;
-            for (int q0 = 0; q0 < m; q0 += per_round) {
-                const int jl = q0 + warp / wps, sub = warp % wps;
-                float v[8];
-#pragma unroll
-                for (int l = 0; l < 8; l++) v[l] = 0.f;
-                if (jl < m) {
-                    const float *Xr = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (s_sid[j0 + jl] - bp.seg_off)) * n;
-#pragma unroll 4
-                    for (int i = sub * 32 + lane; i < n; i += wps * 32) {
-                        const float gi = cv.g[i];
-#pragma unroll
-                        for (int l = 0; l < 6; l++) v[l] = fmaf(__ldcg(Xr + (size_t)l * n + i), gi, v[l]);
-                    }
-                }
-                int idx;
-                const float t = warp_sum_multi<8>(v, idx);
-                if ((lane & 3) == 0) cv.red[warp * 8 + idx] = t;
-                __syncthreads();
-                if (tid < 6 * per_round) {
-                    const int jj = tid / 6, l = tid % 6;
-                    if (q0 + jj < m) {
-                        float s = 0.f;
-                        for (int w = 0; w < wps; w++) s += cv.red[(jj * wps + w) * 8 + l];
-                        cv.cvec[8 * (j0 + q0 + jj) + l] = s;
-                    }
-                }
-                __syncthreads();
             }
         }
-        j0 = j1;
+        hoff += n;
+    }
+    __syncthreads();
+    int wps = 1;
+    while (wps * 2 * nt <= 32) wps *= 2;
+    const int per_round = 32 / wps;
+    for (int q0 = 0; q0 < nt; q0 += per_round) {
+        const int j = q0 + warp / wps, sub = warp % wps;
+        float v[8];
+#pragma unroll
+        for (int l = 0; l < 8; l++) v[l] = 0.f;
+        if (j < nt) {
+            const int k = s_tslot[j], st = s_state[k];
+            const BlobParams &bp = d.bp[s_blob[k]];
+            const int n = bp.coarse_n;
+            if (n > 0 && (prologue || st == CG_ACTIVE || st == CG_RESTART)) {  // warp-uniform
+                const float *g = cv.g + cv.hoff[k];
+                const float *Xr = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (s_sid[j] - bp.seg_off)) * n;
+#pragma unroll 4
+                for (int i = sub * 32 + lane; i < n; i += wps * 32) {
+                    const float gi = g[i];
+#pragma unroll
+                    for (int l = 0; l < 6; l++) v[l] = fmaf(__ldcg(Xr + (size_t)l * n + i), gi, v[l]);
+                }
+            }
+        }
+        int idx;
+        const float t = warp_sum_multi<8>(v, idx);
+        if ((lane & 3) == 0) cv.red[warp * 8 + idx] = t;
+        __syncthreads();
+        if (tid < 6 * per_round) {
+            const int jj = tid / 6, l = tid % 6;
+            if (q0 + jj < nt) {
+                float sum = 0.f;
+                for (int w = 0; w < wps; w++) sum += cv.red[(jj * wps + w) * 8 + l];
+                cv.cvec[8 * (q0 + jj) + l] = sum;
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -2632,9 +2638,10 @@ int cg_smem_plan(int precision, int max_slots, int max_cols, size_t extra_bytes,
 // maximum, as for the register-resident kernel).
 size_t cg_mem_defer_bytes(int precision) { return precision == PREC_FP64 ? 0 : kDeferBytes; }
 
-size_t cg_mem_coarse_bytes(int coarse_nmax, int coarse_hmax)
+size_t cg_mem_coarse_bytes(int coarse_hmax)
 {
-    return sizeof(float) * (8 * (size_t)CG_MAX_SEGS + 8 * 32 + (size_t)coarse_nmax + (size_t)coarse_hmax);
+    // c per segment, reduction floats, blob offsets, then g and P^T s of the CTA's blobs
+    return sizeof(float) * (8 * (size_t)CG_MAX_SEGS + 8 * 32 + (size_t)CG_MAX_SEGS + 2 * (size_t)coarse_hmax);
 }
 
 int cg_mem_smem_allow(int precision, size_t dyn_bytes)

@@ -184,7 +184,7 @@ int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, ::c
 // device, 0 on error
 int cg_max_grid(int precision, int reg, size_t dyn_bytes);
 size_t cg_mem_defer_bytes(int precision);
-size_t cg_mem_coarse_bytes(int coarse_nmax, int coarse_hmax);
+size_t cg_mem_coarse_bytes(int coarse_hmax);
 int cg_mem_smem_allow(int precision, size_t dyn_bytes);
 
 int64_t kernel_launch_count();
