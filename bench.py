@@ -374,10 +374,16 @@ def measure_arm(args, specs, precond: str, world: int, local: int):
     value = aggregate_throughput(N, K, world, total_ms / 1e3)
 
     # end to end through the C ABI with the caller's pinned host buffers (all
-    # N_t nodes in the reference's order): set_nodes (positions and
-    # velocities, H2D) + step + get_nodes (positions, velocities, forces, D2H)
+    # N_t nodes in the reference's order), per step: set_nodes of the step's
+    # inputs (H2D), the step, get_nodes of positions, velocities and forces
+    # (D2H).  The inputs are the positions, plus the velocities for the mass
+    # solvers: a CG_nomass step does not read velocities (FFEA's NoMass
+    # forces never use node.vel, src/Blob.cpp:3853-3905, and euler_integrate
+    # overwrites it with the solution, :3937-3969).
+    from ffea_gb300 import params as Pm
     blobs = [w.blob(i) for i in range(len(specs))]
     Nt = sum(s_.mesh.num_nodes for s_ in specs)
+    reads_vel = [s_.params.solver != Pm.SOLVER_NOMASS for s_ in specs]
     # pinned (page-locked) host arrays, as a caller that streams state would hold
     bufs = [tuple(torch.empty((s_.mesh.num_nodes, 3), dtype=torch.float64, pin_memory=True).numpy()
                   for _ in range(3)) for s_ in specs]
@@ -388,14 +394,16 @@ def measure_arm(args, specs, precond: str, world: int, local: int):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(Ke):
-        for b_, buf in zip(blobs, bufs):
-            b_.set_nodes(buf[0], buf[1])
+        for b_, buf, rv in zip(blobs, bufs, reads_vel):
+            b_.set_nodes(buf[0], buf[1] if rv else None)
         w.run(1)
         for b_, buf in zip(blobs, bufs):
             b_.get_nodes(out=buf)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    h2d = sum((2 if rv else 1) * 3 * 8 * s_.mesh.num_nodes for s_, rv in zip(specs, reads_vel))
     e2e = {"value": aggregate_throughput(N, Ke, world, e2e_s), "unit": "node-steps/s",
-           "h2d_bytes_per_step": 2 * 3 * 8 * Nt, "d2h_bytes_per_step": 3 * 3 * 8 * Nt, "steps": Ke}
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 3 * 3 * 8 * Nt, "steps": Ke,
+           "copies": "H2D: positions (+ velocities for mass solvers); D2H: positions, velocities, forces"}
 
     # profile pass: direct launches with CUDA events around each phase of a step
     prof_steps = 3
