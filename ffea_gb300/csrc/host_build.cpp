@@ -83,7 +83,12 @@ std::vector<int32_t> plan_parts(const std::vector<int32_t> &counts, int32_t ctas
         while (total < target && !q.empty()) {
             const int b = -q.top().second;
             q.pop();
-            if (k[b] >= slices[b]) continue;  // one slice per segment already
+            // at least two slices per segment once a blob is split, so the
+            // last segment keeps more than 32 real rows: a segment is also an
+            // aggregate of the two-level preconditioner, whose six rigid
+            // modes are independent only on a few non-collinear nodes (2
+            // rows would make the coarse matrix singular)
+            if (2 * (k[b] + 1) > slices[b]) continue;
             k[b]++;
             total++;
             q.push({(slices[b] + k[b] - 1) / k[b], -b});

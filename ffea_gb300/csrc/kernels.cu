@@ -647,6 +647,7 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
                 cg.gamma_f = (float)s0;
                 cg.pap_f = cg.alpha_f = cg.beta_f = 0.f;
                 cg.stop_f = (float)(d.bp[bb].epsilon2 * s1);
+                cg.floor_f = (float)(1e-10 * s1);
                 cg.iters = 0;
                 cg.restarts = 0;
                 cg.true_relres2 = -1.0;
@@ -1330,21 +1331,28 @@ __device__ __forceinline__ bool transition_core(CgScalars &cg, const BlobParams 
     const int limit = bp.solver == SOLVER_MASS ? bp.max_iter - 1 : bp.max_iter;
     int finish = 0, bits = 0;
     if (cg.state == CG_ACTIVE) {
-        bool conv, nan;
+        bool conv, nan, breakdown = false, at_floor = false;
         if (fast) {
             const float g = sums[0].hi + sums[0].lo, dl = sums[1].hi + sums[1].lo, rr = sums[2].hi + sums[2].lo;
             conv = rr < cg.stop_f;
             nan = !(rr == rr) || !(g == g) || !(dl == dl);
             if (!(cg.iters > 0 && conv) && !nan && cg.iters < limit) {
-                if (cg.iters == 0) {
-                    cg.beta_f = 0.f;
-                    cg.pap_f = dl;
+                const float beta = cg.iters == 0 ? 0.f : g / cg.gamma_f;
+                const float pap = cg.iters == 0 ? dl : fmaf(-beta * beta, cg.pap_f, dl);
+                if (!(pap > 0.f) || !(g > 0.f)) {
+                    // the FP32 recurrence broke down (p.Ap or r.u not
+                    // positive, so alpha would not be finite).  Below the
+                    // floor this is the precision limit of FP32 vectors
+                    // (an epsilon tighter than FP32 can reach): stop there;
+                    // above it, it is a failure.
+                    breakdown = true;
+                    at_floor = rr < cg.floor_f;
                 } else {
-                    cg.beta_f = g / cg.gamma_f;
-                    cg.pap_f = fmaf(-cg.beta_f * cg.beta_f, cg.pap_f, dl);
+                    cg.beta_f = beta;
+                    cg.pap_f = pap;
+                    cg.alpha_f = g / pap;
+                    cg.gamma_f = g;
                 }
-                cg.alpha_f = g / cg.pap_f;
-                cg.gamma_f = g;
             }
         } else {
             const double g = (double)sums[0].hi + (double)sums[0].lo, dl = (double)sums[1].hi + (double)sums[1].lo;
@@ -1365,9 +1373,14 @@ __device__ __forceinline__ bool transition_core(CgScalars &cg, const BlobParams 
                 cg.gamma = g;
             }
         }
-        if (cg.iters > 0 && conv) {
+        if ((cg.iters > 0 && conv) || (breakdown && at_floor)) {
+            // with the true-residual check on, the FP64 b - A x decides
+            // (converged, or a restart from it)
             if (bp.true_residual) cg.state = CG_VERIFY;
             else finish = CG_CONVERGED;
+        } else if (breakdown) {
+            finish = CG_FAILED;
+            bits = BLOB_FAIL_CG;
         } else if (nan) {
             finish = CG_FAILED;
             bits = BLOB_FAIL_CG | BLOB_FAIL_NAN;

@@ -74,9 +74,11 @@ struct CgScalars {
     // per-iteration path; FP64 runs at 1/64 of the FP32 rate)
     float gamma_f, pap_f, alpha_f, beta_f;
     float stop_f;          // eps^2 f.f: stop when r.r < stop_f
+    float floor_f;         // 1e-10 f.f: an FP32 recurrence that breaks down below this has converged as far as FP32 goes
     int32_t iters;         // matrix-vector products of this solve (the reference's iteration count)
     int32_t state;         // CgState
     int32_t restarts;
+    int32_t reserved;      // (keeps the record a whole number of 8-byte words)
 };
 
 }  // namespace ffea

@@ -209,3 +209,21 @@ def test_two_level_beyond_one_cta_per_segment(gpulib):
             assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (pc, st)
             iters[pc] = st["cg_iters"]
     assert iters[TWO_LEVEL] < 0.6 * iters[JACOBI], iters
+
+
+@pytest.mark.parametrize("pc", [TWO_LEVEL, LEARNED])
+def test_two_level_on_a_tiny_blob(gpulib, pc):
+    """A blob of a few slices (130 corner nodes): every segment, which is
+    also an aggregate of the coarse space, keeps enough rows for its six
+    rigid modes to be independent, so the solve converges (an aggregate of
+    two nodes made the coarse matrix singular)."""
+    from ffea_gb300 import learned
+    s = spec(radius_nm=3.0, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    with _world([s], true_residual=True, preconditioner=pc) as w:
+        assert w.preconditioner() == pc
+        if pc == LEARNED:
+            learned.apply(w, learned.load())
+        for _ in range(3):
+            w.run(1)
+            st = w.blob(0).status()
+            assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, st
