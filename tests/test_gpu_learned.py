@@ -108,3 +108,32 @@ def test_training_gains_over_the_untrained_preconditioner(gpulib):
             res[name] = (iters, loss)
     assert res["trained"][1] < res["untrained"][1], res
     assert res["trained"][0] <= res["untrained"][0] + 2, res
+
+
+def test_torch_custom_op_trains_the_network(gpulib):
+    """ffea::mpnn_loss_grad (torch.library) gives the loss and gradient of
+    the library's own kernels, and torch's Adam on it lowers the loss of the
+    same (rhs, solution) pair."""
+    import torch
+
+    from ffea_gb300 import learned, torch_ops
+    from ffea_gb300.world import World
+    s = spec(radius_nm=8.0, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    with World([s], true_residual=True, preconditioner=2) as w:
+        theta0 = learned.init_params(seed=3)
+        learned.apply(w, theta0)
+        w.run(1)
+        ref_loss, ref_grad = learned.loss_grad(w, theta0)
+        theta = torch.nn.Parameter(torch.from_numpy(theta0.copy()))
+        loss = torch_ops.mpnn_loss(w, theta)
+        assert abs(loss.item() - ref_loss) <= 1e-12 * max(1.0, abs(ref_loss))
+        loss.backward()
+        assert np.array_equal(theta.grad.numpy(), ref_grad)
+        opt = torch.optim.Adam([theta], lr=3e-3)
+        first = loss.item()
+        for _ in range(20):
+            opt.zero_grad()
+            loss = torch_ops.mpnn_loss(w, theta)
+            loss.backward()
+            opt.step()
+        assert torch_ops.mpnn_loss(w, theta).item() < first

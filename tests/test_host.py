@@ -108,3 +108,18 @@ def test_unit_conversions():
     # the second viscosity subtracts an SI shear viscosity (src/Blob.cpp:2865)
     assert abs(m[2] - (A - (2.0 / 3.0) * 1e-3)) < 1e-12
     assert abs(P.kT_at(300.0) - 1.380649e-23 * 300 / 4.141945559999999e-21) < 1e-12
+
+
+def test_torch_custom_op_is_registered():
+    """The training-loop operator registers with torch.library without a GPU
+    and checks the parameter count before it reaches the library."""
+    import pytest
+    import torch
+
+    from ffea_gb300 import learned, torch_ops
+    assert hasattr(torch.ops.ffea.mpnn_loss_grad, "default")
+
+    class _W:
+        handle = 0
+    with pytest.raises(ValueError, match=str(learned.NUM_PARAMS)):
+        torch_ops.mpnn_loss(_W(), torch.zeros(3))
