@@ -6,7 +6,7 @@ Tolerances:
     rhs to 1e-9 relative (2-norm) -- the remaining differences are CG
     round-off with both sides solving to epsilon 1e-12.
   - mixed FP32/FP64 mode: per-step velocity and force error <= 1e-5 relative
-    (2-norm) over the first 100 steps, the spec parity bar.
+    (2-norm) over the first 100 steps, the parity bar of the mixed path.
 """
 import numpy as np
 import pytest
