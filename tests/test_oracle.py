@@ -48,7 +48,7 @@ def test_stream_fingerprint_2e7_draws(oracle):
     # rng[0] of a one-thread run with rng_seed 44: the sequential sum of 2e7
     # draws, and a word-wise FNV-style hash h = (h ^ bits(u)) * 0x100000001b3
     # (start 0xcbf29ce484222325) of the raw doubles; both values were produced
-    # by FFEA's own RngStream objects (oracle/_ref) in this build.
+    # by FFEA's own RngStream objects, compiled from its sources (oracle/_ref).
     total, h = oracle.rng_fingerprint(oracle.ffea_seed(44), 20_000_000)
     assert f"{total:.9f}" == "9999475.672332041"
     assert f"{h:016x}" == "59ab4718a3015f4e"
