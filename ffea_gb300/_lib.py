@@ -64,6 +64,7 @@ SIGNATURES = {
     "ffea_gpu_get_rng_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _u64p]),
     "ffea_gpu_set_rng_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _u64p]),
     "ffea_gpu_energies": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, _dp]),
+    "ffea_gpu_measurements": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _dp]),
     "ffea_gpu_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _ip, _ip, _dp, _ip]),
     "ffea_gpu_get_rhs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp]),
     "ffea_gpu_get_element_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp]),

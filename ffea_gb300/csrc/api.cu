@@ -141,6 +141,7 @@ struct ffea_gpu {
     double *io_stage = nullptr;   // 9 doubles per node of the largest blob (pos, vel, force)
     int *io_moved = nullptr;      // set_nodes: 1 when a position changed
     int32_t io_max_nodes = 0;
+    MeasView meas;                // measurements: node tiles in the reference's order, positions at creation
     int precond = FFEA_GPU_PRECOND_JACOBI;     // in use, after fall-backs
     MpnnBuffers mpnn;                          // learned smoother weights (allocated on first use)
     bool mpnn_ready = false;
@@ -593,6 +594,45 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
         CK(upload(A, h->io_secvel, secvel));
         CK(A.alloc(h->io_stage, 9 * (size_t)h->io_max_nodes));
         CK(A.alloc(h->io_moved, 1));
+        // measurements: Blob::set_pos_0 (src/World.cpp:504) takes the
+        // positions after Blob::init has put every edge midpoint between its
+        // end nodes (linearise_elements, src/Blob.cpp:334-340), last element
+        // first as above; node tiles of MEAS_TILE per blob
+        std::vector<double> pos0(3 * src.size());
+        std::vector<int64_t> off(h->io_off);
+        off.push_back((int64_t)src.size());
+        std::vector<int32_t> tile_blob, tile_first;
+        for (int b = 0; b < num_blobs; b++) {
+            const ffea_gpu_mesh &m = meshes[b];
+            double *p0 = pos0.data() + 3 * off[b];
+            std::copy(m.pos, m.pos + 3 * (size_t)m.num_nodes, p0);
+            for (int32_t e = 0; e < m.num_elements; e++) {
+                const int32_t *t = &m.topology[10 * (size_t)e];
+                for (int k = 0; k < 6; k++)
+                    for (int c = 0; c < 3; c++)
+                        p0[3 * (size_t)t[mid[k][0]] + c] =
+                            .5 * (p0[3 * (size_t)t[mid[k][1]] + c] + p0[3 * (size_t)t[mid[k][2]] + c]);
+            }
+            tile_first.push_back((int32_t)tile_blob.size());
+            tile_blob.resize(tile_blob.size() + (meshes[b].num_nodes + MEAS_TILE - 1) / MEAS_TILE, b);
+        }
+        tile_first.push_back((int32_t)tile_blob.size());
+        MeasView &mv = h->meas;
+        double *p0 = nullptr;
+        int64_t *po = nullptr;
+        int32_t *tb = nullptr, *tf = nullptr;
+        CK(upload(A, p0, pos0));
+        CK(upload(A, po, off));
+        CK(upload(A, tb, tile_blob));
+        CK(upload(A, tf, tile_first));
+        mv.io_src = h->io_src;
+        mv.pos0 = p0;
+        mv.io_off = po;
+        mv.tile_blob = tb;
+        mv.tile_first = tf;
+        mv.n_tiles = (int32_t)tile_blob.size();
+        CK(A.alloc(mv.partials, 4 * (size_t)(H.n_etiles + mv.n_tiles)));
+        CK(A.alloc(mv.out, MEAS_VALUES * (size_t)num_blobs));
     }
     launch_rest_state(d, h->stream);
     if (d.any_mass) launch_mass_matrix(d, h->stream);
@@ -1091,6 +1131,33 @@ int ffea_gpu_energies(ffea_gpu_t *h, int32_t blob, double *strain, double *kinet
     CK(cudaStreamSynchronize(h->stream));
     if (strain) *strain = e[0];
     if (kinetic) *kinetic = e[1];
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_measurements(ffea_gpu_t *h, int32_t first_blob, int32_t count, double *out)
+{
+    if (!h || !out || count < 1 || first_blob < 0 || first_blob + (int64_t)count > h->dev.num_blobs)
+        return FFEA_GPU_ERROR;
+    launch_energies(h->dev, h->stream);
+    launch_measurements(h->dev, h->meas, h->stream);
+    std::vector<double> e(2 * (size_t)count), v(MEAS_VALUES * (size_t)count);
+    CK(cudaMemcpyAsync(e.data(), h->dev.energy + 2 * (size_t)first_blob, sizeof(double) * e.size(),
+                       cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(v.data(), h->meas.out + MEAS_VALUES * (size_t)first_blob, sizeof(double) * v.size(),
+                       cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int32_t b = 0; b < count; b++) {
+        double *o = out + FFEA_GPU_NUM_MEASUREMENTS * (size_t)b;
+        const double *m = v.data() + MEAS_VALUES * (size_t)b;
+        o[FFEA_GPU_MEAS_KINETIC] = e[2 * (size_t)b + 1];
+        o[FFEA_GPU_MEAS_STRAIN] = e[2 * (size_t)b];
+        for (int k = 0; k < 3; k++) {
+            o[FFEA_GPU_MEAS_CENTROID + k] = m[k];
+            o[FFEA_GPU_MEAS_COM + k] = m[4 + k];
+            o[FFEA_GPU_MEAS_ANGMOM + k] = m[7 + k];
+        }
+        o[FFEA_GPU_MEAS_RMSD] = m[3];
+    }
     return FFEA_GPU_OK;
 }
 

@@ -2539,6 +2539,142 @@ __global__ void __launch_bounds__(ELEM_TILE) k_energies(DeviceBatch d)
     }
 }
 
+static_assert(MEAS_TILE == ELEM_TILE, "measurement kernels run element and node tiles in one grid");
+
+// Element mass vol_0 rho (src/Blob.cpp:3797).
+template <typename T>
+__device__ __forceinline__ double element_mass(const DeviceBatch &d, int e)
+{
+    return (double)static_cast<const T *>(d.vol0)[e] * d.mats[d.mat_id[e]].rho;
+}
+
+// Sums of Blob::make_measurements over tiles, FP64.  Element tiles (blocks
+// [0, n_etiles)) add Blob::get_CoM's terms, (m_e p_0 + p_1 + p_2 + p_3) / 4 --
+// the element mass multiplies the first corner only, as the reference's
+// parenthesisation has it (src/Blob.cpp:951-967); node tiles add the
+// centroid over all N_t nodes and the squared displacement from the
+// positions at creation (src/Blob.cpp:1488-1524, remTrans off).  A node of no
+// element never moves and counts at its creation position.  The last block
+// reduces each blob's tiles in a fixed order.
+template <typename T>
+__global__ void __launch_bounds__(ELEM_TILE) k_meas_sums(DeviceBatch d, MeasView m)
+{
+    __shared__ double red[4 * 32];
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    const int t = blockIdx.x;
+    if (t < d.n_etiles) {
+        const BlobParams &bp = d.bp[d.etile_blob[t]];
+        const int le = t * ELEM_TILE - bp.elem_off + threadIdx.x;
+        if (le < bp.elem_cnt) {
+            const int e = bp.elem_off + le;
+            const int4 c = reinterpret_cast<const int4 *>(d.conn)[e];
+            const double mass = element_mass<T>(d, e);
+            for (int k = 0; k < 3; k++)
+                v[k] = (mass * d.pos[3 * (size_t)c.x + k] + d.pos[3 * (size_t)c.y + k] + d.pos[3 * (size_t)c.z + k] +
+                        d.pos[3 * (size_t)c.w + k]) / 4;
+        }
+    } else {
+        const int nt = t - d.n_etiles;
+        const int b = m.tile_blob[nt];
+        const int64_t i0 = m.io_off[b], n = m.io_off[b + 1] - i0;
+        const int64_t li = (int64_t)(nt - m.tile_first[b]) * MEAS_TILE + threadIdx.x;
+        if (li < n) {
+            const int64_t i = i0 + li;
+            const int2 s = m.io_src[i];
+            for (int k = 0; k < 3; k++) {
+                const double p0 = m.pos0[3 * i + k];
+                double p = p0;
+                if (s.x >= 0 && s.y < 0)
+                    p = d.pos[3 * (size_t)s.x + k];
+                else if (s.x >= 0)
+                    p = .5 * (d.pos[3 * (size_t)s.x + k] + d.pos[3 * (size_t)s.y + k]);
+                v[k] = p;
+                v[3] += (p - p0) * (p - p0);
+            }
+        }
+    }
+    double sum[4];
+    block_sum<4, double>(v, sum, red);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 4; k++) m.partials[4 * (size_t)t + k] = sum[k];
+    if (last_block(&d.counters[CNT_MEAS], gridDim.x)) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int bb = warp; bb < d.num_blobs; bb += nw) {
+            const BlobParams &bp = d.bp[bb];
+            const int e0 = bp.elem_off / ELEM_TILE, ec = bp.elem_pad / ELEM_TILE;
+            const int n0 = d.n_etiles + m.tile_first[bb], nc = m.tile_first[bb + 1] - m.tile_first[bb];
+            double com[3] = {0.0, 0.0, 0.0}, cog[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int q = lane; q < ec; q += 32)
+                for (int k = 0; k < 3; k++) com[k] += __ldcg(&m.partials[4 * (size_t)(e0 + q) + k]);
+            for (int q = lane; q < nc; q += 32)
+                for (int k = 0; k < 4; k++) cog[k] += __ldcg(&m.partials[4 * (size_t)(n0 + q) + k]);
+            for (int k = 0; k < 3; k++) com[k] = warp_sum<double>(com[k]);
+            for (int k = 0; k < 4; k++) cog[k] = warp_sum<double>(cog[k]);
+            if (lane == 0) {
+                const double nn = (double)(m.io_off[bb + 1] - m.io_off[bb]);
+                double *o = m.out + MEAS_VALUES * (size_t)bb;
+                for (int k = 0; k < 3; k++) o[k] = cog[k] / nn;
+                o[3] = sqrt(cog[3] / nn);
+                for (int k = 0; k < 3; k++) o[4 + k] = bp.elem_cnt ? com[k] / bp.elem_cnt : 0.0;
+            }
+        }
+        if (threadIdx.x == 0) d.counters[CNT_MEAS] = 0;
+    }
+}
+
+// Angular momentum about the centre of mass, sum over elements of
+// m_e sum_ij MM_ij (r_j x v_i) with MM the linear element's mass matrix / m_e
+// (0.1 diagonal, 0.05 off it); zero for CG_nomass (src/Blob.cpp:1434-1484).
+template <typename T>
+__global__ void __launch_bounds__(ELEM_TILE) k_meas_angmom(DeviceBatch d, MeasView m)
+{
+    __shared__ double red[3 * 32];
+    const int t = blockIdx.x;
+    const int b = d.etile_blob[t];
+    const BlobParams &bp = d.bp[b];
+    const int le = t * ELEM_TILE - bp.elem_off + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    if (bp.solver != SOLVER_NOMASS && le < bp.elem_cnt) {
+        const int e = bp.elem_off + le;
+        const int4 c = reinterpret_cast<const int4 *>(d.conn)[e];
+        const int cn[4] = {c.x, c.y, c.z, c.w};
+        const double *com = m.out + MEAS_VALUES * (size_t)b + 4;
+        double r[4][3], u[4][3];
+        for (int i = 0; i < 4; i++)
+            for (int k = 0; k < 3; k++) {
+                r[i][k] = d.pos[3 * (size_t)cn[i] + k] - com[k];
+                u[i][k] = d.vel[3 * (size_t)cn[i] + k];
+            }
+        double l[3] = {0.0, 0.0, 0.0};
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) {
+                const double mm = i == j ? .1 : .05;
+                l[0] += mm * (r[j][1] * u[i][2] - r[j][2] * u[i][1]);
+                l[1] += mm * (r[j][2] * u[i][0] - r[j][0] * u[i][2]);
+                l[2] += mm * (r[j][0] * u[i][1] - r[j][1] * u[i][0]);
+            }
+        const double mass = element_mass<T>(d, e);
+        for (int k = 0; k < 3; k++) v[k] = mass * l[k];
+    }
+    double sum[3];
+    block_sum<3, double>(v, sum, red);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; k++) m.partials[4 * (size_t)t + k] = sum[k];
+    if (last_block(&d.counters[CNT_ANGMOM], gridDim.x)) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int bb = warp; bb < d.num_blobs; bb += nw) {
+            const int e0 = d.bp[bb].elem_off / ELEM_TILE, ec = d.bp[bb].elem_pad / ELEM_TILE;
+            double l[3] = {0.0, 0.0, 0.0};
+            for (int q = lane; q < ec; q += 32)
+                for (int k = 0; k < 3; k++) l[k] += __ldcg(&m.partials[4 * (size_t)(e0 + q) + k]);
+            for (int k = 0; k < 3; k++) l[k] = warp_sum<double>(l[k]);
+            if (lane == 0)
+                for (int k = 0; k < 3; k++) m.out[MEAS_VALUES * (size_t)bb + 7 + k] = l[k];
+        }
+        if (threadIdx.x == 0) d.counters[CNT_ANGMOM] = 0;
+    }
+}
+
 __global__ void k_rng_draws(const mrg::JumpMat *table, const uint32_t *state, uint64_t offset, int64_t count,
                             double *out)
 {
@@ -2731,6 +2867,12 @@ void launch_euler(const DeviceBatch &d, cudaStream_t s)
 void launch_energies(const DeviceBatch &d, cudaStream_t s)
 {
     PREC_DISPATCH(d, k_energies, d.n_etiles, ELEM_TILE, s, d);
+}
+
+void launch_measurements(const DeviceBatch &d, const MeasView &m, cudaStream_t s)
+{
+    PREC_DISPATCH(d, k_meas_sums, d.n_etiles + m.n_tiles, ELEM_TILE, s, d, m);
+    PREC_DISPATCH(d, k_meas_angmom, d.n_etiles, ELEM_TILE, s, d, m);
 }
 
 template <typename T>

@@ -106,7 +106,25 @@ __host__ __device__ inline float2 split_pos(double p)
 enum MatT { MAT_T_RHO = 0, MAT_T_A = 1, MAT_T_B = 2, MAT_T_G = 3, MAT_T_E = 4, MAT_T_STRIDE = 8 };
 
 // reduction counter slots
-enum CounterSlot { CNT_NODES = 0, CNT_ENERGY = 1, CNT_COUNT = 4 };
+enum CounterSlot { CNT_NODES = 0, CNT_ENERGY = 1, CNT_MEAS = 2, CNT_ANGMOM = 3, CNT_COUNT = 4 };
+
+// Measurements (Blob::make_measurements) need the nodes in the reference's
+// order, which the batch does not keep: per node (row, -1) for a corner node,
+// (row_a, row_b) for an edge midpoint, (-1, -1) for a node of no element,
+// with the positions at creation (Blob::set_pos_0), cut into tiles of
+// MEAS_TILE nodes that each belong to one blob.
+constexpr int MEAS_TILE = 128;
+constexpr int MEAS_VALUES = 10;  // per blob: centroid xyz, RMSD, centre of mass xyz, angular momentum xyz
+struct MeasView {
+    const int2 *io_src = nullptr;
+    const int64_t *io_off = nullptr;      // num_blobs + 1: first node of each blob
+    const double *pos0 = nullptr;         // 3 per node
+    const int32_t *tile_blob = nullptr;   // per node tile
+    const int32_t *tile_first = nullptr;  // num_blobs + 1: first node tile of each blob
+    int32_t n_tiles = 0;
+    double *partials = nullptr;           // 4 per element tile, then 4 per node tile
+    double *out = nullptr;                // MEAS_VALUES per blob
+};
 
 // element kernel modes
 enum ElemMode { ELEM_STEP = 0, ELEM_MATRIX_ONLY = 1 };
@@ -137,6 +155,8 @@ cudaError_t launch_barrier_timeout_selftest(unsigned int *bar, unsigned int spin
                                             cudaStream_t s);
 void launch_euler(const DeviceBatch &d, cudaStream_t s);
 void launch_energies(const DeviceBatch &d, cudaStream_t s);
+// centroid, RMSD, centre of mass and angular momentum of every blob into m.out
+void launch_measurements(const DeviceBatch &d, const MeasView &m, cudaStream_t s);
 void launch_apply(const DeviceBatch &d, cudaStream_t s, const double *in, double *out);
 // standalone w = A u with one of the SpMV variants (0..3), for timing
 void launch_spmv_variant(const DeviceBatch &d, cudaStream_t s, int variant);

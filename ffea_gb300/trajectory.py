@@ -10,6 +10,12 @@ restarts the way ``World::init`` restarts an FFEA run:
   zeros for CG_nomass (``Blob::write_nodes_to_file``, src/Blob.cpp:1143-1178);
   then ``*``, the conformation changes and ``*``
   (``World::print_trajectory_and_measurement_files``, src/World.cpp:4125-4180);
+- measurements (``_measurement.out``): ``World::write_output_header``, the
+  system block of ``SimulationParams::write_to_file`` and the column line
+  (src/World.cpp:551-586, 4084-4096; src/SimulationParams.cpp:813-832), then
+  one ``%-14.6e`` row per frame with ``World::make_measurements``' totals
+  (src/World.cpp:4282-4366): time, kinetic energy when a blob has mass,
+  strain energy, the node-weighted centroid and RMSD, in SI units;
 - checkpoint (``.fcp``): ``RNGStreams dedicated to the thermal stress: %d``
   and one line of six ``%lu`` words per stream, rewritten in place
   (``World::print_checkpoints``, src/World.cpp:4233-4280), read back as in
@@ -29,6 +35,7 @@ s - 1); FFEA prints the solve of step s there.
 from __future__ import annotations
 
 import os
+import time
 from typing import Sequence
 
 import numpy as np
@@ -112,6 +119,83 @@ def read_last_frame(path: str, nodes_per_blob: Sequence[int]):
     raise ValueError(f"{path}: no completely written frame")
 
 
+# ---------------------------------------------------------------- measurements
+def write_measurement_header(fh, params, num_blobs: int, mass_in_system: bool, num_steps: int = 0,
+                             check: int = 1, script: str = "", restart: int = 0) -> None:
+    """The measurement file up to its column line.  ``params`` is the first
+    blob's SimulationParams (meso units): the system block prints one set."""
+    now = time.localtime()
+    fh.write("FFEA Global Measurement File\n\nSimulation Details:\n")
+    fh.write("\tSimulation Began on %d/%d/%d at %d:%d:%d\n" % (now.tm_mday, now.tm_mon, now.tm_year, now.tm_hour,
+                                                            now.tm_min, now.tm_sec))
+    fh.write("\tScript Filename = %s\n" % script)
+    fh.write("\tSimulation Type = %s\n\n" % "Full")
+    fh.write("Parameters:\n\tSystem parameters:\n")
+    fh.write("\trestart = %d\n" % restart)
+    fh.write("\tdt = %e\n" % (params.dt * P.MESO_TIME))
+    fh.write("\tnum_steps = %d\n" % num_steps)
+    fh.write("\tcheck = %d\n" % check)
+    fh.write("\trng_seed = %d\n" % params.rng_seed)
+    fh.write("\tkT = %e\n" % (params.kT * P.MESO_ENERGY))
+    fh.write("\tmax_iterations_cg = %d\n" % params.max_iterations_cg)
+    fh.write("\tepsilon = %e\n" % np.sqrt(params.epsilon2))
+    if params.calc_stokes == 1:
+        fh.write("\tstokes_visc = %e\n" % (params.stokes_visc * P.MESO_PRESSURE * P.MESO_TIME))
+    fh.write("\tnum_blobs = %d\n" % num_blobs)
+    fh.write("\n\tCalculations enabled:\n")
+    fh.write("\tcalc_noise = %d\n" % params.calc_noise)
+    fh.write("\tcalc_stokes = %d\n" % params.calc_stokes)
+    fh.write("\nMeasurements:\n")
+    fh.write("%-14s" % "Time")
+    if mass_in_system:
+        fh.write("%-14s" % "KineticEnergy")
+    fh.write("%-14s" % "StrainEnergy")
+    fh.write("%-14s%-14s%-14s%-14s" % ("Centroid.x", "Centroid.y", "Centroid.z", "RMSD"))
+    fh.write("\n")
+
+
+def measurement_row(step: int, dt: float, meas: np.ndarray, nodes_per_blob: Sequence[int],
+                    mass_in_system: bool) -> str:
+    """World::make_measurements + write_measurements_to_file: ``meas`` holds
+    one ffea_gpu_measurements row per blob (meso units)."""
+    meas = np.asarray(meas, dtype=float).reshape(len(nodes_per_blob), -1)
+    n = np.asarray(nodes_per_blob, dtype=float)
+    kinetic, strain = meas[:, 0].sum(), meas[:, 1].sum()
+    cog = (meas[:, 2:5] * n[:, None]).sum(axis=0) / n.sum()
+    rmsd = np.sqrt((meas[:, 5] * meas[:, 5] * n).sum() / n.sum())
+    out = "%-14.6e" % (step * dt * P.MESO_TIME)
+    if mass_in_system:
+        out += "%-14.6e" % (kinetic * P.MESO_ENERGY)
+    out += "%-14.6e" % (strain * P.MESO_ENERGY)
+    out += "%-14.6e%-14.6e%-14.6e" % tuple(cog * P.MESO_LENGTH)
+    out += "%-14.6e" % (rmsd * P.MESO_LENGTH)
+    return out + "\n"
+
+
+def read_measurements(path: str) -> dict:
+    """The columns of a measurement file as arrays, keyed by their titles
+    (the reading ffeatools' FFEA_measurement.load_global does)."""
+    with open(path) as fh:
+        lines = fh.read().split("\n")
+    at = lines.index("Measurements:")
+    titles = lines[at + 1].split()
+    rows = [[float(x) for x in ln.split()] for ln in lines[at + 2:] if ln.strip() and ln.strip() != "#==RESTART=="]
+    vals = np.array(rows).reshape(-1, len(titles))
+    return {t: vals[:, i] for i, t in enumerate(titles)}
+
+
+def _truncate_measurements(path: str, rows: int) -> None:
+    """Keep the header and the first `rows` measurement rows."""
+    with open(path) as fh:
+        lines = fh.read().split("\n")
+    at = lines.index("Measurements:")
+    body = [ln for ln in lines[at + 2:] if ln.strip()]
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines[:at + 2]) + "\n")
+        for ln in body[:rows]:
+            fh.write(ln + "\n")
+
+
 # ---------------------------------------------------------------- checkpoint
 def write_checkpoint(path: str, states: Sequence[Sequence[int]]) -> None:
     """World::print_checkpoints: the thermal-stress streams' states."""
@@ -146,18 +230,21 @@ def stream_states(world) -> list:
 
 class Recorder:
     """World::run's output side for a GPU World: every `check` steps the RNG
-    checkpoint (rewritten) and a trajectory frame, as FFEA writes them
-    (src/World.cpp:2020-2043).  `restart=True` continues an existing pair of
-    files: positions and velocities from the last complete frame, RNG states
-    from the checkpoint (src/World.cpp:330-385, 655-760), and appends."""
+    checkpoint (rewritten), a trajectory frame and, with `measurement`, a
+    measurement row, as FFEA writes them (src/World.cpp:2020-2043,
+    4126-4226).  `restart=True` continues existing files: positions and
+    velocities from the last complete frame, RNG states from the checkpoint
+    (src/World.cpp:330-385, 655-760), and appends; the measurement file keeps
+    the rows of the frames before the restart frame, which is written again."""
 
     def __init__(self, world, trajectory: str, checkpoint: str, solvers: Sequence[int], check: int = 1,
-                 restart: bool = False):
+                 restart: bool = False, measurement: str | None = None, script: str = "", num_steps: int = 0):
         if check < 1:
             raise ValueError("check must be >= 1")
         self.world, self.check, self.solvers = world, int(check), list(solvers)
-        self.trajectory, self.checkpoint = trajectory, checkpoint
+        self.trajectory, self.checkpoint, self.measurement = trajectory, checkpoint, measurement
         self.nodes = [world.blob(i).n for i in range(world.num_blobs)]
+        self.mass_in_system = any(s != P.SOLVER_NOMASS for s in self.solvers)
         self.step = 0
         self._written = -1  # step of the last frame written
         if restart:
@@ -171,9 +258,15 @@ class Recorder:
             # the restart point is written again by the next frame (FFEA
             # truncates the file to the frame it restarts from)
             self._truncate_after_frame(self.step)
+            if measurement:
+                _truncate_measurements(measurement, self.step // self.check)
         else:
             with open(trajectory, "w") as fh:
                 write_header(fh, self.nodes)
+            if measurement:
+                with open(measurement, "w") as fh:
+                    write_measurement_header(fh, world.params[0], world.num_blobs, self.mass_in_system,
+                                             num_steps, self.check, script)
 
     def _truncate_after_frame(self, step: int) -> None:
         with open(self.trajectory) as fh:
@@ -195,6 +288,11 @@ class Recorder:
         if self.step % self.check == 0 and self.step != self._written:
             write_checkpoint(self.checkpoint, stream_states(self.world))
             self._frame()
+            if self.measurement:
+                row = measurement_row(self.step, self.world.params[0].dt, self.world.measurements(), self.nodes,
+                                      self.mass_in_system)
+                with open(self.measurement, "a") as fh:
+                    fh.write(row)
             self._written = self.step
 
     def run(self, num_steps: int) -> None:

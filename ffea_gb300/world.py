@@ -23,6 +23,18 @@ from .params import PRECISION_MIXED, SOLVER_MASS, SOLVER_NOMASS, SimulationParam
 RNG_PER_BLOB = 0
 RNG_SHARED = 1
 
+# ffea_gpu_measurements' values per blob (FFEA_GPU_MEAS_* order)
+MEASUREMENT_COLUMNS = ("kinetic", "strain", "centroid_x", "centroid_y", "centroid_z", "rmsd", "com_x", "com_y",
+                       "com_z", "angmom_x", "angmom_y", "angmom_z")
+
+
+def measurement_dict(row) -> dict:
+    """One blob's measurement row as {"kinetic", "strain", "centroid" (3),
+    "rmsd", "com" (3), "angmom" (3)}."""
+    row = np.asarray(row, dtype=float)
+    return {"kinetic": float(row[0]), "strain": float(row[1]), "centroid": row[2:5].copy(), "rmsd": float(row[5]),
+            "com": row[6:9].copy(), "angmom": row[9:12].copy()}
+
 
 class _Keep:
     """Owns the numpy arrays a Mesh struct points into until creation returns."""
@@ -76,6 +88,7 @@ class World:
         self.num_nodes = []
         self.num_elements = []
         self.solvers = []
+        self.params = []
         for i, b in enumerate(blobs):
             get = (lambda k: b[k]) if isinstance(b, dict) else (lambda k: getattr(b, k))
             mesh = get("mesh")
@@ -88,6 +101,7 @@ class World:
             self.num_nodes.append(len(np.asarray(pos).reshape(-1, 3)))
             self.num_elements.append(len(np.asarray(topo).reshape(-1, 10)))
             self.solvers.append(p.solver)
+            self.params.append(p)
         n = len(meshes)
         if n == 0:
             raise ValueError("World needs at least one blob")
@@ -177,6 +191,13 @@ class World:
         L.check(L.lib().ffea_gpu_set_smoother_weights(self._h, int(blob), w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
                 "ffea_gpu_set_smoother_weights")
 
+    def measurements(self) -> np.ndarray:
+        """Blob::make_measurements of every blob, one row per blob, columns
+        MEASUREMENT_COLUMNS (meso units); one pass over the batch."""
+        out = np.zeros((self.num_blobs, len(MEASUREMENT_COLUMNS)))
+        L.check(L.lib().ffea_gpu_measurements(self.handle, 0, self.num_blobs, L.ptr(out)), "ffea_gpu_measurements")
+        return out
+
     def blob(self, i: int) -> "Blob":
         return Blob(self, i)
 
@@ -234,6 +255,14 @@ class Blob:
         s, k = ctypes.c_double(), ctypes.c_double()
         L.check(L.lib().ffea_gpu_energies(self.world.handle, self.index, ctypes.byref(s), ctypes.byref(k)))
         return s.value, k.value
+
+    def measurements(self) -> dict:
+        """Blob::make_measurements at the current state (meso units): kinetic
+        and strain energy, centroid, RMSD from the creation positions, centre
+        of mass and angular momentum."""
+        out = np.zeros(len(MEASUREMENT_COLUMNS))
+        L.check(L.lib().ffea_gpu_measurements(self.world.handle, self.index, 1, L.ptr(out)), "ffea_gpu_measurements")
+        return measurement_dict(out)
 
     def status(self):
         inv, it, fb = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

@@ -142,6 +142,25 @@ int ffea_gpu_set_rng_state(ffea_gpu_t *h, int32_t blob, const uint64_t state[6])
  * computes them (src/Blob.cpp:1363-1432); kinetic is 0 for CG_nomass. */
 int ffea_gpu_energies(ffea_gpu_t *h, int32_t blob, double *strain, double *kinetic);
 
+/* Blob::make_measurements (src/Blob.cpp:1363-1527) for blobs first_blob ..
+ * first_blob + count - 1 at the current state: FFEA_GPU_NUM_MEASUREMENTS
+ * values per blob into out, in meso units.  The centroid is the mean of all
+ * N_t node positions; RMSD is taken against the positions given at creation
+ * (Blob::set_pos_0, src/Blob.cpp:1035-1050) without removing the translation;
+ * the centre of mass is Blob::get_CoM's sum (src/Blob.cpp:951-967), where the
+ * element mass multiplies the first corner only and the sum is divided by
+ * the element count; the angular momentum about that point is 0 for
+ * CG_nomass.  Kinetic and strain energy are those of ffea_gpu_energies.  One
+ * pass over the batch: the values of every blob are computed by each call. */
+#define FFEA_GPU_MEAS_KINETIC 0
+#define FFEA_GPU_MEAS_STRAIN 1
+#define FFEA_GPU_MEAS_CENTROID 2  /* x, y, z: Blob::CoG */
+#define FFEA_GPU_MEAS_RMSD 5      /* Blob::rmsd */
+#define FFEA_GPU_MEAS_COM 6       /* x, y, z: Blob::CoM */
+#define FFEA_GPU_MEAS_ANGMOM 9    /* x, y, z: Blob::L */
+#define FFEA_GPU_NUM_MEASUREMENTS 12
+int ffea_gpu_measurements(ffea_gpu_t *h, int32_t first_blob, int32_t count, double *out);
+
 /* Status of the last step: inverted-element count, CG iterations of the last
  * solve, FP64 true relative residual ||b - A x|| / ||b|| of the last solve
  * (NaN when the check is off), and the failure bits (FFEA_GPU_FAIL_*). */

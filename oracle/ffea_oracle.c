@@ -450,6 +450,7 @@ typedef struct {
     double *rhs_copy;                   /* rhs handed to the solver in the last step */
     double *ext;                        /* external forces per node (NULL: none), added every step */
     double *inv_m;                      /* lumped solver: inverse lumped mass per node */
+    double *pos_0;                      /* positions after Blob::init (Blob::set_pos_0) */
 } orc_blob;
 
 static void *orc_alloc(size_t n) { void *p = calloc(n ? n : 1, 1); return p; }
@@ -1215,6 +1216,9 @@ orc_blob *orc_blob_create(int num_nodes, int num_elements, const double *pos, co
             for (int c = 0; c < 3; c++)
                 b->pos[3 * n[mid[m][0]] + c] = .5 * (b->pos[3 * n[mid[m][1]] + c] + b->pos[3 * n[mid[m][2]] + c]);
     }
+    /* World::init then records these positions (src/World.cpp:504, Blob::set_pos_0) */
+    b->pos_0 = orc_alloc(sizeof(double) * 3 * num_nodes);
+    memcpy(b->pos_0, b->pos, sizeof(double) * 3 * num_nodes);
     for (int e = 0; e < num_elements; e++) {
         double J[3][3], (*mi)[3] = (double (*)[3])&b->J_inv_0[9 * e], det;
         orc_jacobian(b, e, J);
@@ -1247,7 +1251,7 @@ void orc_blob_destroy(orc_blob *b)
                     b->is_pinned, b->pinned, b->J_inv_0, b->vol_0, b->vol, b->last_det, b->dpsi, b->visc,
                     b->node_force, b->F_ij, b->rng, b->nm_key, b->nm_col, b->nm_val, b->nm_src_ptr,
                     b->nm_src, b->pre, b->r, b->p, b->z, b->q, b->f, b->work_in, b->work_out, b->m_key,
-                    b->m_col, b->m_val, b->d, b->s, b->rhs_copy, b->ext, b->inv_m};
+                    b->m_col, b->m_val, b->d, b->s, b->rhs_copy, b->ext, b->inv_m, b->pos_0};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
     free(b);
 }
@@ -1377,6 +1381,59 @@ void orc_blob_energies(orc_blob *b, double *strain, double *kinetic)
     }
     *strain = se * 0.5;
     *kinetic = ke * 0.5;
+}
+
+/* The rest of Blob::make_measurements (src/Blob.cpp:1433-1527) at the
+ * current state: out[0..2] the centroid of all nodes, out[3] the RMSD from
+ * pos_0 (remTrans off), out[4..6] the centre of mass as Blob::get_CoM sums it
+ * (src/Blob.cpp:951-967: the element mass multiplies the first corner only,
+ * the sum is divided by the element count), out[7..9] the angular momentum
+ * about that point, left at 0 for CG_nomass. */
+void orc_blob_measurements(const orc_blob *b, double *out)
+{
+    static const double MM[4][4] = {{.1, .05, .05, .05}, {.05, .1, .05, .05}, {.05, .05, .1, .05}, {.05, .05, .05, .1}};
+    double com[3] = {0, 0, 0}, cog[3] = {0, 0, 0}, l[3] = {0, 0, 0}, msd = 0;
+    for (int n = 0; n < b->num_elements; n++) {
+        const int *nd = &b->topo[10 * n];
+        const double mass = b->vol_0[n] * b->rho[n];
+        for (int c = 0; c < 3; c++)
+            com[c] += (mass * b->pos[3 * nd[0] + c] + b->pos[3 * nd[1] + c] + b->pos[3 * nd[2] + c] +
+                       b->pos[3 * nd[3] + c]) / 4;
+    }
+    if (b->num_elements)
+        for (int c = 0; c < 3; c++) com[c] /= b->num_elements;
+    if (b->solver != ORC_SOLVER_NOMASS) {
+        for (int n = 0; n < b->num_elements; n++) {
+            const int *nd = &b->topo[10 * n];
+            double r[4][3], t[3] = {0, 0, 0};
+            for (int i = 0; i < 4; i++)
+                for (int c = 0; c < 3; c++) r[i][c] = b->pos[3 * nd[i] + c] - com[c];
+            for (int i = 0; i < 4; i++) {
+                const double *v = &b->vel[3 * nd[i]];
+                for (int j = 0; j < 4; j++) {
+                    t[0] += MM[i][j] * (r[j][1] * v[2] - r[j][2] * v[1]);
+                    t[1] += MM[i][j] * (r[j][2] * v[0] - r[j][0] * v[2]);
+                    t[2] += MM[i][j] * (r[j][0] * v[1] - r[j][1] * v[0]);
+                }
+            }
+            const double mass = b->vol_0[n] * b->rho[n];
+            for (int c = 0; c < 3; c++) l[c] += mass * t[c];
+        }
+    }
+    for (int i = 0; i < b->num_nodes; i++) {
+        double d[3];
+        for (int c = 0; c < 3; c++) {
+            cog[c] += b->pos[3 * i + c];
+            d[c] = b->pos[3 * i + c] - b->pos_0[3 * i + c];
+        }
+        msd += d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    }
+    for (int c = 0; c < 3; c++) {
+        out[c] = cog[c] / b->num_nodes;
+        out[4 + c] = com[c];
+        out[7 + c] = l[c];
+    }
+    out[3] = sqrt(msd / b->num_nodes);
 }
 
 int orc_num_threads_available(void)

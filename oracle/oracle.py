@@ -74,6 +74,7 @@ def port_lib():
         lib.orc_blob_last_cg_iters.restype = ctypes.c_int
         lib.orc_blob_last_cg_iters.argtypes = [ctypes.c_void_p]
         lib.orc_blob_energies.argtypes = [ctypes.c_void_p, _dp, _dp]
+        lib.orc_blob_measurements.argtypes = [ctypes.c_void_p, _dp]
         lib.orc_blob_apply_nomass.argtypes = [ctypes.c_void_p, _dp, _dp]
         lib.orc_rng_draws.argtypes = [_u64p, ctypes.c_int64, _dp]
         lib.orc_rng_jump.argtypes = [_u64p, ctypes.c_uint64]
@@ -231,6 +232,17 @@ class OracleBlob:
         s = ctypes.c_double(); k = ctypes.c_double()
         self.lib.orc_blob_energies(self.h, ctypes.byref(s), ctypes.byref(k))
         return s.value, k.value
+
+    def measurements(self) -> np.ndarray:
+        """Blob::make_measurements at the current state in ffea_gpu_measurements'
+        order: kinetic, strain, centroid (3), RMSD, centre of mass (3),
+        angular momentum (3)."""
+        if self.pfx != "orc":
+            raise NotImplementedError("measurements are restated by the C oracle only")
+        strain, kinetic = self.energies()
+        rest = np.zeros(10)
+        self.lib.orc_blob_measurements(self.h, _ptr(rest, _dp))
+        return np.concatenate([[kinetic, strain], rest])
 
     def apply_nomass(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)

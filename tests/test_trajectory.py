@@ -22,6 +22,10 @@ class _OracleWorld:
         self.ob = oracle.blob_from_spec(s)
         self.num_blobs = 1
         self.rng_mode = 0
+        self.params = [s.params]
+
+    def measurements(self):
+        return self.ob.measurements()[None, :]
 
     def run(self, n):
         assert self.ob.step(n) == 0
@@ -97,16 +101,24 @@ def test_checkpoint_round_trip(tmp_path):
 
 
 def _restart_identity(make_world, tmp_path, solvers, check=5):
-    a_t, a_c = str(tmp_path / "a.ftj"), str(tmp_path / "a.fcp")
-    b_t, b_c = str(tmp_path / "b.ftj"), str(tmp_path / "b.fcp")
+    a_t, a_c, a_m = str(tmp_path / "a.ftj"), str(tmp_path / "a.fcp"), str(tmp_path / "a_measurement.out")
+    b_t, b_c, b_m = str(tmp_path / "b.ftj"), str(tmp_path / "b.fcp"), str(tmp_path / "b_measurement.out")
     wa = make_world()
-    T.Recorder(wa, a_t, a_c, solvers, check=check).run(2 * check)
+    T.Recorder(wa, a_t, a_c, solvers, check=check, measurement=a_m).run(2 * check)
     wb = make_world()
-    T.Recorder(wb, b_t, b_c, solvers, check=check).run(check)
+    T.Recorder(wb, b_t, b_c, solvers, check=check, measurement=b_m).run(check)
     wc = make_world()  # a fresh process's handle, continued from b's files
-    T.Recorder(wc, b_t, b_c, solvers, check=check, restart=True).run(check)
+    T.Recorder(wc, b_t, b_c, solvers, check=check, restart=True, measurement=b_m).run(check)
     # checkRuns.py:33-46: the final checkpoints are identical
     assert open(a_c).read() == open(b_c).read()
+    # checkRuns.py:48-84: the measurements agree to 5e-4 relative (every row
+    # here; the restart read positions and velocities at %e precision)
+    ma, mb = T.read_measurements(a_m), T.read_measurements(b_m)
+    assert list(ma) == list(mb) and len(ma["Time"]) == len(mb["Time"]) == 3
+    for k in ma:
+        a, b = ma[k], mb[k]
+        d = np.abs(b - a) / np.where(a == 0, 1.0, np.abs(a))
+        assert d.max() <= 5e-4, (k, a, b)
     # the same frames were written, and the final states agree to the
     # precision the trajectory stores positions with (checkRuns.py: 5e-4)
     sa, fa = T.read_last_frame(a_t, [wa.blob(0).n])
