@@ -765,6 +765,34 @@ template <> struct Vec4T<float> { using type = float4; };
 template <> struct Vec4T<double> { using type = Dbl4; };
 
 __device__ __forceinline__ float4 ldcg4(const float4 *p) { return __ldcg(p); }
+
+// Read-only loads of data streamed once per CG iteration (the matrix of the
+// memory-resident solve, larger than L2) with the L2 evict-first priority,
+// so that the vectors gathered and re-read every iteration keep their lines.
+__device__ __forceinline__ uint64_t l2_evict_first()
+{
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ float ld_stream(const float *p, uint64_t pol)
+{
+    float v;
+    asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ double ld_stream(const double *p, uint64_t pol)
+{
+    double v;
+    asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int ld_stream(const int *p, uint64_t pol)
+{
+    int v;
+    asm("ld.global.nc.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
 __device__ __forceinline__ Dbl4 ldcg4(const Dbl4 *p)
 {
     const double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
@@ -833,10 +861,11 @@ __device__ __forceinline__ void sell_row_cg(const DeviceBatch &d, int row, bool 
         // neighbours, so a group costs one memory round trip instead of two
         // (index, then neighbour).  Same slots, same FMA order: same bits.
         const T *val = static_cast<const T *>(d.sell_val);
+        const uint64_t pol = l2_evict_first();
         constexpr int G2 = 2;
         int cn[G2];
 #pragma unroll
-        for (int g = 0; g < G2; g++) cn[g] = g < L ? __ldg(&d.sell_col[base + 32 * g + lane]) : row;
+        for (int g = 0; g < G2; g++) cn[g] = g < L ? ld_stream(&d.sell_col[base + 32 * g + lane], pol) : row;
         for (int j0 = 0; j0 < L; j0 += G2) {
             typename Vec4T<T>::type y[G2];
             T K[G2][9];
@@ -847,9 +876,9 @@ __device__ __forceinline__ void sell_row_cg(const DeviceBatch &d, int row, bool 
                 y[g] = ldcg4(&u4[cn[g]]);
                 const size_t vb = (size_t)(base + 32 * j) * 9 + lane;
 #pragma unroll
-                for (int k = 0; k < 9; k++) K[g][k] = j < L ? __ldg(&val[vb + 32 * k]) : (T)0;
+                for (int k = 0; k < 9; k++) K[g][k] = j < L ? ld_stream(&val[vb + 32 * k], pol) : (T)0;
                 const int jn = j + G2;
-                nx[g] = jn < L ? __ldg(&d.sell_col[base + 32 * jn + lane]) : row;
+                nx[g] = jn < L ? ld_stream(&d.sell_col[base + 32 * jn + lane], pol) : row;
             }
 #pragma unroll
             for (int g = 0; g < G2; g++)
