@@ -96,6 +96,12 @@ SIGNATURES = {
     "ffea_gpu_mpnn_probe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32] + [ctypes.POINTER(ctypes.c_float)] * 5),
     "ffea_gpu_energies_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 5 + [ctypes.c_int32, ctypes.c_int32,
                                                                           ctypes.c_void_p, ctypes.c_void_p]),
+    "ffea_gpu_ssint_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "ffea_gpu_ssint_destroy": (None, [ctypes.c_void_p]),
+    "ffea_gpu_ssint_forces": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int64)]),
+    "ffea_gpu_ssint_forces_device": (ctypes.c_int, [ctypes.c_void_p] * 4),
+    "ffea_gpu_ssint_synchronize": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "ffea_gpu_ssint_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
 }
 
 _lib = None

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT_DIR, "libffea_gb300.so")
-SOURCES = ["kernels.cu", "api.cu", "host_build.cpp", "noalloc.cu", "coarse.cu", "learned.cu"]
+SOURCES = ["kernels.cu", "api.cu", "host_build.cpp", "noalloc.cu", "coarse.cu", "learned.cu", "ssint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -29,6 +29,9 @@ def nvcc() -> str:
 
 def _flags(src: str) -> list[str]:
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing", "-lineinfo"]
+    if src.endswith("ssint.cu"):
+        # products and sums round as in the reference's FP64 code (no FMA contraction)
+        return common + ARCH + ["-Xptxas", "-O3", "-fmad=false"]
     if src.endswith(".cu"):
         return common + ARCH + ["-Xptxas", "-O3"]
     return common + ["-x", "cu"] + ARCH

@@ -201,6 +201,54 @@ int ffea_gpu_rng_draws(const uint64_t state[6], uint64_t offset, int64_t count, 
 /* World::init's six seed words for an rng_seed (src/World.cpp:299-305). */
 int ffea_gpu_ffea_seed(int32_t rng_seed, uint64_t out[6]);
 
+/* --- surface-surface interactions (Lennard-Jones) ------------------------- */
+
+/* Replaces VdW_solver (include/VdW_solver.h:36-127; VdW_solver::init,
+ * src/VdW_solver.cpp:124-157, and ::solve, :168-210) for
+ * "vdw_type = lennard-jones", with the nearest-neighbour grid it walks
+ * (NearestNeighbourLinkedListCube, src/NearestNeighbourLinkedListCube.cpp:27-76)
+ * and the aggregation of face forces onto nodes (src/Blob.cpp:3841-3851).
+ * The resulting node forces enter the blob update through
+ * ffea_gpu_set_external_forces. */
+#define FFEA_GPU_SSINT_MAX_CELLS (1 << 26)
+
+typedef struct ffea_gpu_ssint ffea_gpu_ssint_t;
+
+typedef struct {
+    int32_t num_nodes;        /* nodes of all blobs, one numbering (e.g. blobs concatenated) */
+    int32_t num_faces;        /* surface faces of all blobs, in FFEA's pool order (blob, then face) */
+    const int32_t *faces;     /* 3 corner node indices per face (Face::n[0..2]) */
+    const int32_t *face_blob; /* blob index per face (Face::daddy_blob->blob_index) */
+    const int32_t *face_type; /* interaction type per face; -1 = not active (Blob::get_face) */
+    int32_t num_types;        /* SSINT_matrix::num_ssint_face_types */
+    const double *emin;       /* num_types^2, meso energy / area^2 (src/LJ_matrix.cpp:141) */
+    const double *rmin;       /* num_types^2, meso length (src/LJ_matrix.cpp:142) */
+    int32_t num_blobs;
+    double cell_size;         /* SimulationParams::ssint_cutoff */
+    int32_t nx, ny, nz;       /* SimulationParams::es_N_x/y/z; nx*ny*nz <= FFEA_GPU_SSINT_MAX_CELLS */
+    int32_t inc_self;         /* SimulationParams::inc_self_ssint */
+} ffea_gpu_ssint_desc;
+
+/* Copies the face lists and parameters to the device (VdW_solver::init and
+ * World::init's pool set-up, src/World.cpp:925-960). */
+int ffea_gpu_ssint_create(const ffea_gpu_ssint_desc *desc, ffea_gpu_ssint_t **out);
+void ffea_gpu_ssint_destroy(ffea_gpu_ssint_t *s);
+
+/* One VdW_solver::solve on HOST arrays: pos (3*num_nodes) in, force
+ * (3*num_nodes, the surface forces alone, overwritten) and energy
+ * (num_blobs^2, VdW_solver::fieldenergy[blob of f1][blob of f2]) out;
+ * pairs (may be NULL) receives the number of interacting face pairs.  A
+ * face centroid outside the grid after one periodic wrap is an error, as in
+ * LinkedListCube::add_node_to_stack (src/LinkedListCube.tpp:217-235). */
+int ffea_gpu_ssint_forces(ffea_gpu_ssint_t *s, const double *pos, double *force, double *energy, int64_t *pairs);
+
+/* The same on DEVICE arrays, enqueued on the handle's stream without
+ * waiting; ffea_gpu_ssint_synchronize waits, reports the pair count and
+ * returns the out-of-grid error of that call. */
+int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *pos, double *force, double *energy);
+int ffea_gpu_ssint_synchronize(ffea_gpu_ssint_t *s, int64_t *pairs);
+void *ffea_gpu_ssint_stream(ffea_gpu_ssint_t *s);
+
 /* --- allocation-free measurement ------------------------------------------ */
 
 /* Strain and kinetic energy of one blob, like ffea_gpu_energies, for callers

@@ -260,3 +260,32 @@ def blob_from_spec(spec, impl="port", num_threads=1, epsilon2=None, seed=True):
     if seed:
         b.seed(p.rng_seed)
     return b
+
+
+# ---------------------------------------------------------------- surface interactions
+def ssint_lj(pos, faces, face_blob, face_type, emin, rmin, num_blobs, h, grid, inc_self=0):
+    """FFEA's surface-surface Lennard-Jones pass (oracle/ssint_oracle.c, which
+    cites src/VdW_solver.cpp).  pos: (N, 3) FP64; faces: (F, 3) node indices;
+    emin, rmin: (T, T) in meso units; grid: (nx, ny, nz) cells of size h.
+    Returns (node_force (N, 3), energy (num_blobs, num_blobs), interacting pairs)."""
+    lib = port_lib()
+    fn = lib.oracle_ssint_lj
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, _ip, ctypes.c_int, _dp, _dp, ctypes.c_int,
+                   ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                   ctypes.POINTER(ctypes.c_longlong)]
+    pos = np.ascontiguousarray(pos, np.float64)
+    faces = np.ascontiguousarray(faces, np.int32)
+    face_blob = np.ascontiguousarray(face_blob, np.int32)
+    face_type = np.ascontiguousarray(face_type, np.int32)
+    emin = np.ascontiguousarray(emin, np.float64)
+    rmin = np.ascontiguousarray(rmin, np.float64)
+    force = np.zeros((len(pos), 3))
+    energy = np.zeros((num_blobs, num_blobs))
+    pairs = ctypes.c_longlong(0)
+    rc = fn(len(pos), _ptr(pos, _dp), len(faces), _ptr(faces, _ip), _ptr(face_blob, _ip), _ptr(face_type, _ip),
+            emin.shape[0], _ptr(emin, _dp), _ptr(rmin, _dp), num_blobs, float(h), int(grid[0]), int(grid[1]),
+            int(grid[2]), int(inc_self), _ptr(force, _dp), _ptr(energy, _dp), ctypes.byref(pairs))
+    if rc != 0:
+        raise ValueError("a face centroid lies outside the interaction grid")
+    return force, energy, int(pairs.value)

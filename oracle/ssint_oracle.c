@@ -1,0 +1,212 @@
+/* ssint_oracle.c -- CPU restatement of FFEA's surface-surface Lennard-Jones
+ * interaction ("vdw_type = lennard-jones"), for tests only.
+ *
+ * This is test infrastructure: the tests and the bench's CPU leg call it as
+ * the checker of the GPU kernels in ffea_gb300/csrc/ssint.cu.  Nothing in the
+ * product links it.
+ *
+ * It follows one single-threaded pass of VdW_solver::solve
+ * (src/VdW_solver.cpp:168-210) over the nearest-neighbour grid that
+ * NearestNeighbourLinkedListCube::build_nearest_neighbour_lookup builds
+ * (src/NearestNeighbourLinkedListCube.cpp:27-76), in FFEA's own order:
+ *   - faces of interaction type -1 are not in the pool (Blob::get_face,
+ *     src/Blob.cpp:1642-1648; World::init adds the rest in blob / face order,
+ *     src/World.cpp:940-958);
+ *   - a face's cell is floor(centroid / h) per axis, wrapped once into the box
+ *     (LinkedListCube::pbc, src/LinkedListCube.tpp:284-301); a centroid still
+ *     outside after the wrap is an error (add_node_to_stack, :217-235);
+ *   - each cell is a stack: the face added last is visited first (:228-233);
+ *   - face i visits the 27 cells around its own (adjacent_cell_lookup_table,
+ *     src/VdW_solver.cpp:31-59) and interacts with face j when i < j in pool
+ *     order, the blobs differ unless self-interaction is on, and the unit
+ *     normals do not face the same way (consider_interaction, :338-394; the
+ *     in-front and shared-node checks apply to the other ssint types only);
+ *   - do_lj_interaction (:237-330) integrates the LJ force over both
+ *     triangles with the 3-point Gauss rule (:61-71), calc_lj_force_pair_matrix
+ *     and calc_lj_factors (:664-699, :736-752);
+ *   - face geometry is Face::calc_area_normal_centroid (src/Face.cpp:197-219)
+ *     and barycentric_calc_point (:265-269);
+ *   - face forces go onto nodes in face order (Blob::aggregate_forces_and_solve,
+ *     src/Blob.cpp:3841-3851).
+ * The reference's VdW_solver cannot be compiled here (its header includes
+ * Blob.h, which needs Eigen, absent from the image); the restatement is pinned
+ * to the reference's own known answer instead: the LJ energy of two parallel
+ * unit-cube faces 1 nm apart (tests/physics/cubes_lj/checkE.py, -1.7870e-19 J
+ * within 1 %).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* 3-point rule on a triangle, the constants of src/VdW_solver.cpp:61-71 */
+static const double kW = 0.333333333333333;
+static const double kEta[3][3] = {{0.666666666666667, 0.166666666666667, 0.166666666666667},
+                                  {0.166666666666667, 0.666666666666667, 0.166666666666667},
+                                  {0.166666666666667, 0.166666666666667, 0.666666666666667}};
+
+typedef struct {
+    int face;              /* index into the caller's face list */
+    double v[3][3];        /* corner positions */
+    double normal[3], area;
+    int x, y, z;           /* cell */
+} pool_face;
+
+static void lj_factors(double mag_r, double emin, double rmin6, double *force_mag, double *e)
+{
+    double ri = 1. / mag_r;
+    double ri2 = ri * ri;
+    double ri4 = ri2 * ri2;
+    double ri6 = ri4 * ri2;
+    double ri7 = ri6 * ri;
+    double f6 = rmin6 * ri6;
+    *force_mag = 12 * ri7 * rmin6 * emin * (f6 - 1);
+    *e = kW * kW * emin * f6 * (f6 - 2);
+}
+
+/* do_lj_interaction for faces a (f1) and b (f2); adds to fa[3][3], fb[3][3]
+ * and returns the pair energy (already multiplied by the areas). */
+static double lj_pair(const pool_face *a, const pool_face *b, double emin, double rmin, double fa[3][3],
+                      double fb[3][3])
+{
+    double p[3][3], q[3][3], fpm[3][3][3];
+    for (int k = 0; k < 3; k++)
+        for (int d = 0; d < 3; d++) {
+            p[k][d] = kEta[k][0] * a->v[0][d] + kEta[k][1] * a->v[1][d] + kEta[k][2] * a->v[2][d];
+            q[k][d] = kEta[k][0] * b->v[0][d] + kEta[k][1] * b->v[1][d] + kEta[k][2] * b->v[2][d];
+        }
+    double r2 = rmin * rmin;
+    double r4 = r2 * r2;
+    double r6 = r4 * r2;
+    double energy = 0.0, fm, e;
+    for (int k = 0; k < 3; k++) {
+        double dx = p[k][0] - q[k][0], dy = p[k][1] - q[k][1], dz = p[k][2] - q[k][2];
+        double mag_r = sqrt(dx * dx + dy * dy + dz * dz);
+        lj_factors(mag_r, emin, r6, &fm, &e);
+        energy += e;
+        for (int d = 0; d < 3; d++) fpm[k][k][d] = fm * ((p[k][d] - q[k][d]) / mag_r);
+        for (int l = k + 1; l < 3; l++) {
+            dx = p[k][0] - q[l][0];
+            dy = p[k][1] - q[l][1];
+            dz = p[k][2] - q[l][2];
+            mag_r = sqrt(dx * dx + dy * dy + dz * dz);
+            lj_factors(mag_r, emin, r6, &fm, &e);
+            energy += 2 * e;
+            for (int d = 0; d < 3; d++) {
+                fpm[k][l][d] = fm * ((p[k][d] - q[l][d]) / mag_r);
+                fpm[l][k][d] = fpm[k][l][d];
+            }
+        }
+    }
+    double apaq = a->area * b->area;
+    energy *= apaq;
+    for (int j = 0; j < 3; j++) {
+        double f1[3] = {0, 0, 0}, f2[3] = {0, 0, 0};
+        for (int k = 0; k < 3; k++)
+            for (int l = 0; l < 3; l++) {
+                double c = kW * kW * kEta[l][j];
+                double dd = kW * kW * kEta[k][j];
+                for (int d = 0; d < 3; d++) {
+                    f1[d] += c * fpm[k][l][d];
+                    f2[d] -= dd * fpm[l][k][d];
+                }
+            }
+        for (int d = 0; d < 3; d++) {
+            fa[j][d] += f1[d] * apaq;
+            fb[j][d] += f2[d] * apaq;
+        }
+    }
+    return energy;
+}
+
+/* Returns 0, or -1 when a face centroid lies outside the box after the
+ * single wrap (FFEA reports the same as an error). node_force: num_nodes x 3,
+ * overwritten with the surface forces alone; energy: num_blobs x num_blobs,
+ * overwritten (VdW_solver::fieldenergy, [blob of f1][blob of f2]).
+ * pairs_out (may be NULL): the number of face pairs that interacted. */
+int oracle_ssint_lj(int num_nodes, const double *pos, int num_faces, const int *faces, const int *face_blob,
+                    const int *face_type, int num_types, const double *emin, const double *rmin, int num_blobs,
+                    double h, int nx, int ny, int nz, int inc_self, double *node_force, double *energy,
+                    long long *pairs_out)
+{
+    static const int adj[27][3] = {{-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {-1, 0, -1}, {-1, 0, 0}, {-1, 0, 1},
+                                   {-1, 1, -1},  {-1, 1, 0},  {-1, 1, 1},  {0, -1, -1}, {0, -1, 0}, {0, -1, 1},
+                                   {0, 0, -1},   {0, 0, 0},   {0, 0, 1},   {0, 1, -1},  {0, 1, 0},  {0, 1, 1},
+                                   {1, -1, -1},  {1, -1, 0},  {1, -1, 1},  {1, 0, -1},  {1, 0, 0},  {1, 0, 1},
+                                   {1, 1, -1},   {1, 1, 0},   {1, 1, 1}};
+    int np = 0;
+    pool_face *pool = (pool_face *)malloc(sizeof(pool_face) * (size_t)(num_faces > 0 ? num_faces : 1));
+    double (*fforce)[3][3] = calloc((size_t)(num_faces > 0 ? num_faces : 1), sizeof(double[3][3]));
+    long ncell = (long)nx * ny * nz;
+    int *root = (int *)malloc(sizeof(int) * (size_t)ncell);
+    int *next = (int *)malloc(sizeof(int) * (size_t)(num_faces > 0 ? num_faces : 1));
+    int rc = 0;
+    for (long c = 0; c < ncell; c++) root[c] = -1;
+    memset(energy, 0, sizeof(double) * (size_t)num_blobs * num_blobs);
+    memset(node_force, 0, sizeof(double) * 3 * (size_t)num_nodes);
+    for (int f = 0; f < num_faces; f++) {
+        if (face_type[f] < 0) continue;
+        pool_face *P = &pool[np];
+        P->face = f;
+        for (int i = 0; i < 3; i++)
+            for (int d = 0; d < 3; d++) P->v[i][d] = pos[3 * faces[3 * f + i] + d];
+        double a[3], b[3], n[3];
+        for (int d = 0; d < 3; d++) {
+            a[d] = P->v[1][d] - P->v[0][d];
+            b[d] = P->v[2][d] - P->v[0][d];
+        }
+        n[0] = a[1] * b[2] - a[2] * b[1];
+        n[1] = a[2] * b[0] - a[0] * b[2];
+        n[2] = a[0] * b[1] - a[1] * b[0];
+        double mag = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        P->area = .5 * mag;
+        for (int d = 0; d < 3; d++) P->normal[d] = n[d] / mag;
+        double cen[3];
+        for (int d = 0; d < 3; d++) cen[d] = (1.0 / 3.0) * (P->v[0][d] + P->v[1][d] + P->v[2][d]);
+        int cx = (int)floor(cen[0] / h), cy = (int)floor(cen[1] / h), cz = (int)floor(cen[2] / h);
+        if (cx < 0) cx += nx; else if (cx >= nx) cx -= nx;
+        if (cy < 0) cy += ny; else if (cy >= ny) cy -= ny;
+        if (cz < 0) cz += nz; else if (cz >= nz) cz -= nz;
+        if (cx < 0 || cx >= nx || cy < 0 || cy >= ny || cz < 0 || cz >= nz) {
+            rc = -1;
+            goto done;
+        }
+        P->x = cx;
+        P->y = cy;
+        P->z = cz;
+        long cell = ((long)cx * ny + cy) * nz + cz;
+        next[np] = root[cell];
+        root[cell] = np;
+        np++;
+    }
+    long long pairs = 0;
+    for (int i = 0; i < np; i++) {
+        const pool_face *A = &pool[i];
+        for (int c = 0; c < 27; c++) {
+            int x = A->x + adj[c][0], y = A->y + adj[c][1], z = A->z + adj[c][2];
+            if (x < 0) x += nx; else if (x >= nx) x -= nx;
+            if (y < 0) y += ny; else if (y >= ny) y -= ny;
+            if (z < 0) z += nz; else if (z >= nz) z -= nz;
+            for (int j = root[((long)x * ny + y) * nz + z]; j >= 0; j = next[j]) {
+                if (!(i < j)) continue;
+                const pool_face *B = &pool[j];
+                int ba = face_blob[A->face], bb = face_blob[B->face];
+                if (!inc_self && ba == bb) continue;
+                if (A->normal[0] * B->normal[0] + A->normal[1] * B->normal[1] + A->normal[2] * B->normal[2] > 0.0)
+                    continue;
+                int t = face_type[A->face] * num_types + face_type[B->face];
+                energy[ba * num_blobs + bb] += lj_pair(A, B, emin[t], rmin[t], fforce[i], fforce[j]);
+                pairs++;
+            }
+        }
+    }
+    for (int i = 0; i < np; i++)
+        for (int k = 0; k < 3; k++)
+            for (int d = 0; d < 3; d++) node_force[3 * faces[3 * pool[i].face + k] + d] += fforce[i][k][d];
+    if (pairs_out) *pairs_out = pairs;
+done:
+    free(pool);
+    free(fforce);
+    free(root);
+    free(next);
+    return rc;
+}

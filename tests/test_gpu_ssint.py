@@ -1,0 +1,163 @@
+"""Surface-surface LJ interaction on the GPU (ffea_gpu_ssint_*, through the C
+ABI) against the oracle (oracle/ssint_oracle.c, a restatement of FFEA's
+VdW_solver for "lennard-jones").
+
+Tolerances: the kernels are compiled without FMA contraction, so cell binning,
+the normal test and every pair's arithmetic match the oracle's; the pair
+counts must be equal exactly.  Per-face sums run in another order than FFEA's
+(each pair from both sides), and the energy is summed with atomics, so forces
+agree to 1e-12 of the largest force and energies to 1e-12 relative."""
+import os
+import time
+
+import numpy as np
+import pytest
+
+from ffea_gb300.params import MESO_ENERGY, nm
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "cubes_lj.npz")
+FORCE_TOL = 1e-12
+ENERGY_TOL = 1e-12
+
+
+def _solver(**kw):
+    from ffea_gb300.surface import LJSurfaceSolver
+    return LJSurfaceSolver(**kw)
+
+
+def _compare(kw, pos):
+    s = _solver(**kw)
+    f_gpu, e_gpu, p_gpu = s.forces(pos)
+    f_ref, e_ref, p_ref = oracle.ssint_lj(pos, kw["faces"], kw["face_blob"], kw["face_type"], kw["emin"], kw["rmin"],
+                                          kw["num_blobs"], kw["cell_size"], kw["grid"], kw.get("inc_self", 0))
+    assert p_gpu == p_ref
+    scale = max(np.abs(f_ref).max(), 1e-300)
+    np.testing.assert_allclose(f_gpu, f_ref, rtol=0, atol=FORCE_TOL * scale)
+    np.testing.assert_allclose(e_gpu, e_ref, rtol=ENERGY_TOL, atol=ENERGY_TOL * np.abs(e_ref).max())
+    s.close()
+    return f_gpu, e_gpu, p_gpu
+
+
+def _cubes_kw(g, **over):
+    kw = dict(num_nodes=len(g["pos"]), faces=g["faces"], face_blob=g["face_blob"], face_type=g["face_type"],
+              emin=g["emin"], rmin=g["rmin"], num_blobs=2, cell_size=float(g["h"]), grid=tuple(g["grid"]))
+    kw.update(over)
+    return kw
+
+
+def test_cubes_lj_known_answer_and_golden():
+    g = dict(np.load(GOLDEN))
+    f, e, p = _compare(_cubes_kw(g), g["pos"])
+    assert p == int(g["pairs"])
+    np.testing.assert_allclose(f, g["force"], rtol=0, atol=FORCE_TOL * np.abs(g["force"]).max())
+    e_j = e.sum() * MESO_ENERGY
+    assert abs(e_j - g["known_energy_j"]) <= g["known_tol"] * abs(g["known_energy_j"])
+
+
+def test_cubes_lj_every_face_active_and_self_interaction():
+    g = dict(np.load(GOLDEN))
+    rng = np.random.default_rng(3)
+    ftype = rng.integers(0, 3, len(g["face_type"])).astype(np.int32)
+    ftype[rng.random(len(ftype)) < 0.1] = -1  # some faces inactive
+    pos = g["pos"] + rng.normal(0, 0.02 * nm(1.0), g["pos"].shape)
+    _compare(_cubes_kw(g, face_type=ftype, inc_self=1), pos)
+
+
+def test_small_grid_wrapped_neighbour_cells():
+    g = dict(np.load(GOLDEN))
+    h = float(g["h"]) * 5
+    pos = g["pos"] - g["pos"].mean(0) + h
+    _, _, p = _compare(_cubes_kw(g, cell_size=h, grid=(2, 2, 2)), pos)
+    assert p > 200 * 200
+
+
+def _two_spheres(radius_nm, gap_nm, seed):
+    from ffea_gb300.mesh import sphere_mesh
+    from ffea_gb300.surface import surface_faces
+    m = sphere_mesh(radius_nm, seed=seed)
+    tri = surface_faces(m.pos, m.topology)
+    x = m.pos - m.pos.mean(0)
+    shift = np.array([2 * nm(radius_nm) + nm(gap_nm), 0.0, 0.0])
+    pos = np.concatenate([x, x + shift])
+    n = len(x)
+    faces = np.concatenate([tri, tri + n]).astype(np.int32)
+    blob = np.repeat(np.arange(2, dtype=np.int32), len(tri))
+    h = nm(3.0)
+    span = pos.max(0) - pos.min(0)
+    grid = tuple(int(v) for v in 2 * np.ceil(span / h))  # World::init's box (src/World.cpp:455-466)
+    pos = pos - pos.mean(0) + 0.5 * h * np.array(grid)
+    return pos, faces, blob, grid, h
+
+
+def test_two_spheres_in_contact_with_self_interaction():
+    pos, faces, blob, grid, h = _two_spheres(4.0, 0.6, seed=5)
+    rng = np.random.default_rng(7)
+    T = 2
+    emin = rng.uniform(0.5, 2.0, (T, T))
+    emin = 0.5 * (emin + emin.T)
+    rmin = np.full((T, T), nm(1.0))
+    ftype = rng.integers(0, T, len(faces)).astype(np.int32)
+    kw = dict(num_nodes=len(pos), faces=faces, face_blob=blob, face_type=ftype, emin=emin, rmin=rmin,
+              num_blobs=2, cell_size=h, grid=grid, inc_self=1)
+    f, e, p = _compare(kw, pos)
+    assert p > 0 and e[0, 1] != 0
+
+
+def test_centroid_outside_the_grid_is_an_error_and_the_handle_recovers():
+    from ffea_gb300._lib import FfeaGpuError
+    g = dict(np.load(GOLDEN))
+    s = _solver(**_cubes_kw(g))
+    bad = g["pos"].copy()
+    bad[:, 0] += 3 * float(g["h"]) * g["grid"][0]
+    with pytest.raises(FfeaGpuError, match="outside the interaction grid"):
+        s.forces(bad)
+    f, e, p = s.forces(g["pos"])
+    assert p == int(g["pairs"])
+    s.close()
+
+
+def test_no_active_faces_gives_zero():
+    g = dict(np.load(GOLDEN))
+    s = _solver(**_cubes_kw(g, face_type=np.full(len(g["face_type"]), -1, np.int32)))
+    f, e, p = s.forces(g["pos"])
+    assert p == 0 and not f.any() and not e.any()
+    s.close()
+
+
+def test_throughput_two_20nm_spheres(capsys):
+    """Device-resident timing of one solve (face geometry, grid, pairs, node
+    gather) for two 20 nm spheres 0.6 nm apart; printed, not asserted."""
+    import torch
+    pos, faces, blob, grid, h = _two_spheres(20.0, 0.6, seed=11)
+    kw = dict(num_nodes=len(pos), faces=faces, face_blob=blob, face_type=np.zeros(len(faces), np.int32),
+              emin=np.ones((1, 1)), rmin=np.full((1, 1), nm(1.0)), num_blobs=2, cell_size=h, grid=grid, inc_self=1)
+    s = _solver(**kw)
+    d_pos = torch.tensor(pos, device="cuda")
+    d_f = torch.zeros_like(d_pos)
+    d_e = torch.zeros(4, dtype=torch.float64, device="cuda")
+    st = torch.cuda.ExternalStream(s.stream)
+    for _ in range(3):
+        s.forces_device(d_pos.data_ptr(), d_f.data_ptr(), d_e.data_ptr())
+    pairs = s.synchronize()
+    reps = 20
+    with torch.cuda.stream(st):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        for _ in range(reps):
+            s.forces_device(d_pos.data_ptr(), d_f.data_ptr(), d_e.data_ptr())
+        b.record(st)
+    s.synchronize()
+    ms = a.elapsed_time(b) / reps
+    t0 = time.perf_counter()
+    oracle.ssint_lj(pos, faces, blob, kw["face_type"], kw["emin"], kw["rmin"], 2, h, grid, 1)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    with capsys.disabled():
+        print(f"\nssint two 20 nm spheres: {len(faces)} faces, {pairs} pairs, GPU {ms * 1e3:.1f} us/solve "
+              f"({pairs / ms * 1e-6:.3f} G pairs/s; each pair evaluated from both sides), "
+              f"oracle 1 core {cpu_ms:.1f} ms")
+    f_ref, _, _ = oracle.ssint_lj(pos, faces, blob, kw["face_type"], kw["emin"], kw["rmin"], 2, h, grid, 1)
+    np.testing.assert_allclose(d_f.cpu().numpy(), f_ref, rtol=0, atol=FORCE_TOL * np.abs(f_ref).max())
+    s.close()

@@ -64,7 +64,8 @@ def test_jump_equals_sequential(oracle):
 
 
 def _golden_cases():
-    return sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+    # blob-update step goldens; cubes_lj.npz (surface interactions) has its own tests
+    return sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz")) if not p.endswith("cubes_lj.npz"))
 
 
 @pytest.mark.parametrize("path", _golden_cases(), ids=lambda p: os.path.basename(p)[:-4])
