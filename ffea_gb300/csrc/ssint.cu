@@ -15,10 +15,11 @@
 //   2. k_scan_local / k_scan_blocks   exclusive scan of the cell counts.
 //   3. k_scatter     places every face in its cell's segment.
 //   4. k_sort_cells  sorts each segment by face index (deterministic order).
-//   5. k_pairs       one thread per face, in cell order so that neighbouring
-//                    threads read the same cells: walks the 27 cells around
-//                    its own and integrates the LJ force of every partner the
-//                    reference would pair with it.  A pair (i, j) is evaluated
+//   5. k_pairs       one warp per face, in cell order so that neighbouring
+//                    warps read the same cells: the lanes share the faces of
+//                    the 27 cells around its own and integrate the LJ force
+//                    of every partner the reference would pair with it; a
+//                    fixed shuffle tree sums the lanes.  A pair (i, j) is evaluated
 //                    from both sides, each side keeping only its own face's
 //                    forces: twice the arithmetic of one evaluation, but no
 //                    atomics on forces and a fixed summation order.  The pair
@@ -28,7 +29,10 @@
 //                    face order (a CSR built at creation).
 // The file is compiled with -fmad=false so that every product and sum rounds
 // as in the reference's FP64 code; cell binning and the normal test then
-// decide exactly as FFEA does.
+// decide exactly as FFEA does.  One deliberate difference: the unit direction
+// of each point pair is (p - q) * (1/r) where FFEA divides by r, which saves
+// three FP64 divides per point pair (the kernel is bound by the FP64 pipe)
+// and changes each component by at most one rounding.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -294,7 +298,7 @@ __device__ __forceinline__ double lj_pair(const double *A, const double *B, doub
             energy += (l == k) ? e : 2 * e;
 #pragma unroll
             for (int d = 0; d < 3; d++) {
-                fpm[k][l][d] = fm * ((p[k][d] - q[l][d]) / mag_r);
+                fpm[k][l][d] = fm * ((p[k][d] - q[l][d]) * ri);  // FFEA divides by mag_r: within 1 ulp
                 fpm[l][k][d] = fpm[k][l][d];
             }
         }
@@ -327,21 +331,51 @@ __constant__ int c_adj[27][3] = {{-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {-1, 0,
                                  {1, -1, -1},  {1, -1, 0},  {1, -1, 1},  {1, 0, -1},  {1, 0, 0},  {1, 0, 1},
                                  {1, 1, -1},   {1, 1, 0},   {1, 1, 1}};
 
-__global__ void __launch_bounds__(128) k_pairs(const double *__restrict__ geo, const int *__restrict__ cell,
-                                               const int *__restrict__ sorted,
-                                               const int *__restrict__ start, const int *__restrict__ block,
-                                               long long ncell, int nblocks, int nx, int ny, int nz,
-                                               const int *__restrict__ fblob, const int *__restrict__ ftype,
-                                               const double *__restrict__ emin, const double *__restrict__ rmin,
-                                               int num_types, int num_blobs, int inc_self,
-                                               double *__restrict__ fforce, double *__restrict__ energy,
-                                               unsigned long long *stats)
+constexpr int kPairWarps = 8;  // warps (faces) per CTA of k_pairs
+
+__device__ __forceinline__ double warp_sum_d(double v)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= block[nblocks]) return;  // faces outside the box are not binned
-    const int i = sorted[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One warp per face i (faces taken in cell order): the candidates of the 27
+// cells around i's cell are numbered 0..total-1 through a prefix sum over the
+// cells, lane l tests candidates l, l + 32, ..., and the partners that pass
+// are evaluated from a per-warp queue.  Each lane keeps face i's side of its
+// pairs; a fixed shuffle tree sums the lanes.
+__global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
+    const double *__restrict__ geo, const int *__restrict__ cell, const int *__restrict__ sorted,
+    const int *__restrict__ start, const int *__restrict__ block, long long ncell, int nblocks, int nx, int ny,
+    int nz, const int *__restrict__ fblob, const int *__restrict__ ftype, const double *__restrict__ emin,
+    const double *__restrict__ rmin, int num_types, int num_blobs, int inc_self, double *__restrict__ fforce,
+    double *__restrict__ energy, unsigned long long *stats)
+{
+    __shared__ int s_pre[kPairWarps][28];
+    __shared__ int s_beg[kPairWarps][27];
+    __shared__ int s_q[kPairWarps][64];
+    const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long w = (long long)blockIdx.x * kPairWarps + wi;
+    if (w >= block[nblocks]) return;  // warp-uniform; faces outside the box are not binned
+    const int i = sorted[w];
     const int ci = cell[i];
     const int cz = ci % nz, cy = (ci / nz) % ny, cx = ci / (nz * ny);
+    int len = 0, beg = 0;
+    if (lane < 27) {
+        const int x = wrap(cx + c_adj[lane][0], nx), y = wrap(cy + c_adj[lane][1], ny),
+                  z = wrap(cz + c_adj[lane][2], nz);
+        const long long cc = ((long long)x * ny + y) * nz + z;
+        beg = cell_begin(start, block, cc);
+        len = cell_end(start, block, cc, ncell, nblocks) - beg;
+    }
+    const int incl = warp_incl_scan(len, lane);
+    if (lane < 27) {
+        s_beg[wi][lane] = beg;
+        s_pre[wi][lane] = incl - len;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 26);
+    __syncwarp();
     double A[13];
 #pragma unroll
     for (int k = 0; k < 13; k++) A[k] = geo[16 * (long long)i + k];
@@ -350,44 +384,82 @@ __global__ void __launch_bounds__(128) k_pairs(const double *__restrict__ geo, c
     double e_acc = 0.0;
     int e_key = -1;
     unsigned long long npairs = 0;
-    for (int c = 0; c < 27; c++) {
-        const int x = wrap(cx + c_adj[c][0], nx), y = wrap(cy + c_adj[c][1], ny), z = wrap(cz + c_adj[c][2], nz);
-        const long long cc = ((long long)x * ny + y) * nz + z;
-        const int b = cell_begin(start, block, cc);
-        const int e = cell_end(start, block, cc, ncell, nblocks);
-        for (int s = b; s < e; s++) {
-            const int j = sorted[s];
-            if (j == i) continue;
-            const int bj = fblob[j];
-            if (!inc_self && bi == bj) continue;
-            const double *G = geo + 16 * (long long)j;
-            if (A[9] * G[9] + A[10] * G[10] + A[11] * G[11] > 0.0) continue;
-            double B[13];
+    // one partner j: face i's side of the pair, FFEA's f1 being the lower index
+    auto pair = [&](int j) {
+        const double *G = geo + 16 * (long long)j;
+        double B[13];
 #pragma unroll
-            for (int k = 0; k < 13; k++) B[k] = G[k];
-            if (i < j) {
-                const int tt = ti * num_types + ftype[j];
-                const double en = lj_pair<true>(A, B, emin[tt], rmin[tt], out);
-                const int key = bi * num_blobs + bj;
-                if (key != e_key) {
-                    if (e_key >= 0) atomicAdd(&energy[e_key], e_acc);
-                    e_key = key;
-                    e_acc = 0.0;
-                }
-                e_acc += en;
-                npairs++;
-            } else {
-                const int tt = ftype[j] * num_types + ti;
-                lj_pair<false>(B, A, emin[tt], rmin[tt], out);
+        for (int q = 0; q < 13; q++) B[q] = G[q];
+        if (i < j) {
+            const int tt = ti * num_types + ftype[j];
+            const double en = lj_pair<true>(A, B, emin[tt], rmin[tt], out);
+            const int key = bi * num_blobs + fblob[j];
+            if (key != e_key) {
+                if (e_key >= 0) atomicAdd(&energy[e_key], e_acc);
+                e_key = key;
+                e_acc = 0.0;
             }
+            e_acc += en;
+            npairs++;
+        } else {
+            const int tt = ftype[j] * num_types + ti;
+            lj_pair<false>(B, A, emin[tt], rmin[tt], out);
+        }
+    };
+    // The cheap tests (same face, same blob, normals facing the same way) run
+    // over all candidates; the partners that pass are queued in shared memory
+    // and evaluated 32 at a time, so every lane of the FP64 pair arithmetic
+    // does useful work.
+    int qn = 0;  // warp-uniform queue length, < 64
+    for (int base = 0; base < total; base += 32) {
+        const int k = base + lane;
+        bool ok = false;
+        int j = -1;
+        if (k < total) {
+            int c = 0;
+            while (c < 26 && s_pre[wi][c + 1] <= k) c++;
+            j = sorted[s_beg[wi][c] + (k - s_pre[wi][c])];
+            const double *G = geo + 16 * (long long)j;
+            ok = j != i && (inc_self || bi != fblob[j]) && !(A[9] * G[9] + A[10] * G[10] + A[11] * G[11] > 0.0);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        if (ok) s_q[wi][qn + __popc(m & ((1u << lane) - 1u))] = j;
+        qn += __popc(m);
+        __syncwarp();
+        if (qn >= 32) {
+            pair(s_q[wi][lane]);
+            const int rest = qn - 32;
+            const int moved = lane < rest ? s_q[wi][32 + lane] : 0;
+            __syncwarp();
+            if (lane < rest) s_q[wi][lane] = moved;
+            qn = rest;
+            __syncwarp();
         }
     }
-    if (e_key >= 0) atomicAdd(&energy[e_key], e_acc);
-    if (npairs) atomicAdd(&stats[0], npairs);
+    if (lane < qn) pair(s_q[wi][lane]);
+    // energy: one atomic per distinct (blob, blob) key left in the warp
+    for (;;) {
+        const unsigned pending = __ballot_sync(0xffffffffu, e_key >= 0);
+        if (!pending) break;
+        const int lk = __shfl_sync(0xffffffffu, e_key, __ffs(pending) - 1);
+        const double part = warp_sum_d(e_key == lk ? e_acc : 0.0);
+        if (lane == 0) atomicAdd(&energy[lk], part);
+        if (e_key == lk) e_key = -1;
+    }
 #pragma unroll
     for (int k = 0; k < 3; k++)
 #pragma unroll
-        for (int d = 0; d < 3; d++) fforce[9 * (long long)i + 3 * k + d] = out[k][d];
+        for (int d = 0; d < 3; d++) out[k][d] = warp_sum_d(out[k][d]);
+    unsigned long long np = npairs;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) np += __shfl_xor_sync(0xffffffffu, np, o);
+    if (lane == 0) {
+        if (np) atomicAdd(&stats[0], np);
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int d = 0; d < 3; d++) fforce[9 * (long long)i + 3 * k + d] = out[k][d];
+    }
 }
 
 __global__ void k_node_gather(const int *__restrict__ ptr, const int *__restrict__ ent, int nn,
@@ -534,7 +606,7 @@ extern "C" int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *p
     // error); the kernels below bound every segment by the scan's total
     k_sort_cells<<<(int)((s->ncell + 255) / 256), 256, 0, st>>>(s->ncell, s->nblocks, s->d_start, s->d_block,
                                                                 s->d_sorted);
-    k_pairs<<<fb, 128, 0, st>>>(s->d_geo, s->d_cell, s->d_sorted, s->d_start, s->d_block, s->ncell, s->nblocks, s->nx,
+    k_pairs<<<(na + kPairWarps - 1) / kPairWarps, 32 * kPairWarps, 0, st>>>(s->d_geo, s->d_cell, s->d_sorted, s->d_start, s->d_block, s->ncell, s->nblocks, s->nx,
                                 s->ny, s->nz, s->d_blob, s->d_type, s->d_emin, s->d_rmin, s->num_types,
                                 s->num_blobs, s->inc_self, s->d_fforce, energy, s->d_stats);
     k_node_gather<<<(s->num_nodes + 255) / 256, 256, 0, st>>>(s->d_node_ptr, s->d_node_ent, s->num_nodes,
