@@ -95,11 +95,13 @@ int fail(const char *fmt, ...)
         if (e_ != cudaSuccess) return fail("%s: %s", #call, cudaGetErrorString(e_));        \
     } while (0)
 
-// 3-point rule on a triangle (src/VdW_solver.cpp:61-71)
-__constant__ double c_eta[3][3] = {{0.666666666666667, 0.166666666666667, 0.166666666666667},
-                                   {0.166666666666667, 0.666666666666667, 0.166666666666667},
-                                   {0.166666666666667, 0.166666666666667, 0.666666666666667}};
+// 3-point rule on a triangle (src/VdW_solver.cpp:61-71): weight kW, point k
+// has barycentric coordinate eta(k, d).  Written as constant expressions so
+// that, in the fully unrolled loops, products of constants such as
+// kW * kW * eta fold at compile time (to the same double the reference
+// computes at run time) instead of costing FP64 instructions per pair.
 constexpr double kW = 0.333333333333333;
+__host__ __device__ constexpr double eta(int k, int d) { return k == d ? 0.666666666666667 : 0.166666666666667; }
 
 __device__ __forceinline__ int wrap(int x, int n)
 {
@@ -273,8 +275,8 @@ __device__ __forceinline__ double lj_pair(const double *A, const double *B, doub
     for (int k = 0; k < 3; k++)
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            p[k][d] = c_eta[k][0] * A[d] + c_eta[k][1] * A[3 + d] + c_eta[k][2] * A[6 + d];
-            q[k][d] = c_eta[k][0] * B[d] + c_eta[k][1] * B[3 + d] + c_eta[k][2] * B[6 + d];
+            p[k][d] = eta(k, 0) * A[d] + eta(k, 1) * A[3 + d] + eta(k, 2) * A[6 + d];
+            q[k][d] = eta(k, 0) * B[d] + eta(k, 1) * B[3 + d] + eta(k, 2) * B[6 + d];
         }
     const double r2 = rmin * rmin;
     const double r4 = r2 * r2;
@@ -314,9 +316,9 @@ __device__ __forceinline__ double lj_pair(const double *A, const double *B, doub
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
                     if (A_SIDE)
-                        f[d] += (kW * kW * c_eta[l][j]) * fpm[k][l][d];
+                        f[d] += (kW * kW * eta(l, j)) * fpm[k][l][d];
                     else
-                        f[d] -= (kW * kW * c_eta[k][j]) * fpm[l][k][d];
+                        f[d] -= (kW * kW * eta(k, j)) * fpm[l][k][d];
                 }
             }
 #pragma unroll
