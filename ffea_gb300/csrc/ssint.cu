@@ -29,10 +29,13 @@
 //                    face order (a CSR built at creation).
 // The file is compiled with -fmad=false so that every product and sum rounds
 // as in the reference's FP64 code; cell binning and the normal test then
-// decide exactly as FFEA does.  One deliberate difference: the unit direction
-// of each point pair is (p - q) * (1/r) where FFEA divides by r, which saves
-// three FP64 divides per point pair (the kernel is bound by the FP64 pipe)
-// and changes each component by at most one rounding.
+// decide exactly as FFEA does.  Two deliberate differences, both in the
+// force of a pair, both changing it only at the rounding level: the unit
+// direction of each point pair is (p - q) * (1/r) where FFEA divides by r,
+// and the nine weighted terms per corner are regrouped through column sums
+// of the (symmetric) force matrix.  Together they remove three FP64 divides
+// per point pair and 216 of 243 products per pair side; the kernel is bound
+// by the FP64 pipe.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -306,23 +309,24 @@ __device__ __forceinline__ double lj_pair(const double *A, const double *B, doub
         }
     }
     const double apaq = A[12] * B[12];
+    // FFEA sums W^2 eta * fpm over all nine (k, l) for each corner j.  The
+    // matrix is symmetric, so both sides need only the column sums
+    // S_l = sum_k fpm[k][l]: force1_j = sum_l W^2 eta_l[j] S_l and
+    // force2_j = -sum_k W^2 eta_k[j] S_k.  Same terms, regrouped (27 products
+    // per pair instead of 243; the sums round differently, within 1e-15).
+    double S[3][3];
+#pragma unroll
+    for (int l = 0; l < 3; l++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) S[l][d] = fpm[0][l][d] + fpm[1][l][d] + fpm[2][l][d];
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-        double f[3] = {0, 0, 0};
 #pragma unroll
-        for (int k = 0; k < 3; k++)
-#pragma unroll
-            for (int l = 0; l < 3; l++) {
-#pragma unroll
-                for (int d = 0; d < 3; d++) {
-                    if (A_SIDE)
-                        f[d] += (kW * kW * eta(l, j)) * fpm[k][l][d];
-                    else
-                        f[d] -= (kW * kW * eta(k, j)) * fpm[l][k][d];
-                }
-            }
-#pragma unroll
-        for (int d = 0; d < 3; d++) out[j][d] += f[d] * apaq;
+        for (int d = 0; d < 3; d++) {
+            const double f = (kW * kW * eta(0, j)) * S[0][d] + (kW * kW * eta(1, j)) * S[1][d] +
+                             (kW * kW * eta(2, j)) * S[2][d];
+            out[j][d] += (A_SIDE ? f : -f) * apaq;
+        }
     }
     return energy * apaq;
 }

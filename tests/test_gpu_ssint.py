@@ -2,9 +2,10 @@
 ABI) against the oracle (oracle/ssint_oracle.c, a restatement of FFEA's
 VdW_solver for "lennard-jones").
 
-Tolerances: the kernels are compiled without FMA contraction, so cell binning,
-the normal test and every pair's arithmetic match the oracle's; the pair
-counts must be equal exactly.  Per-face sums run in another order than FFEA's
+Tolerances: the kernels are compiled without FMA contraction, so cell binning
+and the normal test decide as the oracle does, and the pair counts must be
+equal exactly; a pair's force differs from FFEA's only in rounding (a
+reciprocal for a divide, regrouped sums).  Per-face sums run in another order than FFEA's
 (each pair from both sides), and the energy is summed with atomics, so forces
 agree to 1e-12 of the largest force and energies to 1e-12 relative."""
 import os
