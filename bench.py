@@ -45,22 +45,12 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-WORKLOADS = {
-    "sphere40": dict(radius_nm=40.0, cell_nm=1.25, desc="64^3-cell Freudenthal grid cut to a 40 nm sphere"),
-    "sphere20": dict(radius_nm=20.0, cell_nm=1.25, desc="32^3-cell Freudenthal grid cut to a 20 nm sphere"),
-    "sphere10": dict(radius_nm=10.0, cell_nm=1.25, desc="16^3-cell Freudenthal grid cut to a 10 nm sphere"),
-    "sphere61": dict(radius_nm=61.25, cell_nm=1.25,
-                     desc="98^3-cell Freudenthal grid cut to a 61.25 nm sphere (the ~500k-node single blob)"),
-    "replicas256": dict(radius_nm=20.0, cell_nm=1.25, replicas=256,
-                        desc="256 replicas of the 20 nm sphere in one batch, one RNG stream each"),
-    "heldout": dict(radius_nm=None, cell_nm=1.25, radii=(10.0, 20.0, 30.0, 40.0, 50.0),
-                    desc="the learned preconditioner's held-out family in one batch: spheres of radius "
-                         "10, 20, 30, 40 and 50 nm (the network was trained on radii 5-25 nm)"),
-    "ensemble64": dict(radius_nm=None, cell_nm=1.25,
-                       desc="64 independent blobs in one batch: radii log-uniform 5-40 nm at a 1.25 nm cell, "
-                            "moduli x U[0.5, 2], one RNG stream each"),
-}
+from ffea_gb300.workloads import WORKLOADS, replica_seed  # noqa: E402
+
 METRIC = "node-steps/s at CG rel-res 1e-6"
+PRECISION_MIXED_DESC = ("FP32 element forces, matrix and SpMV; CG dot products as FP32 warp sums combined in "
+                        "double-float (TwoSum) across warps and segments; FP32 CG coefficients; FP64 positions, "
+                        "rhs and the FP64 true residual that confirms every solve")
 PRECONDS = {"jacobi": 0, "two-level": 1, "learned": 2}
 L2_BYTES = 129 * 1024 * 1024
 
@@ -78,7 +68,9 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the cpu_baseline sample")
     ap.add_argument("--precond", choices=sorted(PRECONDS), default="learned",
                     help="preconditioner of the headline arm (plain Jacobi-PCG is measured beside it)")
-    ap.add_argument("--no-plain", action="store_true", help="skip the plain Jacobi-PCG arm")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain Jacobi-PCG and two-level arms")
+    ap.add_argument("--parity-steps", type=int, default=5,
+                    help="steps of the parity leg on the measured single-blob workload (0: no parity leg)")
     ap.add_argument("--autotune", action="store_true",
                     help="pick each arm's launch shape with ffea_gb300.autotune on this batch first")
     return ap.parse_args()
@@ -86,29 +78,8 @@ def parse_args():
 
 def build_specs(workload: str, rank: int, precision: str):
     """The blobs of one rank's replica of the workload."""
-    from ffea_gb300 import params as P
-    from ffea_gb300.mesh import make_blob, sphere_mesh
-    w = WORKLOADS[workload]
-    prec = P.PRECISION_MIXED if precision == "mixed" else P.PRECISION_FP64
-
-    def prm(seed):
-        return P.SimulationParams.from_si(dt=1e-14, kT=P.kT_at(300.0) * P.MESO_ENERGY, epsilon=1e-6,
-                                          max_iterations_cg=10000, rng_seed=seed, solver=P.SOLVER_NOMASS,
-                                          precision=prec)
-    if w.get("replicas"):
-        mesh = sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0)
-        return [make_blob(mesh, prm(100000 * (rank + 1) + i)) for i in range(w["replicas"])]
-    if w.get("radii"):
-        return [make_blob(sphere_mesh(r, cell_nm=w["cell_nm"], seed=10 + i), prm(2000 * (rank + 1) + i))
-                for i, r in enumerate(w["radii"])]
-    if w["radius_nm"] is not None:
-        return [make_blob(sphere_mesh(w["radius_nm"], cell_nm=w["cell_nm"], seed=0), prm(replica_seed(rank)))]
-    rng = np.random.default_rng(2)
-    radii = np.exp(rng.uniform(np.log(5.0), np.log(40.0), size=64))
-    scale = rng.uniform(0.5, 2.0, size=64)
-    return [make_blob(sphere_mesh(float(r), cell_nm=w["cell_nm"], seed=i),
-                      prm(1000 * (rank + 1) + i), shear_mod=3.7e8 * g, bulk_mod=1.1e9 * g)
-            for i, (r, g) in enumerate(zip(radii, scale))]
+    from ffea_gb300.workloads import build_specs as specs_of
+    return specs_of(workload, rank, precision)
 
 
 def config_of(args, specs, world_size):
@@ -120,7 +91,7 @@ def config_of(args, specs, world_size):
         "elements": int(sum(s.mesh.num_elements for s in specs)),
         "total_nodes": int(sum(s.mesh.num_nodes for s in specs)),
         "solver": "CG_nomass, epsilon 1e-6, convergence confirmed by an FP64 true residual",
-        "precision": "FP32 element forces + SpMV, FP64 positions/dots" if args.precision == "mixed" else "FP64",
+        "precision": PRECISION_MIXED_DESC if args.precision == "mixed" else "FP64",
         "noise": "on (MRG32k3a, RngStream-exact)",
         "replicas": world_size,
         "l2": "L2 flushed (256 MiB write) between timed steps",
@@ -227,44 +198,51 @@ def ncu_traffic(kernel="k_cg", workload="sphere40"):
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_baseline(specs, budget_s: float):
-    """Oracle (C restatement of FFEA's path) on all host cores, bounded sample:
-    whole timesteps of the workload's blobs in order (OpenMP within each blob)
-    until the budget is spent; node-steps/s over what was stepped."""
+def unlimited_stack() -> str:
+    """`ulimit -s unlimited` for this process, as FFEA's run instructions ask
+    (its CG copies vectors into stack arrays); returns what was set."""
+    import resource
+    try:
+        _, hard = resource.getrlimit(resource.RLIMIT_STACK)
+        resource.setrlimit(resource.RLIMIT_STACK, (hard, hard))
+        return "unlimited" if hard == resource.RLIM_INFINITY else f"{hard} B"
+    except (ValueError, OSError):
+        return "unchanged"
+
+
+def cpu_baseline(specs, budget_s: float, min_steps: int = 3):
+    """FFEA's algorithm (the oracle built with FFEA's release flags) on all
+    host cores, a bounded sample: whole timesteps of the workload's blobs in
+    order (OpenMP within each blob, FFEA_PARALLEL_WITHIN_BLOB) until the
+    budget is spent and at least `min_steps` steps ran; node-steps/s from the
+    median step time."""
     from oracle import oracle as O
     O.build(ref=False)
+    stack = unlimited_stack()
     specs = specs if isinstance(specs, (list, tuple)) else [specs]
     threads = os.cpu_count() or 1
-    done_nodes, total, steps, blobs_used = 0, 0.0, 0, set()
-    k = 0
-    while total < budget_s and (k == 0 or len(specs) > 1 or total < budget_s):
+    rates, total, k, blobs_used = [], 0.0, 0, set()
+    blob, blob_i = None, -1
+    while (total < budget_s or k < min_steps) and k < 1000:
         i = k % len(specs)
-        b = O.blob_from_spec(specs[i], num_threads=threads)
-        t0 = time.perf_counter()
-        rc = b.step(1)
-        first = time.perf_counter() - t0
-        n_steps, t_blob = 1, first
-        while rc == 0 and len(specs) == 1 and total + t_blob + first < budget_s:
-            t = time.perf_counter()
-            rc = b.step(1)
-            t_blob += time.perf_counter() - t
-            n_steps += 1
-        if rc != 0:
+        if i != blob_i:
+            blob, blob_i = O.blob_from_spec(specs[i], num_threads=threads, impl="fast"), i
+        t = time.perf_counter()
+        if blob.step(1) != 0:
             raise RuntimeError("oracle step failed in the CPU baseline")
-        done_nodes += specs[i].mesh.num_linear * n_steps
-        total += t_blob
-        steps += n_steps
+        dt = time.perf_counter() - t
+        rates.append(specs[i].mesh.num_linear / dt)
+        total += dt
         blobs_used.add(i)
         k += 1
-        if len(specs) == 1:
-            break
-    v = done_nodes / total
+    v = statistics.median(rates)
     what = ("the full workload" if len(specs) == 1 else
             f"{len(blobs_used)} of the workload's {len(specs)} blobs, one step each")
     return {"value": v, "unit": "node-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} timestep(s) of {what} after set-up, {total:.1f} s, OpenMP "
-                      f"{threads} threads, per-thread RNG streams as FFEA_PARALLEL_WITHIN_BLOB",
-            "steps": steps, "seconds": total}
+            "sample": f"{k} timestep(s) of {what} after set-up, {total:.1f} s; median of the per-step rates; "
+                      f"oracle built with {O.FAST_FLAGS}; OpenMP {threads} threads, per-thread RNG streams as "
+                      f"FFEA_PARALLEL_WITHIN_BLOB; stack limit {stack}",
+            "steps": k, "seconds": total}
 
 
 # ---------------------------------------------------------------- arms
@@ -273,11 +251,6 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
-
-
-def replica_seed(rank: int) -> int:
-    """Each rank steps its own replica blob with its own RNG stream (no exchange)."""
-    return 44 + rank
 
 
 def max_over_ranks(x: float, world: int, device="cuda") -> float:
@@ -296,16 +269,18 @@ def aggregate_throughput(nodes_per_replica: int, steps: int, world: int, seconds
 
 
 def run_reference(args):
-    """The reference's algorithm (the oracle, FP64, OpenMP over all host
-    cores) on this workload: set-up outside the timed region, `warmup`
-    untimed steps, then `steps` timed steps.  A step is one timestep of one
-    blob of the workload (the blobs of a batch in turn), the bounded sample
-    of the whole job's step."""
+    """The reference's algorithm (the oracle built with FFEA's release flags,
+    FP64, OpenMP over all host cores) on this workload: set-up outside the
+    timed region, `warmup` untimed steps, then `steps` timed steps.  A step
+    is one timestep of one blob of the workload (the blobs of a batch in
+    turn), the bounded sample of the whole job's step; the value comes from
+    the median step."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from oracle import oracle as O
     O.build(ref=False)
+    stack = unlimited_stack()
     specs = build_specs(args.workload, 0, args.precision)
     specs = specs if isinstance(specs, (list, tuple)) else [specs]
     threads = os.cpu_count() or 1
@@ -319,15 +294,15 @@ def run_reference(args):
         return time.perf_counter() - t, specs[i].mesh.num_linear
 
     for i in sorted({k % len(specs) for k in range(args.warmup + args.steps)}):  # set-up, untimed
-        blobs[i] = O.blob_from_spec(specs[i], num_threads=threads)
+        blobs[i] = O.blob_from_spec(specs[i], num_threads=threads, impl="fast")
     for k in range(args.warmup):
         one_step(k)
-    total, nodes = 0.0, 0
+    total, rates = 0.0, []
     for k in range(args.warmup, args.warmup + args.steps):
         dt, n = one_step(k)
         total += dt
-        nodes += n
-    value = nodes / total
+        rates.append(n / dt)
+    value = statistics.median(rates)
     what = ("the full workload" if len(specs) == 1 else
             f"one blob of the workload's {len(specs)} (in turn)")
     line = {
@@ -337,8 +312,9 @@ def run_reference(args):
         "config": config_of(args, specs if len(specs) > 1 else specs[0], 1), "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "node-steps/s", "cores": threads, "kind": "port",
                          "sample": f"each step: one timestep of {what}, after {args.warmup} untimed step(s); "
-                                   f"{args.steps} timed steps took {total:.1f} s; OpenMP {threads} threads, "
-                                   f"per-thread RNG streams as FFEA_PARALLEL_WITHIN_BLOB"},
+                                   f"{args.steps} timed steps took {total:.1f} s; value from the median step; "
+                                   f"oracle built with {O.FAST_FLAGS}; OpenMP {threads} threads, per-thread RNG "
+                                   f"streams as FFEA_PARALLEL_WITHIN_BLOB; stack limit {stack}"},
         "e2e": {"value": value, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     line["config"]["l2"] = "n/a (CPU)"
@@ -469,9 +445,12 @@ def run_gb300(args):
 
     specs = build_specs(args.workload, rank, args.precision)
     main_arm = measure_arm(args, specs, args.precond, world, local)
-    plain = None
+    plain = two_level = None
     if main_arm["preconditioner"] != "jacobi" and not args.no_plain:
         plain = measure_arm(args, specs, "jacobi", world, local)
+    if main_arm["preconditioner"] == "learned" and not args.no_plain:
+        # the same coarse space with every smoother weight 1: what the network adds
+        two_level = measure_arm(args, specs, "two-level", world, local)
     if rank != 0:
         return
     nl, ne, nedges = main_arm["sizes"]
@@ -515,54 +494,70 @@ def run_gb300(args):
     line["config"]["edges"] = int(nedges)
     line["config"]["solver"] = (f"CG_nomass, {main_arm['preconditioner']} preconditioner, epsilon 1e-6, "
                                 "convergence confirmed by an FP64 true residual")
+    arm_keys = ("value", "ms_per_step", "cg_iters_per_step", "cg_us_per_iteration", "e2e", "clocks", "preconditioner")
+
+    def ratio(a, b):
+        return {"node_steps_ratio": a["value"] / b["value"], "e2e_ratio": a["e2e"]["value"] / b["e2e"]["value"],
+                "iteration_ratio": b["cg_iters_per_step"] / max(a["cg_iters_per_step"], 1e-9)}
     if plain is not None:
-        line["plain"] = {k: plain[k] for k in ("value", "ms_per_step", "cg_iters_per_step", "cg_us_per_iteration",
-                                               "e2e", "clocks", "preconditioner")}
-        line["learned_vs_plain"] = {
-            "node_steps_ratio": main_arm["value"] / plain["value"],
-            "e2e_ratio": main_arm["e2e"]["value"] / plain["e2e"]["value"],
-            "iteration_ratio": plain["cg_iters_per_step"] / max(main_arm["cg_iters_per_step"], 1e-9),
-        }
+        line["plain"] = {k: plain[k] for k in arm_keys}
+        line["learned_vs_plain"] = ratio(main_arm, plain)
+    if two_level is not None:
+        line["two_level"] = {k: two_level[k] for k in arm_keys}
+        line["learned_vs_two_level"] = ratio(main_arm, two_level)
+        if plain is not None:
+            line["two_level_vs_plain"] = ratio(two_level, plain)
     if world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(specs, args.cpu_seconds)
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
-        line["parity"] = parity_report(args.precond)
+    if world == 1 and args.parity_steps > 0:
+        line["parity"] = parity_report(args.precond, args.workload if args.workload.startswith("sphere") else "sphere40",
+                                       args.parity_steps)
     print(json.dumps(line), flush=True)
 
 
-def parity_report(precond: str, steps: int = 20):
+def parity_report(precond: str, workload: str = "sphere40", steps: int = 5, small_steps: int = 20):
     """Per-step force (rhs) and velocity error of the measured path against
-    an FP64 oracle run (FFEA's algorithm restated), on the 16^3-cell sphere:
-    the worst relative 2-norm difference over the first `steps` steps.  Both
+    an FP64 oracle run (FFEA's algorithm restated), the worst relative
+    2-norm difference over the first steps: `steps` steps on the measured
+    single-blob workload (the oracle single-stream on all host cores, the
+    same draws as one thread) and `small_steps` on the 10 nm sphere.  Both
     sides solve to epsilon 1e-12 (the mixed path down to its FP32 floor)."""
     from ffea_gb300 import learned
-    from ffea_gb300 import params as P
-    from ffea_gb300.mesh import make_blob, sphere_mesh
+    from ffea_gb300.workloads import build_specs as specs_of
     from ffea_gb300.world import World
     from oracle import oracle as O
     O.build(ref=False)
-    prm = P.SimulationParams.from_si(dt=1e-14, kT=P.kT_at(300.0) * P.MESO_ENERGY, epsilon=1e-12, rng_seed=44,
-                                     solver=P.SOLVER_NOMASS, precision=P.PRECISION_MIXED)
-    spec = make_blob(sphere_mesh(10.0, cell_nm=1.25, seed=0), prm)
-    ref = O.blob_from_spec(spec)
-    worst_v = worst_f = 0.0
-    with World([spec], preconditioner=PRECONDS[precond]) as w:
-        if precond == "learned" and w.preconditioner() == PRECONDS["learned"]:
-            learned.apply(w, learned.load())
-        b = w.blob(0)
-        for _ in range(steps):
-            w.run(1)
-            if ref.step(1) != 0:
-                raise RuntimeError("oracle step failed in the parity report")
-            _, vel, _ = b.get_nodes()
-            _, rvel, _ = ref.nodes()
-            worst_v = max(worst_v, float(np.linalg.norm(vel - rvel) / np.linalg.norm(rvel)))
-            rf = ref.rhs()
-            worst_f = max(worst_f, float(np.linalg.norm(b.rhs() - rf) / np.linalg.norm(rf)))
-    return {"workload": "sphere10: 16^3-cell grid cut to a 10 nm sphere (2,771 linear nodes)",
-            "steps": steps, "precision": "mixed (the measured path) vs the FP64 oracle",
-            "preconditioner": precond, "max_rel_err_velocity": worst_v, "max_rel_err_force": worst_f,
-            "bar": 1e-5}
+    threads = os.cpu_count() or 1
+    out = {"precision": "mixed (the measured path) vs the FP64 oracle", "preconditioner": precond, "bar": 1e-5,
+           "epsilon": "1e-12 on both sides", "oracle_threads": threads}
+    for key, wl, n in (("", workload, steps), ("small_", "sphere10", small_steps)):
+        spec = specs_of(wl, 0, "mixed", epsilon=1e-12)[0]
+        ref = O.blob_from_spec(spec, parallel=threads)
+        worst_v = worst_f = 0.0
+        rng_exact = True
+        t0 = time.perf_counter()
+        with World([spec], preconditioner=PRECONDS[precond]) as w:
+            if precond == "learned" and w.preconditioner() == PRECONDS["learned"]:
+                learned.apply(w, learned.load())
+            b = w.blob(0)
+            for _ in range(n):
+                w.run(1)
+                if ref.step(1) != 0:
+                    raise RuntimeError("oracle step failed in the parity report")
+                _, vel, _ = b.get_nodes()
+                _, rvel, _ = ref.nodes()
+                worst_v = max(worst_v, float(np.linalg.norm(vel - rvel) / np.linalg.norm(rvel)))
+                rf = ref.rhs()
+                worst_f = max(worst_f, float(np.linalg.norm(b.rhs() - rf) / np.linalg.norm(rf)))
+                rng_exact = rng_exact and bool(np.array_equal(b.rng_state(), ref.rng_state()))
+        out[key + "workload"] = f"{wl}: {WORKLOADS[wl]['desc']} ({spec.mesh.num_linear:,} linear nodes)"
+        out[key + "steps"] = n
+        out[key + "max_rel_err_velocity"] = worst_v
+        out[key + "max_rel_err_force"] = worst_f
+        out[key + "rng_state_bit_exact"] = rng_exact
+        out[key + "seconds"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 def main():

@@ -262,6 +262,11 @@ void *ffea_gpu_ssint_stream(ffea_gpu_ssint_t *s);
  *   element), material (rho, A, B, G, E per element), out (2 doubles: strain,
  *   kinetic).  solver selects whether the kinetic term is evaluated (the
  *   mass and lumped-mass paths).
+ *   The topology is NOT checked: this entry point is not told the node count,
+ *   so every index must be a valid node of pos, vel and rest_pos
+ *   (0 <= index < N_t); an index outside reads past the caller's arrays.
+ *   ffea_gpu_create checks the topology it is given; a caller that measures a
+ *   handle's own mesh passes that same topology.
  *   Scratch is a static device array of the library sized for at most
  *   2,097,152 elements; larger meshes are rejected with an error.  Every GPU
  *   that loads the library holds that array (256 KiB) until the process exits.

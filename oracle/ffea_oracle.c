@@ -435,6 +435,7 @@ typedef struct {
     /* params */
     double dt, kT, epsilon2;
     int max_iter, calc_noise, calc_stokes, solver, num_threads;
+    int par_threads;                    /* > 1: parallel single-stream mode (orc_blob_set_parallel) */
     double *rng;                        /* 6 * num_threads exact-integer doubles */
     /* NoMass viscosity-matrix pattern: 3*num_nodes scalar rows */
     int nm_rows; int *nm_key; int *nm_col; double *nm_val;
@@ -454,6 +455,10 @@ typedef struct {
 } orc_blob;
 
 static void *orc_alloc(size_t n) { void *p = calloc(n ? n : 1, 1); return p; }
+
+/* Threads of the row-parallel loops (matrix build, SpMV): every row's sum
+ * runs in the same order whatever the count, so the count changes no bit. */
+static int orc_threads(const orc_blob *b) { return b->par_threads > b->num_threads ? b->par_threads : b->num_threads; }
 
 /* calculate_jacobian (src/tetra_element_linear.cpp:193-205) */
 static void orc_jacobian(const orc_blob *b, int e, double J[3][3])
@@ -599,6 +604,55 @@ static void orc_fluct(const orc_blob *b, int e, double *rng, double stress[3][3]
     stress[2][1] = stress[1][2];
 }
 
+/* One element of Blob::update_internal_forces (src/Blob.cpp:650-733): the
+ * element's nodal forces; returns 1 if the element inverted. */
+static int orc_element(orc_blob *b, int n, double *rng)
+{
+    double J[3][3], stress[3][3], du[12];
+    int inverted = 0;
+    orc_jacobian(b, n, J);
+    if (orc_shape(b, n, J) == ORC_ERROR) inverted = 1;
+    orc_viscosity(b, n);
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) stress[i][j] = 0;
+    orc_shear(b, n, J, stress);
+    orc_bulk(b, n, stress);
+    if (b->calc_noise == 1) orc_fluct(b, n, rng, stress);
+    if (b->solver != ORC_SOLVER_NOMASS) {
+        /* get_element_velocity_vector + mat12_apply (src/tetra_element_linear.cpp:454-469, src/mat_vec_fns.cpp:26-34) */
+        const int *nd = &b->topo[10 * n];
+        double v[12], t[12];
+        for (int a = 0; a < 4; a++) {
+            v[a] = b->vel[3 * nd[a] + 0];
+            v[4 + a] = b->vel[3 * nd[a] + 1];
+            v[8 + a] = b->vel[3 * nd[a] + 2];
+        }
+        const double (*Vm)[12] = (const double (*)[12])&b->visc[144 * n];
+        for (int i = 0; i < 12; i++) t[i] = 0;
+        for (int i = 0; i < 12; i++)
+            for (int j = 0; j < 12; j++) t[i] += Vm[i][j] * v[j];
+        for (int i = 0; i < 12; i++) du[i] = t[i];
+    } else {
+        for (int i = 0; i < 12; i++) du[i] = 0;
+    }
+    /* apply_stress_tensor (src/tetra_element_linear.cpp:441-449) */
+    const double *dpsi = &b->dpsi[12 * n];
+    const double vol = b->vol[n];
+    for (int i = 0; i < 3; i++) {
+        du[4 * i] += vol * (dpsi[0] * stress[i][0] + dpsi[4] * stress[i][1] + dpsi[8] * stress[i][2]);
+        du[4 * i + 1] += vol * (dpsi[1] * stress[i][0] + dpsi[5] * stress[i][1] + dpsi[9] * stress[i][2]);
+        du[4 * i + 2] += vol * (dpsi[2] * stress[i][0] + dpsi[6] * stress[i][1] + dpsi[10] * stress[i][2]);
+        du[4 * i + 3] += vol * (dpsi[3] * stress[i][0] + dpsi[7] * stress[i][1] + dpsi[11] * stress[i][2]);
+    }
+    /* add_element_force_vector (src/tetra_element_linear.cpp:474-489) */
+    double *nf = &b->node_force[30 * n];
+    for (int a = 0; a < 4; a++) {
+        nf[3 * a + 0] -= du[a];
+        nf[3 * a + 1] -= du[4 + a];
+        nf[3 * a + 2] -= du[8 + a];
+    }
+    return inverted;
+}
+
 /* Blob::update_internal_forces (src/Blob.cpp:638-735). */
 static int orc_internal_forces(orc_blob *b)
 {
@@ -610,6 +664,31 @@ static int orc_internal_forces(orc_blob *b)
         b->last_inversions = 0;
         return ORC_OK;
     }
+    if (b->par_threads > 1 && b->num_threads == 1) {
+        /* Parallel evaluation with the single-stream draw order of a
+         * one-thread run: element n takes draws 7n .. 7n+6 of the blob's
+         * stream, so each thread starts from a copy of the stream jumped to
+         * its first element.  Every element's arithmetic is unchanged, so
+         * the results are those of the serial loop, bit for bit. */
+        double start[6];
+        memcpy(start, b->rng, sizeof(start));
+#pragma omp parallel num_threads(b->par_threads) reduction(+ : num_inversions)
+        {
+            int nt = 1, t = 0;
+#ifdef _OPENMP
+            nt = omp_get_num_threads();
+            t = omp_get_thread_num();
+#endif
+            const int e0 = (int)((int64_t)E * t / nt), e1 = (int)((int64_t)E * (t + 1) / nt);
+            double rng[6];
+            memcpy(rng, start, sizeof(rng));
+            if (b->calc_noise == 1) orc_rng_advance(rng, 7ull * (uint64_t)e0);
+            for (int n = e0; n < e1; n++) num_inversions += orc_element(b, n, rng);
+        }
+        if (b->calc_noise == 1) orc_rng_advance(b->rng, 7ull * (uint64_t)E);
+        b->last_inversions = num_inversions;
+        return num_inversions ? ORC_ERROR : ORC_OK;
+    }
 #pragma omp parallel num_threads(b->num_threads) reduction(+ : num_inversions)
     {
         int tid = 0;
@@ -618,49 +697,7 @@ static int orc_internal_forces(orc_blob *b)
 #endif
         double *rng = &b->rng[6 * tid];
 #pragma omp for schedule(guided)
-        for (int n = 0; n < E; n++) {
-            double J[3][3], stress[3][3], du[12];
-            orc_jacobian(b, n, J);
-            if (orc_shape(b, n, J) == ORC_ERROR) num_inversions++;
-            orc_viscosity(b, n);
-            for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) stress[i][j] = 0;
-            orc_shear(b, n, J, stress);
-            orc_bulk(b, n, stress);
-            if (b->calc_noise == 1) orc_fluct(b, n, rng, stress);
-            if (b->solver != ORC_SOLVER_NOMASS) {
-                /* get_element_velocity_vector + mat12_apply (src/tetra_element_linear.cpp:454-469, src/mat_vec_fns.cpp:26-34) */
-                const int *nd = &b->topo[10 * n];
-                double v[12], t[12];
-                for (int a = 0; a < 4; a++) {
-                    v[a] = b->vel[3 * nd[a] + 0];
-                    v[4 + a] = b->vel[3 * nd[a] + 1];
-                    v[8 + a] = b->vel[3 * nd[a] + 2];
-                }
-                const double (*Vm)[12] = (const double (*)[12])&b->visc[144 * n];
-                for (int i = 0; i < 12; i++) t[i] = 0;
-                for (int i = 0; i < 12; i++)
-                    for (int j = 0; j < 12; j++) t[i] += Vm[i][j] * v[j];
-                for (int i = 0; i < 12; i++) du[i] = t[i];
-            } else {
-                for (int i = 0; i < 12; i++) du[i] = 0;
-            }
-            /* apply_stress_tensor (src/tetra_element_linear.cpp:441-449) */
-            const double *dpsi = &b->dpsi[12 * n];
-            const double vol = b->vol[n];
-            for (int i = 0; i < 3; i++) {
-                du[4 * i] += vol * (dpsi[0] * stress[i][0] + dpsi[4] * stress[i][1] + dpsi[8] * stress[i][2]);
-                du[4 * i + 1] += vol * (dpsi[1] * stress[i][0] + dpsi[5] * stress[i][1] + dpsi[9] * stress[i][2]);
-                du[4 * i + 2] += vol * (dpsi[2] * stress[i][0] + dpsi[6] * stress[i][1] + dpsi[10] * stress[i][2]);
-                du[4 * i + 3] += vol * (dpsi[3] * stress[i][0] + dpsi[7] * stress[i][1] + dpsi[11] * stress[i][2]);
-            }
-            /* add_element_force_vector (src/tetra_element_linear.cpp:474-489) */
-            double *nf = &b->node_force[30 * n];
-            for (int a = 0; a < 4; a++) {
-                nf[3 * a + 0] -= du[a];
-                nf[3 * a + 1] -= du[4 + a];
-                nf[3 * a + 2] -= du[8 + a];
-            }
-        }
+        for (int n = 0; n < E; n++) num_inversions += orc_element(b, n, rng);
     }
     b->last_inversions = num_inversions;
     return num_inversions ? ORC_ERROR : ORC_OK;
@@ -833,7 +870,7 @@ static int orc_nomass_init(orc_blob *b)
 static void orc_nomass_build(orc_blob *b)
 {
     const int nnz = b->nm_key[b->nm_rows];
-#pragma omp parallel for num_threads(b->num_threads)
+#pragma omp parallel for num_threads(orc_threads(b))
     for (int x = 0; x < nnz; x++) {
         double sum = 0.0;
         for (int s = b->nm_src_ptr[x]; s < b->nm_src_ptr[x + 1]; s++) {
@@ -850,12 +887,62 @@ static void orc_nomass_build(orc_blob *b)
 static void orc_nomass_apply(orc_blob *b, const double *in, double *out)
 {
     const int rows = b->nm_rows;
-#pragma omp parallel for num_threads(b->num_threads)
+#pragma omp parallel for num_threads(orc_threads(b))
     for (int i = 0; i < rows; i++) {
         double acc = 0.0;
         for (int j = b->nm_key[i]; j < b->nm_key[i + 1]; j++) acc += b->nm_val[j] * in[b->nm_col[j]];
         out[i] = acc;
     }
+}
+
+/* NoMassCGSolver::solve with more than one thread: the same iteration as
+ * orc_nomass_solve below, with the vector updates and the dot products
+ * spread over the threads as FFEA's OpenMP loops spread them
+ * (src/NoMassCGSolver.cpp:209, 236, 253, 268, 281; src/mat_vec_fns.cpp:253,
+ * 268).  The reductions round in a different order than the serial sums. */
+static int orc_nomass_solve_par(orc_blob *b, double *x)
+{
+    const int rows = b->nm_rows, T = orc_threads(b);
+    double *r = b->r, *p = b->p, *z = b->z, *q = b->q, *f = b->f, *pre = b->pre;
+    double delta_new = 0, delta_old, pTq, alpha, f2 = 0;
+#pragma omp parallel for num_threads(T) reduction(+ : delta_new, f2)
+    for (int i = 0; i < rows; i++) {
+        r[i] = x[i];
+        f[i] = x[i];
+        x[i] = 0;
+        z[i] = pre[i] * r[i];
+        p[i] = z[i];
+        delta_new += r[i] * z[i];
+        f2 += f[i] * f[i];
+    }
+    for (int it = 0; it < b->max_iter; it++) {
+        orc_nomass_apply(b, p, q);
+        pTq = 0;
+#pragma omp parallel for num_threads(T) reduction(+ : pTq)
+        for (int i = 0; i < rows; i++) pTq += p[i] * q[i];
+        alpha = delta_new / pTq;
+        double r2 = 0;
+#pragma omp parallel for num_threads(T) reduction(+ : r2)
+        for (int i = 0; i < rows; i++) {
+            x[i] += alpha * p[i];
+            r[i] += -alpha * q[i];
+            r2 += r[i] * r[i];
+        }
+        const double res = (f2 == 0.0) ? 0.0 : r2 / f2;
+        if (res < b->epsilon2) { b->last_iters = it + 1; return ORC_OK; }
+        delta_old = delta_new;
+        delta_new = 0;
+#pragma omp parallel for num_threads(T) reduction(+ : delta_new)
+        for (int i = 0; i < rows; i++) {
+            z[i] = pre[i] * r[i];
+            delta_new += r[i] * z[i];
+        }
+        const double beta = (delta_new / delta_old);
+#pragma omp parallel for num_threads(T)
+        for (int i = 0; i < rows; i++) p[i] = beta * p[i] + z[i];
+    }
+    b->last_iters = b->max_iter;
+    return ORC_ERROR;
 }
 
 /* NoMassCGSolver::solve (src/NoMassCGSolver.cpp:165-197) with its helpers
@@ -866,11 +953,13 @@ static int orc_nomass_solve(orc_blob *b, double *x)
     const int rows = b->nm_rows;
     orc_nomass_build(b);
     /* calc_inverse_diagonal (src/SparseMatrixFixedPattern.cpp:325-333) */
+#pragma omp parallel for num_threads(orc_threads(b))
     for (int i = 0; i < rows; i++) {
         double dg = 0;
         for (int j = b->nm_key[i]; j < b->nm_key[i + 1]; j++) if (b->nm_col[j] == i) dg = b->nm_val[j];
         b->pre[i] = 1.0 / dg;
     }
+    if (orc_threads(b) > 1) return orc_nomass_solve_par(b, x);
     double *r = b->r, *p = b->p, *z = b->z, *q = b->q, *f = b->f, *pre = b->pre;
     double delta_new = 0, delta_old, pTq, alpha;
     /* conjugate_gradient_residual_assume_x_zero (:205-230) */
@@ -1334,6 +1423,20 @@ void orc_blob_get_element_forces(const orc_blob *b, double *out)
     for (int e = 0; e < b->num_elements; e++)
         for (int a = 0; a < 4; a++)
             for (int c = 0; c < 3; c++) out[12 * e + 3 * a + c] = b->node_force[30 * e + 3 * a + c];
+}
+
+/* Parallel single-stream mode (test infrastructure for large meshes): with
+ * one RNG stream (num_threads 1), spread the element loop, the matrix build,
+ * the SpMV and the NoMass CG vector work over `threads` threads while every
+ * draw keeps its serial position in the stream.  Element forces, the matrix
+ * and each SpMV are then bit-identical to a one-thread run; the NoMass CG dot
+ * products sum in another order (FP64 round-off only).  threads <= 1 turns
+ * the mode off.  Returns 0, or -1 if the blob has several streams. */
+int orc_blob_set_parallel(orc_blob *b, int threads)
+{
+    if (b->num_threads != 1 && threads > 1) return -1;
+    b->par_threads = threads > 1 ? threads : 0;
+    return 0;
 }
 
 int orc_blob_last_cg_iters(const orc_blob *b) { return b->last_iters; }

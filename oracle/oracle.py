@@ -15,6 +15,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "liboracle.so")
+FAST_SO = os.path.join(HERE, "liboracle_fast.so")
+FAST_FLAGS = "-O3 -ffast-math -fopenmp (FFEA's GNU release flags without -march=native)"
 REF_SO = os.path.join(HERE, "_ref", "libffea_ref.so")
 REF_KAT = os.path.join(HERE, "_ref", "test_rngstream")
 REFERENCE_SRC = os.environ.get("FFEA_REFERENCE_SRC", "/root/reference")
@@ -27,7 +29,7 @@ _u64p = ctypes.POINTER(ctypes.c_uint64)
 def build(ref: bool | None = None, quiet: bool = True) -> None:
     """Compile the oracle (and the reference objects when their sources exist)."""
     out = subprocess.DEVNULL if quiet else None
-    subprocess.run(["make", "-C", HERE, "port"], check=True, stdout=out)
+    subprocess.run(["make", "-C", HERE, "port", "fast"], check=True, stdout=out)
     if ref is None:
         ref = os.path.isdir(os.path.join(REFERENCE_SRC, "src"))
     if ref:
@@ -83,8 +85,29 @@ def port_lib():
         lib.orc_ffea_seed.argtypes = [ctypes.c_int, _u64p]
         lib.orc_ffea_thread_stream.argtypes = [_u64p, ctypes.c_int, _u64p]
         lib.orc_num_threads_available.restype = ctypes.c_int
+        lib.orc_blob_set_parallel.restype = ctypes.c_int
+        lib.orc_blob_set_parallel.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _port = lib
     return _port
+
+
+_fast = None
+
+
+def fast_lib():
+    """The oracle built with FFEA's release flags (timed CPU baseline only)."""
+    global _fast
+    if _fast is None:
+        if not os.path.exists(FAST_SO):
+            build(ref=False)
+        lib = ctypes.CDLL(FAST_SO)
+        _declare(lib, "orc")
+        lib.orc_blob_last_cg_iters.restype = ctypes.c_int
+        lib.orc_blob_last_cg_iters.argtypes = [ctypes.c_void_p]
+        lib.orc_blob_set_parallel.restype = ctypes.c_int
+        lib.orc_blob_set_parallel.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _fast = lib
+    return _fast
 
 
 def ref_available() -> bool:
@@ -153,8 +176,8 @@ class OracleBlob:
     def __init__(self, pos, topology, material, drag, pinned, dt, kT, epsilon2, max_iterations_cg=1000,
                  calc_noise=1, calc_stokes=1, solver=0, num_threads=1, impl="port"):
         self.impl = impl
-        self.lib = port_lib() if impl == "port" else ref_lib()
-        self.pfx = "orc" if impl == "port" else "ref"
+        self.lib = {"port": port_lib, "fast": fast_lib, "ref": ref_lib}[impl]()
+        self.pfx = "ref" if impl == "ref" else "orc"
         self.pos0 = np.ascontiguousarray(pos, dtype=np.float64)
         self.topo = np.ascontiguousarray(topology, dtype=np.int32)
         self.mat = np.ascontiguousarray(material, dtype=np.float64)
@@ -181,14 +204,14 @@ class OracleBlob:
 
     def set_rng_state(self, st, thread: int = 0):
         st = np.ascontiguousarray(st, dtype=np.uint64)
-        if self.impl == "port":
+        if self.pfx == "orc":
             self.lib.orc_blob_set_rng_state(self.h, thread, _ptr(st, _u64p))
         else:
             self.lib.ref_blob_set_rng_state(self.h, _ptr(st, _u64p))
 
     def rng_state(self, thread: int = 0) -> np.ndarray:
         st = np.zeros(6, np.uint64)
-        if self.impl == "port":
+        if self.pfx == "orc":
             self.lib.orc_blob_get_rng_state(self.h, thread, _ptr(st, _u64p))
         else:
             self.lib.ref_blob_get_rng_state(self.h, _ptr(st, _u64p))
@@ -228,6 +251,16 @@ class OracleBlob:
     def last_cg_iters(self) -> int:
         return self.lib.orc_blob_last_cg_iters(self.h)
 
+    def set_parallel(self, threads: int):
+        """Spread one single-stream blob's step over `threads` host threads with
+        every draw in its serial position (orc_blob_set_parallel): element
+        forces, the matrix and each SpMV stay bit-identical to one thread; only
+        the NoMass CG dot products round in another order."""
+        if self.pfx != "orc":
+            raise NotImplementedError("the parallel single-stream mode is the C oracle's")
+        if self.lib.orc_blob_set_parallel(self.h, int(threads)) != 0:
+            raise ValueError("the parallel single-stream mode needs a blob with one RNG stream")
+
     def energies(self):
         s = ctypes.c_double(); k = ctypes.c_double()
         self.lib.orc_blob_energies(self.h, ctypes.byref(s), ctypes.byref(k))
@@ -251,14 +284,17 @@ class OracleBlob:
         return out.reshape(-1, 3)
 
 
-def blob_from_spec(spec, impl="port", num_threads=1, epsilon2=None, seed=True):
-    """OracleBlob from an ffea_gb300.mesh.BlobSpec-like object."""
+def blob_from_spec(spec, impl="port", num_threads=1, epsilon2=None, seed=True, parallel=0):
+    """OracleBlob from an ffea_gb300.mesh.BlobSpec-like object.  parallel > 1
+    turns on the parallel single-stream mode with that many threads."""
     p = spec.params
     b = OracleBlob(spec.mesh.pos, spec.mesh.topology, spec.material, spec.drag, spec.pinned, p.dt, p.kT,
                    p.epsilon2 if epsilon2 is None else epsilon2, p.max_iterations_cg, p.calc_noise,
                    p.calc_stokes, p.solver, num_threads, impl)
     if seed:
         b.seed(p.rng_seed)
+    if parallel > 1:
+        b.set_parallel(parallel)
     return b
 
 
