@@ -85,6 +85,11 @@ SIGNATURES = {
     "ffea_gpu_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "ffea_gpu_cg_loop_count": (ctypes.c_int64, [ctypes.c_void_p]),
     "ffea_gpu_diag_spmv": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _dp]),
+    "ffea_gpu_diag_coarse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                            ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "ffea_gpu_diag_sgemm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_float,
+                                           ctypes.c_void_p]),
     "ffea_gpu_preconditioner": (ctypes.c_int, [ctypes.c_void_p]),
     "ffea_gpu_selftest_barrier_timeout": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _ip]),
     "ffea_gpu_set_smoother_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32,

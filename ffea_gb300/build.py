@@ -1,8 +1,7 @@
 """Build recipe for libffea_gb300.so (sm_103a), in-tree.
 
 The translation units are compiled in parallel with nvcc and linked into one
-shared library next to this file (with cuBLAS, for the plain FP32 GEMMs of
-the coarse-space inverse).  No cmake, no torch extension machinery:
+shared library next to this file, against the CUDA runtime only.  No cmake, no torch extension machinery:
 the library exposes only the C ABI of include/ffea_gpu.h.
 """
 from __future__ import annotations
@@ -65,7 +64,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
     tmp = LIB + ".tmp"
-    link = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lcublas"]
+    link = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))

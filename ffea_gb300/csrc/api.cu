@@ -6,7 +6,6 @@
 // The whole CG solve of every blob runs inside one cooperative launch that
 // iterates until each blob has converged, so a step (and a run of steps)
 // needs no host synchronisation.
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -145,10 +144,8 @@ struct ffea_gpu {
     int precond = FFEA_GPU_PRECOND_JACOBI;     // in use, after fall-backs
     MpnnBuffers mpnn;                          // learned smoother weights (allocated on first use)
     bool mpnn_ready = false;
-    cublasHandle_t cublas = nullptr;           // coarse-space GEMMs
     ~ffea_gpu()
     {
-        if (cublas) cublasDestroy(cublas);
         if (step_exec) cudaGraphExecDestroy(step_exec);
         if (step_exec_coarse) cudaGraphExecDestroy(step_exec_coarse);
         for (auto &e : ev)
@@ -210,7 +207,6 @@ __global__ void k_nodes_in(DeviceBatch d, const int2 *src, int n, const double *
     }
 }
 
-constexpr size_t kCublasWorkspace = 4u << 20;  // a fixed workspace makes the GEMMs capturable
 constexpr int kCoarseInitIterations = 40;      // Newton-Schulz from I / ||A_c||: log2(cond) + a few
 
 // The coarse matrix of the current mesh and one Newton-Schulz update of its
@@ -219,7 +215,7 @@ int refresh_coarse(ffea_gpu *h, cudaStream_t s, int iterations, bool init)
 {
     if (!h->dev.coarse) return FFEA_GPU_OK;
     launch_coarse_assemble(h->dev, s);
-    if (coarse_refresh(h->dev, h->host.bp, h->cublas, s, iterations, init) != 0)
+    if (coarse_refresh(h->dev, h->host.bp, s, iterations, init) != 0)
         return fail("coarse-space refresh failed: %s", cudaGetErrorString(cudaGetLastError()));
     return FFEA_GPU_OK;
 }
@@ -640,11 +636,6 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     if (d.coarse) {
         // X ~ A_c^-1 of the rest mesh, Newton-Schulz from a scaled identity;
         // every step then refines it for the current mesh
-        if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS) return fail("cublasCreate failed");
-        void *ws = nullptr;
-        CK(A.alloc_bytes(ws, kCublasWorkspace));
-        if (cublasSetWorkspace(h->cublas, ws, kCublasWorkspace) != CUBLAS_STATUS_SUCCESS)
-            return fail("cublasSetWorkspace failed");
         launch_elements(d, h->stream, ELEM_MATRIX_ONLY);
         launch_assemble(d, h->stream);
         if (refresh_coarse(h.get(), h->stream, kCoarseInitIterations, true)) return FFEA_GPU_ERROR;
@@ -1334,5 +1325,29 @@ extern "C" int ffea_gpu_diag_spmv(ffea_gpu_t *h, int32_t variant, int32_t reps, 
     CK(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
     CK(cudaGetLastError());
     *us_per_spmv = 1e3 * (double)ms / reps;
+    return FFEA_GPU_OK;
+}
+
+extern "C" int ffea_gpu_diag_coarse(ffea_gpu_t *h, int32_t blob, int32_t *n, float *coarse_matrix, float *inverse)
+{
+    if (!h || !n) return fail("bad arguments");
+    if (blob < 0 || blob >= (int32_t)h->host.bp.size()) return fail("blob index %d out of range", blob);
+    const BlobParams &bp = h->host.bp[blob];
+    *n = h->dev.coarse ? bp.coarse_n : 0;
+    if (*n == 0) return FFEA_GPU_OK;
+    const size_t bytes = sizeof(float) * (size_t)bp.coarse_n * bp.coarse_n;
+    CK(cudaStreamSynchronize(h->stream));
+    if (coarse_matrix) CK(cudaMemcpy(coarse_matrix, h->dev.coarse_A + bp.coarse_xoff, bytes, cudaMemcpyDeviceToHost));
+    if (inverse) CK(cudaMemcpy(inverse, h->dev.coarse_X + bp.coarse_xoff, bytes, cudaMemcpyDeviceToHost));
+    return FFEA_GPU_OK;
+}
+
+extern "C" int ffea_gpu_diag_sgemm(const float *a, const float *b, const float *d, float *c, int32_t n, int32_t batch,
+                                   float alpha, float beta, void *stream)
+{
+    if (!a || !b || !c || n <= 0 || batch <= 0 || batch > 65535 || (beta != 0.f && !d)) return fail("bad arguments");
+    if (n > 46340) return fail("n = %d: n^2 exceeds the int32 index range of a batch stride", n);
+    sgemm_batched(a, b, beta != 0.f ? d : nullptr, c, n, batch, alpha, beta, static_cast<cudaStream_t>(stream));
+    CK(cudaGetLastError());
     return FFEA_GPU_OK;
 }

@@ -11,13 +11,12 @@
 //   k_coarse_assemble  A_c blocks (s, t) for the segments t coupled to s,
 //                      once per step (the matrix changes with the mesh)
 //   coarse_refresh     X ~ A_c^-1 by Newton-Schulz, X <- 2X - X A_c X (two
-//                      plain FP32 GEMMs through cuBLAS) from the previous
-//                      step's X; `init` starts from X = I / ||A_c||_inf and
+//                      FP32 GEMMs, k_sgemm below) from the previous step's
+//                      X; `init` starts from X = I / ||A_c||_inf and
 //                      iterates to convergence
 //
 // The matrix enters in the same difference form as the solver's SpMV:
 // (A v)_p = sum_q K_pq (v_q - v_p) + zeta_p v_p over the free rows.
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -200,7 +199,146 @@ __global__ void k_scaled_identity(const float *__restrict__ A, float *__restrict
     for (size_t k = threadIdx.x; k < (size_t)n * n; k += blockDim.x) X[k] = (k / n == k % n) ? a : 0.f;
 }
 
+// C = alpha A B + beta D over n x n row-major matrices, one product per
+// blockIdx.z (matrices n^2 apart; D may be null when beta = 0, and C may
+// alias D).  A BM x BN tile of C per CTA of 256 threads, each thread a
+// (BM/16) x (BN/16) register block split in two halves of rows and columns
+// (so its shared-memory reads are float4 or float2 and conflict-free); K in steps of
+// 16 through double-buffered shared memory, the next step's tile loaded into
+// registers while the current one is multiplied.  Every C entry is a
+// sequential FMA chain over k: deterministic.
+template <int BM>
+__global__ void __launch_bounds__(256) k_sgemm(const float *__restrict__ A, const float *__restrict__ B,
+                                               const float *D, float *C, int n, float alpha, float beta)
+{
+    constexpr int BK = 16, TM = BM / 16, H = TM / 2, LA = BM / 16, LB = BM / 16;
+    constexpr int PAD = 4;
+    __shared__ __align__(16) float As[2][BK][BM + PAD];
+    __shared__ __align__(16) float Bs[2][BK][BM + PAD];
+    const size_t off = (size_t)blockIdx.z * n * n;
+    A += off;
+    B += off;
+    C += off;
+    if (D) D += off;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int i0 = blockIdx.y * BM, j0 = blockIdx.x * BM;
+    float acc[TM][TM];
+#pragma unroll
+    for (int i = 0; i < TM; i++)
+#pragma unroll
+        for (int j = 0; j < TM; j++) acc[i][j] = 0.f;
+    float ra[LA], rb[LB];
+    // A tile (BM x BK): element r at row tid/16 + 16 r, column tid%16;
+    // B tile (BK x BM): row tid/BM + (256/BM) r, column tid%BM
+    auto load = [&](int k0) {
+#pragma unroll
+        for (int r = 0; r < LA; r++) {
+            const int row = i0 + (tid >> 4) + 16 * r, col = k0 + (tid & 15);
+            ra[r] = (row < n && col < n) ? A[(size_t)row * n + col] : 0.f;
+        }
+#pragma unroll
+        for (int r = 0; r < LB; r++) {
+            const int row = k0 + tid / BM + (256 / BM) * r, col = j0 + tid % BM;
+            rb[r] = (row < n && col < n) ? B[(size_t)row * n + col] : 0.f;
+        }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int r = 0; r < LA; r++) As[buf][tid & 15][(tid >> 4) + 16 * r] = ra[r];
+#pragma unroll
+        for (int r = 0; r < LB; r++) Bs[buf][tid / BM + (256 / BM) * r][tid % BM] = rb[r];
+    };
+    const int nk = (n + BK - 1) / BK;
+    load(0);
+    store(0);
+    __syncthreads();
+    for (int kt = 0; kt < nk; kt++) {
+        const int buf = kt & 1;
+        if (kt + 1 < nk) load((kt + 1) * BK);
+#pragma unroll
+        for (int k = 0; k < BK; k++) {
+            float a[TM], b[TM];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float *pa = &As[buf][k][h * (BM / 2) + ty * H];
+                const float *pb = &Bs[buf][k][h * (BM / 2) + tx * H];
+                if constexpr (H % 4 == 0) {
+#pragma unroll
+                    for (int q = 0; q < H; q += 4) {
+                        const float4 va = *reinterpret_cast<const float4 *>(pa + q);
+                        const float4 vb = *reinterpret_cast<const float4 *>(pb + q);
+                        a[h * H + q] = va.x;
+                        a[h * H + q + 1] = va.y;
+                        a[h * H + q + 2] = va.z;
+                        a[h * H + q + 3] = va.w;
+                        b[h * H + q] = vb.x;
+                        b[h * H + q + 1] = vb.y;
+                        b[h * H + q + 2] = vb.z;
+                        b[h * H + q + 3] = vb.w;
+                    }
+                } else {
+                    static_assert(H % 2 == 0, "register block halves must be even");
+#pragma unroll
+                    for (int q = 0; q < H; q += 2) {
+                        const float2 va = *reinterpret_cast<const float2 *>(pa + q);
+                        const float2 vb = *reinterpret_cast<const float2 *>(pb + q);
+                        a[h * H + q] = va.x;
+                        a[h * H + q + 1] = va.y;
+                        b[h * H + q] = vb.x;
+                        b[h * H + q + 1] = vb.y;
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < TM; i++)
+#pragma unroll
+                for (int j = 0; j < TM; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+        if (kt + 1 < nk) {
+            store(buf ^ 1);
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < TM; i++) {
+        const int row = i0 + (i / H) * (BM / 2) + ty * H + (i % H);
+        if (row >= n) continue;
+#pragma unroll
+        for (int j = 0; j < TM; j++) {
+            const int col = j0 + (j / H) * (BM / 2) + tx * H + (j % H);
+            if (col >= n) continue;
+            const size_t o = (size_t)row * n + col;
+            float v = alpha * acc[i][j];
+            if (beta != 0.f) v += beta * D[o];
+            C[o] = v;
+        }
+    }
+}
+
 }  // namespace
+
+// One batched product on stream s: 128 x 128 tiles when they fill the GPU
+// at least twice over, 64 x 64 tiles otherwise.
+void sgemm_batched(const float *A, const float *B, const float *D, float *C, int n, int batch, float alpha, float beta,
+                   cudaStream_t s)
+{
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const long long big = (long long)((n + 127) / 128) * ((n + 127) / 128) * batch;
+    if (big >= 2LL * sms) {
+        dim3 grid((n + 127) / 128, (n + 127) / 128, batch);
+        k_sgemm<128><<<grid, 256, 0, s>>>(A, B, D, C, n, alpha, beta);
+    } else {
+        dim3 grid((n + 63) / 64, (n + 63) / 64, batch);
+        k_sgemm<64><<<grid, 256, 0, s>>>(A, B, D, C, n, alpha, beta);
+    }
+    count_launches(1);
+}
 
 void launch_coarse_assemble(const DeviceBatch &d, cudaStream_t s)
 {
@@ -212,15 +350,13 @@ void launch_coarse_assemble(const DeviceBatch &d, cudaStream_t s)
     count_launches(1);
 }
 
-int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cublasHandle_t cb, cudaStream_t s,
-                   int iterations, bool init)
+int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cudaStream_t s, int iterations,
+                   bool init)
 {
     if (!d.coarse) return 0;
-    if (cublasSetStream(cb, s) != CUBLAS_STATUS_SUCCESS) return -1;
-    const float one = 1.f, zero = 0.f, minus_one = -1.f, two = 2.f;
     // runs of consecutive NoMass blobs with the same coarse dimension (their
-    // matrices lie n^2 apart) are updated together by strided-batched GEMMs:
-    // one launch sequence for a whole ensemble of replicas
+    // matrices lie n^2 apart) are updated together by batched products: one
+    // launch sequence for a whole ensemble of replicas
     for (size_t b0 = 0; b0 < bps.size();) {
         const BlobParams &bp = bps[b0];
         const int n = bp.coarse_n;
@@ -233,7 +369,6 @@ int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cub
                (int64_t)bps[b1].coarse_xoff == (int64_t)bp.coarse_xoff + (int64_t)(b1 - b0) * n * n)
             b1++;
         const int batch = (int)(b1 - b0);
-        const long long stride = (long long)n * n;
         float *A = d.coarse_A + bp.coarse_xoff, *X = d.coarse_X + bp.coarse_xoff;
         float *Tm = d.coarse_T, *Xn = d.coarse_Xn;
         if (init) {
@@ -241,17 +376,9 @@ int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cub
             count_launches(1);
         }
         for (int it = 0; it < iterations; it++) {
-            // T = A X; Xn = 2 X - X T; X = sym(Xn).  The matrices are
-            // symmetric, so row- and column-major readings agree.
-            if (cublasSgemmStridedBatched(cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, A, n, stride, X, n, stride,
-                                          &zero, Tm, n, stride, batch) != CUBLAS_STATUS_SUCCESS)
-                return -1;
-            if (cudaMemcpyAsync(Xn, X, sizeof(float) * (size_t)stride * batch, cudaMemcpyDeviceToDevice, s) !=
-                cudaSuccess)
-                return -1;
-            if (cublasSgemmStridedBatched(cb, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &minus_one, X, n, stride, Tm, n,
-                                          stride, &two, Xn, n, stride, batch) != CUBLAS_STATUS_SUCCESS)
-                return -1;
+            // T = A X; Xn = 2 X - X T; X = sym(Xn)
+            sgemm_batched(A, X, nullptr, Tm, n, batch, 1.f, 0.f, s);
+            sgemm_batched(X, Tm, X, Xn, n, batch, -1.f, 2.f, s);
             dim3 grid((n + 255) / 256, n, batch);
             k_symmetrize<<<grid, 256, 0, s>>>(Xn, X, n);
             count_launches(1);

@@ -178,10 +178,18 @@ __device__ __forceinline__ DF df_add(DF a, DF b)
 // Force sum of the node kernel: FP64 in FP64 mode; in mixed precision a
 // double-float sum of the FP32 element forces, which keeps the FP64 pipes
 // (1/64 of the FP32 rate on GB300) out of the per-corner loop.
+// merge(o) adds another partial sum; xor_shfl(m) is lane ^ m's partial.
 template <typename T> struct ForceSum {
     double v = 0.0;
     __device__ __forceinline__ void add(T x) { v += (double)x; }
     __device__ __forceinline__ void add_d(double x) { v += x; }
+    __device__ __forceinline__ void merge(const ForceSum &o) { v += o.v; }
+    __device__ __forceinline__ ForceSum xor_shfl(int m) const
+    {
+        ForceSum r;
+        r.v = __shfl_xor_sync(0xffffffffu, v, m);
+        return r;
+    }
     __device__ __forceinline__ double value() const { return v; }
 };
 template <> struct ForceSum<float> {
@@ -191,6 +199,13 @@ template <> struct ForceSum<float> {
     {
         const float h = (float)x;
         v = df_add(v, DF{h, (float)(x - (double)h)});
+    }
+    __device__ __forceinline__ void merge(const ForceSum &o) { v = df_add(v, o.v); }
+    __device__ __forceinline__ ForceSum xor_shfl(int m) const
+    {
+        ForceSum r;
+        r.v = DF{__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
+        return r;
     }
     __device__ __forceinline__ double value() const { return (double)v.hi + (double)v.lo; }
 };
@@ -516,96 +531,95 @@ __global__ void k_lumped_mass(DeviceBatch d)
 // Node kernel: rhs and the CG start (for a lumped-mass blob the solve
 // itself, x = M_lumped^-1 f, MassLumpedSolver::solve src/MassLumpedSolver.cpp:81-89).
 template <typename T>
-__global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_given_rhs)
+__global__ void __launch_bounds__(NODE_TILE * NODE_LANES) k_nodes(DeviceBatch d, int use_given_rhs)
 {
+    // NODE_LANES lanes per row: the lanes split the row's gather list
+    // (entries q, q + NODE_LANES, ...), combine their partial sums in a fixed
+    // order, then lanes 0..2 each finish one component.
+    static_assert(NODE_LANES == 4, "the combine below is a two-step butterfly");
     __shared__ double red[2 * 32];
     const int tile = blockIdx.x;
     const int b = d.tile_blob[tile];
     const BlobParams &bp = d.bp[b];
-    const int row = tile * NODE_TILE + threadIdx.x;
+    const int q = threadIdx.x & (NODE_LANES - 1);
+    const int row = tile * NODE_TILE + threadIdx.x / NODE_LANES;
     const int local = row - bp.node_off;
     const bool failed = d.status[b] != 0;
     const bool valid = local < bp.node_cnt && !(d.flags[row] & NODE_PINNED) && !failed;
     const bool nomass = bp.solver == SOLVER_NOMASS;
-    ForceSum<T> fs[3];
-    T D[3] = {(T)0, (T)0, (T)0};
     const double drag = bp.calc_stokes == 1 ? d.drag[row] : 0.0;
-    if (valid) {
+    ForceSum<T> fs[3];
+    if (valid && !use_given_rhs) {
         // external forces first, as FFEA adds them to Blob::force before the
         // element contributions (src/World.cpp:1907, src/Blob.cpp:647)
-        if (d.ext && !use_given_rhs) {
+        if (d.ext && q == 0) {
 #pragma unroll
             for (int i = 0; i < 3; i++) fs[i].add_d(d.ext[3 * (size_t)row + i]);
         }
         const T *ef = static_cast<const T *>(d.efrc);
-        const T *g = static_cast<const T *>(d.g);
-        const T *mt = static_cast<const T *>(d.mat_t);
-        // unrolled so that the loads of several (element, corner) entries
-        // are in flight together; the sums keep their order
-#pragma unroll 4
-        for (int k = d.gather_ptr[row]; k < d.gather_ptr[row + 1]; k++) {
+#pragma unroll 2
+        for (int k = d.gather_ptr[row] + q; k < d.gather_ptr[row + 1]; k += NODE_LANES) {
             const int gi = d.gather_idx[k];
             const int el = gi >> 2, a = gi & 3;
-            if (!use_given_rhs) {
 #pragma unroll
-                for (int i = 0; i < 3; i++) fs[i].add(ef[12 * (size_t)el + 3 * a + i]);
-            }
-            if (nomass) {
-                T ga[3];
-                load_g<T>(g, el, a, ga);
-                const T *m = mt + MAT_T_STRIDE * (size_t)d.mat_id[el];
-                const T mA = m[MAT_T_A], mB = m[MAT_T_B];
-                const T gg = ga[0] * ga[0] + ga[1] * ga[1] + ga[2] * ga[2];
-#pragma unroll
-                for (int i = 0; i < 3; i++) D[i] += mA * (gg + ga[i] * ga[i]) + mB * ga[i] * ga[i];
-            }
+            for (int i = 0; i < 3; i++) fs[i].add(ef[12 * (size_t)el + 3 * a + i]);
         }
-        if (!use_given_rhs) {
-            if (!nomass && bp.calc_stokes == 1) {
+    }
+    // (lane 0 + lane 1) + (lane 2 + lane 3), the lower lane's partial first,
+    // so every lane of the row ends with the same sum
 #pragma unroll
-                for (int i = 0; i < 3; i++) fs[i].add_d(-(d.vel[3 * (size_t)row + i] * drag));
-            }
-            if (bp.calc_noise == 1 && bp.calc_stokes == 1) {
-                // draws from k_noise, amplitudes sqrt((24 kT drag) / dt) set up once
-                const T *nz = static_cast<const T *>(d.node_noise) + 3 * (size_t)bp.noise_node_off;
-                const T *na = static_cast<const T *>(d.node_amp), *fa = static_cast<const T *>(d.fold_amp);
-                if (drag != 0.0) {
-                    const T *z = nz + 3 * (size_t)d.orig[row];
-                    const T amp = na[row];
+    for (int m = 1; m < NODE_LANES; m <<= 1) {
 #pragma unroll
-                    for (int i = 0; i < 3; i++) fs[i].add(-(z[i] * amp));
-                }
-                // secondary nodes with a drag: half of their force lands here
-                for (int k = d.fold_ptr[row]; k < d.fold_ptr[row + 1]; k++) {
-                    const T *z = nz + 3 * (size_t)d.fold_sec[k];
-                    const T amp = fa[k];
-#pragma unroll
-                    for (int i = 0; i < 3; i++) fs[i].add((T)0.5 * (-(z[i] * amp)));
-                }
+        for (int i = 0; i < 3; i++) {
+            const ForceSum<T> o = fs[i].xor_shfl(m);
+            if (q & m) {
+                ForceSum<T> lo = o;
+                lo.merge(fs[i]);
+                fs[i] = lo;
+            } else {
+                fs[i].merge(o);
             }
         }
     }
-    double f[3];
-#pragma unroll
-    for (int i = 0; i < 3; i++) f[i] = fs[i].value();
-    if (use_given_rhs && valid) {
-#pragma unroll
-        for (int i = 0; i < 3; i++) f[i] = d.rhs[3 * (size_t)row + i];
+    const int c = q < 3 ? q : 0;  // this lane's component (lane 3 repeats 0 and stores nothing)
+    ForceSum<T> fc = c == 0 ? fs[0] : (c == 1 ? fs[1] : fs[2]);
+    if (valid && !use_given_rhs) {
+        if (!nomass && bp.calc_stokes == 1) fc.add_d(-(d.vel[3 * (size_t)row + c] * drag));
+        if (bp.calc_noise == 1 && bp.calc_stokes == 1) {
+            // draws from k_noise, amplitudes sqrt((24 kT drag) / dt) set up once
+            const T *nz = static_cast<const T *>(d.node_noise) + 3 * (size_t)bp.noise_node_off;
+            const T *na = static_cast<const T *>(d.node_amp), *fa = static_cast<const T *>(d.fold_amp);
+            if (drag != 0.0) fc.add(-(nz[3 * (size_t)d.orig[row] + c] * na[row]));
+            // secondary nodes with a drag: half of their force lands here
+            for (int k = d.fold_ptr[row]; k < d.fold_ptr[row + 1]; k++)
+                fc.add((T)0.5 * (-(nz[3 * (size_t)d.fold_sec[k] + c] * fa[k])));
+        }
     }
+    double f = fc.value();
+    if (use_given_rhs && valid) f = d.rhs[3 * (size_t)row + c];
+    const bool store = q < 3;
     T *dinv = static_cast<T *>(d.dinv);
-    if (nomass) {
-#pragma unroll
-        for (int i = 0; i < 3; i++) dinv[3 * (size_t)row + i] = valid ? (T)1 / (D[i] + (T)drag) : (T)1;
+    if (nomass && store) {
+        // Jacobi diagonal of component c: zeta_p - sum_q K_pq[c][c] over the
+        // row's assembled blocks (padding slots hold zeros).  The viscosity
+        // diagonal block is minus the sum of the row's off-diagonal blocks,
+        // as the gradients of a linear element's shape functions sum to zero.
+        T Dc = (T)0;
+        if (valid) {
+            const int sl = row >> 5, L = d.slice_len[sl], base = d.slice_ptr[sl] + (row & 31);
+            const T *val = static_cast<const T *>(d.sell_val);
+            for (int j = 0; j < L; j++) Dc -= val[sell_vidx(base + 32 * j, 4 * c)];
+        }
+        dinv[3 * (size_t)row + c] = valid ? (T)1 / (Dc + (T)drag) : (T)1;
     }
     // CG start: x = 0, r = f, u = D^-1 r, w = s = p = 0
     T *x = static_cast<T *>(d.x), *r = static_cast<T *>(d.r), *u = static_cast<T *>(d.u);
     T *p = static_cast<T *>(d.p), *sv = static_cast<T *>(d.s), *w = static_cast<T *>(d.w);
     double gam = 0.0, ff = 0.0;
     const bool lumped = bp.solver == SOLVER_LUMPED;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const size_t k = 3 * (size_t)row + i;
-        const double fi = valid ? f[i] : 0.0;
+    if (store) {
+        const size_t k = 3 * (size_t)row + c;
+        const double fi = valid ? f : 0.0;
         if (!use_given_rhs) d.rhs[k] = fi;
         const T ri = (T)fi;
         const T ui = dinv[k] * ri;
@@ -615,8 +629,8 @@ __global__ void __launch_bounds__(NODE_TILE) k_nodes(DeviceBatch d, int use_give
         p[k] = (T)0;
         sv[k] = (T)0;
         w[k] = (T)0;
-        gam += (double)ri * (double)ui;
-        ff += fi * fi;
+        gam = (double)ri * (double)ui;
+        ff = fi * fi;
     }
     const double in[2] = {gam, ff};
     double sums[2];
@@ -2773,7 +2787,7 @@ void launch_noise(const DeviceBatch &d, cudaStream_t s)
 
 void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs)
 {
-    PREC_DISPATCH(d, k_nodes, d.n_tiles, NODE_TILE, s, d, use_given_rhs);
+    PREC_DISPATCH(d, k_nodes, d.n_tiles, NODE_TILE * NODE_LANES, s, d, use_given_rhs);
 }
 
 template <typename T>

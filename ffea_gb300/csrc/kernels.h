@@ -8,7 +8,6 @@
 
 #include "layout.h"
 
-struct cublasContext;  // cublas_v2.h: cublasHandle_t is a cublasContext *
 
 namespace ffea {
 
@@ -197,8 +196,12 @@ int mpnn_backward(const DeviceBatch &d, MpnnBuffers &B, const float *theta_dev, 
 // mesh, and `iterations` Newton-Schulz updates of X ~ A_c^-1 per blob
 // (`init`: from I / ||A_c||_inf).  0 on success.
 void launch_coarse_assemble(const DeviceBatch &d, cudaStream_t s);
-int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, ::cublasContext *cb, cudaStream_t s,
-                   int iterations, bool init);
+int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cudaStream_t s, int iterations,
+                   bool init);
+// C = alpha A B + beta D over `batch` row-major n x n FP32 matrices n^2 apart
+// (D may be null when beta = 0), enqueued on s
+void sgemm_batched(const float *A, const float *B, const float *D, float *C, int n, int batch, float alpha, float beta,
+                   cudaStream_t s);
 // CTAs of the persistent CG kernel (register-resident variant with dyn_bytes
 // of dynamic shared memory, or not) that fit co-resident on the current
 // device, 0 on error

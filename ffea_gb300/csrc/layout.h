@@ -15,6 +15,7 @@
 namespace ffea {
 
 constexpr int NODE_TILE = 256;   // rows per CTA of node-space kernels
+constexpr int NODE_LANES = 4;    // threads per row of the node kernel (k_nodes)
 constexpr int ELEM_TILE = 128;   // elements per CTA of the element kernel
 constexpr int EDGE_TILE = 256;
 constexpr int MAX_BLOBS = 1 << 20;

@@ -157,6 +157,20 @@ class World:
         L.check(L.lib().ffea_gpu_diag_spmv(self._h, int(variant), int(reps), ctypes.byref(us)), "diag_spmv")
         return us.value
 
+    def coarse(self, blob: int = 0):
+        """(A_c, X) of a blob's two-level coarse space as float32 arrays (n x n),
+        or None when the handle has none."""
+        n = ctypes.c_int32()
+        L.check(L.lib().ffea_gpu_diag_coarse(self._h, int(blob), ctypes.byref(n), None, None), "diag_coarse")
+        if n.value == 0:
+            return None
+        a = np.zeros((n.value, n.value), np.float32)
+        x = np.zeros((n.value, n.value), np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.check(L.lib().ffea_gpu_diag_coarse(self._h, int(blob), ctypes.byref(n), a.ctypes.data_as(fp),
+                                             x.ctypes.data_as(fp)), "diag_coarse")
+        return a, x
+
     def set_timing(self, on: bool):
         L.check(L.lib().ffea_gpu_set_timing(self._h, 1 if on else 0))
 

@@ -291,6 +291,19 @@ int ffea_gpu_last_error(char *buf, size_t len);
  * scratch vector w. */
 int ffea_gpu_diag_spmv(ffea_gpu_t *h, int32_t variant, int32_t reps, double *us_per_spmv);
 
+/* The two-level preconditioner's dense coarse matrix A_c of one blob and
+ * its current inverse X ~ A_c^-1 (Newton-Schulz), each n x n FP32 row-major,
+ * copied to host arrays (either may be NULL; query n first with both NULL).
+ * n = 0 when the handle has no coarse space.  No reference counterpart. */
+int ffea_gpu_diag_coarse(ffea_gpu_t *h, int32_t blob, int32_t *n, float *coarse_matrix, float *inverse);
+
+/* The coarse space's dense product on DEVICE arrays: c = alpha a b + beta d
+ * for `batch` row-major n x n FP32 matrices n^2 apart (d may be NULL when
+ * beta = 0; c may be d), enqueued on `stream` (cudaStream_t).  No reference
+ * counterpart: a test point for the Newton-Schulz update. */
+int ffea_gpu_diag_sgemm(const float *a, const float *b, const float *d, float *c, int32_t n, int32_t batch,
+                        float alpha, float beta, void *stream);
+
 /* Number of kernel launches the library issued so far (all handles). */
 int64_t ffea_gpu_kernel_launches(void);
 
