@@ -25,8 +25,11 @@ replicas of the 20 nm sphere), ensemble64 (64 uneven blobs), heldout (the
 learned preconditioner's held-out family, 10-50 nm).  Each line carries the
 roofline of k_cg and of every step kernel (kernel_roofline).
 
-N > 1 runs under torchrun, one replica blob per GPU with its own RNG stream
-(the path does not shard a single blob: replicas only, weak scaling).
+N > 1 runs under torchrun, one process per GPU and no exchange while
+stepping (weak scaling).  A single-blob workload runs one replica per GPU
+with its own RNG stream (a single blob does not shard).  A multi-blob
+workload runs N replicas of its blobs, packed over the GPUs by estimated
+bytes per step (ffea_gb300.partition).
 """
 from __future__ import annotations
 
@@ -263,6 +266,16 @@ def max_over_ranks(x: float, world: int, device="cuda") -> float:
     return float(t.item())
 
 
+def sum_over_ranks(x: float, world: int, device="cuda") -> float:
+    """The whole job's total of a per-rank count (host-side, after the timed region)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+    return float(t.item())
+
+
 def aggregate_throughput(nodes_per_replica: int, steps: int, world: int, seconds: float) -> float:
     """Whole-job node-steps/s: every replica advances all its linear nodes each step."""
     return nodes_per_replica * steps * world / seconds
@@ -378,7 +391,8 @@ def measure_arm(args, specs, precond: str, world: int, local: int):
     loops = w.cg_loop_count() - loops0
     launches = kernel_launches() - launches0
     total_ms = max_over_ranks(total_ms, world)
-    value = aggregate_throughput(N, K, world, total_ms / 1e3)
+    N_job = sum_over_ranks(N, world)  # every rank's linear nodes (replicas or ensemble shards)
+    value = N_job * K / (total_ms / 1e3)
 
     # end to end through the C ABI with the caller's pinned host buffers (all
     # N_t nodes in the reference's order), per step: set_nodes of the step's
@@ -408,7 +422,7 @@ def measure_arm(args, specs, precond: str, world: int, local: int):
             b_.get_nodes(out=buf)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     h2d = sum((2 if rv else 1) * 3 * 8 * s_.mesh.num_nodes for s_, rv in zip(specs, reads_vel))
-    e2e = {"value": aggregate_throughput(N, Ke, world, e2e_s), "unit": "node-steps/s",
+    e2e = {"value": N_job * Ke / e2e_s, "unit": "node-steps/s",
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 3 * 3 * 8 * Nt, "steps": Ke,
            "copies": "H2D: positions (+ velocities for mass solvers); D2H: positions, velocities, forces"}
 
@@ -445,7 +459,19 @@ def run_gb300(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    specs = build_specs(args.workload, rank, args.precision)
+    from ffea_gb300 import partition, workloads
+    shard = None
+    if world > 1 and workloads.blob_count(args.workload) > 1:
+        # an ensemble shards: `world` replicas of the workload's blobs, packed
+        # over the ranks by estimated bytes per step (no exchange while stepping)
+        plan, loads = partition.ensemble_plan(workloads.blob_radii(args.workload), world)
+        specs = workloads.build_items(args.workload, plan[rank], args.precision)
+        shard = {"method": "greedy size-balanced bin packing by estimated HBM bytes per step "
+                           "(ffea_gb300.partition)", "replicas": world,
+                 "blobs_total": sum(len(b) for b in plan), "blobs_per_rank": [len(b) for b in plan],
+                 "load_imbalance": max(loads) / (sum(loads) / len(loads))}
+    else:
+        specs = build_specs(args.workload, rank, args.precision)
     main_arm = measure_arm(args, specs, args.precond, world, local)
     plain = two_level = None
     if main_arm["preconditioner"] != "jacobi" and not args.no_plain:
@@ -494,6 +520,8 @@ def run_gb300(args):
     }
     if main_arm["autotune"]:
         line["autotune"] = main_arm["autotune"]
+    if shard is not None:
+        line["config"]["sharding"] = shard
     line["config"]["edges"] = int(nedges)
     line["config"]["solver"] = (f"CG_nomass, {main_arm['preconditioner']} preconditioner, epsilon 1e-6, "
                                 "convergence confirmed by an FP64 true residual")

@@ -87,6 +87,8 @@ SIGNATURES = {
     "ffea_gpu_diag_spmv": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _dp]),
     "ffea_gpu_diag_coarse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
                                             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "ffea_gpu_diag_cg_vectors": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp]),
     "ffea_gpu_diag_sgemm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_float,
                                            ctypes.c_void_p]),

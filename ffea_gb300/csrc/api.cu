@@ -551,6 +551,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     }
     CK(A.alloc(d.epartials, 2 * (size_t)H.n_etiles));
     CK(A.alloc(d.cg, (size_t)H.num_blobs));
+    CK(A.alloc(d.last_sums, 3 * (size_t)H.num_blobs));
     CK(A.alloc(d.counters, (size_t)CNT_COUNT));
     CK(A.alloc(d.status, (size_t)H.num_blobs));
     CK(A.alloc(d.inverted, (size_t)H.num_blobs));
@@ -1349,5 +1350,22 @@ extern "C" int ffea_gpu_diag_sgemm(const float *a, const float *b, const float *
     if (n > 46340) return fail("n = %d: n^2 exceeds the int32 index range of a batch stride", n);
     sgemm_batched(a, b, beta != 0.f ? d : nullptr, c, n, batch, alpha, beta, static_cast<cudaStream_t>(stream));
     CK(cudaGetLastError());
+    return FFEA_GPU_OK;
+}
+
+extern "C" int ffea_gpu_diag_cg_vectors(ffea_gpu_t *h, int32_t blob, int32_t *rows, void *r, void *u, void *w,
+                                        double *sums)
+{
+    if (!h || !rows) return fail("bad arguments");
+    if (blob < 0 || blob >= (int32_t)h->host.bp.size()) return fail("blob index %d out of range", blob);
+    const BlobParams &bp = h->host.bp[blob];
+    *rows = bp.node_pad;  // the blob's rows with its padding rows (zero vectors)
+    CK(cudaStreamSynchronize(h->stream));
+    const size_t ts = h->dev.precision == PREC_FP64 ? sizeof(double) : sizeof(float);
+    const size_t off = 3 * (size_t)bp.node_off * ts, bytes = 3 * (size_t)bp.node_pad * ts;
+    if (r) CK(cudaMemcpy(r, static_cast<char *>(h->dev.r) + off, bytes, cudaMemcpyDeviceToHost));
+    if (u) CK(cudaMemcpy(u, static_cast<char *>(h->dev.u) + off, bytes, cudaMemcpyDeviceToHost));
+    if (w) CK(cudaMemcpy(w, static_cast<char *>(h->dev.w) + off, bytes, cudaMemcpyDeviceToHost));
+    if (sums) CK(cudaMemcpy(sums, h->dev.last_sums + 3 * (size_t)blob, 3 * sizeof(double), cudaMemcpyDeviceToHost));
     return FFEA_GPU_OK;
 }

@@ -1491,6 +1491,14 @@ __device__ __forceinline__ void cg_coefs<double>(const CgScalars &cg, double &al
     beta = cg.beta;
 }
 
+// The iteration's reduced sums (r.u, w.u, r.r) as the transition received
+// them, kept per blob for inspection of the reduction's accuracy.
+__device__ __forceinline__ void record_sums(const DeviceBatch &d, int b, const DF sums[3])
+{
+#pragma unroll
+    for (int i = 0; i < 3; i++) d.last_sums[3 * (size_t)b + i] = (double)sums[i].hi + (double)sums[i].lo;
+}
+
 // The transition run by the CTA that arrived last at a reducing barrier
 // (exactly once per blob), on the blob's record in global memory.
 __device__ __forceinline__ void cg_transition(const DeviceBatch &d, int b, const DF sums[3])
@@ -1505,6 +1513,7 @@ __device__ __forceinline__ void cg_transition(const DeviceBatch &d, int b, const
         for (int i = 0; i < (int)(sizeof(CgScalars) / 8); i++) dst[i] = __ldcg(src + i);
     }
     int bits;
+    record_sums(d, b, sums);
     if (transition_core(cg, d.bp[b], sums, &bits, d.precision == PREC_MIXED)) {
         atomicSub(&d.bar[2], 1u);
         if (bits) atomicOr(&d.status[b], bits);
@@ -1828,6 +1837,7 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
             DF sums[3];
             block_blob_sums(d, part, b, sums, sm);
             if (threadIdx.x == 0) {
+                if (blockIdx.x == 0) record_sums(d, b, sums);
                 int bits;
                 if (transition_core(s_cg[b], d.bp[b], sums, &bits, fast) && bits && blockIdx.x == 0)
                     atomicOr(&d.status[b], bits);
@@ -1841,6 +1851,7 @@ __device__ __forceinline__ unsigned int local_reduce(const DeviceBatch &d, const
             DF sums[3];
             warp_blob_sums(d, part, b, sums);
             if (lane == 0) {
+                if (blockIdx.x == 0) record_sums(d, b, sums);
                 int bits;
                 if (transition_core(s_cg[b], d.bp[b], sums, &bits, fast) && bits && blockIdx.x == 0)
                     atomicOr(&d.status[b], bits);

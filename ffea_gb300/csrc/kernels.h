@@ -84,6 +84,7 @@ struct DeviceBatch {
     // reductions / status
     double *partials = nullptr;     // 4 per node tile (node kernel); CG: two buffers of part_stride floats per segment
     CgScalars *cg = nullptr;        // per blob
+    double *last_sums = nullptr;    // per blob: r.u, w.u, r.r of the last reduction (written by CTA 0)
     unsigned int *counters = nullptr;  // one per reduction site
     unsigned int *bar = nullptr;    // grid barrier: arrival count, generation
     int32_t *status = nullptr;      // per blob failure bits

@@ -91,3 +91,45 @@ def build_specs(workload: str, rank: int = 0, precision: str = "mixed", epsilon:
 def blob_count(workload: str) -> int:
     w = WORKLOADS[workload]
     return int(w.get("replicas") or (len(w["radii"]) if w.get("radii") else 0) or w.get("blobs") or 1)
+
+
+def blob_radii(workload: str):
+    """Radius (nm) of every blob of one replica of the workload, in blob order."""
+    w = WORKLOADS[workload]
+    if w.get("replicas"):
+        return [w["radius_nm"]] * w["replicas"]
+    if w.get("radii"):
+        return list(w["radii"])
+    if w.get("blobs"):
+        return [r for r, _ in ensemble_members(w["blobs"])]
+    return [w["radius_nm"]]
+
+
+def build_items(workload: str, items, precision: str = "mixed", epsilon: float = 1e-6):
+    """The blobs (replica, index) of `items`: blob `index` of the workload's
+    replica `replica`, with that replica's RNG seed, so that the blobs a rank
+    steps do not depend on which rank steps them.  Meshes shared by several
+    items are built once."""
+    from .mesh import make_blob, sphere_mesh
+    w = WORKLOADS[workload]
+    cache = {}
+
+    def mesh(radius, seed):
+        key = (radius, seed)
+        if key not in cache:
+            cache[key] = sphere_mesh(radius, cell_nm=w["cell_nm"], seed=seed)
+        return cache[key]
+
+    out = []
+    for rep, i in items:
+        if w.get("replicas"):
+            out.append(make_blob(mesh(w["radius_nm"], 0), params(100000 * (rep + 1) + i, precision, epsilon)))
+        elif w.get("radii"):
+            out.append(make_blob(mesh(w["radii"][i], 10 + i), params(2000 * (rep + 1) + i, precision, epsilon)))
+        elif w.get("blobs"):
+            r, g = ensemble_members(w["blobs"])[i]
+            out.append(make_blob(mesh(r, i), params(1000 * (rep + 1) + i, precision, epsilon),
+                                 shear_mod=3.7e8 * g, bulk_mod=1.1e9 * g))
+        else:
+            out.append(make_blob(mesh(w["radius_nm"], 0), params(replica_seed(rep), precision, epsilon)))
+    return out

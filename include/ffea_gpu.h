@@ -304,6 +304,18 @@ int ffea_gpu_diag_coarse(ffea_gpu_t *h, int32_t blob, int32_t *n, float *coarse_
 int ffea_gpu_diag_sgemm(const float *a, const float *b, const float *d, float *c, int32_t n, int32_t batch,
                         float alpha, float beta, void *stream);
 
+/* The CG vectors r, u = M r and w = A u of one blob's rows as the solver
+ * holds them in memory (the arithmetic type: float in mixed precision,
+ * double in FP64; 3 per row, the handle's internal row order; `rows` rows,
+ * the blob's rows and its padding rows, whose vectors are zero: query `rows`
+ * first with NULL arrays),
+ * and the sums r.u, w.u, r.r of the solver's last reduction for that blob.
+ * The vectors are kept in memory by the memory-resident solve (environment
+ * FFEA_GPU_CG_MEMORY_STATE=1 at creation forces it); after a converged solve
+ * they and the sums belong to the same iteration.  Any pointer may be NULL.
+ * No reference counterpart: a test point for the reductions' accuracy. */
+int ffea_gpu_diag_cg_vectors(ffea_gpu_t *h, int32_t blob, int32_t *rows, void *r, void *u, void *w, double *sums);
+
 /* Number of kernel launches the library issued so far (all handles). */
 int64_t ffea_gpu_kernel_launches(void);
 

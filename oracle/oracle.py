@@ -19,21 +19,34 @@ FAST_SO = os.path.join(HERE, "liboracle_fast.so")
 FAST_FLAGS = "-O3 -ffast-math -fopenmp (FFEA's GNU release flags without -march=native)"
 REF_SO = os.path.join(HERE, "_ref", "libffea_ref.so")
 REF_KAT = os.path.join(HERE, "_ref", "test_rngstream")
-REFERENCE_SRC = os.environ.get("FFEA_REFERENCE_SRC", "/root/reference")
+SOURCE_RECORD = os.path.join(HERE, "_ref", "SOURCE")
+
+
+def reference_src():
+    """The FFEA source tree: FFEA_REFERENCE_SRC, else the tree the reference
+    objects in oracle/_ref were built from (recorded there by `make ref`);
+    None when neither is known or the tree is absent."""
+    path = os.environ.get("FFEA_REFERENCE_SRC")
+    if not path and os.path.exists(SOURCE_RECORD):
+        with open(SOURCE_RECORD) as fh:
+            path = fh.read().strip()
+    return path if path and os.path.isdir(os.path.join(path, "src")) else None
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 
 
-def build(ref: bool | None = None, quiet: bool = True) -> None:
-    """Compile the oracle (and the reference objects when their sources exist)."""
+def build(ref: bool | None = None, quiet: bool = True, source: str | None = None) -> None:
+    """Compile the oracle, and the reference objects from the FFEA sources at
+    `source` (default reference_src()) when they are present."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", HERE, "port", "fast"], check=True, stdout=out)
+    src = source or reference_src()
     if ref is None:
-        ref = os.path.isdir(os.path.join(REFERENCE_SRC, "src"))
-    if ref:
-        subprocess.run(["make", "-C", HERE, "-j8", "ref", f"REF={REFERENCE_SRC}"], check=True, stdout=out)
+        ref = src is not None
+    if ref and src:
+        subprocess.run(["make", "-C", HERE, "-j8", "ref", f"REF={src}"], check=True, stdout=out)
 
 
 def _ptr(a, t):

@@ -92,4 +92,9 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", ".."))
+    from oracle import oracle as O
+    src = sys.argv[1] if len(sys.argv) > 1 else O.reference_src()
+    if not src:
+        raise SystemExit("usage: make_cubes_lj.py <FFEA source tree> (or set FFEA_REFERENCE_SRC)")
+    main(src)

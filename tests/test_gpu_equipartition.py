@@ -98,3 +98,37 @@ def test_mass_solver_equipartition(gpulib):
     ke_ratio, se_ratio = np.mean(ke) / ke_th, np.mean(se) / se_th
     assert abs(ke_ratio - 1.0) < 0.04, ke_ratio
     assert abs(se_ratio - 1.0) < 0.03, se_ratio
+
+
+def test_equipartition_256_replicas_20nm_learned(gpulib):
+    """The ensemble statistics at their stated size: 256 replicas of the
+    32^3-cell, 20 nm sphere (19,663 corner nodes each, 5.03 M in the batch)
+    with distinct RNG seeds, NoMass, the learned two-level preconditioner
+    with the committed network weights, every solve at relative residual
+    1e-6 and confirmed by the FP64 true residual, mixed precision.  1,000
+    steps of burn-in (3.7 relaxation times eta/G), then 8 samples 250 steps
+    apart (3,000 steps in all).  The mean strain energy must be
+    kT (3N - 6) / 2 within 2 % (the reference's criterion,
+    tests/physics/sphere_63_120_nomass/averages.py:51-55, at a tighter
+    tolerance); the per-sample spread sqrt(2 / (3N - 6)) = 0.58 % makes the
+    mean of 2,048 samples good to about 0.02 %."""
+    from ffea_gb300 import learned
+    from ffea_gb300.workloads import build_specs
+    from ffea_gb300.world import PRECOND_LEARNED, World
+    specs = build_specs("replicas256", 0, "mixed", epsilon=1e-6)
+    assert len(specs) == 256 and specs[0].mesh.num_linear == 19663
+    n = specs[0].mesh.num_linear
+    expected = specs[0].params.kT * (3 * n - 6) / 2
+    samples = []
+    with World(specs, true_residual=True, preconditioner=PRECOND_LEARNED) as w:
+        assert w.preconditioner() == PRECOND_LEARNED
+        learned.apply(w, learned.load())
+        w.run(1000)
+        for _ in range(8):
+            w.run(250)
+            samples.append([w.blob(i).energies()[0] for i in range(len(specs))])
+            for i in range(len(specs)):
+                st = w.blob(i).status()
+                assert st["fail_bits"] == 0 and st["true_relres"] < 1e-6, (i, st)
+    ratio = np.asarray(samples).mean() / expected
+    assert abs(ratio - 1.0) < 0.02, ratio

@@ -89,8 +89,13 @@ def test_oracle_matches_reference_golden(oracle, path):
         assert np.array_equal(b.rng_state(), g[f"rng_{s}"]), s
 
 
-REF_MESH = os.path.join(os.environ.get("FFEA_REFERENCE_SRC", "/root/reference"),
-                        "tests/physics/sphere_63_120_structure/sphere_63_120")
+def _ref_mesh():
+    from oracle import oracle as O
+    src = O.reference_src()
+    return os.path.join(src, "tests/physics/sphere_63_120_structure/sphere_63_120") if src else ""
+
+
+REF_MESH = _ref_mesh()
 
 
 @pytest.mark.skipif(not os.path.exists(REF_MESH + ".node"), reason="FFEA sources not present")
