@@ -548,6 +548,8 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
         // Newton-Schulz scratch for a run of equal-size blobs at once
         CK(A.alloc(d.coarse_T, std::max((size_t)coarse_nmax * coarse_nmax, (size_t)coarse_total)));
         CK(A.alloc(d.coarse_Xn, std::max((size_t)coarse_nmax * coarse_nmax, (size_t)coarse_total)));
+        if (const size_t np = coarse_part_floats(H.bp)) CK(A.alloc(d.coarse_part, np));
+        CK(A.alloc(d.coarse_asm, 36 * (size_t)(CG_SEG_MAX_ROWS / 256) * std::max<size_t>(1, H.seg_nbr.size())));
     }
     CK(A.alloc(d.epartials, 2 * (size_t)H.n_etiles));
     CK(A.alloc(d.cg, (size_t)H.num_blobs));
@@ -1348,8 +1350,17 @@ extern "C" int ffea_gpu_diag_sgemm(const float *a, const float *b, const float *
 {
     if (!a || !b || !c || n <= 0 || batch <= 0 || batch > 65535 || (beta != 0.f && !d)) return fail("bad arguments");
     if (n > 46340) return fail("n = %d: n^2 exceeds the int32 index range of a batch stride", n);
-    sgemm_batched(a, b, beta != 0.f ? d : nullptr, c, n, batch, alpha, beta, static_cast<cudaStream_t>(stream));
-    CK(cudaGetLastError());
+    // the split-K scratch of a large product (diagnostics may allocate)
+    const int sp = sgemm_splits(n, batch);
+    float *part = nullptr;
+    if (sp > 1) CK(cudaMalloc(&part, sizeof(float) * (size_t)sp * batch * n * n));
+    sgemm_batched(a, b, beta != 0.f ? d : nullptr, c, n, batch, alpha, beta, part, static_cast<cudaStream_t>(stream));
+    cudaError_t e = cudaGetLastError();
+    if (part) {
+        if (e == cudaSuccess) e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+        cudaFree(part);
+    }
+    CK(e);
     return FFEA_GPU_OK;
 }
 

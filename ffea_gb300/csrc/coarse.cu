@@ -9,7 +9,9 @@
 // matrix of each blob (6 x segments square, dense).
 //
 //   k_coarse_assemble  A_c blocks (s, t) for the segments t coupled to s,
-//                      once per step (the matrix changes with the mesh)
+//   k_coarse_sum       at every refresh (the matrix changes with the mesh):
+//                      partial blocks per quarter of a segment's rows, then
+//                      their sum in a fixed order
 //   coarse_refresh     X ~ A_c^-1 by Newton-Schulz, X <- 2X - X A_c X (two
 //                      FP32 GEMMs, k_sgemm below) from the previous step's
 //                      X; `init` starts from X = I / ||A_c||_inf and
@@ -29,7 +31,7 @@ namespace ffea {
 namespace {
 
 constexpr int kAsmThreads = 256;
-constexpr int kAsmRows = CG_SEG_MAX_ROWS / kAsmThreads;  // rows per thread
+constexpr int kAsmParts = CG_SEG_MAX_ROWS / kAsmThreads;  // CTAs per segment, one row per thread
 
 // C (6 x 6, row-major) += Phi_p^T K Phi_q for rest offsets dp, dq.
 __device__ __forceinline__ void add_block(float C[36], const float dp[3], const float K[9], const float dq[3])
@@ -76,49 +78,73 @@ __device__ __forceinline__ void load_K(const DeviceBatch &d, int base, int j, in
     for (int k = 0; k < 9; k++) K[k] = (float)val[vb + 32 * k];
 }
 
-// One CTA per segment s of a NoMass blob.  A row's slots are sorted by
-// column and segments are contiguous row ranges, so the slots of each coupled
-// segment t form one run: a cursor per row walks them once over the targets.
-// Each (s, t) block is a fixed-order block reduction (deterministic).
+// Sums of 32 values per lane over a warp by a transposed butterfly (16 + 8
+// + 4 + 2 + 1 shuffles): at each offset a lane keeps half of its values and
+// adds its partner's copy of that half.  Lane l returns the warp total of
+// value l (a fixed order per value: deterministic).
+__device__ __forceinline__ float warp_sum32_transposed(float (&v)[36])
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+        const bool upper = (lane & h) != 0;
+#pragma unroll
+        for (int i = 0; i < h; i++) {
+            const float send = upper ? v[i] : v[i + h];
+            const float keep = upper ? v[i + h] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+        }
+    }
+    return v[0];
+}
+
+// Partial coarse blocks: CTA (s, part) of a NoMass blob's segment s takes
+// rows part * 256 .. part * 256 + 255 of the segment, one row per thread.  A
+// row's slots are sorted by column and segments are contiguous row ranges,
+// so the slots of each coupled segment t form one run: a cursor per row walks
+// them once over the targets.  Each (s, t) block of the CTA's rows is a
+// fixed-order block reduction, written to part slot (k, part) of the
+// segment's neighbour entry k; k_coarse_sum adds the parts in order.
 template <typename T>
 __global__ void __launch_bounds__(kAsmThreads) k_coarse_assemble(DeviceBatch d)
 {
-    const int s = blockIdx.x;
+    const int s = blockIdx.x, part = blockIdx.y;
     const int b = d.seg_blob[s];
     const BlobParams &bp = d.bp[b];
     if (bp.solver != SOLVER_NOMASS) return;  // CTA-uniform
     const int r0 = d.seg_row0[s], nrows = d.seg_rows[s];
-    const int nc = bp.coarse_n, ls = s - bp.seg_off;
-    float *Ac = d.coarse_A + bp.coarse_xoff;
     const int lane32 = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ float red[36][kAsmThreads / 32];
 
-    int cursor[kAsmRows];
-#pragma unroll
-    for (int i = 0; i < kAsmRows; i++) cursor[i] = 0;
+    const int rr = part * kAsmThreads + threadIdx.x;
+    const int p = r0 + rr;
+    const bool active = rr < nrows && !(d.flags[p] & NODE_PINNED);
+    float dp[3] = {0.f, 0.f, 0.f};
+    int L = 0, base = 0;
+    const int lane = p & 31;
+    if (active) {
+        const float4 fp = d.phi[p];
+        dp[0] = fp.x;
+        dp[1] = fp.y;
+        dp[2] = fp.z;
+        L = d.slice_len[p >> 5];
+        base = d.slice_ptr[p >> 5];
+    }
+    int j = 0;
     for (int k = d.seg_nbr_ptr[s]; k < d.seg_nbr_ptr[s + 1]; k++) {
         const int t = d.seg_nbr[k];
         float C[36];
 #pragma unroll
         for (int i = 0; i < 36; i++) C[i] = 0.f;
-#pragma unroll
-        for (int i = 0; i < kAsmRows; i++) {
-            const int rr = threadIdx.x + i * kAsmThreads;
-            if (rr >= nrows) continue;
-            const int p = r0 + rr;
-            if (d.flags[p] & NODE_PINNED) continue;
-            const float4 fp = d.phi[p];
-            const float dp[3] = {fp.x, fp.y, fp.z};
-            const int sl = p >> 5, lane = p & 31;
-            const int L = d.slice_len[sl], base = d.slice_ptr[sl];
+        if (active) {
             float K[9];
             if (t == s) {
                 // diagonal of A in difference form: zeta_p I - sum_q K_pq
                 float S[9];
 #pragma unroll
                 for (int m = 0; m < 9; m++) S[m] = 0.f;
-                for (int j = 0; j < L; j++) {
-                    load_K<T>(d, base, j, lane, K);
+                for (int jj = 0; jj < L; jj++) {
+                    load_K<T>(d, base, jj, lane, K);
 #pragma unroll
                     for (int m = 0; m < 9; m++) S[m] -= K[m];
                 }
@@ -128,7 +154,6 @@ __global__ void __launch_bounds__(kAsmThreads) k_coarse_assemble(DeviceBatch d)
                 S[8] += z;
                 add_block(C, dp, S, dp);
             }
-            int j = cursor[i];
             while (j < L) {
                 const int q = d.sell_col[base + 32 * j + lane];
                 const int tq = d.seg_of_row[q];
@@ -141,24 +166,48 @@ __global__ void __launch_bounds__(kAsmThreads) k_coarse_assemble(DeviceBatch d)
                 }
                 j++;
             }
-            cursor[i] = j;
         }
-        // fixed-order block reduction of the 36 entries
+        // fixed-order block reduction of the 36 entries: 32 by the transposed
+        // butterfly, 4 by plain butterflies, then the warps in order
+        float tail[4];
 #pragma unroll
-        for (int i = 0; i < 36; i++) {
-            float v = C[i];
+        for (int i = 0; i < 4; i++) {
+            float v = C[32 + i];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane32 == 0) red[i][warp] = v;
+            tail[i] = v;
         }
+        red[lane32][warp] = warp_sum32_transposed(C);
+        if (lane32 < 4) red[32 + lane32][warp] = tail[lane32];
         __syncthreads();
         if (threadIdx.x < 36) {
             float v = 0.f;
+#pragma unroll
             for (int w = 0; w < kAsmThreads / 32; w++) v += red[threadIdx.x][w];
-            const int li = threadIdx.x / 6, mi = threadIdx.x % 6, lt = t - bp.seg_off;
-            Ac[(size_t)(6 * ls + li) * nc + (6 * lt + mi)] = v;
+            d.coarse_asm[((size_t)k * kAsmParts + part) * 36 + threadIdx.x] = v;
         }
         __syncthreads();
+    }
+}
+
+// A_c block (s, t) of every neighbour entry k of segment s: the sum of the
+// kAsmParts partial blocks in part order.
+__global__ void k_coarse_sum(DeviceBatch d)
+{
+    const int s = blockIdx.x;
+    const int b = d.seg_blob[s];
+    const BlobParams &bp = d.bp[b];
+    if (bp.solver != SOLVER_NOMASS) return;
+    const int nc = bp.coarse_n, ls = s - bp.seg_off;
+    float *Ac = d.coarse_A + bp.coarse_xoff;
+    const int k0 = d.seg_nbr_ptr[s], nk = d.seg_nbr_ptr[s + 1] - k0;
+    for (int x = threadIdx.x; x < 36 * nk; x += blockDim.x) {
+        const int k = k0 + x / 36, i = x % 36;
+        float v = 0.f;
+#pragma unroll
+        for (int pt = 0; pt < kAsmParts; pt++) v += d.coarse_asm[((size_t)k * kAsmParts + pt) * 36 + i];
+        const int li = i / 6, mi = i % 6, lt = d.seg_nbr[k] - bp.seg_off;
+        Ac[(size_t)(6 * ls + li) * nc + (6 * lt + mi)] = v;
     }
 }
 
@@ -207,19 +256,27 @@ __global__ void k_scaled_identity(const float *__restrict__ A, float *__restrict
 // 16 through double-buffered shared memory, the next step's tile loaded into
 // registers while the current one is multiplied.  Every C entry is a
 // sequential FMA chain over k: deterministic.
+//
+// Split-K (splits > 1): blockIdx.z = product * splits + split; the CTA sums
+// k over its chunk [split * kchunk, (split + 1) * kchunk) only and writes the
+// raw partial tile to part (one n x n block per z); k_splitk_sum then adds
+// the splits in order and applies alpha, beta and D.
 template <int BM>
-__global__ void __launch_bounds__(256) k_sgemm(const float *__restrict__ A, const float *__restrict__ B,
-                                               const float *D, float *C, int n, float alpha, float beta)
+__global__ void __launch_bounds__(256, 2) k_sgemm(const float *__restrict__ A, const float *__restrict__ B,
+                                               const float *D, float *C, int n, float alpha, float beta,
+                                               int splits, int kchunk, float *__restrict__ part)
 {
     constexpr int BK = 16, TM = BM / 16, H = TM / 2, LA = BM / 16, LB = BM / 16;
     constexpr int PAD = 4;
     __shared__ __align__(16) float As[2][BK][BM + PAD];
     __shared__ __align__(16) float Bs[2][BK][BM + PAD];
-    const size_t off = (size_t)blockIdx.z * n * n;
+    const int prod = blockIdx.z / splits, sp = blockIdx.z % splits;
+    const size_t off = (size_t)prod * n * n;
     A += off;
     B += off;
     C += off;
     if (D) D += off;
+    const int kbeg = sp * kchunk, kend = min(n, kbeg + kchunk);
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int i0 = blockIdx.y * BM, j0 = blockIdx.x * BM;
     float acc[TM][TM];
@@ -234,12 +291,12 @@ __global__ void __launch_bounds__(256) k_sgemm(const float *__restrict__ A, cons
 #pragma unroll
         for (int r = 0; r < LA; r++) {
             const int row = i0 + (tid >> 4) + 16 * r, col = k0 + (tid & 15);
-            ra[r] = (row < n && col < n) ? A[(size_t)row * n + col] : 0.f;
+            ra[r] = (row < n && col < kend) ? A[(size_t)row * n + col] : 0.f;
         }
 #pragma unroll
         for (int r = 0; r < LB; r++) {
             const int row = k0 + tid / BM + (256 / BM) * r, col = j0 + tid % BM;
-            rb[r] = (row < n && col < n) ? B[(size_t)row * n + col] : 0.f;
+            rb[r] = (row < kend && col < n) ? B[(size_t)row * n + col] : 0.f;
         }
     };
     auto store = [&](int buf) {
@@ -248,13 +305,13 @@ __global__ void __launch_bounds__(256) k_sgemm(const float *__restrict__ A, cons
 #pragma unroll
         for (int r = 0; r < LB; r++) Bs[buf][tid / BM + (256 / BM) * r][tid % BM] = rb[r];
     };
-    const int nk = (n + BK - 1) / BK;
-    load(0);
+    const int nk = (kend - kbeg + BK - 1) / BK;
+    load(kbeg);
     store(0);
     __syncthreads();
     for (int kt = 0; kt < nk; kt++) {
         const int buf = kt & 1;
-        if (kt + 1 < nk) load((kt + 1) * BK);
+        if (kt + 1 < nk) load(kbeg + (kt + 1) * BK);
 #pragma unroll
         for (int k = 0; k < BK; k++) {
             float a[TM], b[TM];
@@ -308,6 +365,10 @@ __global__ void __launch_bounds__(256) k_sgemm(const float *__restrict__ A, cons
             const int col = j0 + (j / H) * (BM / 2) + tx * H + (j % H);
             if (col >= n) continue;
             const size_t o = (size_t)row * n + col;
+            if (splits > 1) {
+                part[(size_t)blockIdx.z * n * n + o] = acc[i][j];
+                continue;
+            }
             float v = alpha * acc[i][j];
             if (beta != 0.f) v += beta * D[o];
             C[o] = v;
@@ -315,12 +376,25 @@ __global__ void __launch_bounds__(256) k_sgemm(const float *__restrict__ A, cons
     }
 }
 
+// The split-K epilogue: C = alpha (sum of the splits, in split order) + beta D.
+__global__ void k_splitk_sum(const float *__restrict__ part, const float *D, float *C, int n, int splits,
+                             float alpha, float beta)
+{
+    const size_t nn = (size_t)n * n;
+    const size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nn) return;
+    const size_t prod = blockIdx.y;
+    const float *p = part + prod * splits * nn + o;
+    float acc = 0.f;
+    for (int sp = 0; sp < splits; sp++) acc += p[(size_t)sp * nn];
+    float v = alpha * acc;
+    if (beta != 0.f) v += beta * D[prod * nn + o];
+    C[prod * nn + o] = v;
+}
+
 }  // namespace
 
-// One batched product on stream s: 128 x 128 tiles when they fill the GPU
-// at least twice over, 64 x 64 tiles otherwise.
-void sgemm_batched(const float *A, const float *B, const float *D, float *C, int n, int batch, float alpha, float beta,
-                   cudaStream_t s)
+int sgemm_sms()
 {
     static int sms = 0;
     if (sms == 0) {
@@ -329,13 +403,45 @@ void sgemm_batched(const float *A, const float *B, const float *D, float *C, int
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }
-    const long long big = (long long)((n + 127) / 128) * ((n + 127) / 128) * batch;
-    if (big >= 2LL * sms) {
+    return sms;
+}
+
+// K splits of a batched product: 1 when its 128 x 128 tiles fill the GPU,
+// else enough to give about two tiles per SM (chunks of at least 128 k).
+int sgemm_splits(int n, int batch)
+{
+    const long long tiles = (long long)((n + 127) / 128) * ((n + 127) / 128) * batch;
+    const int sms = sgemm_sms();
+    if (tiles >= sms || n < 256) return 1;
+    const int want = (int)((2LL * sms + tiles - 1) / tiles);
+    return std::max(1, std::min(want, n / 128));
+}
+
+// One batched product on stream s.  128 x 128 tiles when they fill the GPU
+// or, for larger matrices, with the K dimension split (`part` then holds
+// sgemm_splits(n, batch) n x n floats per product); 64 x 64 tiles for
+// small matrices.
+void sgemm_batched(const float *A, const float *B, const float *D, float *C, int n, int batch, float alpha, float beta,
+                   float *part, cudaStream_t s)
+{
+    const long long tiles = (long long)((n + 127) / 128) * ((n + 127) / 128) * batch;
+    const int splits = part ? sgemm_splits(n, batch) : 1;
+    if (splits > 1) {
+        const int kchunk = ((n + splits - 1) / splits + 15) / 16 * 16;
+        dim3 grid((n + 127) / 128, (n + 127) / 128, batch * splits);
+        k_sgemm<128><<<grid, 256, 0, s>>>(A, B, D, C, n, alpha, beta, splits, kchunk, part);
+        const size_t nn = (size_t)n * n;
+        dim3 g2((unsigned)((nn + 255) / 256), batch);
+        k_splitk_sum<<<g2, 256, 0, s>>>(part, D, C, n, splits, alpha, beta);
+        count_launches(2);
+        return;
+    }
+    if (tiles >= sgemm_sms() || n >= 256) {
         dim3 grid((n + 127) / 128, (n + 127) / 128, batch);
-        k_sgemm<128><<<grid, 256, 0, s>>>(A, B, D, C, n, alpha, beta);
+        k_sgemm<128><<<grid, 256, 0, s>>>(A, B, D, C, n, alpha, beta, 1, n, nullptr);
     } else {
         dim3 grid((n + 63) / 64, (n + 63) / 64, batch);
-        k_sgemm<64><<<grid, 256, 0, s>>>(A, B, D, C, n, alpha, beta);
+        k_sgemm<64><<<grid, 256, 0, s>>>(A, B, D, C, n, alpha, beta, 1, n, nullptr);
     }
     count_launches(1);
 }
@@ -343,20 +449,20 @@ void sgemm_batched(const float *A, const float *B, const float *D, float *C, int
 void launch_coarse_assemble(const DeviceBatch &d, cudaStream_t s)
 {
     if (!d.coarse || d.n_segs == 0) return;
+    const dim3 grid(d.n_segs, kAsmParts);
     if (d.precision == PREC_FP64)
-        k_coarse_assemble<double><<<d.n_segs, kAsmThreads, 0, s>>>(d);
+        k_coarse_assemble<double><<<grid, kAsmThreads, 0, s>>>(d);
     else
-        k_coarse_assemble<float><<<d.n_segs, kAsmThreads, 0, s>>>(d);
-    count_launches(1);
+        k_coarse_assemble<float><<<grid, kAsmThreads, 0, s>>>(d);
+    k_coarse_sum<<<d.n_segs, 256, 0, s>>>(d);
+    count_launches(2);
 }
 
-int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cudaStream_t s, int iterations,
-                   bool init)
+// Runs of consecutive NoMass blobs with the same coarse dimension whose
+// matrices lie n^2 apart: each run is updated by one batched product.
+template <typename F>
+void for_each_coarse_run(const std::vector<BlobParams> &bps, F f)
 {
-    if (!d.coarse) return 0;
-    // runs of consecutive NoMass blobs with the same coarse dimension (their
-    // matrices lie n^2 apart) are updated together by batched products: one
-    // launch sequence for a whole ensemble of replicas
     for (size_t b0 = 0; b0 < bps.size();) {
         const BlobParams &bp = bps[b0];
         const int n = bp.coarse_n;
@@ -368,7 +474,28 @@ int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cud
         while (b1 < bps.size() && b1 - b0 < 65535 && bps[b1].solver == SOLVER_NOMASS && bps[b1].coarse_n == n &&
                (int64_t)bps[b1].coarse_xoff == (int64_t)bp.coarse_xoff + (int64_t)(b1 - b0) * n * n)
             b1++;
-        const int batch = (int)(b1 - b0);
+        f(bp, n, (int)(b1 - b0));
+        b0 = b1;
+    }
+}
+
+size_t coarse_part_floats(const std::vector<BlobParams> &bps)
+{
+    size_t need = 0;
+    for_each_coarse_run(bps, [&](const BlobParams &, int n, int batch) {
+        const int sp = sgemm_splits(n, batch);
+        if (sp > 1) need = std::max(need, (size_t)sp * batch * n * n);
+    });
+    return need;
+}
+
+int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cudaStream_t s, int iterations,
+                   bool init)
+{
+    if (!d.coarse) return 0;
+    // a run of equal-size blobs (an ensemble of replicas) is updated by one
+    // launch sequence of batched products
+    for_each_coarse_run(bps, [&](const BlobParams &bp, int n, int batch) {
         float *A = d.coarse_A + bp.coarse_xoff, *X = d.coarse_X + bp.coarse_xoff;
         float *Tm = d.coarse_T, *Xn = d.coarse_Xn;
         if (init) {
@@ -377,14 +504,13 @@ int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cud
         }
         for (int it = 0; it < iterations; it++) {
             // T = A X; Xn = 2 X - X T; X = sym(Xn)
-            sgemm_batched(A, X, nullptr, Tm, n, batch, 1.f, 0.f, s);
-            sgemm_batched(X, Tm, X, Xn, n, batch, -1.f, 2.f, s);
+            sgemm_batched(A, X, nullptr, Tm, n, batch, 1.f, 0.f, d.coarse_part, s);
+            sgemm_batched(X, Tm, X, Xn, n, batch, -1.f, 2.f, d.coarse_part, s);
             dim3 grid((n + 255) / 256, n, batch);
             k_symmetrize<<<grid, 256, 0, s>>>(Xn, X, n);
             count_launches(1);
         }
-        b0 = b1;
-    }
+    });
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -34,6 +34,8 @@ struct DeviceBatch {
     int32_t *seg_nbr_ptr = nullptr, *seg_nbr = nullptr;   // segments coupled to each segment (itself included)
     float *coarse_A = nullptr, *coarse_X = nullptr;       // per blob: A_c and X ~ A_c^-1 (coarse_xoff)
     float *coarse_T = nullptr, *coarse_Xn = nullptr;      // Newton-Schulz scratch (coarse_nmax^2)
+    float *coarse_part = nullptr;                         // split-K partial products of the Newton-Schulz GEMMs
+    float *coarse_asm = nullptr;                          // partial A_c blocks: 36 floats x CG_SEG_MAX_ROWS / 256 per neighbour entry
     int32_t cg_dyn_smem = 0;      // REG: dynamic shared memory bytes of that copy
     // blobs
     BlobParams *bp = nullptr;
@@ -200,9 +202,13 @@ void launch_coarse_assemble(const DeviceBatch &d, cudaStream_t s);
 int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cudaStream_t s, int iterations,
                    bool init);
 // C = alpha A B + beta D over `batch` row-major n x n FP32 matrices n^2 apart
-// (D may be null when beta = 0), enqueued on s
+// (D may be null when beta = 0), enqueued on s.  part: split-K scratch of
+// sgemm_splits(n, batch) * batch * n^2 floats, or null (no split).
 void sgemm_batched(const float *A, const float *B, const float *D, float *C, int n, int batch, float alpha, float beta,
-                   cudaStream_t s);
+                   float *part, cudaStream_t s);
+int sgemm_splits(int n, int batch);
+// floats of split-K scratch the coarse refresh of these blobs needs (0: none)
+size_t coarse_part_floats(const std::vector<BlobParams> &bps);
 // CTAs of the persistent CG kernel (register-resident variant with dyn_bytes
 // of dynamic shared memory, or not) that fit co-resident on the current
 // device, 0 on error
