@@ -35,6 +35,32 @@ class Mesh(ctypes.Structure):
     ]
 
 
+SCRIPT_PATH_MAX = 1024
+
+
+class ScriptParams(ctypes.Structure):
+    """ffea_gpu_script_params"""
+    _fields_ = [
+        ("dt", ctypes.c_double),
+        ("kT", ctypes.c_double),
+        ("epsilon2", ctypes.c_double),
+        ("stokes_visc", ctypes.c_double),
+        ("num_steps", ctypes.c_int64),
+        ("check", ctypes.c_int32),
+        ("rng_seed", ctypes.c_int32),
+        ("max_iterations_cg", ctypes.c_int32),
+        ("calc_noise", ctypes.c_int32),
+        ("calc_stokes", ctypes.c_int32),
+        ("restart", ctypes.c_int32),
+        ("num_blobs", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("trajectory_out_fname", ctypes.c_char * SCRIPT_PATH_MAX),
+        ("measurement_out_fname", ctypes.c_char * SCRIPT_PATH_MAX),
+        ("checkpoint_in", ctypes.c_char * SCRIPT_PATH_MAX),
+        ("checkpoint_out", ctypes.c_char * SCRIPT_PATH_MAX),
+    ]
+
+
 class Params(ctypes.Structure):
     _fields_ = [
         ("dt", ctypes.c_double),
@@ -87,6 +113,13 @@ SIGNATURES = {
     "ffea_gpu_diag_spmv": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _dp]),
     "ffea_gpu_diag_coarse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
                                             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "ffea_gpu_script_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "ffea_gpu_script_free": (None, [ctypes.c_void_p]),
+    "ffea_gpu_script_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScriptParams)]),
+    "ffea_gpu_script_get_blob": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Mesh),
+                                                ctypes.POINTER(Params)]),
+    "ffea_gpu_script_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                              ctypes.POINTER(ctypes.c_void_p)]),
     "ffea_gpu_diag_cg_vectors": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp]),
     "ffea_gpu_diag_sgemm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT_DIR, "libffea_gb300.so")
-SOURCES = ["kernels.cu", "api.cu", "host_build.cpp", "noalloc.cu", "coarse.cu", "learned.cu", "ssint.cu"]
+SOURCES = ["kernels.cu", "api.cu", "host_build.cpp", "noalloc.cu", "coarse.cu", "learned.cu", "ssint.cu",
+           "script.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -233,12 +233,14 @@ class Recorder:
     checkpoint (rewritten), a trajectory frame and, with `measurement`, a
     measurement row, as FFEA writes them (src/World.cpp:2020-2043,
     4126-4226).  `restart=True` continues existing files: positions and
-    velocities from the last complete frame, RNG states from the checkpoint
+    velocities from the last complete frame, RNG states from `checkpoint_in`
+    (default: the checkpoint file itself)
     (src/World.cpp:330-385, 655-760), and appends; the measurement file keeps
     the rows of the frames before the restart frame, which is written again."""
 
     def __init__(self, world, trajectory: str, checkpoint: str, solvers: Sequence[int], check: int = 1,
-                 restart: bool = False, measurement: str | None = None, script: str = "", num_steps: int = 0):
+                 restart: bool = False, measurement: str | None = None, script: str = "", num_steps: int = 0,
+                 checkpoint_in: str | None = None):
         if check < 1:
             raise ValueError("check must be >= 1")
         self.world, self.check, self.solvers = world, int(check), list(solvers)
@@ -251,7 +253,8 @@ class Recorder:
             self.step, frame = read_last_frame(trajectory, self.nodes)
             for i, (pos, vel) in enumerate(frame):
                 world.blob(i).set_nodes(pos, vel)
-            states = read_checkpoint(checkpoint)
+            # FFEA restarts from checkpoint_in and writes checkpoint_out
+            states = read_checkpoint(checkpoint_in or checkpoint)
             shared = len(states) == 1 and world.num_blobs > 1
             for i in range(world.num_blobs):
                 world.blob(i).set_rng_state(states[0 if shared else i])

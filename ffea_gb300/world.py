@@ -114,6 +114,30 @@ class World:
         self.rng_mode = int(rng_mode)
         L.lib().ffea_gpu_set_graph_mode(self._h, 1 if graph else 0)
 
+    @classmethod
+    def from_script(cls, path: str, precision: int = PRECISION_MIXED, preconditioner: int = PRECOND_JACOBI,
+                    true_residual: bool = True, graph: bool = True) -> "World":
+        """Every blob of an FFEA script (.ffea) in one handle, read by the
+        library's C++ front end (ffea_gpu_script_load / _create)."""
+        from .script import Script
+        with Script(path) as sc:
+            h = ctypes.c_void_p()
+            L.check(L.lib().ffea_gpu_script_create(sc.handle, int(precision), int(preconditioner),
+                                                   int(true_residual), ctypes.byref(h)), "ffea_gpu_script_create")
+            w = cls.__new__(cls)
+            w._h = h
+            w.num_blobs = sc.num_blobs
+            w.rng_mode = RNG_SHARED
+            w.num_nodes, w.num_elements, w.solvers, w.params = [], [], [], []
+            for i in range(sc.num_blobs):
+                b = sc.blob(i)
+                w.num_nodes.append(len(b["pos"]))
+                w.num_elements.append(len(b["topology"]))
+                w.params.append(sc.simulation_params(i, precision))
+                w.solvers.append(w.params[-1].solver)
+        L.lib().ffea_gpu_set_graph_mode(w._h, 1 if graph else 0)
+        return w
+
     # -- lifetime
     def close(self):
         if getattr(self, "_h", None):

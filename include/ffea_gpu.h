@@ -201,6 +201,51 @@ int ffea_gpu_rng_draws(const uint64_t state[6], uint64_t offset, int64_t count, 
 /* World::init's six seed words for an rng_seed (src/World.cpp:299-305). */
 int ffea_gpu_ffea_seed(int32_t rng_seed, uint64_t out[6]);
 
+/* --- FFEA script front end ----------------------------------------------- */
+
+/* An FFEA input script (.ffea) read the way FFEA reads it
+ * (SimulationParams::extract_params / assign, src/SimulationParams.cpp:184-550;
+ * World::read_and_build_system, src/World.cpp:2205-2720) with its blob files
+ * (.node, .top, .mat, .stokes, .pin: Blob::load_*, src/Blob.cpp:2415-2947,
+ * 3691-3755), in meso units.  The subset is the blob update's: per blob one
+ * DYNAMIC conformation, solver CG_nomass / CG / masslumped, scale, centroid,
+ * velocity.  Parameters that switch on work outside the update (surface
+ * interactions, electrostatics, kinetics, springs, constant forces, rods,
+ * several conformations) are rejected with an error naming them;
+ * calc_steric is accepted and not computed. */
+#define FFEA_GPU_SCRIPT_PATH_MAX 1024
+
+typedef struct ffea_gpu_script ffea_gpu_script_t;
+
+/* The run settings of a script after SimulationParams::assign's unit
+ * conversions (file names resolved against the script's directory; the
+ * output names default to <script>.ftj, <script>.fm, <script>.fcp). */
+typedef struct {
+    double dt, kT, epsilon2, stokes_visc;   /* meso units */
+    int64_t num_steps;
+    int32_t check, rng_seed, max_iterations_cg, calc_noise, calc_stokes, restart, num_blobs, reserved;
+    char trajectory_out_fname[FFEA_GPU_SCRIPT_PATH_MAX];
+    char measurement_out_fname[FFEA_GPU_SCRIPT_PATH_MAX];
+    char checkpoint_in[FFEA_GPU_SCRIPT_PATH_MAX];   /* empty if none */
+    char checkpoint_out[FFEA_GPU_SCRIPT_PATH_MAX];
+} ffea_gpu_script_params;
+
+int ffea_gpu_script_load(const char *path, ffea_gpu_script_t **out);
+void ffea_gpu_script_free(ffea_gpu_script_t *s);
+int ffea_gpu_script_get_params(const ffea_gpu_script_t *s, ffea_gpu_script_params *out);
+
+/* Blob `blob` of the script as ffea_gpu_create takes it.  The mesh arrays
+ * belong to the script (valid until ffea_gpu_script_free); params carry the
+ * script's values with precision MIXED, true_residual 1 and preconditioner
+ * JACOBI, which the caller may change. */
+int ffea_gpu_script_get_blob(const ffea_gpu_script_t *s, int32_t blob, ffea_gpu_mesh *mesh, ffea_gpu_params *params);
+
+/* Every blob of the script in one batch handle, drawing from one RNG stream
+ * in a one-thread FFEA run's order (FFEA_GPU_RNG_SHARED; for a single blob
+ * the same as its own stream). */
+int ffea_gpu_script_create(const ffea_gpu_script_t *s, int32_t precision, int32_t preconditioner,
+                           int32_t true_residual, ffea_gpu_t **out);
+
 /* --- surface-surface interactions (Lennard-Jones) ------------------------- */
 
 /* Replaces VdW_solver (include/VdW_solver.h:36-127; VdW_solver::init,

@@ -369,3 +369,25 @@ void ref_rng_advance(const uint64_t *state, long e, long c, uint64_t *out)
 }
 
 }  // extern "C"
+
+// FFEA's own reading of a script's <param> block: FFEA_input_reader::
+// file_to_lines, SimulationParams::extract_params (src/SimulationParams.cpp:
+// 184-550) and validate (:580-720, which fills in the default output names).
+// out: dt, kT, epsilon2, stokes_visc, num_steps, check, rng_seed,
+// max_iterations_cg, calc_noise, calc_stokes, restart, num_blobs.
+// Returns 0, or -1 where FFEA's reading fails.
+#include "FFEA_input_reader.h"
+extern "C" int ref_script_params(const char *path, double *out)
+{
+    FFEA_input_reader reader;
+    std::vector<std::string> lines;
+    if (reader.file_to_lines(path, &lines) != FFEA_OK) return -1;
+    SimulationParams p;
+    p.FFEA_script_filename = path;
+    if (p.extract_params(lines) != FFEA_OK) return -1;
+    const double v[12] = {p.dt, p.kT, p.epsilon2, p.stokes_visc, (double)p.num_steps, (double)p.check,
+                          (double)p.rng_seed, (double)p.max_iterations_cg, (double)p.calc_noise,
+                          (double)p.calc_stokes, (double)p.restart, (double)p.num_blobs};
+    for (int i = 0; i < 12; i++) out[i] = v[i];
+    return 0;
+}

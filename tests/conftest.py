@@ -30,3 +30,12 @@ def gpulib():
     B.build()
     from ffea_gb300 import _lib as L
     return L.lib()
+
+
+@pytest.fixture(scope="session")
+def gpulib_cpu():
+    """The built library for its host-only entry points (no GPU needed)."""
+    from ffea_gb300 import build as B
+    B.build()
+    from ffea_gb300 import _lib as L
+    return L.lib()
