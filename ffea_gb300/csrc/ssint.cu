@@ -14,7 +14,10 @@
 //                    LinkedListCube::pbc) and counts the cell's faces.
 //   2. k_scan_local / k_scan_blocks   exclusive scan of the cell counts.
 //   3. k_scatter     places every face in its cell's segment.
-//   4. k_sort_cells  sorts each segment by face index (deterministic order).
+//   4. k_sort_cells  sorts each segment by face index (deterministic order):
+//      k_sort_large  a thread per cell of up to 64 faces, a CTA per cell of up
+//                    to 4096 (bitonic, in shared memory); a fuller cell makes
+//                    the call an error (the grid is far too coarse).
 //   5. k_pairs       one warp per face, in cell order so that neighbouring
 //                    warps read the same cells: the lanes share the faces of
 //                    the 27 cells around its own and integrate the LJ force
@@ -22,7 +25,9 @@
 //                    fixed shuffle tree sums the lanes.  A pair (i, j) is evaluated
 //                    from both sides, each side keeping only its own face's
 //                    forces: twice the arithmetic of one evaluation, but no
-//                    atomics on forces and a fixed summation order.  The pair
+//                    atomics on forces and a fixed summation order (the
+//                    per-blob-pair energies use FP64 atomics, so their last
+//                    bits may vary from run to run).  The pair
 //                    is always evaluated with the lower pool index as FFEA's
 //                    f1, so both sides reproduce FFEA's arithmetic.
 //   6. k_node_gather one thread per node: sums its faces' corner forces in
@@ -37,6 +42,8 @@
 // per point pair and 216 of 243 products per pair side; the kernel is bound
 // by the FP64 pipe.
 #include <cuda_runtime.h>
+
+#include <climits>
 
 #include <cmath>
 #include <cstdarg>
@@ -74,7 +81,8 @@ struct ffea_gpu_ssint {
     int *d_node_ent = nullptr;  // face * 3 + corner, face order
     double *d_emin = nullptr, *d_rmin = nullptr;
     double *d_pos = nullptr, *d_force = nullptr, *d_energy = nullptr;  // staging of the host entry point
-    unsigned long long *d_stats = nullptr;  // [0] pairs, [1] out-of-box faces
+    unsigned long long *d_stats = nullptr;  // [0] pairs, [1] out-of-box faces, [2] large cells, [3] oversized cells
+    int *d_large = nullptr;                 // cells of more than kSortSmall faces (k_sort_large)
 };
 
 namespace {
@@ -247,14 +255,32 @@ __global__ void k_scatter(const int *__restrict__ cell, int nf, const int *__res
     sorted[slot] = f;
 }
 
-// Each segment sorted by face index.
+// Each cell's faces sorted by face index.  A cell of at most kSortSmall
+// faces is insertion-sorted by its thread; a larger one, up to kSortMax
+// faces, is listed for k_sort_large (one CTA per cell); a cell above that is
+// counted in stats[3] and makes the call an error, so that a grid far too
+// coarse for the mesh fails at once instead of one thread sorting many
+// thousands of faces.
+constexpr int kSortSmall = 64;
+constexpr int kSortMax = 4096;
+constexpr int kSortLargeCtas = 256;
+
 __global__ void k_sort_cells(long long ncell, int nblocks, const int *__restrict__ start,
-                             const int *__restrict__ block, int *__restrict__ sorted)
+                             const int *__restrict__ block, int *__restrict__ sorted, int *__restrict__ large,
+                             unsigned long long *stats)
 {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     const int b = cell_begin(start, block, c);
     const int e = cell_end(start, block, c, ncell, nblocks);
+    if (e - b > kSortMax) {
+        atomicAdd(&stats[3], 1ull);
+        return;
+    }
+    if (e - b > kSortSmall) {
+        large[atomicAdd(&stats[2], 1ull)] = (int)c;
+        return;
+    }
     for (int i = b + 1; i < e; i++) {
         const int v = sorted[i];
         int j = i - 1;
@@ -263,6 +289,44 @@ __global__ void k_sort_cells(long long ncell, int nblocks, const int *__restrict
             j--;
         }
         sorted[j + 1] = v;
+    }
+}
+
+// The listed large cells, one CTA each (grid-stride over the list): a
+// bitonic sort in shared memory of the cell's face indices, padded to a
+// power of two.
+__global__ void __launch_bounds__(256) k_sort_large(long long ncell, int nblocks, const int *__restrict__ start,
+                                                    const int *__restrict__ block, int *__restrict__ sorted,
+                                                    const int *__restrict__ large,
+                                                    const unsigned long long *__restrict__ stats)
+{
+    __shared__ int v[kSortMax];
+    const int nl = (int)stats[2];
+    for (int k = blockIdx.x; k < nl; k += gridDim.x) {
+        const long long c = large[k];
+        const int b = cell_begin(start, block, c);
+        const int n = cell_end(start, block, c, ncell, nblocks) - b;  // kSortSmall < n <= kSortMax
+        int m = 1;
+        while (m < n) m <<= 1;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) v[i] = i < n ? sorted[b + i] : INT_MAX;
+        __syncthreads();
+        for (int size = 2; size <= m; size <<= 1)
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                    const int j = i ^ stride;
+                    if (j > i) {
+                        const bool up = (i & size) == 0;
+                        const int a = v[i], bb = v[j];
+                        if ((a > bb) == up) {
+                            v[i] = bb;
+                            v[j] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        for (int i = threadIdx.x; i < n; i += blockDim.x) sorted[b + i] = v[i];
+        __syncthreads();
     }
 }
 
@@ -364,6 +428,7 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
     const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long w = (long long)blockIdx.x * kPairWarps + wi;
     if (w >= block[nblocks]) return;  // warp-uniform; faces outside the box are not binned
+    if (stats[3]) return;             // a cell too full to sort: the call fails, nothing to evaluate
     const int i = sorted[w];
     const int ci = cell[i];
     const int cz = ci % nz, cy = (ci / nz) % ny, cx = ci / (nz * ny);
@@ -553,7 +618,8 @@ extern "C" int ffea_gpu_ssint_create(const ffea_gpu_ssint_desc *d, ffea_gpu_ssin
             dalloc(&s->d_sorted, na) || dalloc(&s->d_node_ptr, d->num_nodes + 1) ||
             dalloc(&s->d_node_ent, 3 * (size_t)na) || dalloc(&s->d_emin, T2) || dalloc(&s->d_rmin, T2) ||
             dalloc(&s->d_pos, 3 * (size_t)d->num_nodes) || dalloc(&s->d_force, 3 * (size_t)d->num_nodes) ||
-            dalloc(&s->d_energy, (size_t)d->num_blobs * d->num_blobs) || dalloc(&s->d_stats, 2))
+            dalloc(&s->d_energy, (size_t)d->num_blobs * d->num_blobs) || dalloc(&s->d_stats, 4) ||
+            dalloc(&s->d_large, (size_t)na / (kSortSmall + 1) + 1))
             return FFEA_GPU_ERROR;
         if (na) {
             SSINT_CUDA(cudaMemcpy(s->d_corner, corner.data(), sizeof(int) * 3 * na, cudaMemcpyHostToDevice));
@@ -581,7 +647,7 @@ extern "C" void ffea_gpu_ssint_destroy(ffea_gpu_ssint_t *s)
     if (s->stream) cudaStreamSynchronize(s->stream);
     void *bufs[] = {s->d_corner, s->d_blob, s->d_type, s->d_geo, s->d_cell, s->d_fforce, s->d_count,
                     s->d_start, s->d_block, s->d_sorted, s->d_node_ptr, s->d_node_ent, s->d_emin, s->d_rmin,
-                    s->d_pos, s->d_force, s->d_energy, s->d_stats};
+                    s->d_pos, s->d_force, s->d_energy, s->d_stats, s->d_large};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -596,7 +662,7 @@ extern "C" int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *p
     cudaStream_t st = s->stream;
     const int na = s->num_active;
     SSINT_CUDA(cudaMemsetAsync(energy, 0, sizeof(double) * s->num_blobs * s->num_blobs, st));
-    SSINT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * 2, st));
+    SSINT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * 4, st));
     if (na == 0) {
         SSINT_CUDA(cudaMemsetAsync(force, 0, sizeof(double) * 3 * (size_t)s->num_nodes, st));
         return FFEA_GPU_OK;
@@ -611,7 +677,9 @@ extern "C" int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *p
     // faces outside the box are left out of the grid (and make the call an
     // error); the kernels below bound every segment by the scan's total
     k_sort_cells<<<(int)((s->ncell + 255) / 256), 256, 0, st>>>(s->ncell, s->nblocks, s->d_start, s->d_block,
-                                                                s->d_sorted);
+                                                                s->d_sorted, s->d_large, s->d_stats);
+    k_sort_large<<<kSortLargeCtas, 256, 0, st>>>(s->ncell, s->nblocks, s->d_start, s->d_block, s->d_sorted,
+                                                 s->d_large, s->d_stats);
     k_pairs<<<(na + kPairWarps - 1) / kPairWarps, 32 * kPairWarps, 0, st>>>(s->d_geo, s->d_cell, s->d_sorted, s->d_start, s->d_block, s->ncell, s->nblocks, s->nx,
                                 s->ny, s->nz, s->d_blob, s->d_type, s->d_emin, s->d_rmin, s->num_types,
                                 s->num_blobs, s->inc_self, s->d_fforce, energy, s->d_stats);
@@ -624,11 +692,14 @@ extern "C" int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *p
 extern "C" int ffea_gpu_ssint_synchronize(ffea_gpu_ssint_t *s, int64_t *pairs)
 {
     if (!s) return fail("ffea_gpu_ssint_synchronize: null handle");
-    unsigned long long st[2] = {0, 0};
+    unsigned long long st[4] = {0, 0, 0, 0};
     SSINT_CUDA(cudaMemcpyAsync(st, s->d_stats, sizeof(st), cudaMemcpyDeviceToHost, s->stream));
     SSINT_CUDA(cudaStreamSynchronize(s->stream));
     if (pairs) *pairs = (int64_t)st[0];
     if (st[1]) return fail("%llu face centroids lie outside the interaction grid (FFEA reports this as an error)", st[1]);
+    if (st[3])
+        return fail("%llu grid cells hold more than %d faces each: the interaction grid is too coarse for this mesh "
+                    "(use more, smaller cells)", st[3], kSortMax);
     return FFEA_GPU_OK;
 }
 

@@ -288,8 +288,14 @@ void ffea_gpu_ssint_destroy(ffea_gpu_ssint_t *s);
 int ffea_gpu_ssint_forces(ffea_gpu_ssint_t *s, const double *pos, double *force, double *energy, int64_t *pairs);
 
 /* The same on DEVICE arrays, enqueued on the handle's stream without
- * waiting; ffea_gpu_ssint_synchronize waits, reports the pair count and
- * returns the out-of-grid error of that call. */
+ * waiting.  Its errors -- face centroids outside the grid, or a grid cell
+ * holding more than 4096 faces (a grid far too coarse for the mesh) -- are
+ * only known on the device: call ffea_gpu_ssint_synchronize after it to
+ * wait, read the pair count and get that call's error; a caller that only
+ * synchronises the stream itself does not see them.
+ * Forces are summed in a fixed order (bit-reproducible run to run); the
+ * per-blob-pair energies are summed with FP64 atomics, so their last bits
+ * can vary from run to run. */
 int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *pos, double *force, double *energy);
 int ffea_gpu_ssint_synchronize(ffea_gpu_ssint_t *s, int64_t *pairs);
 void *ffea_gpu_ssint_stream(ffea_gpu_ssint_t *s);

@@ -6,7 +6,8 @@ Tolerances: the kernels are compiled without FMA contraction, so cell binning
 and the normal test decide as the oracle does, and the pair counts must be
 equal exactly; a pair's force differs from FFEA's only in rounding (a
 reciprocal for a divide, regrouped sums).  Per-face sums run in another order than FFEA's
-(each pair from both sides), and the energy is summed with atomics, so forces
+(each pair from both sides), and the energy is summed with atomics (its last bits
+may vary from run to run; the forces do not), so forces
 agree to 1e-12 of the largest force and energies to 1e-12 relative."""
 import os
 import time
@@ -161,4 +162,48 @@ def test_throughput_two_20nm_spheres(capsys):
               f"oracle 1 core {cpu_ms:.1f} ms")
     f_ref, _, _ = oracle.ssint_lj(pos, faces, blob, kw["face_type"], kw["emin"], kw["rmin"], 2, h, grid, 1)
     np.testing.assert_allclose(d_f.cpu().numpy(), f_ref, rtol=0, atol=FORCE_TOL * np.abs(f_ref).max())
+    s.close()
+
+
+def test_large_cells_sorted_by_a_cta_each():
+    """A coarse grid (8 nm cells over two 4 nm spheres) puts more than 64
+    faces in a cell, so the cells are sorted by the one-CTA-per-cell path:
+    the results match the oracle and repeat bit for bit."""
+    pos, faces, blob, _, _ = _two_spheres(4.0, 0.6, seed=5)
+    h = nm(8.0)
+    span = pos.max(0) - pos.min(0)
+    grid = tuple(int(v) for v in 2 * np.ceil(span / h))
+    pos = pos - pos.mean(0) + 0.5 * h * np.array(grid)
+    cells = np.floor((pos[faces].mean(1)) / h).astype(int)
+    _, per_cell = np.unique(cells[:, 0] * 10000 + cells[:, 1] * 100 + cells[:, 2], return_counts=True)
+    assert per_cell.max() > 64, per_cell.max()
+    kw = dict(num_nodes=len(pos), faces=faces, face_blob=blob, face_type=np.zeros(len(faces), np.int32),
+              emin=np.ones((1, 1)), rmin=np.full((1, 1), nm(1.0)), num_blobs=2, cell_size=h, grid=grid, inc_self=1)
+    f1, _, p1 = _compare(kw, pos)
+    s = _solver(**kw)
+    f2, _, p2 = s.forces(pos)
+    s.close()
+    assert p1 == p2 and np.array_equal(f1, f2)
+
+
+def test_overfull_cell_is_an_error():
+    """More than 4096 faces in one cell (one 20 nm sphere in a single-cell
+    grid) fails the call at once with a message, instead of a long serial sort."""
+    from ffea_gb300._lib import FfeaGpuError
+    from ffea_gb300.mesh import sphere_mesh
+    from ffea_gb300.surface import surface_faces
+    m = sphere_mesh(20.0, seed=2)
+    tri = surface_faces(m.pos, m.topology).astype(np.int32)
+    assert len(tri) > 4096
+    h = 1.1 * float((m.pos.max(0) - m.pos.min(0)).max())
+    pos = m.pos - m.pos.mean(0) + 0.5 * h
+    kw = dict(num_nodes=len(pos), faces=tri, face_blob=np.zeros(len(tri), np.int32),
+              face_type=np.zeros(len(tri), np.int32), emin=np.ones((1, 1)), rmin=np.full((1, 1), nm(1.0)),
+              num_blobs=1, cell_size=h, grid=(1, 1, 1), inc_self=1)
+    s = _solver(**kw)
+    t = time.perf_counter()
+    for _ in range(2):
+        with pytest.raises(FfeaGpuError, match="too coarse"):
+            s.forces(pos)
+    assert time.perf_counter() - t < 10.0
     s.close()
