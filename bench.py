@@ -180,13 +180,14 @@ def step_kernel_bytes(num_linear: int, num_elements: int, num_edges: int, num_to
     """Algorithmic bytes per launch of the per-step kernels in the same model:
     element forces 12 N + 168 E (positions, connectivity, rest state,
     material and sign in; nodal forces, scaled gradients and sign out);
-    the draws 4 (7 E + 3 N_t) (one FP32 value written per draw); the
-    viscosity assembly 40 E + 64 E + 36 B (element coefficients and source
-    indices in, block values out); the node gather 64 E + 16 N; the update
-    48 N."""
+    the draws 4 (7 E + 3 N) (one FP32 value written per draw generated: the
+    elements' and those of the nodes with a Stokes drag, here the corner
+    nodes); the viscosity assembly 40 E + 64 E + 36 B (element coefficients
+    and source indices in, block values out); the node gather 64 E + 16 N.
+    The update (48 N) runs at the end of the solve kernel."""
     N, E, B = num_linear, num_elements, num_linear + 2 * num_edges
-    return {"noise": 4 * (7 * E + 3 * num_total), "elements": 12 * N + 168 * E,
-            "assemble": 40 * E + 64 * E + 36 * B, "nodes": 64 * E + 16 * N, "euler": 48 * N}
+    return {"noise": 4 * (7 * E + 3 * N), "elements": 12 * N + 168 * E,
+            "assemble": 40 * E + 64 * E + 36 * B, "nodes": 64 * E + 16 * N}
 
 
 def ncu_traffic(kernel="k_cg", workload="sphere40"):
@@ -486,7 +487,7 @@ def run_gb300(args):
     # iterations over its measured duration
     iters_p = main_arm["cg_iters_profiled"]
     cg_ms = main_arm["phase_ms_per_step"]["cg"]
-    alg = int(iters_p * cg_iteration_bytes(nl, nedges))
+    alg = int(iters_p * cg_iteration_bytes(nl, nedges)) + 48 * nl  # the iterations, then the Euler update
     peak, peak_kind = measured_peak()
     achieved = alg / (cg_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": "k_cg", "achieved": round(achieved, 1), "peak": peak,

@@ -232,20 +232,24 @@ int capture_step_graph(ffea_gpu *h, bool with_coarse, cudaGraphExec_t *out, int6
     cudaStream_t s = h->stream;
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    // every launcher counts its launches: the count across the capture is
+    // the graph's kernels per replay (taken back out below, as nothing ran)
+    const int64_t launches0 = kernel_launch_count();
     launch_noise(d, s);
     launch_elements(d, s, ELEM_STEP);
     if (d.any_nomass) launch_assemble(d, s);
     int rc = with_coarse ? refresh_coarse(h, s, 1, false) : FFEA_GPU_OK;
     launch_nodes(d, s, 0);
-    cudaError_t le = launch_cg(d, s);
-    launch_euler(d, s);
+    cudaError_t le = launch_cg(d, s, true);  // the solve, then the Euler update and RNG advance
     cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    const int64_t captured = kernel_launch_count() - launches0;
+    count_launches(-captured);
     if (rc != FFEA_GPU_OK || le != cudaSuccess || ce != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         cudaGetLastError();
         return fail("capturing the step graph failed: %s / %s", cudaGetErrorString(le), cudaGetErrorString(ce));
     }
-    *fixed = 4 + (d.noise_runs ? 1 : 0) + (d.any_nomass ? 1 : 0) + (with_coarse ? 2 : 0);
+    *fixed = captured;
     cudaError_t e = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail("cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
@@ -884,9 +888,8 @@ int enqueue_steps(ffea_gpu *h, int32_t nsteps, bool allow_direct)
         CK(mark(4));
         launch_nodes(d, h->stream, 0);
         CK(mark(5));
-        CK(launch_cg(d, h->stream));
+        CK(launch_cg(d, h->stream, true));  // with the Euler update and RNG advance
         CK(mark(6));
-        launch_euler(d, h->stream);
         CK(mark(7));
         if (h->timing) {
             CK(cudaEventSynchronize(h->ev[FFEA_GPU_NUM_KERNEL_TIMES]));

@@ -657,10 +657,21 @@ bool build_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const ffea_gpu_
             const ffea_gpu_params &p = params[b];
             const int64_t ed = (p.calc_noise == 1 && !H.bp[b].all_pinned) ? 7ll * meshes[b].num_elements : 0;
             const int64_t nd = (p.calc_noise == 1 && p.calc_stokes == 1) ? 3ll * meshes[b].num_nodes : 0;
+            // the node kernel reads the draws of nodes with a Stokes drag only
+            // (a zero drag multiplies its draws by zero): generate the draws
+            // up to the last such node; the stream still advances by all
+            // 3 N_t draws of the step (stream_step)
+            int64_t nd_used = 0;
+            if (nd && meshes[b].stokes_drag)
+                for (int32_t n = meshes[b].num_nodes - 1; n >= 0; n--)
+                    if (meshes[b].stokes_drag[n] != 0.0) {
+                        nd_used = 3ll * (n + 1);
+                        break;
+                    }
             H.noise_run_off[2 * b] = (int32_t)runs;
             runs += (ed + NOISE_RUN - 1) / NOISE_RUN;
             H.noise_run_off[2 * b + 1] = (int32_t)runs;
-            runs += (nd + NOISE_RUN - 1) / NOISE_RUN;
+            runs += (nd_used + NOISE_RUN - 1) / NOISE_RUN;
             H.bp[b].noise_node_off = (int32_t)nodes;
             if (nd) nodes += meshes[b].num_nodes;
         }

@@ -2415,6 +2415,49 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         running = reduce();
     }
     publish_x();
+    if (d.cg_euler && !s_err) {
+        // the step's Euler update (Blob::euler_integrate, src/Blob.cpp:3937-3969)
+        // of the own rows, for blobs that had not failed before the solve and
+        // whose solve converged (this CTA's copy of their state), and the
+        // advance of every RNG stream by one step's draws (CTA 0)
+        if (!local) refresh();
+        for (int j = 0; j < nt; j++) {
+            const int k = s_tslot[j], b = s_blob[k];
+            const BlobParams &bp = d.bp[b];
+            const int row = s_row0[j] + tid;
+            if (tid >= s_rows[j] || row - bp.node_off >= bp.node_cnt) continue;
+            if (s_state[k] != CG_CONVERGED || __ldcg(&d.status[b]) != 0) continue;
+            const double dt = bp.dt;
+#pragma unroll
+            for (int cc2 = 0; cc2 < 3; cc2++) {
+                const size_t kk = 3 * (size_t)row + cc2;
+                const double xi = REG ? (double)sx[cc2 * CG_THREADS + tid] : (double)X()[kk];
+                double pn;
+                if (bp.solver == SOLVER_NOMASS) {
+                    d.vel[kk] = xi;
+                    pn = d.pos[kk] + xi * dt;
+                } else {
+                    const double v = d.vel[kk] + xi * dt;
+                    d.vel[kk] = v;
+                    pn = d.pos[kk] + v * dt;
+                }
+                d.pos[kk] = pn;
+                if (d.pos_df) d.pos_df[kk] = split_pos(pn);
+            }
+        }
+        if (c == 0) {
+            __syncthreads();  // this CTA's status bits of the solve are visible to its threads
+            for (int st = tid; st < d.num_streams; st += CG_THREADS) {
+                if (d.num_streams == d.num_blobs && __ldcg(&d.status[st]) != 0) continue;  // per-blob streams
+                uint32_t w[6];
+#pragma unroll
+                for (int i = 0; i < 6; i++) w[i] = d.stream_state[6 * st + i];
+                mrg::apply(d.stream_step[st], w);
+#pragma unroll
+                for (int i = 0; i < 6; i++) d.stream_state[6 * st + i] = w[i];
+            }
+        }
+    }
     if (local && c == 0)
         for (int b = tid; b < d.num_blobs; b += CG_THREADS) d.cg[b] = s_cg[b];
     if (tid == 0) {
@@ -2895,8 +2938,10 @@ cudaError_t launch_barrier_timeout_selftest(unsigned int *bar, unsigned int spin
     return cudaLaunchKernelEx(&cfg, k_barrier_timeout_selftest, bar, spin_limit, out);
 }
 
-cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s)
+cudaError_t launch_cg(const DeviceBatch &dev, cudaStream_t s, bool euler)
 {
+    DeviceBatch d = dev;
+    d.cg_euler = euler ? 1 : 0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)d.cg_grid);
     cfg.blockDim = dim3(CG_THREADS);

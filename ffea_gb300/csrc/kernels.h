@@ -22,6 +22,7 @@ struct DeviceBatch {
     int32_t cg_grid = 0;          // CTAs of the persistent CG kernel
     int32_t cg_reg = 0;           // 1: one CG segment per CTA, row state kept in registers
     int32_t cg_local = 0;         // 1: every CTA reduces the dot products itself (few segments and blobs)
+    int32_t cg_euler = 0;         // 1 (per launch): the CG kernel ends with the Euler update of the step
     int32_t cg_cache_slots = 0;   // REG: matrix slots per row whose values are copied to shared memory
     int32_t cg_cache_cols = 0;    // REG: matrix slots per row whose column indices are copied
     int32_t part_stride = 8;      // floats per segment slot of the CG partials (32 with the coarse space)
@@ -149,7 +150,9 @@ void launch_assemble(const DeviceBatch &d, cudaStream_t s);
 // the step's random draws (nothing when no blob draws)
 void launch_noise(const DeviceBatch &d, cudaStream_t s);
 void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs);
-cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s);
+// the persistent solve; with `euler` it also applies the step's Euler update
+// and RNG advance (what launch_euler does) to the blobs whose solve converged
+cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s, bool euler = false);
 // The CG kernel's grid barrier with a target that no arrival reaches and the
 // given spin limit, on `ctas` co-resident CTAs; *out counts the CTAs that
 // reported the time-out (bar: 8 zeroed words, out: one zeroed int).

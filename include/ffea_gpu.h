@@ -419,7 +419,8 @@ int ffea_gpu_mpnn_probe(ffea_gpu_t *h, int32_t blob, const float *theta, const f
 
 /* Per-phase timing of the last ffea_gpu_step call, measured with CUDA events
  * on the handle's stream (milliseconds): elements, assembly, node gather,
- * CG solve, update.  Only filled when timing was enabled. */
+ * CG solve with the update, and 0 (the former separate update).  Only
+ * filled when timing was enabled. */
 int ffea_gpu_set_timing(ffea_gpu_t *h, int32_t enable);
 int ffea_gpu_phase_times(ffea_gpu_t *h, double out_ms[5]);
 
@@ -427,8 +428,9 @@ int ffea_gpu_phase_times(ffea_gpu_t *h, double out_ms[5]);
  * last ffea_gpu_step call): random draws (k_noise), element forces
  * (k_elements), viscosity assembly (k_assemble), coarse-space refresh (every
  * tenth step with the two-level preconditioner, else 0), node gather
- * (k_nodes), CG solve (k_cg), update (k_euler).  No reference counterpart:
- * it exists for the per-kernel roofline. */
+ * (k_nodes), CG solve with the Euler update at its end (k_cg), and a last
+ * slot, now 0, that held the separate update kernel.  No reference
+ * counterpart: it exists for the per-kernel roofline. */
 #define FFEA_GPU_NUM_KERNEL_TIMES 7
 int ffea_gpu_kernel_times(ffea_gpu_t *h, double out_ms[FFEA_GPU_NUM_KERNEL_TIMES]);
 
