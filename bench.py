@@ -72,6 +72,8 @@ def parse_args():
     ap.add_argument("--precond", choices=sorted(PRECONDS), default="learned",
                     help="preconditioner of the headline arm (plain Jacobi-PCG is measured beside it)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain Jacobi-PCG and two-level arms")
+    ap.add_argument("--no-memory-resident", action="store_true",
+                    help="skip the in-process memory-resident solve measurement (sphere61) of the default run")
     ap.add_argument("--parity-steps", type=int, default=5,
                     help="steps of the parity leg on the measured single-blob workload (0: no parity leg)")
     ap.add_argument("--autotune", action="store_true",
@@ -188,6 +190,57 @@ def step_kernel_bytes(num_linear: int, num_elements: int, num_edges: int, num_to
     N, E, B = num_linear, num_elements, num_linear + 2 * num_edges
     return {"noise": 4 * (7 * E + 3 * N), "elements": 12 * N + 168 * E,
             "assemble": 40 * E + 64 * E + 36 * B, "nodes": 64 * E + 16 * N}
+
+
+def ncu_summary_value(key, kernel="k_cg", workload="sphere40"):
+    """A `key: value` figure from the committed ncu summary of a kernel, if present."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    try:
+        with open(path) as fh:
+            m = re.search(re.escape(key) + r":\s*([0-9.eE+]+)", fh.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def memory_resident_roofline(args, peak):
+    """The solve where HBM is the bound: one blob of 514,965 corner nodes
+    (98^3-cell, 61.25 nm sphere) runs the memory-resident solve (more CG
+    segments than SMs; the matrix, about 300 MB, does not fit in L2).
+    Learned two-level preconditioner, steps timed per kernel over one
+    coarse-refresh cycle.  frac: the algorithmic bytes (40 B + 148 N per
+    iteration, 48 N for the update) over the solve's time; dram_frac: the
+    DRAM bytes per iteration of the committed ncu capture of this kernel on
+    this workload over the same time."""
+    from ffea_gb300 import learned
+    from ffea_gb300.workloads import build_specs as specs_of
+    from ffea_gb300.world import World
+    specs = specs_of("sphere61", 0, args.precision)
+    with World(specs, graph=True, true_residual=True, preconditioner=PRECONDS["learned"]) as w:
+        if w.preconditioner() == PRECONDS["learned"]:
+            learned.apply(w, learned.load())
+        w.run(3)
+        nl, _, nedges = w.sizes()
+        n = int(os.environ.get("FFEA_GPU_COARSE_REFRESH", "10"))
+        loops0 = w.cg_loop_count()
+        w.set_timing(True)
+        w.run(n)
+        cg_ms = float(w.phase_times()[3]) / n
+        w.set_timing(False)
+        iters = (w.cg_loop_count() - loops0) / n
+    alg = iters * cg_iteration_bytes(nl, nedges) + 48 * nl
+    gbs = alg / (cg_ms / 1e3) / 1e9
+    out = {"workload": f"sphere61: {WORKLOADS['sphere61']['desc']} ({nl:,} corner nodes)",
+           "kernel": "k_cg (memory-resident)", "us": round(cg_ms * 1e3, 1), "cg_iters": iters,
+           "us_per_iteration": round(cg_ms * 1e3 / max(iters, 1e-9), 2),
+           "algorithmic_bytes": int(alg), "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    dram_it = ncu_summary_value("dram_bytes_per_iteration", workload="sphere61")
+    if dram_it:
+        dgbs = dram_it * iters / (cg_ms / 1e3) / 1e9
+        out.update({"dram_bytes_per_iteration": dram_it, "dram_gbs": round(dgbs, 1),
+                    "dram_frac": round(dgbs / peak, 4),
+                    "dram_source": "profiles/k_cg_sphere61.md (one ncu capture of this kernel on this workload)"})
+    return out
 
 
 def ncu_traffic(kernel="k_cg", workload="sphere40"):
@@ -539,6 +592,8 @@ def run_gb300(args):
         line["learned_vs_two_level"] = ratio(main_arm, two_level)
         if plain is not None:
             line["two_level_vs_plain"] = ratio(two_level, plain)
+    if world == 1 and args.workload == "sphere40" and not args.no_memory_resident:
+        kernels["cg_memory_resident"] = memory_resident_roofline(args, peak)
     if world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(specs, args.cpu_seconds)
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -1378,7 +1378,15 @@ extern "C" int ffea_gpu_diag_cg_vectors(ffea_gpu_t *h, int32_t blob, int32_t *ro
     const size_t ts = h->dev.precision == PREC_FP64 ? sizeof(double) : sizeof(float);
     const size_t off = 3 * (size_t)bp.node_off * ts, bytes = 3 * (size_t)bp.node_pad * ts;
     if (r) CK(cudaMemcpy(r, static_cast<char *>(h->dev.r) + off, bytes, cudaMemcpyDeviceToHost));
-    if (u) CK(cudaMemcpy(u, static_cast<char *>(h->dev.u) + off, bytes, cudaMemcpyDeviceToHost));
+    if (u) {
+        // u from its published 16-byte copy (x, y, z, 0 per row), which the
+        // memory-resident iteration keeps current
+        std::vector<char> u4(4 * (size_t)bp.node_pad * ts);
+        CK(cudaMemcpy(u4.data(), static_cast<char *>(h->dev.u4) + 4 * (size_t)bp.node_off * ts, u4.size(),
+                      cudaMemcpyDeviceToHost));
+        for (size_t r = 0; r < (size_t)bp.node_pad; r++)
+            std::memcpy(static_cast<char *>(u) + 3 * r * ts, u4.data() + 4 * r * ts, 3 * ts);
+    }
     if (w) CK(cudaMemcpy(w, static_cast<char *>(h->dev.w) + off, bytes, cudaMemcpyDeviceToHost));
     if (sums) CK(cudaMemcpy(sums, h->dev.last_sums + 3 * (size_t)blob, 3 * sizeof(double), cudaMemcpyDeviceToHost));
     return FFEA_GPU_OK;

@@ -2152,7 +2152,15 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         W pg = 0, pr = 0;
         RowState<T> loc;
         RowState<T> &S = REG ? reg : loc;
-        if (!REG && valid) load_fields<T>(d, row, loc, RF_X | RF_R | RF_U | RF_W | RF_S | RF_P | RF_DINV);
+        if (!REG && valid) {
+            // u of the last iteration from its published copy (the plain u
+            // array is not kept up to date by the memory-resident iteration)
+            load_fields<T>(d, row, loc, RF_X | RF_R | RF_W | RF_S | RF_P | RF_DINV);
+            const V4 uo = U4()[row];
+            loc.u[0] = uo.x;
+            loc.u[1] = uo.y;
+            loc.u[2] = uo.z;
+        }
         float4 fm = make_float4(0.f, 0.f, 0.f, 0.f);  // mcoarse: the row's rest offset and omega
         if (mcoarse && valid) fm = d.phi[row];
         if (valid) {
@@ -2177,7 +2185,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
             }
             U4()[row] = V4{S.u[0], S.u[1], S.u[2], (T)0};
         }
-        if (!REG && valid) store_fields<T>(d, row, loc, RF_X | RF_R | RF_U | RF_S | RF_P);
+        if (!REG && valid) store_fields<T>(d, row, loc, RF_X | RF_R | RF_S | RF_P);
         if constexpr (kDefer) {
             const float inf[3] = {(float)pg, 0.f, (float)pr};
             if (mcoarse) {
@@ -2218,7 +2226,18 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         double vr = 0.0, vg = 0.0;
         RowState<T> loc;
         RowState<T> &S = REG ? reg : loc;
-        if (!REG && valid) load_fields<T>(d, row, loc, RF_R | RF_U | (state == CG_VERIFY ? RF_DINV : 0));
+        // an ACTIVE iteration only needs w.u here (r.u and r.r came from
+        // phase A); the prologue and a restart also sum r.u and r.r
+        const bool need_r = prologue || state != CG_ACTIVE;
+        if (!REG && valid) {
+            if (need_r) load_fields<T>(d, row, loc, RF_R | (state == CG_VERIFY ? RF_DINV : 0));
+            if (state != CG_VERIFY) {
+                const V4 uo = U4()[row];  // the u the product reads (published in phase A)
+                loc.u[0] = uo.x;
+                loc.u[1] = uo.y;
+                loc.u[2] = uo.z;
+            }
+        }
         if (valid) {
             if (state != CG_VERIFY) {
                 T au[3];
@@ -2228,8 +2247,13 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                 for (int cc2 = 0; cc2 < 3; cc2++) {
                     S.w[cc2] = au[cc2];
                     pd += au[cc2] * S.u[cc2];
-                    pg += S.r[cc2] * S.u[cc2];
-                    pr += S.r[cc2] * S.r[cc2];
+                }
+                if (REG || need_r) {
+#pragma unroll
+                    for (int cc2 = 0; cc2 < 3; cc2++) {
+                        pg += S.r[cc2] * S.u[cc2];
+                        pr += S.r[cc2] * S.r[cc2];
+                    }
                 }
             } else {
                 double rt[3];

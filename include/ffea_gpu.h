@@ -43,7 +43,10 @@ extern "C" {
 #define FFEA_GPU_SOLVER_LUMPED 2   /* <solver = masslumped>: MassLumpedSolver */
 
 #define FFEA_GPU_PRECISION_FP64 0  /* every kernel in FP64 */
-#define FFEA_GPU_PRECISION_MIXED 1 /* FP32 element forces and SpMV; FP64 positions, dots, residuals */
+#define FFEA_GPU_PRECISION_MIXED 1 /* FP32 element forces, SpMV and CG vectors; FP64 positions and true
+                                    * residual.  With true_residual on, the FP32 iterate bounds the
+                                    * relative residual it can confirm at about 1e-7: tighter epsilons
+                                    * need FP64 (a solve that cannot reach epsilon fails). */
 /* Preconditioner of the NoMass CG solve.  JACOBI is NoMassCGSolver's
  * (src/NoMassCGSolver.cpp:278-291).  TWO_LEVEL adds a coarse correction
  * P A_c^-1 P^T r over six rigid modes per CG segment (a compact block of

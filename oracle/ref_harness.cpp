@@ -391,3 +391,53 @@ extern "C" int ref_script_params(const char *path, double *out)
     for (int i = 0; i < 12; i++) out[i] = v[i];
     return 0;
 }
+
+// FFEA's own overlap of two tetrahedra (volumeIntersectionII,
+// src/VolumeIntersection.cpp:951-1190) and its steric pair evaluation through
+// Face (Face::checkTetraIntersection and getTetraIntersectionVolumeTotal-
+// GradientAndShapeFunctions, src/Face.cpp:399-403, 473-514), for pinning the
+// steric restatement.  A and B: 4 x 3 corner positions each.
+#include "Face.h"
+#include "VolumeIntersection.h"
+extern "C" double ref_overlap_volume(const double *A, const double *B, int calc_cm, double *cm)
+{
+    arr3 a[4], b[4], c = {0, 0, 0};
+    for (int i = 0; i < 4; i++)
+        for (int d = 0; d < 3; d++) {
+            a[i][d] = A[3 * i + d];
+            b[i][d] = B[3 * i + d];
+        }
+    const double v = volumeIntersectionII<scalar, arr3>(a[0], a[1], a[2], a[3], b[0], b[1], b[2], b[3], calc_cm != 0, c);
+    if (cm)
+        for (int d = 0; d < 3; d++) cm[d] = c[d];
+    return v;
+}
+
+// out: [0] overlap test, [1] returned flag, [2] volume, [3..5] dV/dr,
+// [6..9] phi1, [10..13] phi2 (dr the finite-difference step)
+extern "C" void ref_steric_pair(const double *A, const double *B, double dr, double *out)
+{
+    static mesh_node na[4], nb[4];
+    Face f1, f2;
+    for (int i = 0; i < 4; i++) {
+        na[i].pos.assign(A[3 * i], A[3 * i + 1], A[3 * i + 2]);
+        nb[i].pos.assign(B[3 * i], B[3 * i + 1], B[3 * i + 2]);
+        f1.n[i] = &na[i];
+        f2.n[i] = &nb[i];
+    }
+    grr3 g = {0, 0, 0};
+    grr4 p1 = {0, 0, 0, 0}, p2 = {0, 0, 0, 0};
+    geoscalar vol = 0;
+    out[0] = f1.checkTetraIntersection(&f2) ? 1.0 : 0.0;
+    out[1] = f1.getTetraIntersectionVolumeTotalGradientAndShapeFunctions(&f2, dr, g, vol, p1, p2) ? 1.0 : 0.0;
+    out[2] = vol;
+    for (int d = 0; d < 3; d++) out[3 + d] = g[d];
+    for (int i = 0; i < 4; i++) {
+        out[6 + i] = p1[i];
+        out[10 + i] = p2[i];
+    }
+    for (int i = 0; i < 4; i++) {
+        f1.n[i] = nullptr;
+        f2.n[i] = nullptr;
+    }
+}

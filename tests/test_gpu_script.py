@@ -60,7 +60,7 @@ def test_one_blob_script_fp64_matches_oracle(gpulib, oracle, tmp_path):
     from ffea_gb300.script import Script
     from ffea_gb300.world import World
     param = PARAM.replace("<num_blobs = 2>", "<num_blobs = 1>").replace("(1,1)", "(1)").replace(
-        "<epsilon = 1e-8>", "<epsilon = 1e-12>")
+        "<epsilon = 1e-6>", "<epsilon = 1e-12>")
     system = SYSTEM[:SYSTEM.index("    <blob>\n        <motion_state")] + "</system>\n"
     path = _write(tmp_path, param, system)
     with Script(path) as sc:

@@ -32,7 +32,7 @@ PARAM = """<param>
     <rng_seed = 31>
     <trajectory_out_fname = out/run_trajectory.ftj>
     <measurement_out_fname = out/run_measurement.out>
-    <epsilon = 1e-8>
+    <epsilon = 1e-6>
     <max_iterations_cg = 700>
     <kappa = 1e9>
     <!-- a comment
@@ -136,7 +136,7 @@ def test_params_and_blobs(gpulib_cpu, script):
         assert p["num_blobs"] == 2 and sc.num_blobs == 2
         assert p["dt"] == 2e-14 / P.MESO_TIME
         assert p["kT"] == 4.11e-21 / P.MESO_ENERGY
-        assert p["epsilon2"] == 1e-8 * 1e-8
+        assert p["epsilon2"] == 1e-6 * 1e-6
         assert p["stokes_visc"] == 2e-3 / (P.MESO_PRESSURE * P.MESO_TIME)
         assert (p["num_steps"], p["check"], p["rng_seed"], p["max_iterations_cg"]) == (1000, 5, 31, 700)
         assert (p["calc_noise"], p["calc_stokes"], p["restart"]) == (1, 1, 0)
