@@ -60,17 +60,21 @@ void set_last_error(const char *msg);  // api.cu
 struct ffea_gpu_ssint {
     int num_nodes = 0, num_faces = 0, num_active = 0, num_types = 0, num_blobs = 0;
     int nx = 0, ny = 0, nz = 0, inc_self = 0;
+    int type = FFEA_GPU_SSINT_LJ;
+    double steric_factor = 0.0, steric_dr = 0.0;
     long long ncell = 0;
     int nblocks = 0;
     double h = 0.0;
     cudaStream_t stream = nullptr;
     // per active face, in the caller's face order
-    int *d_corner = nullptr;    // 3 node indices
+    int *d_corner = nullptr;    // 4 node indices: the corners, then the element's fourth node (-1: none)
     int *d_blob = nullptr;
     int *d_type = nullptr;
-    double *d_geo = nullptr;    // 16 doubles: corners (9), unit normal (3), area, pad
+    double *d_geo = nullptr;    // 16 doubles: corners (9), unit normal (3), area, fourth node (3)
     int *d_cell = nullptr;      // -1: outside the box
-    double *d_fforce = nullptr; // 9 doubles: force on each corner
+    double *d_fforce = nullptr; // 12 doubles: force on each corner and on the fourth node
+    int *d_stlist = nullptr;    // steric types: the partners whose tetrahedra overlap (MAX_STERIC_PARTNERS each)
+    int *d_stcnt = nullptr;     // their number per face
     // grid
     int *d_count = nullptr;     // ncell
     int *d_start = nullptr;     // ncell, block-local exclusive prefix
@@ -78,10 +82,11 @@ struct ffea_gpu_ssint {
     int *d_sorted = nullptr;    // num_active faces in cell order
     // nodes
     int *d_node_ptr = nullptr;  // num_nodes + 1
-    int *d_node_ent = nullptr;  // face * 3 + corner, face order
-    double *d_emin = nullptr, *d_rmin = nullptr;
+    int *d_node_ent = nullptr;  // face * 4 + corner (3: the fourth node), face order
+    double *d_emin = nullptr, *d_rmin = nullptr, *d_k0 = nullptr;
     double *d_pos = nullptr, *d_force = nullptr, *d_energy = nullptr;  // staging of the host entry point
-    unsigned long long *d_stats = nullptr;  // [0] pairs, [1] out-of-box faces, [2] large cells, [3] oversized cells
+    unsigned long long *d_stats = nullptr;  // [0] pairs, [1] out-of-box faces, [2] large cells, [3] oversized cells,
+                                            // [4] faces with too many steric partners
     int *d_large = nullptr;                 // cells of more than kSortSmall faces (k_sort_large)
 };
 
@@ -130,10 +135,11 @@ __global__ void k_face_geom(const double *__restrict__ pos, const int *__restric
     double v[3][3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const int n = corner[3 * f + k];
+        const int n = corner[4 * f + k];
 #pragma unroll
         for (int d = 0; d < 3; d++) v[k][d] = pos[3 * (long long)n + d];
     }
+    const int apex = corner[4 * f + 3];
     double a[3], b[3], nrm[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
@@ -152,6 +158,8 @@ __global__ void k_face_geom(const double *__restrict__ pos, const int *__restric
 #pragma unroll
     for (int d = 0; d < 3; d++) g[9 + d] = nrm[d] / mag;
     g[12] = .5 * mag;
+#pragma unroll
+    for (int d = 0; d < 3; d++) g[13 + d] = apex >= 0 ? pos[3 * (long long)apex + d] : 0.0;
     int c[3];
     const int dims[3] = {nx, ny, nz};
     bool inside = true;
@@ -330,12 +338,18 @@ __global__ void __launch_bounds__(256) k_sort_large(long long ncell, int nblocks
     }
 }
 
-// do_lj_interaction for f1 = A, f2 = B (src/VdW_solver.cpp:237-330 with
-// calc_lj_force_pair_matrix / calc_lj_factors, :664-699, :736-752).  Adds
-// force1 (A_SIDE) or force2 (!A_SIDE) to out[3][3] and returns the pair energy.
-template <bool A_SIDE>
-__device__ __forceinline__ double lj_pair(const double *A, const double *B, double emin, double rmin,
-                                          double out[3][3])
+// The integrated point-pair potentials of one face pair, for f1 = A, f2 = B:
+//   POT_LJ    do_lj_interaction (src/VdW_solver.cpp:237-330) with
+//             calc_lj_force_pair_matrix / calc_lj_factors (:664-699, :736-752);
+//   POT_SOFT  do_gensoft_interaction (:488-563) with
+//             calc_gensoft_force_pair_matrix / calc_gensoft_factors (:701-734, :754-771).
+// Adds force1 (A_SIDE) or force2 (!A_SIDE) to out[0..2] and returns the pair
+// energy.  k0: the soft potential's k0 (unused by POT_LJ).
+constexpr int POT_LJ = 0, POT_SOFT = 1;
+
+template <int POT, bool A_SIDE>
+__device__ __forceinline__ double pot_pair(const double *A, const double *B, double emin, double rmin, double k0,
+                                           double out[4][3])
 {
     double p[3][3], q[3][3];
 #pragma unroll
@@ -357,13 +371,26 @@ __device__ __forceinline__ double lj_pair(const double *A, const double *B, doub
             const double dx = p[k][0] - q[l][0], dy = p[k][1] - q[l][1], dz = p[k][2] - q[l][2];
             const double mag_r = sqrt(dx * dx + dy * dy + dz * dz);
             const double ri = 1. / mag_r;
-            const double ri2 = ri * ri;
-            const double ri4 = ri2 * ri2;
-            const double ri6 = ri4 * ri2;
-            const double ri7 = ri6 * ri;
-            const double f6 = r6 * ri6;
-            const double fm = 12 * ri7 * r6 * emin * (f6 - 1);
-            const double e = kW * kW * emin * f6 * (f6 - 2);
+            double fm, e;
+            if constexpr (POT == POT_LJ) {
+                const double ri2 = ri * ri;
+                const double ri4 = ri2 * ri2;
+                const double ri6 = ri4 * ri2;
+                const double ri7 = ri6 * ri;
+                const double f6 = r6 * ri6;
+                fm = 12 * ri7 * r6 * emin * (f6 - 1);
+                e = kW * kW * emin * f6 * (f6 - 2);
+            } else {
+                const double mag_r_2 = mag_r * mag_r;
+                const double gf2 = mag_r_2 / r2;
+                const double gf3 = gf2 * mag_r / rmin;
+                const double k0rm = k0 * rmin;
+                const double k0rm2 = k0rm * rmin;
+                const double epsonrm = emin / rmin;
+                fm = 2 * (k0rm - 6 * epsonrm) * gf3 + 3 * (4 * epsonrm - k0rm) * gf2 + k0 * mag_r;
+                e = kW * kW *
+                    ((0.5 * k0rm2 - 3 * emin) * gf2 * gf2 + (4 * emin - k0rm2) * gf3 + 0.5 * k0 * mag_r_2 - emin);
+            }
             energy += (l == k) ? e : 2 * e;
 #pragma unroll
             for (int d = 0; d < 3; d++) {
@@ -395,6 +422,254 @@ __device__ __forceinline__ double lj_pair(const double *A, const double *B, doub
     return energy * apaq;
 }
 
+// ---- steric: the overlap of two tetrahedra -------------------------------
+// The overlap of tetrahedra A and B is clipped out of A by B's four
+// half-spaces: each face polygon clipped in turn (Sutherland-Hodgman) and each
+// cut closed by a cap polygon, its points ordered by angle.  Two tetrahedra
+// intersect in at most 8 half-spaces, so the polyhedron has at most 8 faces
+// of at most 7 vertices.  Its volume is a fan of tetrahedra from the mean of
+// its vertices; its "centre" is what FFEA's volumeIntersectionII returns
+// (findCM, src/VolumeIntersection.cpp:95-104): the mean of its distinct
+// vertices.  Points closer than 1e-9 of the tetrahedra's extent are one.
+constexpr int kStV = 8, kStF = 8, kStC = 16, kStU = 32;
+
+struct StPolyh {
+    int nf;
+    int n[kStF];
+    double v[kStF][kStV][3];
+};
+
+__device__ __forceinline__ double st_dot(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+__device__ __forceinline__ double st_tet_volume(const double *a, const double *b, const double *c, const double *d)
+{
+    const double u0 = b[0] - a[0], u1 = b[1] - a[1], u2 = b[2] - a[2];
+    const double v0 = c[0] - a[0], v1 = c[1] - a[1], v2 = c[2] - a[2];
+    const double w0 = d[0] - a[0], w1 = d[1] - a[1], w2 = d[2] - a[2];
+    const double x0 = v1 * w2 - v2 * w1, x1 = v2 * w0 - v0 * w2, x2 = v0 * w1 - v1 * w0;
+    return (u0 * x0 + u1 * x1 + u2 * x2) / 6.0;
+}
+
+__device__ __forceinline__ void st_add_unique(double (*pts)[3], int &n, int cap, const double *x, double tol2)
+{
+    for (int u = 0; u < n; u++) {
+        const double e0 = x[0] - pts[u][0], e1 = x[1] - pts[u][1], e2 = x[2] - pts[u][2];
+        if (e0 * e0 + e1 * e1 + e2 * e2 <= tol2) return;
+    }
+    if (n < cap) {
+        pts[n][0] = x[0];
+        pts[n][1] = x[1];
+        pts[n][2] = x[2];
+        n++;
+    }
+}
+
+__constant__ int c_tri[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+
+// clip P by n . x <= off; false when nothing is left
+__device__ bool st_clip(StPolyh &P, const double *nrm, double off, double tol2)
+{
+    double smin = 0.0, smax = 0.0;
+    bool first = true;
+    for (int f = 0; f < P.nf; f++)
+        for (int k = 0; k < P.n[f]; k++) {
+            const double sv = st_dot(nrm, P.v[f][k]) - off;
+            if (first || sv < smin) smin = sv;
+            if (first || sv > smax) smax = sv;
+            first = false;
+        }
+    if (first || smin >= 0) {
+        P.nf = 0;
+        return false;
+    }
+    if (smax <= 0) return true;
+    double cap[kStC][3];
+    int nc = 0, nf = 0;
+    for (int f = 0; f < P.nf; f++) {
+        double out[kStV][3];
+        int no = 0;
+        const int m = P.n[f];
+        for (int k = 0; k < m; k++) {
+            const double *a = P.v[f][k], *b = P.v[f][k + 1 < m ? k + 1 : 0];
+            const double sa = st_dot(nrm, a) - off, sb = st_dot(nrm, b) - off;
+            if (sa <= 0) {
+                if (no < kStV) {
+                    out[no][0] = a[0];
+                    out[no][1] = a[1];
+                    out[no][2] = a[2];
+                    no++;
+                }
+                if (sa == 0) st_add_unique(cap, nc, kStC, a, tol2);
+            }
+            if ((sa < 0 && sb > 0) || (sa > 0 && sb < 0)) {
+                const double t = sa / (sa - sb);
+                double x[3];
+                for (int c = 0; c < 3; c++) x[c] = a[c] + t * (b[c] - a[c]);
+                if (no < kStV) {
+                    out[no][0] = x[0];
+                    out[no][1] = x[1];
+                    out[no][2] = x[2];
+                    no++;
+                }
+                st_add_unique(cap, nc, kStC, x, tol2);
+            }
+        }
+        if (no >= 3) {
+            for (int k = 0; k < no; k++)
+                for (int c = 0; c < 3; c++) P.v[nf][k][c] = out[k][c];
+            P.n[nf++] = no;
+        }
+    }
+    P.nf = nf;
+    if (nf == 0) return false;
+    if (nc >= 3 && nf < kStF) {
+        double ctr[3] = {0, 0, 0};
+        for (int k = 0; k < nc; k++)
+            for (int d = 0; d < 3; d++) ctr[d] += cap[k][d];
+        for (int d = 0; d < 3; d++) ctr[d] /= nc;
+        int far = 0;
+        double best = -1;
+        for (int k = 0; k < nc; k++) {
+            const double e0 = cap[k][0] - ctr[0], e1 = cap[k][1] - ctr[1], e2 = cap[k][2] - ctr[2];
+            const double l = e0 * e0 + e1 * e1 + e2 * e2;
+            if (l > best) {
+                best = l;
+                far = k;
+            }
+        }
+        if (best > 0) {
+            const double u[3] = {cap[far][0] - ctr[0], cap[far][1] - ctr[1], cap[far][2] - ctr[2]};
+            const double w[3] = {nrm[1] * u[2] - nrm[2] * u[1], nrm[2] * u[0] - nrm[0] * u[2],
+                                 nrm[0] * u[1] - nrm[1] * u[0]};
+            double ang[kStC];
+            for (int k = 0; k < nc; k++) {
+                const double e[3] = {cap[k][0] - ctr[0], cap[k][1] - ctr[1], cap[k][2] - ctr[2]};
+                ang[k] = atan2(st_dot(e, w), st_dot(e, u));
+            }
+            for (int i = 1; i < nc; i++) {  // insertion sort by angle
+                const double a = ang[i], v0 = cap[i][0], v1 = cap[i][1], v2 = cap[i][2];
+                int j = i - 1;
+                while (j >= 0 && ang[j] > a) {
+                    ang[j + 1] = ang[j];
+                    cap[j + 1][0] = cap[j][0];
+                    cap[j + 1][1] = cap[j][1];
+                    cap[j + 1][2] = cap[j][2];
+                    j--;
+                }
+                ang[j + 1] = a;
+                cap[j + 1][0] = v0;
+                cap[j + 1][1] = v1;
+                cap[j + 1][2] = v2;
+            }
+            const int nn = nc < kStV ? nc : kStV;
+            for (int k = 0; k < nn; k++)
+                for (int c = 0; c < 3; c++) P.v[P.nf][k][c] = cap[k][c];
+            P.n[P.nf++] = nn;
+        }
+    }
+    return true;
+}
+
+// overlap volume of tetrahedra A and B (4 x 3 each); with cm, FFEA's centre
+__device__ double st_overlap(const double (*A)[3], const double (*B)[3], double *cm)
+{
+    double ext = 0.0;
+    for (int i = 0; i < 4; i++)
+        for (int d = 0; d < 3; d++) {
+            ext = fmax(ext, fabs(A[i][d] - A[0][d]));
+            ext = fmax(ext, fabs(B[i][d] - A[0][d]));
+        }
+    const double tol2 = (1e-9 * ext) * (1e-9 * ext);
+    StPolyh P;
+    P.nf = 4;
+    for (int f = 0; f < 4; f++) {
+        P.n[f] = 3;
+        for (int k = 0; k < 3; k++)
+            for (int c = 0; c < 3; c++) P.v[f][k][c] = A[c_tri[f][k]][c];
+    }
+    for (int f = 0; f < 4; f++) {
+        // the half-space of B's face f (opposite vertex f) that holds B
+        const double *t0 = B[c_tri[f][0]], *t1 = B[c_tri[f][1]], *t2 = B[c_tri[f][2]];
+        const double u[3] = {t1[0] - t0[0], t1[1] - t0[1], t1[2] - t0[2]};
+        const double v[3] = {t2[0] - t0[0], t2[1] - t0[1], t2[2] - t0[2]};
+        double nrm[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+        double off = st_dot(nrm, t0);
+        if (st_dot(nrm, B[f]) > off) {
+            nrm[0] = -nrm[0];
+            nrm[1] = -nrm[1];
+            nrm[2] = -nrm[2];
+            off = -off;
+        }
+        if (!st_clip(P, nrm, off, tol2)) {
+            if (cm) cm[0] = cm[1] = cm[2] = 0.0;
+            return 0.0;
+        }
+    }
+    double o[3] = {0, 0, 0};
+    int nv = 0;
+    for (int f = 0; f < P.nf; f++)
+        for (int k = 0; k < P.n[f]; k++) {
+            for (int d = 0; d < 3; d++) o[d] += P.v[f][k][d];
+            nv++;
+        }
+    for (int d = 0; d < 3; d++) o[d] /= nv;
+    double vol = 0.0;
+    for (int f = 0; f < P.nf; f++)
+        for (int k = 1; k + 1 < P.n[f]; k++) vol += fabs(st_tet_volume(o, P.v[f][0], P.v[f][k], P.v[f][k + 1]));
+    if (cm) {
+        double uniq[kStU][3];
+        int nu = 0;
+        for (int f = 0; f < P.nf; f++)
+            for (int k = 0; k < P.n[f]; k++) st_add_unique(uniq, nu, kStU, P.v[f][k], tol2);
+        cm[0] = cm[1] = cm[2] = 0.0;
+        for (int u = 0; u < nu; u++)
+            for (int d = 0; d < 3; d++) cm[d] += uniq[u][d];
+        for (int d = 0; d < 3; d++) cm[d] *= 1.0 / nu;
+    }
+    return vol;
+}
+
+// One steric pair, f1 = A, f2 = B (the tetrahedra of the faces' elements):
+// Face::getTetraIntersectionVolumeTotalGradientAndShapeFunctions
+// (src/Face.cpp:473-514) and do_steric_interaction's scaling
+// (src/VdW_solver.cpp:470-483).  false when they do not overlap; else adds
+// the A side's (phi1 k dV/dr) or the B side's (-phi2 k dV/dr) node forces to
+// out and sets vol = k V.
+__device__ bool steric_pair(const double (*A)[3], const double (*B)[3], double dr, double k, bool a_side,
+                            double out[4][3], double &vol)
+{
+    double cm[3];
+    const double V = st_overlap(A, B, cm);
+    if (V == 0) return false;
+    // getLocalCoordinatesForLinTet (src/mat_vec_fns_II.cpp:725-734) of the
+    // side's own tetrahedron
+    const double (*T)[3] = a_side ? A : B;
+    double phi[4];
+    phi[0] = st_tet_volume(cm, T[1], T[2], T[3]);
+    phi[1] = -st_tet_volume(cm, T[0], T[2], T[3]);
+    phi[2] = st_tet_volume(cm, T[0], T[1], T[3]);
+    phi[3] = -st_tet_volume(cm, T[0], T[1], T[2]);
+    const double tv = st_tet_volume(T[0], T[1], T[2], T[3]);
+    for (int i = 0; i < 4; i++) phi[i] /= tv;
+    double g[3];
+    for (int dir = 0; dir < 3; dir++) {
+        double S[4][3];
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 3; j++) S[i][j] = B[i][j] + (j == dir ? dr : 0.0);
+        const double vb = st_overlap(A, S, nullptr);
+        g[dir] = (vb - V) / dr;
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 3; j++) S[i][j] = A[i][j] + (j == dir ? dr : 0.0);
+        const double va = st_overlap(B, S, nullptr);
+        g[dir] -= (va - V) / dr;
+    }
+    vol = V * k;
+    for (int d = 0; d < 3; d++) g[d] *= k;
+    for (int i = 0; i < 4; i++)
+        for (int d = 0; d < 3; d++) out[i][d] += a_side ? phi[i] * g[d] : -1.0 * phi[i] * g[d];
+    return true;
+}
+
 __constant__ int c_adj[27][3] = {{-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {-1, 0, -1}, {-1, 0, 0}, {-1, 0, 1},
                                  {-1, 1, -1},  {-1, 1, 0},  {-1, 1, 1},  {0, -1, -1}, {0, -1, 0}, {0, -1, 1},
                                  {0, 0, -1},   {0, 0, 0},   {0, 0, 1},   {0, 1, -1},  {0, 1, 0},  {0, 1, 1},
@@ -410,27 +685,13 @@ __device__ __forceinline__ double warp_sum_d(double v)
     return v;
 }
 
-// One warp per face i (faces taken in cell order): the candidates of the 27
-// cells around i's cell are numbered 0..total-1 through a prefix sum over the
-// cells, lane l tests candidates l, l + 32, ..., and the partners that pass
-// are evaluated from a per-warp queue.  Each lane keeps face i's side of its
-// pairs; a fixed shuffle tree sums the lanes.
-__global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
-    const double *__restrict__ geo, const int *__restrict__ cell, const int *__restrict__ sorted,
-    const int *__restrict__ start, const int *__restrict__ block, long long ncell, int nblocks, int nx, int ny,
-    int nz, const int *__restrict__ fblob, const int *__restrict__ ftype, const double *__restrict__ emin,
-    const double *__restrict__ rmin, int num_types, int num_blobs, int inc_self, double *__restrict__ fforce,
-    double *__restrict__ energy, unsigned long long *stats)
+// The faces of the 27 cells around face i's cell for one warp: s_beg / s_pre
+// hold each cell's first sorted slot and the candidates before it; returns
+// the number of candidates.
+__device__ __forceinline__ int warp_cells(int ci, int nx, int ny, int nz, const int *__restrict__ start,
+                                          const int *__restrict__ block, long long ncell, int nblocks, int lane,
+                                          int *s_beg, int *s_pre)
 {
-    __shared__ int s_pre[kPairWarps][28];
-    __shared__ int s_beg[kPairWarps][27];
-    __shared__ int s_q[kPairWarps][64];
-    const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long w = (long long)blockIdx.x * kPairWarps + wi;
-    if (w >= block[nblocks]) return;  // warp-uniform; faces outside the box are not binned
-    if (stats[3]) return;             // a cell too full to sort: the call fails, nothing to evaluate
-    const int i = sorted[w];
-    const int ci = cell[i];
     const int cz = ci % nz, cy = (ci / nz) % ny, cx = ci / (nz * ny);
     int len = 0, beg = 0;
     if (lane < 27) {
@@ -442,16 +703,223 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
     }
     const int incl = warp_incl_scan(len, lane);
     if (lane < 27) {
-        s_beg[wi][lane] = beg;
-        s_pre[wi][lane] = incl - len;
+        s_beg[lane] = beg;
+        s_pre[lane] = incl - len;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 26);
     __syncwarp();
+    return total;
+}
+
+// candidate k (< total) of the warp's cells
+__device__ __forceinline__ int warp_candidate(int k, const int *s_beg, const int *s_pre, const int *__restrict__ sorted)
+{
+    int c = 0;
+    while (c < 26 && s_pre[c + 1] <= k) c++;
+    return sorted[s_beg[c] + (k - s_pre[c])];
+}
+
+// consider_interaction's checks for the types other than lennard-jones
+// (src/VdW_solver.cpp:359-388): faces in front of each other, and within
+// one blob (with self-interaction on) no shared node.  Symmetric in (i, j).
+__device__ __forceinline__ bool steric_type_ok(const double *A, const double *G, bool same_blob, int inc_self,
+                                               const int *ni, const int *nj)
+{
+    double sa = 0.0, sb = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const double sep = (1.0 / 3.0) * (G[d] + G[3 + d] + G[6 + d]) - (1.0 / 3.0) * (A[d] + A[3 + d] + A[6 + d]);
+        sa += sep * A[9 + d];
+        sb += sep * G[9 + d];
+    }
+    if (sa < 0 && sb > 0) return false;
+    if (inc_self && same_blob) {
+        if (ni[3] == nj[3]) return false;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int w = 0; w < 4; w++)
+                if (ni[u] == nj[w]) return false;
+    }
+    return true;
+}
+
+// the element tetrahedron of face f: its corners, then the fourth node
+__device__ __forceinline__ void face_tet(const double *__restrict__ geo, int f, double T[4][3])
+{
+    const double *g = geo + 16 * (long long)f;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) T[k][d] = g[3 * k + d];
+#pragma unroll
+    for (int d = 0; d < 3; d++) T[3][d] = g[13 + d];
+}
+
+constexpr int kStericWarps = 4;  // warps (faces) per CTA of k_steric
+
+// The steric part of the steric types, one warp per face i in cell order:
+// every partner j of the 27 cells that consider_interaction admits and whose
+// element tetrahedron's bounding box meets i's is queued; the queue is
+// evaluated a lane per pair, each pair as (lower index, higher index) = FFEA's
+// (f1, f2), so both sides compute the same overlap.  Face i's side of the
+// forces goes to fforce (12 values, written here: this kernel runs first), the
+// partners that overlapped to i's steric list (k_pairs skips them), the energy
+// and the pair count from the side with the lower index.
+__global__ void __launch_bounds__(32 * kStericWarps) k_steric(
+    const double *__restrict__ geo, const int *__restrict__ sorted, const int *__restrict__ cell,
+    const int *__restrict__ start, const int *__restrict__ block, long long ncell, int nblocks, int nx, int ny,
+    int nz, const int *__restrict__ fblob, const int *__restrict__ corner, int num_blobs, int inc_self,
+    double steric_factor, double steric_dr, double *__restrict__ fforce, int *__restrict__ stlist,
+    int *__restrict__ stcnt, double *__restrict__ energy, unsigned long long *stats)
+{
+    __shared__ int s_pre[kStericWarps][28];
+    __shared__ int s_beg[kStericWarps][27];
+    __shared__ int s_q[kStericWarps][64];
+    const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long w = (long long)blockIdx.x * kStericWarps + wi;
+    if (w >= block[nblocks]) return;  // warp-uniform
+    if (stats[3]) return;             // the call fails (a cell too full to sort)
+    const int i = sorted[w];
+    const int total = warp_cells(cell[i], nx, ny, nz, start, block, ncell, nblocks, lane, s_beg[wi], s_pre[wi]);
+    const double *A = geo + 16 * (long long)i;
+    const int bi = fblob[i];
+    int ni[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) ni[u] = corner[4 * i + u];
+    double Ti[4][3];
+    face_tet(geo, i, Ti);
+    double lo_i[3], hi_i[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        lo_i[d] = fmin(fmin(Ti[0][d], Ti[1][d]), fmin(Ti[2][d], Ti[3][d]));
+        hi_i[d] = fmax(fmax(Ti[0][d], Ti[1][d]), fmax(Ti[2][d], Ti[3][d]));
+    }
+    double out[4][3];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) out[u][d] = 0.0;
+    int listed = 0;
+    unsigned long long npairs = 0;
+    auto evaluate = [&](bool have, int j) {
+        bool hit = false;
+        if (have) {
+            double Tj[4][3], vol;
+            face_tet(geo, j, Tj);
+            hit = i < j ? steric_pair(Ti, Tj, steric_dr, steric_factor, true, out, vol)
+                        : steric_pair(Tj, Ti, steric_dr, steric_factor, false, out, vol);
+            if (hit && i < j) {
+                atomicAdd(&energy[bi * num_blobs + fblob[j]], vol);
+                npairs++;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int slot = listed + __popc(m & ((1u << lane) - 1u));
+            if (slot < FFEA_GPU_SSINT_MAX_STERIC_PARTNERS) stlist[FFEA_GPU_SSINT_MAX_STERIC_PARTNERS * i + slot] = j;
+        }
+        listed += __popc(m);
+    };
+    int qn = 0;  // warp-uniform queue length, < 64
+    for (int base = 0; base < total; base += 32) {
+        const int k = base + lane;
+        bool ok = false;
+        int j = -1;
+        if (k < total) {
+            j = warp_candidate(k, s_beg[wi], s_pre[wi], sorted);
+            const double *G = geo + 16 * (long long)j;
+            const bool same = bi == fblob[j];
+            ok = j != i && (inc_self || !same) && !(A[9] * G[9] + A[10] * G[10] + A[11] * G[11] > 0.0);
+            if (ok) {
+                int nj[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) nj[u] = corner[4 * j + u];
+                ok = steric_type_ok(A, G, same, inc_self, ni, nj);
+            }
+            if (ok) {  // bounding boxes of the two tetrahedra
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const double a0 = G[d], a1 = G[3 + d], a2 = G[6 + d], a3 = G[13 + d];
+                    const double lo = fmin(fmin(a0, a1), fmin(a2, a3)), hi = fmax(fmax(a0, a1), fmax(a2, a3));
+                    if (hi < lo_i[d] || lo > hi_i[d]) ok = false;
+                }
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        if (ok) s_q[wi][qn + __popc(m & ((1u << lane) - 1u))] = j;
+        qn += __popc(m);
+        __syncwarp();
+        if (qn >= 32) {
+            evaluate(true, s_q[wi][lane]);
+            const int rest = qn - 32;
+            const int moved = lane < rest ? s_q[wi][32 + lane] : 0;
+            __syncwarp();
+            if (lane < rest) s_q[wi][lane] = moved;
+            qn = rest;
+            __syncwarp();
+        }
+    }
+    if (qn > 0) evaluate(lane < qn, lane < qn ? s_q[wi][lane] : -1);
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) out[u][d] = warp_sum_d(out[u][d]);
+    unsigned long long np = npairs;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) np += __shfl_xor_sync(0xffffffffu, np, o);
+    if (lane == 0) {
+        if (np) atomicAdd(&stats[0], np);
+        stcnt[i] = min(listed, FFEA_GPU_SSINT_MAX_STERIC_PARTNERS);
+        if (listed > FFEA_GPU_SSINT_MAX_STERIC_PARTNERS) atomicAdd(&stats[4], 1ull);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int d = 0; d < 3; d++) fforce[12 * (long long)i + 3 * u + d] = out[u][d];
+    }
+}
+
+// One warp per face i (faces taken in cell order): the candidates of the 27
+// cells around i's cell are numbered 0..total-1 through a prefix sum over the
+// cells, lane l tests candidates l, l + 32, ..., and the partners that pass
+// are evaluated from a per-warp queue.  Each lane keeps face i's side of its
+// pairs; a fixed shuffle tree sums the lanes.  POT: Lennard-Jones or the soft
+// potential; STERIC: the steric types' pair checks apply, the partners of i's
+// steric list are skipped (k_steric gave them the steric force) and the
+// forces add to what k_steric wrote.
+template <int POT, bool STERIC>
+__global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
+    const double *__restrict__ geo, const int *__restrict__ cell, const int *__restrict__ sorted,
+    const int *__restrict__ start, const int *__restrict__ block, long long ncell, int nblocks, int nx, int ny,
+    int nz, const int *__restrict__ fblob, const int *__restrict__ ftype, const double *__restrict__ emin,
+    const double *__restrict__ rmin, const double *__restrict__ k0, const int *__restrict__ corner,
+    const int *__restrict__ stlist, const int *__restrict__ stcnt, int num_types, int num_blobs, int inc_self,
+    double *__restrict__ fforce, double *__restrict__ energy, unsigned long long *stats)
+{
+    __shared__ int s_pre[kPairWarps][28];
+    __shared__ int s_beg[kPairWarps][27];
+    __shared__ int s_q[kPairWarps][64];
+    __shared__ int s_st[kPairWarps][FFEA_GPU_SSINT_MAX_STERIC_PARTNERS];
+    const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long w = (long long)blockIdx.x * kPairWarps + wi;
+    if (w >= block[nblocks]) return;  // warp-uniform; faces outside the box are not binned
+    if (stats[3]) return;             // a cell too full to sort: the call fails, nothing to evaluate
+    const int i = sorted[w];
+    const int total = warp_cells(cell[i], nx, ny, nz, start, block, ncell, nblocks, lane, s_beg[wi], s_pre[wi]);
+    int nst = 0;
+    int ni[4] = {0, 0, 0, 0};
+    if constexpr (STERIC) {
+        nst = stcnt[i];
+        if (lane < nst) s_st[wi][lane] = stlist[FFEA_GPU_SSINT_MAX_STERIC_PARTNERS * i + lane];
+#pragma unroll
+        for (int u = 0; u < 4; u++) ni[u] = corner[4 * i + u];
+        __syncwarp();
+    }
     double A[13];
 #pragma unroll
     for (int k = 0; k < 13; k++) A[k] = geo[16 * (long long)i + k];
     const int bi = fblob[i], ti = ftype[i];
-    double out[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double out[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     double e_acc = 0.0;
     int e_key = -1;
     unsigned long long npairs = 0;
@@ -463,7 +931,7 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
         for (int q = 0; q < 13; q++) B[q] = G[q];
         if (i < j) {
             const int tt = ti * num_types + ftype[j];
-            const double en = lj_pair<true>(A, B, emin[tt], rmin[tt], out);
+            const double en = pot_pair<POT, true>(A, B, emin[tt], rmin[tt], k0 ? k0[tt] : 0.0, out);
             const int key = bi * num_blobs + fblob[j];
             if (key != e_key) {
                 if (e_key >= 0) atomicAdd(&energy[e_key], e_acc);
@@ -474,7 +942,7 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
             npairs++;
         } else {
             const int tt = ftype[j] * num_types + ti;
-            lj_pair<false>(B, A, emin[tt], rmin[tt], out);
+            pot_pair<POT, false>(B, A, emin[tt], rmin[tt], k0 ? k0[tt] : 0.0, out);
         }
     };
     // The cheap tests (same face, same blob, normals facing the same way) run
@@ -487,11 +955,19 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
         bool ok = false;
         int j = -1;
         if (k < total) {
-            int c = 0;
-            while (c < 26 && s_pre[wi][c + 1] <= k) c++;
-            j = sorted[s_beg[wi][c] + (k - s_pre[wi][c])];
+            j = warp_candidate(k, s_beg[wi], s_pre[wi], sorted);
             const double *G = geo + 16 * (long long)j;
             ok = j != i && (inc_self || bi != fblob[j]) && !(A[9] * G[9] + A[10] * G[10] + A[11] * G[11] > 0.0);
+            if constexpr (STERIC) {
+                if (ok) {
+                    int nj[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) nj[u] = corner[4 * j + u];
+                    ok = steric_type_ok(A, G, bi == fblob[j], inc_self, ni, nj);
+                }
+                for (int t = 0; ok && t < nst; t++)
+                    if (s_st[wi][t] == j) ok = false;  // the steric force applied instead
+            }
         }
         const unsigned m = __ballot_sync(0xffffffffu, ok);
         if (ok) s_q[wi][qn + __popc(m & ((1u << lane) - 1u))] = j;
@@ -527,9 +1003,12 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
     if (lane == 0) {
         if (np) atomicAdd(&stats[0], np);
 #pragma unroll
-        for (int k = 0; k < 3; k++)
+        for (int k = 0; k < 4; k++)
 #pragma unroll
-            for (int d = 0; d < 3; d++) fforce[9 * (long long)i + 3 * k + d] = out[k][d];
+            for (int d = 0; d < 3; d++) {
+                double *f = &fforce[12 * (long long)i + 3 * k + d];
+                *f = STERIC ? *f + out[k][d] : out[k][d];
+            }
     }
 }
 
@@ -542,7 +1021,7 @@ __global__ void k_node_gather(const int *__restrict__ ptr, const int *__restrict
     double f[3] = {0.0, 0.0, 0.0};
     for (int k = ptr[n]; k < ptr[n + 1]; k++) {
         const int fc = ent[k];
-        if (cell[fc / 3] < 0) continue;
+        if (cell[fc / 4] < 0) continue;
 #pragma unroll
         for (int d = 0; d < 3; d++) f[d] += fforce[3 * (long long)fc + d];
     }
@@ -573,27 +1052,38 @@ extern "C" int ffea_gpu_ssint_create(const ffea_gpu_ssint_desc *d, ffea_gpu_ssin
     const long long ncell = (long long)d->nx * d->ny * d->nz;
     if (ncell > FFEA_GPU_SSINT_MAX_CELLS)
         return fail("ffea_gpu_ssint_create: %lld cells exceed the maximum %d", ncell, FFEA_GPU_SSINT_MAX_CELLS);
+    const int stype = d->ssint_type;
+    if (stype < FFEA_GPU_SSINT_LJ || stype > FFEA_GPU_SSINT_GENSOFT) return fail("unknown ssint_type %d", stype);
+    const bool steric = stype != FFEA_GPU_SSINT_LJ;
+    if (steric && d->num_faces && !d->face_apex) return fail("the steric types need face_apex (Face::n[3] per face)");
+    if (steric && !(d->steric_dr > 0.0)) return fail("steric_dr must be positive");
+    if (stype == FFEA_GPU_SSINT_GENSOFT && !d->k0) return fail("gensoft needs k0");
     std::vector<int> corner, blob, type;
     for (int f = 0; f < d->num_faces; f++) {
         if (d->face_type[f] < 0) continue;  // not ssint-active: not in the pool (src/Blob.cpp:1642-1648)
         if (d->face_type[f] >= d->num_types) return fail("face %d: interaction type %d >= num_types", f, d->face_type[f]);
         if (d->face_blob[f] < 0 || d->face_blob[f] >= d->num_blobs) return fail("face %d: blob %d out of range", f, d->face_blob[f]);
-        for (int k = 0; k < 3; k++) {
-            const int n = d->faces[3 * f + k];
-            if (n < 0 || n >= d->num_nodes) return fail("face %d: node %d out of range", f, n);
+        for (int k = 0; k < 4; k++) {
+            const int n = k < 3 ? d->faces[3 * f + k] : (steric ? d->face_apex[f] : -1);
+            if (n < -1 || n >= d->num_nodes || (n < 0 && k < 3) || (n < 0 && steric))
+                return fail("face %d: node %d out of range", f, n);
             corner.push_back(n);
         }
         blob.push_back(d->face_blob[f]);
         type.push_back(d->face_type[f]);
     }
     const int na = (int)blob.size();
-    // node -> (active face, corner) entries in face order
-    std::vector<int> ptr(d->num_nodes + 1, 0), ent(3 * (size_t)na);
-    for (int i = 0; i < 3 * na; i++) ptr[corner[i] + 1]++;
+    // node -> (active face, node of the face) entries in face order (the
+    // fourth node only for the steric types)
+    std::vector<int> ptr(d->num_nodes + 1, 0), ent;
+    for (int i = 0; i < 4 * na; i++)
+        if (corner[i] >= 0) ptr[corner[i] + 1]++;
     for (int n = 0; n < d->num_nodes; n++) ptr[n + 1] += ptr[n];
+    ent.resize((size_t)ptr[d->num_nodes]);
     {
         std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-        for (int i = 0; i < 3 * na; i++) ent[fill[corner[i]]++] = i;
+        for (int i = 0; i < 4 * na; i++)
+            if (corner[i] >= 0) ent[fill[corner[i]]++] = i;
     }
     auto *s = new ffea_gpu_ssint();
     s->num_nodes = d->num_nodes;
@@ -605,6 +1095,9 @@ extern "C" int ffea_gpu_ssint_create(const ffea_gpu_ssint_desc *d, ffea_gpu_ssin
     s->ny = d->ny;
     s->nz = d->nz;
     s->inc_self = d->inc_self ? 1 : 0;
+    s->type = stype;
+    s->steric_factor = d->steric_factor;
+    s->steric_dr = d->steric_dr;
     s->h = d->cell_size;
     s->ncell = ncell;
     s->nblocks = (int)((ncell + kScanBlock - 1) / kScanBlock);
@@ -612,24 +1105,30 @@ extern "C" int ffea_gpu_ssint_create(const ffea_gpu_ssint_desc *d, ffea_gpu_ssin
     int rc = FFEA_GPU_OK;
     auto run = [&]() -> int {
         SSINT_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
-        if (dalloc(&s->d_corner, 3 * (size_t)na) || dalloc(&s->d_blob, na) || dalloc(&s->d_type, na) ||
-            dalloc(&s->d_geo, 16 * (size_t)na) || dalloc(&s->d_cell, na) || dalloc(&s->d_fforce, 9 * (size_t)na) ||
+        if (dalloc(&s->d_corner, 4 * (size_t)na) || dalloc(&s->d_blob, na) || dalloc(&s->d_type, na) ||
+            dalloc(&s->d_geo, 16 * (size_t)na) || dalloc(&s->d_cell, na) || dalloc(&s->d_fforce, 12 * (size_t)na) ||
             dalloc(&s->d_count, ncell) || dalloc(&s->d_start, ncell) || dalloc(&s->d_block, s->nblocks + 1) ||
             dalloc(&s->d_sorted, na) || dalloc(&s->d_node_ptr, d->num_nodes + 1) ||
-            dalloc(&s->d_node_ent, 3 * (size_t)na) || dalloc(&s->d_emin, T2) || dalloc(&s->d_rmin, T2) ||
+            dalloc(&s->d_node_ent, ent.size()) || dalloc(&s->d_emin, T2) || dalloc(&s->d_rmin, T2) ||
             dalloc(&s->d_pos, 3 * (size_t)d->num_nodes) || dalloc(&s->d_force, 3 * (size_t)d->num_nodes) ||
-            dalloc(&s->d_energy, (size_t)d->num_blobs * d->num_blobs) || dalloc(&s->d_stats, 4) ||
+            dalloc(&s->d_energy, (size_t)d->num_blobs * d->num_blobs) || dalloc(&s->d_stats, 5) ||
             dalloc(&s->d_large, (size_t)na / (kSortSmall + 1) + 1))
             return FFEA_GPU_ERROR;
+        if (steric && (dalloc(&s->d_stlist, (size_t)FFEA_GPU_SSINT_MAX_STERIC_PARTNERS * na) ||
+                       dalloc(&s->d_stcnt, na)))
+            return FFEA_GPU_ERROR;
+        if (stype == FFEA_GPU_SSINT_GENSOFT && dalloc(&s->d_k0, T2)) return FFEA_GPU_ERROR;
         if (na) {
-            SSINT_CUDA(cudaMemcpy(s->d_corner, corner.data(), sizeof(int) * 3 * na, cudaMemcpyHostToDevice));
+            SSINT_CUDA(cudaMemcpy(s->d_corner, corner.data(), sizeof(int) * 4 * na, cudaMemcpyHostToDevice));
             SSINT_CUDA(cudaMemcpy(s->d_blob, blob.data(), sizeof(int) * na, cudaMemcpyHostToDevice));
             SSINT_CUDA(cudaMemcpy(s->d_type, type.data(), sizeof(int) * na, cudaMemcpyHostToDevice));
-            SSINT_CUDA(cudaMemcpy(s->d_node_ent, ent.data(), sizeof(int) * 3 * na, cudaMemcpyHostToDevice));
         }
+        if (!ent.empty())
+            SSINT_CUDA(cudaMemcpy(s->d_node_ent, ent.data(), sizeof(int) * ent.size(), cudaMemcpyHostToDevice));
         SSINT_CUDA(cudaMemcpy(s->d_node_ptr, ptr.data(), sizeof(int) * (d->num_nodes + 1), cudaMemcpyHostToDevice));
         SSINT_CUDA(cudaMemcpy(s->d_emin, d->emin, sizeof(double) * T2, cudaMemcpyHostToDevice));
         SSINT_CUDA(cudaMemcpy(s->d_rmin, d->rmin, sizeof(double) * T2, cudaMemcpyHostToDevice));
+        if (s->d_k0) SSINT_CUDA(cudaMemcpy(s->d_k0, d->k0, sizeof(double) * T2, cudaMemcpyHostToDevice));
         return FFEA_GPU_OK;
     };
     rc = run();
@@ -647,7 +1146,7 @@ extern "C" void ffea_gpu_ssint_destroy(ffea_gpu_ssint_t *s)
     if (s->stream) cudaStreamSynchronize(s->stream);
     void *bufs[] = {s->d_corner, s->d_blob, s->d_type, s->d_geo, s->d_cell, s->d_fforce, s->d_count,
                     s->d_start, s->d_block, s->d_sorted, s->d_node_ptr, s->d_node_ent, s->d_emin, s->d_rmin,
-                    s->d_pos, s->d_force, s->d_energy, s->d_stats, s->d_large};
+                    s->d_pos, s->d_force, s->d_energy, s->d_stats, s->d_large, s->d_stlist, s->d_stcnt, s->d_k0};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -662,7 +1161,7 @@ extern "C" int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *p
     cudaStream_t st = s->stream;
     const int na = s->num_active;
     SSINT_CUDA(cudaMemsetAsync(energy, 0, sizeof(double) * s->num_blobs * s->num_blobs, st));
-    SSINT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * 4, st));
+    SSINT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * 5, st));
     if (na == 0) {
         SSINT_CUDA(cudaMemsetAsync(force, 0, sizeof(double) * 3 * (size_t)s->num_nodes, st));
         return FFEA_GPU_OK;
@@ -680,9 +1179,21 @@ extern "C" int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *p
                                                                 s->d_sorted, s->d_large, s->d_stats);
     k_sort_large<<<kSortLargeCtas, 256, 0, st>>>(s->ncell, s->nblocks, s->d_start, s->d_block, s->d_sorted,
                                                  s->d_large, s->d_stats);
-    k_pairs<<<(na + kPairWarps - 1) / kPairWarps, 32 * kPairWarps, 0, st>>>(s->d_geo, s->d_cell, s->d_sorted, s->d_start, s->d_block, s->ncell, s->nblocks, s->nx,
-                                s->ny, s->nz, s->d_blob, s->d_type, s->d_emin, s->d_rmin, s->num_types,
-                                s->num_blobs, s->inc_self, s->d_fforce, energy, s->d_stats);
+    const int pw = (na + kPairWarps - 1) / kPairWarps;
+    if (s->type != FFEA_GPU_SSINT_LJ)
+        k_steric<<<(na + kStericWarps - 1) / kStericWarps, 32 * kStericWarps, 0, st>>>(
+            s->d_geo, s->d_sorted, s->d_cell, s->d_start, s->d_block, s->ncell, s->nblocks, s->nx, s->ny, s->nz,
+            s->d_blob, s->d_corner, s->num_blobs, s->inc_self, s->steric_factor, s->steric_dr, s->d_fforce,
+            s->d_stlist, s->d_stcnt, energy, s->d_stats);
+#define SSINT_PAIRS(POT, STERIC)                                                                                   \
+    k_pairs<POT, STERIC><<<pw, 32 * kPairWarps, 0, st>>>(                                                           \
+        s->d_geo, s->d_cell, s->d_sorted, s->d_start, s->d_block, s->ncell, s->nblocks, s->nx, s->ny, s->nz,        \
+        s->d_blob, s->d_type, s->d_emin, s->d_rmin, s->d_k0, s->d_corner, s->d_stlist, s->d_stcnt, s->num_types,     \
+        s->num_blobs, s->inc_self, s->d_fforce, energy, s->d_stats)
+    if (s->type == FFEA_GPU_SSINT_LJ) SSINT_PAIRS(POT_LJ, false);
+    else if (s->type == FFEA_GPU_SSINT_LJSTERIC) SSINT_PAIRS(POT_LJ, true);
+    else if (s->type == FFEA_GPU_SSINT_GENSOFT) SSINT_PAIRS(POT_SOFT, true);
+#undef SSINT_PAIRS
     k_node_gather<<<(s->num_nodes + 255) / 256, 256, 0, st>>>(s->d_node_ptr, s->d_node_ent, s->num_nodes,
                                                               s->d_fforce, s->d_cell, force);
     SSINT_CUDA(cudaGetLastError());
@@ -692,7 +1203,7 @@ extern "C" int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *p
 extern "C" int ffea_gpu_ssint_synchronize(ffea_gpu_ssint_t *s, int64_t *pairs)
 {
     if (!s) return fail("ffea_gpu_ssint_synchronize: null handle");
-    unsigned long long st[4] = {0, 0, 0, 0};
+    unsigned long long st[5] = {0, 0, 0, 0, 0};
     SSINT_CUDA(cudaMemcpyAsync(st, s->d_stats, sizeof(st), cudaMemcpyDeviceToHost, s->stream));
     SSINT_CUDA(cudaStreamSynchronize(s->stream));
     if (pairs) *pairs = (int64_t)st[0];
@@ -700,6 +1211,9 @@ extern "C" int ffea_gpu_ssint_synchronize(ffea_gpu_ssint_t *s, int64_t *pairs)
     if (st[3])
         return fail("%llu grid cells hold more than %d faces each: the interaction grid is too coarse for this mesh "
                     "(use more, smaller cells)", st[3], kSortMax);
+    if (st[4])
+        return fail("%llu faces' tetrahedra overlap more than %d others (their steric partners beyond that are "
+                    "not excluded from the Lennard-Jones or soft pairs)", st[4], FFEA_GPU_SSINT_MAX_STERIC_PARTNERS);
     return FFEA_GPU_OK;
 }
 

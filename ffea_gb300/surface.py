@@ -1,9 +1,10 @@
-"""Surface-surface Lennard-Jones interactions on the GPU (ffea_gpu_ssint_*).
+"""Surface-surface interactions on the GPU (ffea_gpu_ssint_*).
 
-The host-side mirror of FFEA's VdW_solver for "vdw_type = lennard-jones"
-(include/VdW_solver.h:36-127, src/VdW_solver.cpp:124-210): created once from
-the surface faces of every blob, then called once per step with the node
-positions, like VdW_solver::solve.  The node forces it returns are what
+The host-side mirror of FFEA's VdW_solver and its steric variants
+(include/VdW_solver.h:36-127, src/VdW_solver.cpp:124-210; Steric_solver,
+LJSteric_solver, GenSoftSSINT_solver) for ssint_type lennard-jones, steric,
+ljsteric and gensoft: created once from the surface faces of every blob, then
+called once per step with the node positions, like VdW_solver::solve.  The node forces it returns are what
 Blob::aggregate_forces_and_solve adds from the faces (src/Blob.cpp:3841-3851);
 pass them to the blob update with ffea_gpu_set_external_forces.
 """
@@ -24,19 +25,32 @@ class SsintDesc(ctypes.Structure):
         ("emin", ctypes.POINTER(ctypes.c_double)), ("rmin", ctypes.POINTER(ctypes.c_double)),
         ("num_blobs", ctypes.c_int32), ("cell_size", ctypes.c_double),
         ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32), ("inc_self", ctypes.c_int32),
+        ("ssint_type", ctypes.c_int32), ("face_apex", ctypes.POINTER(ctypes.c_int32)),
+        ("steric_factor", ctypes.c_double), ("steric_dr", ctypes.c_double),
+        ("k0", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
-class LJSurfaceSolver:
-    """VdW_solver (lennard-jones) over all blobs' surface faces.
+# SimulationParams::ssint_type
+SSINT_LJ, SSINT_STERIC, SSINT_LJSTERIC, SSINT_GENSOFT = 0, 1, 2, 3
+SSINT_TYPES = {"lennard-jones": SSINT_LJ, "steric": SSINT_STERIC, "ljsteric": SSINT_LJSTERIC,
+               "gensoft": SSINT_GENSOFT}
+
+
+class SurfaceSolver:
+    """VdW_solver (or a steric variant) over all blobs' surface faces.
 
     num_nodes: nodes of all blobs in one numbering; faces (F, 3) corner node
     indices in FFEA's pool order; face_blob, face_type (F,), type -1 inactive;
     emin, rmin (T, T) in meso units; grid (nx, ny, nz) cells of size
-    cell_size (ssint_cutoff); inc_self as inc_self_ssint."""
+    cell_size (ssint_cutoff); inc_self as inc_self_ssint.  The steric types
+    (ssint_type SSINT_STERIC, SSINT_LJSTERIC, SSINT_GENSOFT) also take
+    face_apex (F,), the fourth node of each face's element (Face::n[3]),
+    steric_factor and steric_dr (SimulationParams), and gensoft k0 (T, T) in
+    meso units."""
 
     def __init__(self, num_nodes, faces, face_blob, face_type, emin, rmin, num_blobs, cell_size, grid,
-                 inc_self=0):
+                 inc_self=0, ssint_type=SSINT_LJ, face_apex=None, steric_factor=1.0, steric_dr=5e-3, k0=None):
         L = _lib.lib()
         self._keep = [np.ascontiguousarray(faces, np.int32), np.ascontiguousarray(face_blob, np.int32),
                       np.ascontiguousarray(face_type, np.int32), np.ascontiguousarray(emin, np.float64),
@@ -44,9 +58,15 @@ class LJSurfaceSolver:
         f, b, t, e, r = self._keep
         if e.ndim != 2 or e.shape[0] != e.shape[1] or r.shape != e.shape:
             raise ValueError("emin and rmin must be square (num_types, num_types) arrays")
+        apex = None if face_apex is None else np.ascontiguousarray(face_apex, np.int32)
+        kk = None if k0 is None else np.ascontiguousarray(k0, np.float64)
+        if kk is not None and kk.shape != e.shape:
+            raise ValueError("k0 must be a (num_types, num_types) array")
+        self._keep += [apex, kk]
         d = SsintDesc(int(num_nodes), len(b), _lib.ptr(f, _lib._ip), _lib.ptr(b, _lib._ip), _lib.ptr(t, _lib._ip),
                       e.shape[0], _lib.ptr(e), _lib.ptr(r), int(num_blobs), float(cell_size),
-                      int(grid[0]), int(grid[1]), int(grid[2]), int(inc_self))
+                      int(grid[0]), int(grid[1]), int(grid[2]), int(inc_self), int(ssint_type),
+                      _lib.ptr(apex, _lib._ip), float(steric_factor), float(steric_dr), _lib.ptr(kk))
         h = ctypes.c_void_p()
         _lib.check(L.ffea_gpu_ssint_create(ctypes.byref(d), ctypes.byref(h)), "ffea_gpu_ssint_create")
         self._h = h
@@ -91,10 +111,15 @@ class LJSurfaceSolver:
             pass
 
 
-def surface_faces(verts, tets):
+# the name of the Lennard-Jones-only solver, kept for its callers
+LJSurfaceSolver = SurfaceSolver
+
+
+def surface_faces(verts, tets, with_apex=False):
     """Outward surface triangles of a tetrahedral mesh: faces of exactly one
     tetrahedron, ordered so that (n1 - n0) x (n2 - n0) points away from the
-    tetrahedron's fourth corner (FFEA's .surf convention)."""
+    tetrahedron's fourth corner (FFEA's .surf convention).  with_apex: also
+    return that fourth corner per face (Face::n[3], for the steric types)."""
     tets = np.asarray(tets)[:, :4]
     verts = np.asarray(verts, np.float64)
     loc = np.array([[1, 2, 3, 0], [0, 2, 3, 1], [0, 1, 3, 2], [0, 1, 2, 3]])
@@ -109,4 +134,6 @@ def surface_faces(verts, tets):
     n = np.cross(a, b)
     flip = np.einsum("ij,ij->i", n, verts[opp] - verts[tri[:, 0]]) > 0
     tri[flip] = tri[flip][:, [0, 2, 1]]
+    if with_apex:
+        return tri.astype(np.int32), opp.astype(np.int32)
     return tri.astype(np.int32)

@@ -249,16 +249,25 @@ int ffea_gpu_script_get_blob(const ffea_gpu_script_t *s, int32_t blob, ffea_gpu_
 int ffea_gpu_script_create(const ffea_gpu_script_t *s, int32_t precision, int32_t preconditioner,
                            int32_t true_residual, ffea_gpu_t **out);
 
-/* --- surface-surface interactions (Lennard-Jones) ------------------------- */
+/* --- surface-surface interactions ----------------------------------------- */
 
 /* Replaces VdW_solver (include/VdW_solver.h:36-127; VdW_solver::init,
- * src/VdW_solver.cpp:124-157, and ::solve, :168-210) for
- * "vdw_type = lennard-jones", with the nearest-neighbour grid it walks
- * (NearestNeighbourLinkedListCube, src/NearestNeighbourLinkedListCube.cpp:27-76)
- * and the aggregation of face forces onto nodes (src/Blob.cpp:3841-3851).
- * The resulting node forces enter the blob update through
- * ffea_gpu_set_external_forces. */
+ * src/VdW_solver.cpp:124-157, and ::solve, :168-210) and its variants
+ * Steric_solver, LJSteric_solver and GenSoftSSINT_solver
+ * (src/Steric_solver.cpp, src/LJSteric_solver.cpp, src/GenSoftSSINT_solver.cpp)
+ * for ssint_type lennard-jones, steric, ljsteric and gensoft, with the
+ * nearest-neighbour grid they walk (NearestNeighbourLinkedListCube,
+ * src/NearestNeighbourLinkedListCube.cpp:27-76) and the aggregation of face
+ * forces onto nodes (src/Blob.cpp:3841-3851).  The resulting node forces
+ * enter the blob update through ffea_gpu_set_external_forces. */
 #define FFEA_GPU_SSINT_MAX_CELLS (1 << 26)
+
+#define FFEA_GPU_SSINT_LJ 0        /* lennard-jones */
+#define FFEA_GPU_SSINT_STERIC 1    /* steric: overlap volume of the faces' element tetrahedra */
+#define FFEA_GPU_SSINT_LJSTERIC 2  /* steric where the tetrahedra overlap, else lennard-jones */
+#define FFEA_GPU_SSINT_GENSOFT 3   /* steric where the tetrahedra overlap, else the soft polynomial */
+/* a face's tetrahedron overlaps at most this many others in one call (more is an error) */
+#define FFEA_GPU_SSINT_MAX_STERIC_PARTNERS 32
 
 typedef struct ffea_gpu_ssint ffea_gpu_ssint_t;
 
@@ -275,6 +284,13 @@ typedef struct {
     double cell_size;         /* SimulationParams::ssint_cutoff */
     int32_t nx, ny, nz;       /* SimulationParams::es_N_x/y/z; nx*ny*nz <= FFEA_GPU_SSINT_MAX_CELLS */
     int32_t inc_self;         /* SimulationParams::inc_self_ssint */
+    /* the steric types (ssint_type other than FFEA_GPU_SSINT_LJ; zero-initialise the
+     * fields below for lennard-jones) */
+    int32_t ssint_type;       /* FFEA_GPU_SSINT_*: SimulationParams::ssint_type */
+    const int32_t *face_apex; /* per face, the fourth node of its element (Face::n[3]) */
+    double steric_factor;     /* SimulationParams::steric_factor */
+    double steric_dr;         /* SimulationParams::steric_dr (meso length) */
+    const double *k0;         /* num_types^2, gensoft k0 in meso energy / area (src/LJ_matrix.cpp:245) */
 } ffea_gpu_ssint_desc;
 
 /* Copies the face lists and parameters to the device (VdW_solver::init and

@@ -338,3 +338,63 @@ def ssint_lj(pos, faces, face_blob, face_type, emin, rmin, num_blobs, h, grid, i
     if rc != 0:
         raise ValueError("a face centroid lies outside the interaction grid")
     return force, energy, int(pairs.value)
+
+
+def ssint(pos, faces, face_blob, face_type, emin, rmin, num_blobs, h, grid, inc_self=0, ssint_type=0,
+          face_apex=None, steric_factor=1.0, steric_dr=5e-3, k0=None):
+    """FFEA's surface-surface pass for any ssint type (oracle/ssint_oracle.c
+    with oracle/steric_oracle.c): 0 lennard-jones, 1 steric, 2 ljsteric,
+    3 gensoft.  Returns (node_force (N, 3), energy (B, B), interacting pairs)."""
+    lib = port_lib()
+    fn = lib.oracle_ssint
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, _ip, _ip, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int,
+                   ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                   ctypes.c_double, ctypes.c_double, _dp, _dp, ctypes.POINTER(ctypes.c_longlong)]
+    pos = np.ascontiguousarray(pos, np.float64)
+    faces = np.ascontiguousarray(faces, np.int32)
+    apex = None if face_apex is None else np.ascontiguousarray(face_apex, np.int32)
+    face_blob = np.ascontiguousarray(face_blob, np.int32)
+    face_type = np.ascontiguousarray(face_type, np.int32)
+    emin = np.ascontiguousarray(emin, np.float64)
+    rmin = np.ascontiguousarray(rmin, np.float64)
+    kk = None if k0 is None else np.ascontiguousarray(k0, np.float64)
+    force = np.zeros((len(pos), 3))
+    energy = np.zeros((num_blobs, num_blobs))
+    pairs = ctypes.c_longlong(0)
+    rc = fn(len(pos), _ptr(pos, _dp), len(faces), _ptr(faces, _ip), _ptr(apex, _ip), _ptr(face_blob, _ip),
+            _ptr(face_type, _ip), emin.shape[0], _ptr(emin, _dp), _ptr(rmin, _dp), _ptr(kk, _dp), num_blobs,
+            float(h), int(grid[0]), int(grid[1]), int(grid[2]), int(inc_self), int(ssint_type),
+            float(steric_factor), float(steric_dr), _ptr(force, _dp), _ptr(energy, _dp), ctypes.byref(pairs))
+    if rc != 0:
+        raise ValueError("a face centroid lies outside the interaction grid")
+    return force, energy, int(pairs.value)
+
+
+def steric_overlap(A, B):
+    """(volume, FFEA's centre) of the overlap of tetrahedra A and B (4 x 3 each)."""
+    lib = port_lib()
+    lib.steric_overlap.restype = ctypes.c_double
+    lib.steric_overlap.argtypes = [_dp, _dp, _dp]
+    A = np.ascontiguousarray(A, np.float64)
+    B = np.ascontiguousarray(B, np.float64)
+    cm = np.zeros(3)
+    v = lib.steric_overlap(_ptr(A, _dp), _ptr(B, _dp), _ptr(cm, _dp))
+    return v, cm
+
+
+def steric_pair(A, B, dr, k=1.0):
+    """One steric pair (oracle/steric_oracle.c): None without overlap, else
+    (k V, forces on A's 4 nodes, forces on B's)."""
+    lib = port_lib()
+    lib.steric_pair.restype = ctypes.c_int
+    lib.steric_pair.argtypes = [_dp, _dp, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp]
+    A = np.ascontiguousarray(A, np.float64)
+    B = np.ascontiguousarray(B, np.float64)
+    vol = np.zeros(1)
+    f1 = np.zeros((4, 3))
+    f2 = np.zeros((4, 3))
+    if not lib.steric_pair(_ptr(A, _dp), _ptr(B, _dp), float(dr), float(k), _ptr(vol, _dp), _ptr(f1, _dp),
+                           _ptr(f2, _dp)):
+        return None
+    return float(vol[0]), f1, f2

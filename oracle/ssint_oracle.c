@@ -46,10 +46,19 @@ static const double kEta[3][3] = {{0.666666666666667, 0.166666666666667, 0.16666
 
 typedef struct {
     int face;              /* index into the caller's face list */
-    double v[3][3];        /* corner positions */
-    double normal[3], area;
+    double v[4][3];        /* corner positions, then the element's fourth node (steric types) */
+    int node[4];           /* their node indices (node[3] = -1 without the fourth node) */
+    double normal[3], area, centroid[3];
     int x, y, z;           /* cell */
 } pool_face;
+
+/* interaction types (SimulationParams::ssint_type; Steric_solver,
+ * LJSteric_solver, GenSoftSSINT_solver) */
+enum { SS_LJ = 0, SS_STERIC = 1, SS_LJSTERIC = 2, SS_GENSOFT = 3 };
+
+/* steric_oracle.c */
+int steric_pair(const double A[4][3], const double B[4][3], double dr, double k, double *vol, double f1[4][3],
+                double f2[4][3]);
 
 static void lj_factors(double mag_r, double emin, double rmin6, double *force_mag, double *e)
 {
@@ -65,8 +74,8 @@ static void lj_factors(double mag_r, double emin, double rmin6, double *force_ma
 
 /* do_lj_interaction for faces a (f1) and b (f2); adds to fa[3][3], fb[3][3]
  * and returns the pair energy (already multiplied by the areas). */
-static double lj_pair(const pool_face *a, const pool_face *b, double emin, double rmin, double fa[3][3],
-                      double fb[3][3])
+static double lj_pair(const pool_face *a, const pool_face *b, double emin, double rmin, double fa[4][3],
+                      double fb[4][3])
 {
     double p[3][3], q[3][3], fpm[3][3][3];
     for (int k = 0; k < 3; k++)
@@ -118,15 +127,83 @@ static double lj_pair(const pool_face *a, const pool_face *b, double emin, doubl
     return energy;
 }
 
+/* calc_gensoft_factors (src/VdW_solver.cpp:754-771) */
+static void gensoft_factors(double mag_r, double emin, double rmin, double k0, double *force_mag, double *e)
+{
+    const double mag_r_2 = mag_r * mag_r;
+    const double rmin_2 = rmin * rmin;
+    const double gf2 = mag_r_2 / rmin_2;
+    const double gf3 = gf2 * mag_r / rmin;
+    const double k0rm = k0 * rmin;
+    const double k0rm2 = k0rm * rmin;
+    const double epsonrm = emin / rmin;
+    *force_mag = 2 * (k0rm - 6 * epsonrm) * gf3 + 3 * (4 * epsonrm - k0rm) * gf2 + k0 * mag_r;
+    const double emag = (0.5 * k0rm2 - 3 * emin) * gf2 * gf2 + (4 * emin - k0rm2) * gf3 + 0.5 * k0 * mag_r_2 - emin;
+    *e = kW * kW * emag;
+}
+
+/* do_gensoft_interaction for faces a (f1) and b (f2) with
+ * calc_gensoft_force_pair_matrix (src/VdW_solver.cpp:488-563, 701-734); adds
+ * to fa[3][3], fb[3][3] and returns the pair energy. */
+static double gensoft_pair(const pool_face *a, const pool_face *b, double emin, double rmin, double k0,
+                           double fa[4][3], double fb[4][3])
+{
+    double p[3][3], q[3][3], fpm[3][3][3];
+    for (int k = 0; k < 3; k++)
+        for (int d = 0; d < 3; d++) {
+            p[k][d] = kEta[k][0] * a->v[0][d] + kEta[k][1] * a->v[1][d] + kEta[k][2] * a->v[2][d];
+            q[k][d] = kEta[k][0] * b->v[0][d] + kEta[k][1] * b->v[1][d] + kEta[k][2] * b->v[2][d];
+        }
+    double energy = 0.0, fm, e;
+    for (int k = 0; k < 3; k++) {
+        double dx = p[k][0] - q[k][0], dy = p[k][1] - q[k][1], dz = p[k][2] - q[k][2];
+        double mag_r = sqrt(dx * dx + dy * dy + dz * dz);
+        gensoft_factors(mag_r, emin, rmin, k0, &fm, &e);
+        energy += e;
+        for (int d = 0; d < 3; d++) fpm[k][k][d] = fm * ((p[k][d] - q[k][d]) / mag_r);
+        for (int l = k + 1; l < 3; l++) {
+            dx = p[k][0] - q[l][0];
+            dy = p[k][1] - q[l][1];
+            dz = p[k][2] - q[l][2];
+            mag_r = sqrt(dx * dx + dy * dy + dz * dz);
+            gensoft_factors(mag_r, emin, rmin, k0, &fm, &e);
+            energy += 2 * e;
+            for (int d = 0; d < 3; d++) {
+                fpm[k][l][d] = fm * ((p[k][d] - q[l][d]) / mag_r);
+                fpm[l][k][d] = fpm[k][l][d];
+            }
+        }
+    }
+    const double apaq = a->area * b->area;
+    energy *= apaq;
+    for (int j = 0; j < 3; j++) {
+        double f1[3] = {0, 0, 0}, f2[3] = {0, 0, 0};
+        for (int k = 0; k < 3; k++)
+            for (int l = 0; l < 3; l++) {
+                const double c = kW * kW * kEta[l][j];
+                const double dd = kW * kW * kEta[k][j];
+                for (int d = 0; d < 3; d++) {
+                    f1[d] += c * fpm[k][l][d];
+                    f2[d] -= dd * fpm[l][k][d];
+                }
+            }
+        for (int d = 0; d < 3; d++) {
+            fa[j][d] += f1[d] * apaq;
+            fb[j][d] += f2[d] * apaq;
+        }
+    }
+    return energy;
+}
+
 /* Returns 0, or -1 when a face centroid lies outside the box after the
  * single wrap (FFEA reports the same as an error). node_force: num_nodes x 3,
  * overwritten with the surface forces alone; energy: num_blobs x num_blobs,
  * overwritten (VdW_solver::fieldenergy, [blob of f1][blob of f2]).
  * pairs_out (may be NULL): the number of face pairs that interacted. */
-int oracle_ssint_lj(int num_nodes, const double *pos, int num_faces, const int *faces, const int *face_blob,
-                    const int *face_type, int num_types, const double *emin, const double *rmin, int num_blobs,
-                    double h, int nx, int ny, int nz, int inc_self, double *node_force, double *energy,
-                    long long *pairs_out)
+int oracle_ssint(int num_nodes, const double *pos, int num_faces, const int *faces, const int *face_apex,
+                 const int *face_blob, const int *face_type, int num_types, const double *emin, const double *rmin,
+                 const double *k0, int num_blobs, double h, int nx, int ny, int nz, int inc_self, int ssint_type,
+                 double steric_factor, double steric_dr, double *node_force, double *energy, long long *pairs_out)
 {
     static const int adj[27][3] = {{-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {-1, 0, -1}, {-1, 0, 0}, {-1, 0, 1},
                                    {-1, 1, -1},  {-1, 1, 0},  {-1, 1, 1},  {0, -1, -1}, {0, -1, 0}, {0, -1, 1},
@@ -135,7 +212,7 @@ int oracle_ssint_lj(int num_nodes, const double *pos, int num_faces, const int *
                                    {1, 1, -1},   {1, 1, 0},   {1, 1, 1}};
     int np = 0;
     pool_face *pool = (pool_face *)malloc(sizeof(pool_face) * (size_t)(num_faces > 0 ? num_faces : 1));
-    double (*fforce)[3][3] = calloc((size_t)(num_faces > 0 ? num_faces : 1), sizeof(double[3][3]));
+    double (*fforce)[4][3] = calloc((size_t)(num_faces > 0 ? num_faces : 1), sizeof(double[4][3]));
     long ncell = (long)nx * ny * nz;
     int *root = (int *)malloc(sizeof(int) * (size_t)ncell);
     int *next = (int *)malloc(sizeof(int) * (size_t)(num_faces > 0 ? num_faces : 1));
@@ -147,8 +224,12 @@ int oracle_ssint_lj(int num_nodes, const double *pos, int num_faces, const int *
         if (face_type[f] < 0) continue;
         pool_face *P = &pool[np];
         P->face = f;
-        for (int i = 0; i < 3; i++)
+        for (int i = 0; i < 3; i++) {
+            P->node[i] = faces[3 * f + i];
             for (int d = 0; d < 3; d++) P->v[i][d] = pos[3 * faces[3 * f + i] + d];
+        }
+        P->node[3] = face_apex ? face_apex[f] : -1;
+        for (int d = 0; d < 3; d++) P->v[3][d] = face_apex ? pos[3 * face_apex[f] + d] : 0.0;
         double a[3], b[3], n[3];
         for (int d = 0; d < 3; d++) {
             a[d] = P->v[1][d] - P->v[0][d];
@@ -160,7 +241,7 @@ int oracle_ssint_lj(int num_nodes, const double *pos, int num_faces, const int *
         double mag = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
         P->area = .5 * mag;
         for (int d = 0; d < 3; d++) P->normal[d] = n[d] / mag;
-        double cen[3];
+        double *cen = P->centroid;
         for (int d = 0; d < 3; d++) cen[d] = (1.0 / 3.0) * (P->v[0][d] + P->v[1][d] + P->v[2][d]);
         int cx = (int)floor(cen[0] / h), cy = (int)floor(cen[1] / h), cz = (int)floor(cen[2] / h);
         if (cx < 0) cx += nx; else if (cx >= nx) cx -= nx;
@@ -193,15 +274,54 @@ int oracle_ssint_lj(int num_nodes, const double *pos, int num_faces, const int *
                 if (!inc_self && ba == bb) continue;
                 if (A->normal[0] * B->normal[0] + A->normal[1] * B->normal[1] + A->normal[2] * B->normal[2] > 0.0)
                     continue;
+                if (ssint_type != SS_LJ) {
+                    /* faces in front of each other; no shared node within a blob */
+                    double sep[3];
+                    for (int d = 0; d < 3; d++) sep[d] = B->centroid[d] - A->centroid[d];
+                    if (sep[0] * A->normal[0] + sep[1] * A->normal[1] + sep[2] * A->normal[2] < 0 &&
+                        sep[0] * B->normal[0] + sep[1] * B->normal[1] + sep[2] * B->normal[2] > 0)
+                        continue;
+                    if (inc_self && ba == bb) {
+                        if (A->node[3] == B->node[3]) continue;
+                        int shared = 0;
+                        for (int u = 0; u < 4; u++)
+                            for (int w = 0; w < 4; w++) shared |= A->node[u] == B->node[w];
+                        if (shared) continue;
+                    }
+                }
                 int t = face_type[A->face] * num_types + face_type[B->face];
-                energy[ba * num_blobs + bb] += lj_pair(A, B, emin[t], rmin[t], fforce[i], fforce[j]);
-                pairs++;
+                int done = 0;
+                if (ssint_type != SS_LJ) {
+                    /* steric where the element tetrahedra overlap */
+                    double vol, f1[4][3], f2[4][3];
+                    if (steric_pair((const double (*)[3])A->v, (const double (*)[3])B->v, steric_dr, steric_factor,
+                                    &vol, f1, f2)) {
+                        for (int u = 0; u < 4; u++)
+                            for (int d = 0; d < 3; d++) {
+                                fforce[i][u][d] += f1[u][d];
+                                fforce[j][u][d] += f2[u][d];
+                            }
+                        energy[ba * num_blobs + bb] += vol;
+                        done = 1;
+                    }
+                }
+                if (!done && (ssint_type == SS_LJ || ssint_type == SS_LJSTERIC)) {
+                    energy[ba * num_blobs + bb] += lj_pair(A, B, emin[t], rmin[t], fforce[i], fforce[j]);
+                    done = 1;
+                } else if (!done && ssint_type == SS_GENSOFT) {
+                    energy[ba * num_blobs + bb] += gensoft_pair(A, B, emin[t], rmin[t], k0[t], fforce[i], fforce[j]);
+                    done = 1;
+                }
+                pairs += done;
             }
         }
     }
     for (int i = 0; i < np; i++)
-        for (int k = 0; k < 3; k++)
-            for (int d = 0; d < 3; d++) node_force[3 * faces[3 * pool[i].face + k] + d] += fforce[i][k][d];
+        for (int k = 0; k < 4; k++) {
+            const int nd = pool[i].node[k];
+            if (nd < 0) continue;
+            for (int d = 0; d < 3; d++) node_force[3 * nd + d] += fforce[i][k][d];
+        }
     if (pairs_out) *pairs_out = pairs;
 done:
     free(pool);
@@ -209,4 +329,14 @@ done:
     free(root);
     free(next);
     return rc;
+}
+
+/* The Lennard-Jones pass alone (vdw_type = lennard-jones). */
+int oracle_ssint_lj(int num_nodes, const double *pos, int num_faces, const int *faces, const int *face_blob,
+                    const int *face_type, int num_types, const double *emin, const double *rmin, int num_blobs,
+                    double h, int nx, int ny, int nz, int inc_self, double *node_force, double *energy,
+                    long long *pairs_out)
+{
+    return oracle_ssint(num_nodes, pos, num_faces, faces, NULL, face_blob, face_type, num_types, emin, rmin, NULL,
+                        num_blobs, h, nx, ny, nz, inc_self, SS_LJ, 0.0, 0.0, node_force, energy, pairs_out);
 }

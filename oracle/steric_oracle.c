@@ -42,8 +42,12 @@
 #include <stdlib.h>
 #include <string.h>
 
-#define ST_MAXV 24 /* vertices of one face polygon */
-#define ST_MAXF 12 /* faces of the clipped polyhedron: 4 + 4 caps + slack */
+/* The overlap of two tetrahedra is an intersection of 8 half-spaces: at most
+ * 8 faces, each a polygon bounded by the 7 others. */
+#define ST_MAXV 8  /* vertices of one face polygon */
+#define ST_MAXF 8  /* faces of the clipped polyhedron */
+#define ST_MAXC 16 /* distinct points of one cut */
+#define ST_MAXU 32 /* distinct vertices of the overlap */
 
 typedef struct {
     int n;
@@ -115,7 +119,19 @@ static void st_halfspace(const double T[4][3], int f, double n[3], double *off)
  * plane with no vertex strictly outside leaves P as it is; one with no
  * vertex strictly inside leaves nothing (a convex polyhedron with a face on
  * the plane lies on one side of it, so a cutting plane never holds a face). */
-static int st_clip(st_polyh *P, const double n[3], double off)
+/* adds x to pts (n of them, at most cap) unless a point within tol2 (squared
+ * distance) is there already */
+static void st_add_unique(double (*pts)[3], int *n, int cap, const double x[3], double tol2)
+{
+    for (int u = 0; u < *n; u++) {
+        double e[3];
+        st_sub(x, pts[u], e);
+        if (st_dot(e, e) <= tol2) return;
+    }
+    if (*n < cap) memcpy(pts[(*n)++], x, sizeof(double) * 3);
+}
+
+static int st_clip(st_polyh *P, const double n[3], double off, double tol2)
 {
     double smin = 0.0, smax = 0.0;
     int first = 1;
@@ -131,7 +147,7 @@ static int st_clip(st_polyh *P, const double n[3], double off)
         return 0;
     }
     if (smax <= 0) return 1;
-    double cap[2 * ST_MAXF * ST_MAXV][3];
+    double cap[ST_MAXC][3];
     int nc = 0, nf = 0;
     for (int f = 0; f < P->nf; f++) {
         const st_poly *in = &P->f[f];
@@ -142,14 +158,14 @@ static int st_clip(st_polyh *P, const double n[3], double off)
             const double sa = st_dot(n, a) - off, sb = st_dot(n, b) - off;
             if (sa <= 0) {
                 if (out.n < ST_MAXV) memcpy(out.v[out.n++], a, sizeof(double) * 3);
-                if (sa == 0 && nc < 2 * ST_MAXF * ST_MAXV) memcpy(cap[nc++], a, sizeof(double) * 3);
+                if (sa == 0) st_add_unique(cap, &nc, ST_MAXC, a, tol2);
             }
             if ((sa < 0 && sb > 0) || (sa > 0 && sb < 0)) {
                 const double t = sa / (sa - sb);
                 double x[3];
                 for (int c = 0; c < 3; c++) x[c] = a[c] + t * (b[c] - a[c]);
                 if (out.n < ST_MAXV) memcpy(out.v[out.n++], x, sizeof(double) * 3);
-                if (nc < 2 * ST_MAXF * ST_MAXV) memcpy(cap[nc++], x, sizeof(double) * 3);
+                st_add_unique(cap, &nc, ST_MAXC, x, tol2);
             }
         }
         if (out.n >= 3) P->f[nf++] = out;
@@ -176,7 +192,7 @@ static int st_clip(st_polyh *P, const double n[3], double off)
         if (best > 0) {
             st_sub(cap[far], c, u);
             st_cross(n, u, w);
-            double ang[2 * ST_MAXF * ST_MAXV];
+            double ang[ST_MAXC];
             for (int k = 0; k < nc; k++) {
                 double e[3];
                 st_sub(cap[k], c, e);
@@ -211,12 +227,19 @@ static int st_clip(st_polyh *P, const double n[3], double off)
  * 1e-9 of the tetrahedra's extent are one vertex. */
 double steric_overlap(const double A[4][3], const double B[4][3], double *cm)
 {
+    double ext = 0.0;
+    for (int i = 0; i < 4; i++)
+        for (int d = 0; d < 3; d++) {
+            ext = fmax(ext, fabs(A[i][d] - A[0][d]));
+            ext = fmax(ext, fabs(B[i][d] - A[0][d]));
+        }
+    const double tol2 = (1e-9 * ext) * (1e-9 * ext);
     st_polyh P;
     st_tet_faces(A, &P);
     for (int f = 0; f < 4; f++) {
         double n[3], off;
         st_halfspace(B, f, n, &off);
-        if (!st_clip(&P, n, off)) {
+        if (!st_clip(&P, n, off, tol2)) {
             if (cm) cm[0] = cm[1] = cm[2] = 0.0;
             return 0.0;
         }
@@ -239,26 +262,10 @@ double steric_overlap(const double A[4][3], const double B[4][3], double *cm)
         }
     }
     if (cm) {
-        double ext = 0.0;
-        for (int i = 0; i < 4; i++)
-            for (int d = 0; d < 3; d++) {
-                ext = fmax(ext, fabs(A[i][d] - A[0][d]));
-                ext = fmax(ext, fabs(B[i][d] - A[0][d]));
-            }
-        const double tol2 = (1e-9 * ext) * (1e-9 * ext);
-        double uniq[ST_MAXF * ST_MAXV][3];
+        double uniq[ST_MAXU][3];
         int nu = 0;
         for (int f = 0; f < P.nf; f++)
-            for (int k = 0; k < P.f[f].n; k++) {
-                const double *x = P.f[f].v[k];
-                int seen = 0;
-                for (int u = 0; u < nu && !seen; u++) {
-                    double e[3];
-                    st_sub(x, uniq[u], e);
-                    seen = st_dot(e, e) <= tol2;
-                }
-                if (!seen && nu < ST_MAXF * ST_MAXV) memcpy(uniq[nu++], x, sizeof(double) * 3);
-            }
+            for (int k = 0; k < P.f[f].n; k++) st_add_unique(uniq, &nu, ST_MAXU, P.f[f].v[k], tol2);
         cm[0] = cm[1] = cm[2] = 0.0;
         for (int u = 0; u < nu; u++)
             for (int d = 0; d < 3; d++) cm[d] += uniq[u][d];

@@ -207,3 +207,39 @@ def test_overfull_cell_is_an_error():
             s.forces(pos)
     assert time.perf_counter() - t < 10.0
     s.close()
+
+
+@pytest.mark.parametrize("ssint_type", [1, 2, 3])
+@pytest.mark.parametrize("inc_self", [0, 1])
+def test_steric_types_match_oracle(ssint_type, inc_self):
+    """steric, ljsteric and gensoft on two spheres pushed 0.6 nm into each
+    other (element tetrahedra overlap across the contact): the GPU against
+    the oracle (oracle/steric_oracle.c, pinned to FFEA's own geometry code
+    in tests/test_steric_oracle.py).  The overlap of each pair is the same
+    clipping arithmetic on both sides; forces agree to 1e-9 of the largest,
+    energies to 1e-9, the interacting pair counts exactly."""
+    from tests.test_steric_oracle import overlapping_spheres
+    pos, faces, apex, blob, h, grid = overlapping_spheres()
+    rng = np.random.default_rng(11)
+    T = 2
+    emin = rng.uniform(0.5, 2.0, (T, T))
+    emin = 0.5 * (emin + emin.T)
+    rmin = np.full((T, T), nm(1.0))
+    k0 = np.full((T, T), 0.3)
+    ftype = rng.integers(0, T, len(faces)).astype(np.int32)
+    kw = dict(num_nodes=len(pos), faces=faces, face_blob=blob, face_type=ftype, emin=emin, rmin=rmin, num_blobs=2,
+              cell_size=h, grid=grid, inc_self=inc_self, ssint_type=ssint_type, face_apex=apex, steric_factor=50.0,
+              steric_dr=5e-3, k0=k0)
+    s = _solver(**kw)
+    f_gpu, e_gpu, p_gpu = s.forces(pos)
+    s.close()
+    f_ref, e_ref, p_ref = oracle.ssint(pos, faces, blob, ftype, emin, rmin, 2, h, grid, inc_self, ssint_type, apex,
+                                       50.0, 5e-3, k0)
+    assert p_gpu == p_ref and p_ref > 0
+    scale = np.abs(f_ref).max()
+    np.testing.assert_allclose(f_gpu, f_ref, rtol=0, atol=1e-9 * scale)
+    np.testing.assert_allclose(e_gpu, e_ref, rtol=1e-9, atol=1e-9 * np.abs(e_ref).max())
+    # the steric share: the same pass with the steric part alone
+    if ssint_type != 1:
+        _, e_st, p_st = oracle.ssint(pos, faces, blob, ftype, emin, rmin, 2, h, grid, inc_self, 1, apex, 50.0, 5e-3)
+        assert 0 < p_st < p_ref
