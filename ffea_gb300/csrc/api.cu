@@ -407,9 +407,6 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     const char *force_mem = std::getenv("FFEA_GPU_CG_MEMORY_STATE");
     d.n_segs = n_segs;
     d.cg_reg = n_segs <= reg_cap && !(force_mem && force_mem[0] == '1');
-    // FFEA_GPU_CG_PREFETCH=0 turns the memory-resident solve's L2 prefetch off
-    const char *pfe = std::getenv("FFEA_GPU_CG_PREFETCH");
-    d.cg_prefetch = !(pfe && pfe[0] == '0');
     d.cg_grid = n_segs <= reg_cap ? n_segs : std::min(mem_cap, n_segs);
     d.cg_cache_slots = d.cg_reg ? cache_slots : 0;
     d.cg_cache_cols = d.cg_reg ? cache_cols : 0;

@@ -1799,20 +1799,6 @@ __device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const floa
     }
 }
 
-// Bulk prefetch of [p, p + bytes) into L2 by the copy engine (no registers,
-// no completion to wait for), in pieces of at most 64 KiB.  p and bytes are
-// multiples of 16 and the range lies inside one allocation.
-__device__ __forceinline__ void l2_prefetch(const void *p, size_t bytes)
-{
-    const char *c = static_cast<const char *>(p);
-    while (bytes > 0) {
-        const unsigned n = bytes > 65536 ? 65536u : (unsigned)bytes;
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(c), "r"(n) : "memory");
-        c += n;
-        bytes -= n;
-    }
-}
-
 // L2 load issued where it stands (volatile asm keeps it ahead of the
 // barriers that follow, so its latency overlaps the reduction's own loads)
 __device__ __forceinline__ float ld_early(const float *p)
@@ -2350,28 +2336,6 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
         }
     };
 
-    // memory-resident solve: the next segment's data into L2 while this one
-    // is processed, by thread 0 (segments are 32-row aligned and every array
-    // holds whole 32-row slices, so each range is 16-byte aligned and inside
-    // its allocation)
-    const bool pf = !REG && d.cg_prefetch;
-    auto prefetch_matrix = [&](int j) {
-        if (!pf || tid != 0 || j >= nt) return;
-        const int sl0 = s_row0[j] >> 5, sl1 = (s_row0[j] + s_rows[j] + 31) >> 5;
-        const size_t e0 = (size_t)d.slice_ptr[sl0], e1 = (size_t)d.slice_ptr[sl1];
-        // (the value arrays of a kind of solver exist only when a blob of the
-        // batch uses it)
-        if (d.any_nomass) l2_prefetch(static_cast<const T *>(d.sell_val) + 9 * e0, 9 * (e1 - e0) * sizeof(T));
-        if (d.any_mass) l2_prefetch(static_cast<const T *>(d.sell_mval) + e0, (e1 - e0) * sizeof(T));
-        l2_prefetch(d.sell_col + e0, (e1 - e0) * sizeof(int));
-    };
-    auto prefetch_rows = [&](int j) {
-        if (!pf || tid != 0 || j >= nt) return;
-        const size_t r0 = (size_t)s_row0[j], nr = (size_t)((s_rows[j] + 31) & ~31);
-        for (const void *a : {d.x, d.r, d.w, d.s, d.p, d.dinv})
-            l2_prefetch(static_cast<const T *>(a) + 3 * r0, 3 * nr * sizeof(T));
-        if (mcoarse) l2_prefetch(d.phi + r0, nr * sizeof(float4));
-    };
     unsigned int n_bar = 0;  // counting barriers passed
     // sums of the iteration's partials and the transitions; the running-blob count
     auto reduce = [&]() -> unsigned int {
@@ -2465,19 +2429,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DeviceBatch d)
                                s_alpha, s_beta, false);
         if (local || mcoarse) parity ^= 1;
         if (REG && s_state[0] == CG_VERIFY) publish_x();
-        for (int j = 0; j < nt; j++) {
-            prefetch_rows(j + 1);
-            if (j + 1 == nt) prefetch_matrix(0);  // for phase B, after the barrier
-            phase_a(j);
-        }
+        for (int j = 0; j < nt; j++) phase_a(j);
         defer_flush();
         counting_barrier(d.bar, (++n_bar) * (unsigned int)G, &s_err);
         if (s_err) break;
-        for (int j = 0; j < nt; j++) {
-            prefetch_matrix(j + 1);
-            if (j + 1 == nt) prefetch_rows(0);  // for the next phase A
-            phase_b(j, false);
-        }
+        for (int j = 0; j < nt; j++) phase_b(j, false);
         defer_flush();
         loops++;
         running = reduce();

@@ -23,7 +23,6 @@ struct DeviceBatch {
     int32_t cg_reg = 0;           // 1: one CG segment per CTA, row state kept in registers
     int32_t cg_local = 0;         // 1: every CTA reduces the dot products itself (few segments and blobs)
     int32_t cg_euler = 0;         // 1 (per launch): the CG kernel ends with the Euler update of the step
-    int32_t cg_prefetch = 0;      // memory-resident solve: L2 bulk prefetch of the next segment's data
     int32_t cg_cache_slots = 0;   // REG: matrix slots per row whose values are copied to shared memory
     int32_t cg_cache_cols = 0;    // REG: matrix slots per row whose column indices are copied
     int32_t part_stride = 8;      // floats per segment slot of the CG partials (32 with the coarse space)
