@@ -1,10 +1,18 @@
-// ssint.cu -- surface-surface Lennard-Jones interaction of FFEA on the GPU.
+// ssint.cu -- surface-surface interactions of FFEA on the GPU.
 //
 // Replaces VdW_solver::solve for "vdw_type = lennard-jones"
-// (src/VdW_solver.cpp:168-210, 237-330, 338-394, 664-752) together with the
-// nearest-neighbour grid it walks (NearestNeighbourLinkedListCube::
-// build_nearest_neighbour_lookup, src/NearestNeighbourLinkedListCube.cpp:27-76)
-// and the aggregation of face forces onto nodes (src/Blob.cpp:3841-3851).
+// (src/VdW_solver.cpp:168-210, 237-330, 338-394, 664-752), "steric"
+// (Steric_solver, src/VdW_solver.cpp:458-486), "ljsteric" (LJSteric_solver:
+// steric where the faces' element tetrahedra overlap, Lennard-Jones
+// elsewhere) and "gensoft" (GenSoftSSINT_solver, src/VdW_solver.cpp:488-563,
+// 701-771), together with the nearest-neighbour grid they walk
+// (NearestNeighbourLinkedListCube::build_nearest_neighbour_lookup,
+// src/NearestNeighbourLinkedListCube.cpp:27-76) and the aggregation of face
+// forces onto nodes (src/Blob.cpp:3841-3851).  The steric types first run
+// k_steric (overlap volume of the two element tetrahedra by convex clipping,
+// its forward-difference gradient and FFEA's barycentric weights, between
+// steps 4 and 5 below), whose force lands on the four nodes of each face's
+// element; k_pairs then skips the pairs k_steric handled.
 //
 // GPU layout and passes (one stream, no host round trip between them):
 //   1. k_face_geom   one thread per active face: gathers its three corners,
