@@ -14,9 +14,9 @@
 //                diagonal, and the CG start (Blob.cpp:3826-3928,
 //                NoMassCGSolver.cpp:205-230)
 //   k_cg         the whole Jacobi-PCG solve in one persistent cooperative
-//                launch (NoMassCGSolver.cpp:165-197, ConjugateGradientSolver.cpp:206-232)
-//   k_euler      velocity / position update and RNG stream advance
-//                (Blob.cpp:3937-3969)
+//                launch (NoMassCGSolver.cpp:165-197, ConjugateGradientSolver.cpp:206-232),
+//                ending with the velocity / position update and the RNG
+//                stream advance (Blob.cpp:3937-3969)
 // Reductions are deterministic: fixed butterflies inside warps and CTAs, one
 // partial per node tile, and fixed-order per-blob sums.  No floating-point
 // atomics are used anywhere.
@@ -2503,48 +2503,6 @@ __global__ void k_barrier_timeout_selftest(unsigned int *bar, unsigned int spin_
     if (threadIdx.x == 0 && s_err) atomicAdd(out, 1);
 }
 
-// Euler update (src/Blob.cpp:3937-3969) and the RNG advance to the next step.
-template <typename T>
-__global__ void __launch_bounds__(NODE_TILE) k_euler(DeviceBatch d)
-{
-    const int tile = blockIdx.x;
-    const int b = d.tile_blob[tile];
-    const BlobParams &bp = d.bp[b];
-    const int row = tile * NODE_TILE + threadIdx.x;
-    if (row < d.num_streams) {  // the grid has at least 256 threads per blob
-        const int s = row;
-        bool advance = true;
-        if (d.num_streams == d.num_blobs) advance = d.status[s] == 0;  // per-blob streams
-        if (advance) {
-            uint32_t st[6];
-#pragma unroll
-            for (int i = 0; i < 6; i++) st[i] = d.stream_state[6 * s + i];
-            mrg::apply(d.stream_step[s], st);
-#pragma unroll
-            for (int i = 0; i < 6; i++) d.stream_state[6 * s + i] = st[i];
-        }
-    }
-    if (row - bp.node_off >= bp.node_cnt || d.status[b]) return;
-    const double dt = bp.dt;
-    const T *x = static_cast<const T *>(d.x);
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const size_t k = 3 * (size_t)row + i;
-        const double xi = (double)x[k];
-        double p;
-        if (bp.solver == SOLVER_NOMASS) {
-            d.vel[k] = xi;
-            p = d.pos[k] + xi * dt;
-        } else {
-            const double v = d.vel[k] + xi * dt;
-            d.vel[k] = v;
-            p = d.pos[k] + v * dt;
-        }
-        d.pos[k] = p;
-        if (d.pos_df) d.pos_df[k] = split_pos(p);
-    }
-}
-
 // out = A in (FP64 vectors and arithmetic); pinned rows and padding give 0.
 template <typename T>
 __global__ void __launch_bounds__(NODE_TILE) k_apply(DeviceBatch d, const double *in, double *out)
@@ -2980,11 +2938,6 @@ cudaError_t launch_cg(const DeviceBatch &dev, cudaStream_t s, bool euler)
     if (d.precision == PREC_FP64)
         return d.cg_reg ? cudaLaunchKernelEx(&cfg, k_cg<double, true>, d) : cudaLaunchKernelEx(&cfg, k_cg<double, false>, d);
     return d.cg_reg ? cudaLaunchKernelEx(&cfg, k_cg<float, true>, d) : cudaLaunchKernelEx(&cfg, k_cg<float, false>, d);
-}
-
-void launch_euler(const DeviceBatch &d, cudaStream_t s)
-{
-    PREC_DISPATCH(d, k_euler, d.n_tiles, NODE_TILE, s, d);
 }
 
 void launch_energies(const DeviceBatch &d, cudaStream_t s)

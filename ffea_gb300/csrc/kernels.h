@@ -151,14 +151,13 @@ void launch_assemble(const DeviceBatch &d, cudaStream_t s);
 void launch_noise(const DeviceBatch &d, cudaStream_t s);
 void launch_nodes(const DeviceBatch &d, cudaStream_t s, int use_given_rhs);
 // the persistent solve; with `euler` it also applies the step's Euler update
-// and RNG advance (what launch_euler does) to the blobs whose solve converged
+// (src/Blob.cpp:3937-3969) and RNG advance to the blobs whose solve converged
 cudaError_t launch_cg(const DeviceBatch &d, cudaStream_t s, bool euler = false);
 // The CG kernel's grid barrier with a target that no arrival reaches and the
 // given spin limit, on `ctas` co-resident CTAs; *out counts the CTAs that
 // reported the time-out (bar: 8 zeroed words, out: one zeroed int).
 cudaError_t launch_barrier_timeout_selftest(unsigned int *bar, unsigned int spin_limit, int *out, int ctas,
                                             cudaStream_t s);
-void launch_euler(const DeviceBatch &d, cudaStream_t s);
 void launch_energies(const DeviceBatch &d, cudaStream_t s);
 // centroid, RMSD, centre of mass and angular momentum of every blob into m.out
 void launch_measurements(const DeviceBatch &d, const MeasView &m, cudaStream_t s);
