@@ -124,7 +124,7 @@ struct ffea_gpu {
     int graph_mode = 1;
     int timing = 0;
     double phase_ms[5] = {0, 0, 0, 0, 0};
-    double kernel_ms[FFEA_GPU_NUM_KERNEL_TIMES] = {};  // noise, elements, assembly, coarse, nodes, CG, update
+    double kernel_ms[FFEA_GPU_NUM_KERNEL_TIMES] = {};  // noise, elements, assembly, coarse, nodes, CG (+ update), 0
     cudaEvent_t ev[FFEA_GPU_NUM_KERNEL_TIMES + 1] = {};
     int64_t fixed_per_step = 0;  // kernels of a step graph outside the CG loop
     size_t tsize = 4;
@@ -136,6 +136,7 @@ struct ffea_gpu {
     int2 *io_src = nullptr;
     std::vector<int2> io_src_host;  // the same map on the host (external-force folding)
     std::vector<double> ext_host;   // external forces per row (3 per row, folded), mirror of dev.ext
+    std::vector<uint32_t> stream_gen;  // per RNG stream: generation of its state (mirror of dev.stream_gen)
     double *io_secvel = nullptr;  // secondary-node velocities (mass blobs keep them; NoMass report 0)
     double *io_stage = nullptr;   // 9 doubles per node of the largest blob (pos, vel, force)
     int *io_moved = nullptr;      // set_nodes: 1 when a position changed
@@ -482,6 +483,13 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(upload(A, d.stream_step, H.stream_step));
     CK(upload(A, d.noise_run_off, H.noise_run_off));
     d.noise_runs = H.noise_run_off.back();
+    if (d.noise_runs > 0) {
+        // no kept run state yet: every run jumps in the first step
+        CK(upload(A, d.noise_run_state, std::vector<uint32_t>(6 * (size_t)d.noise_runs, 0u)));
+        CK(upload(A, d.noise_run_gen, std::vector<uint32_t>((size_t)d.noise_runs, 0xffffffffu)));
+    }
+    h->stream_gen.assign((size_t)H.num_streams, 0u);
+    CK(upload(A, d.stream_gen, h->stream_gen));
     CK(upload(A, d.pos, H.pos));
     if (H.precision == PREC_MIXED) {
         std::vector<float2> pdf(H.pos.size());
@@ -1115,7 +1123,12 @@ int ffea_gpu_set_rng_state(ffea_gpu_t *h, int32_t blob, const uint64_t state[6])
     CK(cudaStreamSynchronize(h->stream));
     uint32_t st[6];
     for (int i = 0; i < 6; i++) st[i] = (uint32_t)state[i];
-    CK(cudaMemcpy(h->dev.stream_state + 6 * h->host.bp[blob].stream, st, sizeof(st), cudaMemcpyHostToDevice));
+    const int sm = h->host.bp[blob].stream;
+    CK(cudaMemcpy(h->dev.stream_state + 6 * sm, st, sizeof(st), cudaMemcpyHostToDevice));
+    // the noise kernel's kept run states belong to the old state: a new
+    // generation makes every run of this stream jump again
+    h->stream_gen[sm] += 1;
+    CK(cudaMemcpy(h->dev.stream_gen + sm, &h->stream_gen[sm], sizeof(uint32_t), cudaMemcpyHostToDevice));
     return FFEA_GPU_OK;
 }
 

@@ -262,9 +262,14 @@ __global__ void k_rest_state(DeviceBatch d)
 }
 
 // The step's random draws, ahead of the element and node kernels.  Each
-// thread jumps once to the start of its run (mrg::jump, four table products)
-// and draws NOISE_RUN consecutive values from there, so the jump is paid once
-// per 32 draws rather than once per element or node; every secondary node's
+// thread draws NOISE_RUN consecutive values from the start of its run, so
+// the stream position is found once per 32 draws rather than once per
+// element or node.  A run sits at the same offset in the stream every step,
+// so its start state for the next step is this one advanced by the stream's
+// draws per step (one product with A^(draws per step), the advance the step
+// itself ends with); that state is kept, and only a run whose stream was set
+// from outside since (a new generation) jumps from the stream state
+// (mrg::jump, four table products).  Every secondary node's
 // draws, which two linear nodes fold in, are made once.  The values are the
 // same centred draws the consumers took from their own jumps: element e of a
 // blob uses draws elem_draw_base + 7 le .. +6 (src/tetra_element_linear.cpp:417-436),
@@ -305,11 +310,34 @@ __global__ void __launch_bounds__(NOISE_THREADS) k_noise(DeviceBatch d)
             cnt = (int)min((uint32_t)NOISE_RUN, total - first);
             dst = kind == 0 ? static_cast<T *>(d.elem_noise) + 7 * (size_t)bp.elem_off + first
                             : static_cast<T *>(d.node_noise) + 3 * (size_t)bp.noise_node_off + first;
+            const int sm = bp.stream;
+            const uint32_t gen = d.stream_gen[sm];
+            const size_t R = (size_t)d.noise_runs;
             uint32_t st[6];
+            if (d.noise_run_gen[run] == gen) {
 #pragma unroll
-            for (int i = 0; i < 6; i++) st[i] = d.stream_state[6 * bp.stream + i];
-            mrg::jump(d.jump_table, (kind == 0 ? bp.elem_draw_base : bp.node_draw_base) + first, st);
-            for (int i = 0; i < cnt; i++) stage[warp][lane][i] = draw<T>(st);
+                for (int i = 0; i < 6; i++) st[i] = d.noise_run_state[i * R + run];
+            } else {
+#pragma unroll
+                for (int i = 0; i < 6; i++) st[i] = d.stream_state[6 * sm + i];
+                mrg::jump(d.jump_table, (kind == 0 ? bp.elem_draw_base : bp.node_draw_base) + first, st);
+            }
+            // the run's start in the next step (a blob whose step fails takes
+            // no further step, so its kept states are never read)
+            uint32_t nx[6];
+#pragma unroll
+            for (int i = 0; i < 6; i++) nx[i] = st[i];
+            mrg::apply(d.stream_step[sm], nx);
+#pragma unroll
+            for (int i = 0; i < 6; i++) d.noise_run_state[i * R + run] = nx[i];
+            d.noise_run_gen[run] = gen;
+            if (cnt == NOISE_RUN) {
+                // a whole run, unrolled: the state words rotate by renaming
+#pragma unroll
+                for (int i = 0; i < NOISE_RUN; i++) stage[warp][lane][i] = draw<T>(st);
+            } else {
+                for (int i = 0; i < cnt; i++) stage[warp][lane][i] = draw<T>(st);
+            }
         }
     }
     __syncwarp();

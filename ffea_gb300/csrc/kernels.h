@@ -55,6 +55,12 @@ struct DeviceBatch {
     // (from bp.noise_node_off); runs of NOISE_RUN draws, prefix per (blob, kind)
     int32_t noise_runs = 0;
     int32_t *noise_run_off = nullptr;
+    // each run's start state for the next step (6 planes of noise_runs
+    // words) and the stream generation it belongs to; a stream's generation
+    // changes when its state is set from outside (set_rng_state)
+    uint32_t *noise_run_state = nullptr;
+    uint32_t *noise_run_gen = nullptr;
+    uint32_t *stream_gen = nullptr;
     void *elem_noise = nullptr;
     void *node_noise = nullptr;
     // nodes (FP64 state and rhs)

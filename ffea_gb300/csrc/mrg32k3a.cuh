@@ -39,13 +39,17 @@ struct JumpMat {
     uint32_t a[18];
 };
 
-// x mod (2^32 - c) for any 64-bit x, c < 2^15: fold the high word twice.
+// x mod M = 2^32 - C for any 64-bit x, C < 2^15: fold the high word twice
+// (2^32 = C mod M).  After the first fold t < 2^32 (C + 1), after the second
+// t < 2^32 + C (C + 1) = M + C (C + 2) < 2 M, so one conditional subtraction
+// leaves the residue in [0, M).
 template <uint32_t M, uint32_t C>
 MRG_HD uint32_t reduce64(uint64_t x)
 {
-    uint64_t t = (x >> 32) * C + (x & 0xffffffffull);  // < 2^48
-    t = (t >> 32) * C + (t & 0xffffffffull);           // < 2^33
-    while (t >= M) t -= M;
+    static_assert(C < (1u << 15), "the bound below needs C (C + 2) < M");
+    uint64_t t = (x >> 32) * C + (x & 0xffffffffull);  // < 2^32 (C + 1)
+    t = (t >> 32) * C + (t & 0xffffffffull);           // < M + C (C + 2)
+    if (t >= M) t -= M;
     return (uint32_t)t;
 }
 
