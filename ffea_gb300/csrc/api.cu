@@ -543,7 +543,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(A.alloc_bytes(d.efrc, 12 * (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.elem_noise, 7 * (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.node_noise, std::max<size_t>(3 * (size_t)H.noise_nodes, 2) * ts));
-    CK(A.alloc_bytes(d.g, H.any_nomass ? 9 * (size_t)H.ne_pad * ts : 16));
+    CK(A.alloc_bytes(d.g, H.any_nomass ? 12 * (size_t)H.ne_pad * ts : 16));
     CK(A.alloc_bytes(d.sell_val, H.any_nomass ? 9 * (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.sell_mval, H.any_mass ? (size_t)d.n_entries * ts : 16));
     CK(A.alloc_bytes(d.mass_diag, H.any_mass ? (size_t)H.nl_pad * ts : 16));

@@ -210,18 +210,34 @@ template <> struct ForceSum<float> {
     __device__ __forceinline__ double value() const { return (double)v.hi + (double)v.lo; }
 };
 
+// The scaled gradients g_a = sqrt(V) dpsi_a of one element, all four corners
+// (12 values, corner 0 = -(g_1 + g_2 + g_3) formed when they are written),
+// read as three 16-byte vectors: the assembly reads each element's gradients
+// once per edge, and one vector load replaces four scalar ones.
 template <typename T>
-__device__ __forceinline__ void load_g(const T *g, int el, int a, T out[3])
+__device__ __forceinline__ void load_g4(const T *g, int el, T out[12]);
+template <>
+__device__ __forceinline__ void load_g4<float>(const float *g, int el, float out[12])
 {
-    const T *ge = g + 9 * (size_t)el;
-    if (a > 0) {
-        out[0] = ge[3 * (a - 1)];
-        out[1] = ge[3 * (a - 1) + 1];
-        out[2] = ge[3 * (a - 1) + 2];
-    } else {
-        out[0] = -(ge[0] + ge[3] + ge[6]);
-        out[1] = -(ge[1] + ge[4] + ge[7]);
-        out[2] = -(ge[2] + ge[5] + ge[8]);
+    const float4 *ge = reinterpret_cast<const float4 *>(g + 12 * (size_t)el);
+#pragma unroll
+    for (int v = 0; v < 3; v++) {
+        const float4 q = __ldg(ge + v);
+        out[4 * v] = q.x;
+        out[4 * v + 1] = q.y;
+        out[4 * v + 2] = q.z;
+        out[4 * v + 3] = q.w;
+    }
+}
+template <>
+__device__ __forceinline__ void load_g4<double>(const double *g, int el, double out[12])
+{
+    const double2 *ge = reinterpret_cast<const double2 *>(g + 12 * (size_t)el);
+#pragma unroll
+    for (int v = 0; v < 6; v++) {
+        const double2 q = __ldg(ge + v);
+        out[2 * v] = q.x;
+        out[2 * v + 1] = q.y;
     }
 }
 
@@ -381,13 +397,28 @@ __global__ void __launch_bounds__(ELEM_TILE) k_elements(DeviceBatch d, int mode)
     const T *dpsi = geo.dpsi;
 
     if (bp.solver == SOLVER_NOMASS) {
-        // scaled gradients for the assembly: g_a = sqrt(vol) dpsi_a, corners 1..3
+        // scaled gradients for the assembly: g_a = sqrt(vol) dpsi_a of
+        // corners 1..3, and corner 0 as minus their sum (the gradients of a
+        // linear element's shape functions sum to zero)
         const T sv = sqrt(vol);
-        T *gout = static_cast<T *>(d.g) + 9 * (size_t)e;
+        T gv[12];
 #pragma unroll
         for (int a = 1; a < 4; a++)
 #pragma unroll
-            for (int i = 0; i < 3; i++) gout[3 * (a - 1) + i] = sv * dpsi[4 * i + a];
+            for (int i = 0; i < 3; i++) gv[3 * a + i] = sv * dpsi[4 * i + a];
+#pragma unroll
+        for (int i = 0; i < 3; i++) gv[i] = -(gv[3 + i] + gv[6 + i] + gv[9 + i]);
+        T *gout = static_cast<T *>(d.g) + 12 * (size_t)e;
+        if (sizeof(T) == 4) {
+            float4 *o = reinterpret_cast<float4 *>(gout);
+#pragma unroll
+            for (int v = 0; v < 3; v++)
+                o[v] = make_float4((float)gv[4 * v], (float)gv[4 * v + 1], (float)gv[4 * v + 2], (float)gv[4 * v + 3]);
+        } else {
+            double2 *o = reinterpret_cast<double2 *>(gout);
+#pragma unroll
+            for (int v = 0; v < 6; v++) o[v] = make_double2((double)gv[2 * v], (double)gv[2 * v + 1]);
+        }
     }
     if (mode != ELEM_STEP) return;
 
@@ -484,9 +515,15 @@ __global__ void __launch_bounds__(EDGE_TILE) k_assemble(DeviceBatch d)
     for (int k = d.edge_cptr[e]; k < d.edge_cptr[e + 1]; k++) {
         const int ci = d.edge_cidx[k];
         const int el = ci >> 4, a = (ci >> 2) & 3, bb = ci & 3;
+        T ge[12];
+        load_g4<T>(g, el, ge);
         T ga[3], gb[3];
-        load_g<T>(g, el, a, ga);
-        load_g<T>(g, el, bb, gb);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            // select corner a and b of the four (unrolled: no local memory)
+            ga[i] = a == 0 ? ge[i] : a == 1 ? ge[3 + i] : a == 2 ? ge[6 + i] : ge[9 + i];
+            gb[i] = bb == 0 ? ge[i] : bb == 1 ? ge[3 + i] : bb == 2 ? ge[6 + i] : ge[9 + i];
+        }
         const T *m = static_cast<const T *>(d.mat_t) + MAT_T_STRIDE * (size_t)d.mat_id[el];
         const T A = m[MAT_T_A], B = m[MAT_T_B];
         const T gab = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
