@@ -540,7 +540,7 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(A.alloc(d.det_sign, (size_t)H.ne_pad));
     CK(A.alloc_bytes(d.jinv0, 9 * (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.vol0, (size_t)H.ne_pad * ts));
-    CK(A.alloc_bytes(d.efrc, 12 * (size_t)H.ne_pad * ts));
+    CK(A.alloc_bytes(d.efrc, 16 * (size_t)H.ne_pad * ts));  // a 4-vector per corner
     CK(A.alloc_bytes(d.elem_noise, 7 * (size_t)H.ne_pad * ts));
     CK(A.alloc_bytes(d.node_noise, std::max<size_t>(3 * (size_t)H.noise_nodes, 2) * ts));
     CK(A.alloc_bytes(d.g, H.any_nomass ? 12 * (size_t)H.ne_pad * ts : 16));
@@ -1212,8 +1212,10 @@ int ffea_gpu_get_element_forces(ffea_gpu_t *h, int32_t blob, double *out)
     CK(cudaStreamSynchronize(h->stream));
     const BlobParams &bp = h->host.bp[blob];
     std::vector<double> v;
-    if (copy_typed_to_double(h, h->dev.efrc, 12 * (size_t)bp.elem_off, 12 * (size_t)bp.elem_cnt, v)) return FFEA_GPU_ERROR;
-    std::memcpy(out, v.data(), v.size() * sizeof(double));
+    if (copy_typed_to_double(h, h->dev.efrc, 16 * (size_t)bp.elem_off, 16 * (size_t)bp.elem_cnt, v)) return FFEA_GPU_ERROR;
+    // (x, y, z, 0) per corner on the device, 3 per corner out
+    for (size_t c = 0; c < 4 * (size_t)bp.elem_cnt; c++)
+        for (int i = 0; i < 3; i++) out[3 * c + i] = v[4 * c + i];
     return FFEA_GPU_OK;
 }
 

@@ -490,13 +490,22 @@ __global__ void __launch_bounds__(ELEM_TILE) k_elements(DeviceBatch d, int mode)
 #pragma unroll
             for (int j = 0; j < 3; j++) S[i][j] += A * (L[i][j] + L[j][i]) + (i == j ? B * tr : (T)0);
     }
-    // nodal forces: node_force[a] = -vol * S dpsi_a (src/tetra_element_linear.cpp:441-489)
-    T *fo = static_cast<T *>(d.efrc) + 12 * (size_t)e;
+    // nodal forces: node_force[a] = -vol * S dpsi_a (src/tetra_element_linear.cpp:441-489),
+    // one 4-vector per corner (x, y, z, 0) so that the node gather reads a
+    // corner with one vector load
+    T *fo = static_cast<T *>(d.efrc) + 16 * (size_t)e;
 #pragma unroll
-    for (int a = 0; a < 4; a++)
+    for (int a = 0; a < 4; a++) {
+        T f[3];
 #pragma unroll
-        for (int i = 0; i < 3; i++)
-            fo[3 * a + i] = -(vol * (dpsi[a] * S[i][0] + dpsi[4 + a] * S[i][1] + dpsi[8 + a] * S[i][2]));
+        for (int i = 0; i < 3; i++) f[i] = -(vol * (dpsi[a] * S[i][0] + dpsi[4 + a] * S[i][1] + dpsi[8 + a] * S[i][2]));
+        if (sizeof(T) == 4) {
+            reinterpret_cast<float4 *>(fo)[a] = make_float4((float)f[0], (float)f[1], (float)f[2], 0.f);
+        } else {
+            reinterpret_cast<double2 *>(fo)[2 * a] = make_double2((double)f[0], (double)f[1]);
+            reinterpret_cast<double2 *>(fo)[2 * a + 1] = make_double2((double)f[2], 0.0);
+        }
+    }
 }
 
 // Viscosity blocks: K_pq = sum over elements e holding edge (p,q) of
@@ -624,10 +633,22 @@ __global__ void __launch_bounds__(NODE_TILE * NODE_LANES) k_nodes(DeviceBatch d,
         const T *ef = static_cast<const T *>(d.efrc);
 #pragma unroll 2
         for (int k = d.gather_ptr[row] + q; k < d.gather_ptr[row + 1]; k += NODE_LANES) {
-            const int gi = d.gather_idx[k];
-            const int el = gi >> 2, a = gi & 3;
+            const int gi = d.gather_idx[k];  // (element << 2) | corner: the corner's 4-vector
+            T f[3];
+            if (sizeof(T) == 4) {
+                const float4 v = __ldg(reinterpret_cast<const float4 *>(ef) + gi);
+                f[0] = (T)v.x;
+                f[1] = (T)v.y;
+                f[2] = (T)v.z;
+            } else {
+                const double2 v0 = __ldg(reinterpret_cast<const double2 *>(ef) + 2 * (size_t)gi);
+                const double2 v1 = __ldg(reinterpret_cast<const double2 *>(ef) + 2 * (size_t)gi + 1);
+                f[0] = (T)v0.x;
+                f[1] = (T)v0.y;
+                f[2] = (T)v1.x;
+            }
 #pragma unroll
-            for (int i = 0; i < 3; i++) fs[i].add(ef[12 * (size_t)el + 3 * a + i]);
+            for (int i = 0; i < 3; i++) fs[i].add(f[i]);
         }
     }
     // (lane 0 + lane 1) + (lane 2 + lane 3), the lower lane's partial first,
