@@ -784,19 +784,21 @@ __device__ __forceinline__ void counting_barrier(unsigned int *bar, unsigned int
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(&bar[5], 1u);
-        volatile unsigned int *vb = bar;
+        // release: the CTA's writes (ordered before this thread by the CTA
+        // barrier) are visible to every CTA that acquires the count after it
+        asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(&bar[5]), "r"(1u));
         unsigned int spins = 0;
-        while ((int)(vb[5] - target) < 0) {
-            if (++spins > spin_limit || vb[4]) {
+        for (;;) {
+            unsigned int n;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(n) : "l"(&bar[5]));
+            if ((int)(n - target) >= 0) break;
+            if (++spins > spin_limit || ((volatile unsigned int *)bar)[4]) {
                 *s_err = 1;
                 atomicExch(&bar[4], 1u);
                 break;
             }
             __nanosleep(32);
         }
-        __threadfence();
     }
     __syncthreads();
 }
