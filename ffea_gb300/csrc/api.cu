@@ -572,7 +572,13 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     CK(A.alloc(d.energy, 2 * (size_t)H.num_blobs));
     CK(A.alloc(d.bar, 8));
     CK(A.alloc(d.loop_count, 1));
-    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    // a blocking stream: the zero fills (cudaMemset) and host-to-device
+    // copies (cudaMemcpy) that set up and update the handle's buffers run on
+    // the legacy default stream and can still be in flight when those calls
+    // return; a non-blocking stream would not wait for them (seen as network
+    // weights zeroed after their upload, so that every smoother weight came
+    // out as 1, in some processes and not others)
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamDefault));
     for (auto &e : h->ev) CK(cudaEventCreate(&e));
     // secondary-node initial velocities (they never change: their rows are identity)
     {

@@ -1112,7 +1112,10 @@ extern "C" int ffea_gpu_ssint_create(const ffea_gpu_ssint_desc *d, ffea_gpu_ssin
     const int T2 = d->num_types * d->num_types;
     int rc = FFEA_GPU_OK;
     auto run = [&]() -> int {
-        SSINT_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        // blocking: its kernels must follow the uploads below, which run on
+        // the legacy default stream and may still be in flight when
+        // cudaMemcpy returns
+        SSINT_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamDefault));
         if (dalloc(&s->d_corner, 4 * (size_t)na) || dalloc(&s->d_blob, na) || dalloc(&s->d_type, na) ||
             dalloc(&s->d_geo, 16 * (size_t)na) || dalloc(&s->d_cell, na) || dalloc(&s->d_fforce, 12 * (size_t)na) ||
             dalloc(&s->d_count, ncell) || dalloc(&s->d_start, ncell) || dalloc(&s->d_block, s->nblocks + 1) ||
