@@ -137,3 +137,34 @@ def test_torch_custom_op_trains_the_network(gpulib):
             loss.backward()
             opt.step()
         assert torch_ops.mpnn_loss(w, theta).item() < first
+
+
+@pytest.mark.parametrize("memory_state", ["0", "1"])
+def test_committed_weights_take_effect_in_a_batch(gpulib, monkeypatch, memory_state):
+    """The network's smoother weights reach the solve of every blob of a
+    batch, in the register-resident and the memory-resident solve: after
+    two steps each blob's velocities differ from those of the same batch
+    with every weight 1 (the two-level preconditioner), and two learned
+    worlds agree bit for bit.  (The weights' upload once raced with the
+    zero fill of their buffer, which left every weight at 1 in some
+    processes.)"""
+    from ffea_gb300 import learned
+    specs = [spec(radius_nm=r, seed=i, rng_seed=40 + i, precision=P.PRECISION_MIXED, epsilon=1e-6)
+             for i, r in enumerate((6.0, 8.0, 5.0))]
+    theta = learned.load()
+    vels = {}
+    for name, pc in (("two-level", TWO_LEVEL), ("learned", LEARNED), ("learned-again", LEARNED)):
+        monkeypatch.setenv("FFEA_GPU_CG_MEMORY_STATE", memory_state)
+        w = _world(specs, true_residual=True, preconditioner=pc)
+        monkeypatch.delenv("FFEA_GPU_CG_MEMORY_STATE", raising=False)
+        with w:
+            assert w.preconditioner() == pc
+            if pc == LEARNED:
+                learned.apply(w, theta)
+            w.run(2)
+            vels[name] = [w.blob(i).get_nodes()[1].copy() for i in range(len(specs))]
+            for i in range(len(specs)):
+                assert w.blob(i).status()["fail_bits"] == 0
+    for i in range(len(specs)):
+        assert np.array_equal(vels["learned"][i], vels["learned-again"][i]), i
+        assert not np.array_equal(vels["learned"][i], vels["two-level"][i]), i
