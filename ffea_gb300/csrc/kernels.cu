@@ -792,7 +792,9 @@ __device__ __forceinline__ void counting_barrier(unsigned int *bar, unsigned int
             unsigned int n;
             asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(n) : "l"(&bar[5]));
             if ((int)(n - target) >= 0) break;
-            if (++spins > spin_limit || ((volatile unsigned int *)bar)[4]) {
+            // the time-out flag only every 16th poll: a poll is then one L2
+            // round trip, not two, and the last arrival is seen sooner
+            if ((++spins & 15) == 0 && (spins > spin_limit || ((volatile unsigned int *)bar)[4])) {
                 *s_err = 1;
                 atomicExch(&bar[4], 1u);
                 break;
