@@ -142,6 +142,9 @@ SIGNATURES = {
     "ffea_gpu_ssint_forces_device": (ctypes.c_int, [ctypes.c_void_p] * 4),
     "ffea_gpu_ssint_synchronize": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "ffea_gpu_ssint_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "ffea_gpu_ssint_set_pbc": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "ffea_gpu_ssint_blob_corr": (ctypes.c_int, [ctypes.c_int32, _dp, _dp, _dp]),
+    "ffea_gpu_ssint_set_sticky_wall": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
 }
 
 _lib = None

@@ -81,6 +81,8 @@ struct ffea_gpu_ssint {
     double *d_geo = nullptr;    // 16 doubles: corners (9), unit normal (3), area, fourth node (3)
     int *d_cell = nullptr;      // -1: outside the box
     double *d_fforce = nullptr; // 12 doubles: force on each corner and on the fourth node
+    double *d_corr = nullptr;   // periodic blob corrections (num_blobs^2 x 3), when set
+    int has_corr = 0, sticky = 0;
     int *d_stlist = nullptr;    // steric types: the partners whose tetrahedra overlap (MAX_STERIC_PARTNERS each)
     int *d_stcnt = nullptr;     // their number per face
     // grid
@@ -730,13 +732,17 @@ __device__ __forceinline__ int warp_candidate(int k, const int *s_beg, const int
 // consider_interaction's checks for the types other than lennard-jones
 // (src/VdW_solver.cpp:359-388): faces in front of each other, and within
 // one blob (with self-interaction on) no shared node.  Symmetric in (i, j).
+// With periodic corrections, cs = blob_corr[blob of A][blob of G] enters the
+// separation (c_G - c_A - cs; FFEA's c2 - c1 - blob_corr[b1][b2] with its
+// faces in either order, blob_corr being antisymmetric).
 __device__ __forceinline__ bool steric_type_ok(const double *A, const double *G, bool same_blob, int inc_self,
-                                               const int *ni, const int *nj)
+                                               const int *ni, const int *nj, const double *cs)
 {
     double sa = 0.0, sb = 0.0;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        const double sep = (1.0 / 3.0) * (G[d] + G[3 + d] + G[6 + d]) - (1.0 / 3.0) * (A[d] + A[3 + d] + A[6 + d]);
+        double sep = (1.0 / 3.0) * (G[d] + G[3 + d] + G[6 + d]) - (1.0 / 3.0) * (A[d] + A[3 + d] + A[6 + d]);
+        if (cs) sep -= cs[d];
         sa += sep * A[9 + d];
         sb += sep * G[9 + d];
     }
@@ -778,8 +784,8 @@ __global__ void __launch_bounds__(32 * kStericWarps) k_steric(
     const double *__restrict__ geo, const int *__restrict__ sorted, const int *__restrict__ cell,
     const int *__restrict__ start, const int *__restrict__ block, long long ncell, int nblocks, int nx, int ny,
     int nz, const int *__restrict__ fblob, const int *__restrict__ corner, int num_blobs, int inc_self,
-    double steric_factor, double steric_dr, double *__restrict__ fforce, int *__restrict__ stlist,
-    int *__restrict__ stcnt, double *__restrict__ energy, unsigned long long *stats)
+    double steric_factor, double steric_dr, const double *__restrict__ corr, double *__restrict__ fforce,
+    int *__restrict__ stlist, int *__restrict__ stcnt, double *__restrict__ energy, unsigned long long *stats)
 {
     __shared__ int s_pre[kStericWarps][28];
     __shared__ int s_beg[kStericWarps][27];
@@ -815,8 +821,27 @@ __global__ void __launch_bounds__(32 * kStericWarps) k_steric(
         if (have) {
             double Tj[4][3], vol;
             face_tet(geo, j, Tj);
-            hit = i < j ? steric_pair(Ti, Tj, steric_dr, steric_factor, true, out, vol)
-                        : steric_pair(Tj, Ti, steric_dr, steric_factor, false, out, vol);
+            if (i < j) {
+                // periodic: f2's tetrahedron minus blob_corr[b1][b2]
+                // (Face::getTetraIntersectionVolumeTotalGradientAndShapeFunctions,
+                // src/Face.cpp:517-531)
+                if (corr) {
+                    const double *c = corr + 3 * ((long long)bi * num_blobs + fblob[j]);
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+#pragma unroll
+                        for (int d = 0; d < 3; d++) Tj[u][d] -= c[d];
+                }
+                hit = steric_pair(Ti, Tj, steric_dr, steric_factor, true, out, vol);
+            } else {
+                double Tb[4][3];
+                const double *c = corr ? corr + 3 * ((long long)fblob[j] * num_blobs + bi) : nullptr;
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int d = 0; d < 3; d++) Tb[u][d] = c ? Ti[u][d] - c[d] : Ti[u][d];
+                hit = steric_pair(Tj, Tb, steric_dr, steric_factor, false, out, vol);
+            }
             if (hit && i < j) {
                 atomicAdd(&energy[bi * num_blobs + fblob[j]], vol);
                 npairs++;
@@ -839,16 +864,20 @@ __global__ void __launch_bounds__(32 * kStericWarps) k_steric(
             const double *G = geo + 16 * (long long)j;
             const bool same = bi == fblob[j];
             ok = j != i && (inc_self || !same) && !(A[9] * G[9] + A[10] * G[10] + A[11] * G[11] > 0.0);
+            // periodic: the partner as seen from face i, shifted by
+            // -blob_corr[bi][bj]
+            const double *cs = corr ? corr + 3 * ((long long)bi * num_blobs + fblob[j]) : nullptr;
             if (ok) {
                 int nj[4];
 #pragma unroll
                 for (int u = 0; u < 4; u++) nj[u] = corner[4 * j + u];
-                ok = steric_type_ok(A, G, same, inc_self, ni, nj);
+                ok = steric_type_ok(A, G, same, inc_self, ni, nj, cs);
             }
             if (ok) {  // bounding boxes of the two tetrahedra
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
-                    const double a0 = G[d], a1 = G[3 + d], a2 = G[6 + d], a3 = G[13 + d];
+                    const double sh = cs ? cs[d] : 0.0;
+                    const double a0 = G[d] - sh, a1 = G[3 + d] - sh, a2 = G[6 + d] - sh, a3 = G[13 + d] - sh;
                     const double lo = fmin(fmin(a0, a1), fmin(a2, a3)), hi = fmax(fmax(a0, a1), fmax(a2, a3));
                     if (hi < lo_i[d] || lo > hi_i[d]) ok = false;
                 }
@@ -902,7 +931,8 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
     int nz, const int *__restrict__ fblob, const int *__restrict__ ftype, const double *__restrict__ emin,
     const double *__restrict__ rmin, const double *__restrict__ k0, const int *__restrict__ corner,
     const int *__restrict__ stlist, const int *__restrict__ stcnt, int num_types, int num_blobs, int inc_self,
-    double *__restrict__ fforce, double *__restrict__ energy, unsigned long long *stats)
+    const double *__restrict__ corr, double *__restrict__ fforce, double *__restrict__ energy,
+    unsigned long long *stats)
 {
     __shared__ int s_pre[kPairWarps][28];
     __shared__ int s_beg[kPairWarps][27];
@@ -939,7 +969,18 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
         for (int q = 0; q < 13; q++) B[q] = G[q];
         if (i < j) {
             const int tt = ti * num_types + ftype[j];
-            const double en = pot_pair<POT, true>(A, B, emin[tt], rmin[tt], k0 ? k0[tt] : 0.0, out);
+            double en;
+            if (corr) {
+                // periodic: f1's corners minus blob_corr[b2][b1]
+                // (Face::barycentric_calc_point_f2, src/Face.cpp:271-277)
+                const double *c = corr + 3 * ((long long)fblob[j] * num_blobs + bi);
+                double As[13];
+#pragma unroll
+                for (int q = 0; q < 13; q++) As[q] = q < 9 ? A[q] - c[q % 3] : A[q];
+                en = pot_pair<POT, true>(As, B, emin[tt], rmin[tt], k0 ? k0[tt] : 0.0, out);
+            } else {
+                en = pot_pair<POT, true>(A, B, emin[tt], rmin[tt], k0 ? k0[tt] : 0.0, out);
+            }
             const int key = bi * num_blobs + fblob[j];
             if (key != e_key) {
                 if (e_key >= 0) atomicAdd(&energy[e_key], e_acc);
@@ -950,6 +991,11 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
             npairs++;
         } else {
             const int tt = ftype[j] * num_types + ti;
+            if (corr) {
+                const double *c = corr + 3 * ((long long)bi * num_blobs + fblob[j]);
+#pragma unroll
+                for (int q = 0; q < 9; q++) B[q] -= c[q % 3];
+            }
             pot_pair<POT, false>(B, A, emin[tt], rmin[tt], k0 ? k0[tt] : 0.0, out);
         }
     };
@@ -971,7 +1017,8 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
                     int nj[4];
 #pragma unroll
                     for (int u = 0; u < 4; u++) nj[u] = corner[4 * j + u];
-                    ok = steric_type_ok(A, G, bi == fblob[j], inc_self, ni, nj);
+                    ok = steric_type_ok(A, G, bi == fblob[j], inc_self, ni, nj,
+                                        corr ? corr + 3 * ((long long)bi * num_blobs + fblob[j]) : nullptr);
                 }
                 for (int t = 0; ok && t < nst; t++)
                     if (s_st[wi][t] == j) ok = false;  // the steric force applied instead
@@ -1017,6 +1064,46 @@ __global__ void __launch_bounds__(32 * kPairWarps) k_pairs(
                 double *f = &fforce[12 * (long long)i + 3 * k + d];
                 *f = STERIC ? *f + out[k][d] : out[k][d];
             }
+    }
+}
+
+// The sticky xz walls (VdW_solver::solve_sticky_wall / do_sticky_xz_interaction,
+// src/VdW_solver.cpp:216-235, 396-456), after the pair pass: every face whose
+// cell lies in the grid's bottom (y = 0) or top (y = ny - 1) row and faces
+// that wall feels a y force from it, the Lennard-Jones factor of its own type
+// at the height of its Gauss points, added to its corners (the energy is not
+// recorded, as in FFEA).  One thread per face.
+__global__ void k_sticky(const double *__restrict__ geo, const int *__restrict__ cell, int na,
+                         const int *__restrict__ ftype, const double *__restrict__ emin,
+                         const double *__restrict__ rmin, int num_types, int ny, int nz, double h,
+                         double *__restrict__ fforce)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= na || cell[i] < 0) return;
+    const int cy = (cell[i] / nz) % ny;
+    if (cy != 0 && cy != ny - 1) return;
+    const bool bottom = cy == 0;
+    const double *g = geo + 16 * (long long)i;
+    if ((bottom && g[10] > 0) || (!bottom && g[10] < 0)) return;
+    const double y_wall = bottom ? 0.0 : h * ny;
+    const int tt = ftype[i] * num_types + ftype[i];
+    const double r6 = pow(rmin[tt], 6.0), em = emin[tt];
+    double py[3], fm[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        py[k] = eta(k, 0) * g[1] + eta(k, 1) * g[4] + eta(k, 2) * g[7];
+        const double r = py[k] - y_wall;
+        fm[k] = -(12 * r6 * em * (pow(r, -7.0) - r6 * pow(r, -13.0)));
+    }
+    const double asq = g[12] * g[12];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        double fy = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int l = 0; l < 3; l++) fy += kW * kW * eta(l, j) * fm[k < l ? k : l];
+        fforce[12 * (long long)i + 3 * j + 1] += fy * asq;
     }
 }
 
@@ -1157,7 +1244,8 @@ extern "C" void ffea_gpu_ssint_destroy(ffea_gpu_ssint_t *s)
     if (s->stream) cudaStreamSynchronize(s->stream);
     void *bufs[] = {s->d_corner, s->d_blob, s->d_type, s->d_geo, s->d_cell, s->d_fforce, s->d_count,
                     s->d_start, s->d_block, s->d_sorted, s->d_node_ptr, s->d_node_ent, s->d_emin, s->d_rmin,
-                    s->d_pos, s->d_force, s->d_energy, s->d_stats, s->d_large, s->d_stlist, s->d_stcnt, s->d_k0};
+                    s->d_pos, s->d_force, s->d_energy, s->d_stats, s->d_large, s->d_stlist, s->d_stcnt, s->d_k0,
+                    s->d_corr};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -1194,20 +1282,65 @@ extern "C" int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *p
     if (s->type != FFEA_GPU_SSINT_LJ)
         k_steric<<<(na + kStericWarps - 1) / kStericWarps, 32 * kStericWarps, 0, st>>>(
             s->d_geo, s->d_sorted, s->d_cell, s->d_start, s->d_block, s->ncell, s->nblocks, s->nx, s->ny, s->nz,
-            s->d_blob, s->d_corner, s->num_blobs, s->inc_self, s->steric_factor, s->steric_dr, s->d_fforce,
-            s->d_stlist, s->d_stcnt, energy, s->d_stats);
+            s->d_blob, s->d_corner, s->num_blobs, s->inc_self, s->steric_factor, s->steric_dr,
+            s->has_corr ? s->d_corr : nullptr, s->d_fforce, s->d_stlist, s->d_stcnt, energy, s->d_stats);
 #define SSINT_PAIRS(POT, STERIC)                                                                                   \
     k_pairs<POT, STERIC><<<pw, 32 * kPairWarps, 0, st>>>(                                                           \
         s->d_geo, s->d_cell, s->d_sorted, s->d_start, s->d_block, s->ncell, s->nblocks, s->nx, s->ny, s->nz,        \
         s->d_blob, s->d_type, s->d_emin, s->d_rmin, s->d_k0, s->d_corner, s->d_stlist, s->d_stcnt, s->num_types,     \
-        s->num_blobs, s->inc_self, s->d_fforce, energy, s->d_stats)
+        s->num_blobs, s->inc_self, s->has_corr ? s->d_corr : nullptr, s->d_fforce, energy, s->d_stats)
     if (s->type == FFEA_GPU_SSINT_LJ) SSINT_PAIRS(POT_LJ, false);
     else if (s->type == FFEA_GPU_SSINT_LJSTERIC) SSINT_PAIRS(POT_LJ, true);
     else if (s->type == FFEA_GPU_SSINT_GENSOFT) SSINT_PAIRS(POT_SOFT, true);
 #undef SSINT_PAIRS
+    if (s->sticky)
+        k_sticky<<<fb, 128, 0, st>>>(s->d_geo, s->d_cell, na, s->d_type, s->d_emin, s->d_rmin, s->num_types, s->ny,
+                                     s->nz, s->h, s->d_fforce);
     k_node_gather<<<(s->num_nodes + 255) / 256, 256, 0, st>>>(s->d_node_ptr, s->d_node_ent, s->num_nodes,
                                                               s->d_fforce, s->d_cell, force);
     SSINT_CUDA(cudaGetLastError());
+    return FFEA_GPU_OK;
+}
+
+extern "C" int ffea_gpu_ssint_set_pbc(ffea_gpu_ssint_t *s, const double *blob_corr)
+{
+    if (!s) return fail("ffea_gpu_ssint_set_pbc: null handle");
+    if (!blob_corr) {
+        s->has_corr = 0;
+        return FFEA_GPU_OK;
+    }
+    const size_t n = 3 * (size_t)s->num_blobs * s->num_blobs;
+    if (!s->d_corr) SSINT_CUDA(cudaMalloc(&s->d_corr, sizeof(double) * n));
+    // ordered on the handle's stream before the next pass
+    SSINT_CUDA(cudaMemcpyAsync(s->d_corr, blob_corr, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
+    SSINT_CUDA(cudaStreamSynchronize(s->stream));
+    s->has_corr = 1;
+    return FFEA_GPU_OK;
+}
+
+extern "C" int ffea_gpu_ssint_set_sticky_wall(ffea_gpu_ssint_t *s, int32_t enable)
+{
+    if (!s) return fail("ffea_gpu_ssint_set_sticky_wall: null handle");
+    if (enable && s->ny < 2)
+        return fail("the sticky wall needs at least two rows of cells in y (FFEA's row loop would not end)");
+    s->sticky = enable ? 1 : 0;
+    return FFEA_GPU_OK;
+}
+
+extern "C" int ffea_gpu_ssint_blob_corr(int32_t num_blobs, const double *centroids, const double box[3],
+                                        double *blob_corr)
+{
+    if (num_blobs < 0 || (num_blobs > 0 && (!centroids || !box || !blob_corr)))
+        return fail("ffea_gpu_ssint_blob_corr: null argument");
+    for (int i = 0; i < num_blobs; ++i) {
+        for (int d = 0; d < 3; d++) blob_corr[3 * ((size_t)i * num_blobs + i) + d] = 0.0;
+        for (int j = i + 1; j < num_blobs; ++j)
+            for (int d = 0; d < 3; d++) {
+                const double v = box[d] * floor((centroids[3 * j + d] - centroids[3 * i + d] + 0.5 * box[d]) / box[d]);
+                blob_corr[3 * ((size_t)i * num_blobs + j) + d] = v;
+                blob_corr[3 * ((size_t)j * num_blobs + i) + d] = -1 * v;
+            }
+    }
     return FFEA_GPU_OK;
 }
 

@@ -47,10 +47,12 @@ class SurfaceSolver:
     (ssint_type SSINT_STERIC, SSINT_LJSTERIC, SSINT_GENSOFT) also take
     face_apex (F,), the fourth node of each face's element (Face::n[3]),
     steric_factor and steric_dr (SimulationParams), and gensoft k0 (T, T) in
-    meso units."""
+    meso units.  sticky_wall: the xz walls of sticky_wall_xz; periodic blob
+    corrections (force_pbc) are set per pass with set_pbc."""
 
     def __init__(self, num_nodes, faces, face_blob, face_type, emin, rmin, num_blobs, cell_size, grid,
-                 inc_self=0, ssint_type=SSINT_LJ, face_apex=None, steric_factor=1.0, steric_dr=5e-3, k0=None):
+                 inc_self=0, ssint_type=SSINT_LJ, face_apex=None, steric_factor=1.0, steric_dr=5e-3, k0=None,
+                 sticky_wall=False):
         L = _lib.lib()
         self._keep = [np.ascontiguousarray(faces, np.int32), np.ascontiguousarray(face_blob, np.int32),
                       np.ascontiguousarray(face_type, np.int32), np.ascontiguousarray(emin, np.float64),
@@ -72,6 +74,29 @@ class SurfaceSolver:
         self._h = h
         self.num_nodes = int(num_nodes)
         self.num_blobs = int(num_blobs)
+        self.box = float(cell_size) * np.asarray(grid[:3], np.float64)
+        if sticky_wall:
+            _lib.check(L.ffea_gpu_ssint_set_sticky_wall(h, 1), "ffea_gpu_ssint_set_sticky_wall")
+
+    def set_pbc(self, blob_corr=None):
+        """Periodic blob corrections (num_blobs, num_blobs, 3) for the next
+        passes, as World::calc_blob_corr_matrix makes them (blob_corr()
+        below); None turns them off."""
+        if blob_corr is None:
+            _lib.check(_lib.lib().ffea_gpu_ssint_set_pbc(self._h, None), "ffea_gpu_ssint_set_pbc")
+            return
+        bc = np.ascontiguousarray(blob_corr, np.float64)
+        if bc.shape != (self.num_blobs, self.num_blobs, 3):
+            raise ValueError(f"blob_corr must have shape ({self.num_blobs}, {self.num_blobs}, 3)")
+        _lib.check(_lib.lib().ffea_gpu_ssint_set_pbc(self._h, _lib.ptr(bc)), "ffea_gpu_ssint_set_pbc")
+
+    def blob_corr(self, centroids):
+        """World::calc_blob_corr_matrix for blob centroids (num_blobs, 3) in this grid's box."""
+        c = np.ascontiguousarray(centroids, np.float64).reshape(-1, 3)
+        out = np.zeros((len(c), len(c), 3))
+        _lib.check(_lib.lib().ffea_gpu_ssint_blob_corr(len(c), _lib.ptr(c), _lib.ptr(self.box), _lib.ptr(out)),
+                   "ffea_gpu_ssint_blob_corr")
+        return out
 
     def forces(self, pos):
         """One solve: returns (node forces (N, 3), energy (B, B), interacting pairs)."""

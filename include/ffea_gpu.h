@@ -317,6 +317,31 @@ int ffea_gpu_ssint_forces(ffea_gpu_ssint_t *s, const double *pos, double *force,
  * can vary from run to run. */
 int ffea_gpu_ssint_forces_device(ffea_gpu_ssint_t *s, const double *pos, double *force, double *energy);
 int ffea_gpu_ssint_synchronize(ffea_gpu_ssint_t *s, int64_t *pairs);
+
+/* Periodic blob corrections for the following passes (force_pbc): blob_corr
+ * is num_blobs x num_blobs x 3 doubles (host), as World::calc_blob_corr_matrix
+ * fills it (src/World.cpp:4460-4483); NULL turns them off.  In a pair (f1 =
+ * the lower pool index) the Lennard-Jones and soft potentials take f1's
+ * corners minus blob_corr[b2][b1] (Face::barycentric_calc_point_f2,
+ * src/Face.cpp:271-277), the steric overlap f2's tetrahedron minus
+ * blob_corr[b1][b2] (src/Face.cpp:517-531), and the in-front test the
+ * separation c2 - c1 - blob_corr[b1][b2] (src/VdW_solver.cpp:365-369).
+ * Replaces the solve(blob_corr) argument of VdW_solver. */
+int ffea_gpu_ssint_set_pbc(ffea_gpu_ssint_t *s, const double *blob_corr);
+
+/* World::calc_blob_corr_matrix on the host: blob_corr[i][j] = box *
+ * floor((c_j - c_i + box / 2) / box) per axis for i < j, its negation for
+ * j < i, zero on the diagonal; centroids: 3 per blob; box: the grid's extent
+ * (cell size x cells per axis). */
+int ffea_gpu_ssint_blob_corr(int32_t num_blobs, const double *centroids, const double box[3], double *blob_corr);
+
+/* The sticky xz walls (sticky_wall_xz = 1; VdW_solver::solve_sticky_wall,
+ * src/VdW_solver.cpp:216-235, 396-456), applied after the pair pass of the
+ * following calls: the faces of the grid's bottom and top rows of cells
+ * that face the wall at y = 0 (y = cell_size x ny) feel the Lennard-Jones
+ * force of their own type pair in y.  Needs ny >= 2 (FFEA's row loop does
+ * not end for ny = 1).  The wall energy is not recorded, as in FFEA. */
+int ffea_gpu_ssint_set_sticky_wall(ffea_gpu_ssint_t *s, int32_t enable);
 void *ffea_gpu_ssint_stream(ffea_gpu_ssint_t *s);
 
 /* --- allocation-free measurement ------------------------------------------ */

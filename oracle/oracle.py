@@ -341,16 +341,19 @@ def ssint_lj(pos, faces, face_blob, face_type, emin, rmin, num_blobs, h, grid, i
 
 
 def ssint(pos, faces, face_blob, face_type, emin, rmin, num_blobs, h, grid, inc_self=0, ssint_type=0,
-          face_apex=None, steric_factor=1.0, steric_dr=5e-3, k0=None):
+          face_apex=None, steric_factor=1.0, steric_dr=5e-3, k0=None, blob_corr=None, sticky_wall=False):
     """FFEA's surface-surface pass for any ssint type (oracle/ssint_oracle.c
     with oracle/steric_oracle.c): 0 lennard-jones, 1 steric, 2 ljsteric,
-    3 gensoft.  Returns (node_force (N, 3), energy (B, B), interacting pairs)."""
+    3 gensoft; blob_corr (B, B, 3) the periodic corrections (force_pbc),
+    sticky_wall the xz walls.  Returns (node_force (N, 3), energy (B, B),
+    interacting pairs)."""
     lib = port_lib()
     fn = lib.oracle_ssint
     fn.restype = ctypes.c_int
     fn.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, _ip, _ip, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int,
                    ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                   ctypes.c_double, ctypes.c_double, _dp, _dp, ctypes.POINTER(ctypes.c_longlong)]
+                   ctypes.c_double, ctypes.c_double, _dp, ctypes.c_int, _dp, _dp, ctypes.POINTER(ctypes.c_longlong)]
+    bc = None if blob_corr is None else np.ascontiguousarray(blob_corr, np.float64).reshape(-1)
     pos = np.ascontiguousarray(pos, np.float64)
     faces = np.ascontiguousarray(faces, np.int32)
     apex = None if face_apex is None else np.ascontiguousarray(face_apex, np.int32)
@@ -365,10 +368,25 @@ def ssint(pos, faces, face_blob, face_type, emin, rmin, num_blobs, h, grid, inc_
     rc = fn(len(pos), _ptr(pos, _dp), len(faces), _ptr(faces, _ip), _ptr(apex, _ip), _ptr(face_blob, _ip),
             _ptr(face_type, _ip), emin.shape[0], _ptr(emin, _dp), _ptr(rmin, _dp), _ptr(kk, _dp), num_blobs,
             float(h), int(grid[0]), int(grid[1]), int(grid[2]), int(inc_self), int(ssint_type),
-            float(steric_factor), float(steric_dr), _ptr(force, _dp), _ptr(energy, _dp), ctypes.byref(pairs))
+            float(steric_factor), float(steric_dr), _ptr(bc, _dp), int(bool(sticky_wall)), _ptr(force, _dp),
+            _ptr(energy, _dp), ctypes.byref(pairs))
+    if rc == -2:
+        raise ValueError("the sticky wall needs at least two rows of cells in y")
     if rc != 0:
         raise ValueError("a face centroid lies outside the interaction grid")
     return force, energy, int(pairs.value)
+
+
+def blob_corr(centroids, box):
+    """World::calc_blob_corr_matrix: (B, B, 3) periodic corrections of blob centroids (B, 3) in a box (3)."""
+    lib = port_lib()
+    lib.oracle_blob_corr.restype = None
+    lib.oracle_blob_corr.argtypes = [ctypes.c_int, _dp, _dp, _dp]
+    c = np.ascontiguousarray(centroids, np.float64).reshape(-1, 3)
+    b = np.ascontiguousarray(box, np.float64).reshape(3)
+    out = np.zeros((len(c), len(c), 3))
+    lib.oracle_blob_corr(len(c), _ptr(c, _dp), _ptr(b, _dp), _ptr(out, _dp))
+    return out
 
 
 def steric_overlap(A, B):

@@ -28,6 +28,16 @@
  *     and barycentric_calc_point (:265-269);
  *   - face forces go onto nodes in face order (Blob::aggregate_forces_and_solve,
  *     src/Blob.cpp:3841-3851).
+ * Periodic blob corrections (force_pbc, World::calc_blob_corr_matrix,
+ * src/World.cpp:4460-4483; blob_corr[b1][b2] = box * floor((c2 - c1 + box/2) /
+ * box) per axis, antisymmetric): the in-front test uses c2 - c1 -
+ * blob_corr[b1][b2] (:365-369), the LJ and soft potentials take f1's points
+ * as sum eta (x - blob_corr[b2][b1]) (Face::barycentric_calc_point_f2,
+ * src/Face.cpp:271-277), the steric overlap f2's tetrahedron minus
+ * blob_corr[b1][b2] (src/Face.cpp:517-531).  The sticky wall
+ * (VdW_solver::solve_sticky_wall / do_sticky_xz_interaction, :216-235,
+ * :396-456) runs after the pair pass over the faces of the grid's bottom and
+ * top rows of cells.
  * The reference's VdW_solver cannot be compiled here (its header includes
  * Blob.h, which needs Eigen, absent from the image); the restatement is pinned
  * to the reference's own known answer instead: the LJ energy of two parallel
@@ -74,15 +84,29 @@ static void lj_factors(double mag_r, double emin, double rmin6, double *force_ma
 
 /* do_lj_interaction for faces a (f1) and b (f2); adds to fa[3][3], fb[3][3]
  * and returns the pair energy (already multiplied by the areas). */
-static double lj_pair(const pool_face *a, const pool_face *b, double emin, double rmin, double fa[4][3],
-                      double fb[4][3])
+/* f1's Gauss points: barycentric_calc_point (src/Face.cpp:265-269), or with a
+ * periodic correction c = blob_corr[b2][b1] barycentric_calc_point_f2
+ * (:271-277), sum eta (x - c) */
+static void f1_points(const pool_face *a, const double *c, double p[3][3])
 {
-    double p[3][3], q[3][3], fpm[3][3][3];
     for (int k = 0; k < 3; k++)
         for (int d = 0; d < 3; d++) {
-            p[k][d] = kEta[k][0] * a->v[0][d] + kEta[k][1] * a->v[1][d] + kEta[k][2] * a->v[2][d];
-            q[k][d] = kEta[k][0] * b->v[0][d] + kEta[k][1] * b->v[1][d] + kEta[k][2] * b->v[2][d];
+            if (c)
+                p[k][d] = kEta[k][0] * (a->v[0][d] - c[d]) + kEta[k][1] * (a->v[1][d] - c[d]) +
+                          kEta[k][2] * (a->v[2][d] - c[d]);
+            else
+                p[k][d] = kEta[k][0] * a->v[0][d] + kEta[k][1] * a->v[1][d] + kEta[k][2] * a->v[2][d];
         }
+}
+
+static double lj_pair(const pool_face *a, const pool_face *b, const double *corr21, double emin, double rmin,
+                      double fa[4][3], double fb[4][3])
+{
+    double p[3][3], q[3][3], fpm[3][3][3];
+    f1_points(a, corr21, p);
+    for (int k = 0; k < 3; k++)
+        for (int d = 0; d < 3; d++)
+            q[k][d] = kEta[k][0] * b->v[0][d] + kEta[k][1] * b->v[1][d] + kEta[k][2] * b->v[2][d];
     double r2 = rmin * rmin;
     double r4 = r2 * r2;
     double r6 = r4 * r2;
@@ -145,15 +169,14 @@ static void gensoft_factors(double mag_r, double emin, double rmin, double k0, d
 /* do_gensoft_interaction for faces a (f1) and b (f2) with
  * calc_gensoft_force_pair_matrix (src/VdW_solver.cpp:488-563, 701-734); adds
  * to fa[3][3], fb[3][3] and returns the pair energy. */
-static double gensoft_pair(const pool_face *a, const pool_face *b, double emin, double rmin, double k0,
-                           double fa[4][3], double fb[4][3])
+static double gensoft_pair(const pool_face *a, const pool_face *b, const double *corr21, double emin, double rmin,
+                           double k0, double fa[4][3], double fb[4][3])
 {
     double p[3][3], q[3][3], fpm[3][3][3];
+    f1_points(a, corr21, p);
     for (int k = 0; k < 3; k++)
-        for (int d = 0; d < 3; d++) {
-            p[k][d] = kEta[k][0] * a->v[0][d] + kEta[k][1] * a->v[1][d] + kEta[k][2] * a->v[2][d];
+        for (int d = 0; d < 3; d++)
             q[k][d] = kEta[k][0] * b->v[0][d] + kEta[k][1] * b->v[1][d] + kEta[k][2] * b->v[2][d];
-        }
     double energy = 0.0, fm, e;
     for (int k = 0; k < 3; k++) {
         double dx = p[k][0] - q[k][0], dy = p[k][1] - q[k][1], dz = p[k][2] - q[k][2];
@@ -200,11 +223,39 @@ static double gensoft_pair(const pool_face *a, const pool_face *b, double emin, 
  * overwritten with the surface forces alone; energy: num_blobs x num_blobs,
  * overwritten (VdW_solver::fieldenergy, [blob of f1][blob of f2]).
  * pairs_out (may be NULL): the number of face pairs that interacted. */
+/* do_sticky_xz_interaction (src/VdW_solver.cpp:396-456) of one face against
+ * the wall y = y_wall: the y force on its corners (the energy is not kept,
+ * as in FFEA) */
+static void sticky_face(const pool_face *f, int bottom, double y_wall, double emin, double rmin, double ff[4][3])
+{
+    if ((bottom && f->normal[1] > 0) || (!bottom && f->normal[1] < 0)) return;
+    double py[3], fpm[3][3];
+    for (int k = 0; k < 3; k++) py[k] = kEta[k][0] * f->v[0][1] + kEta[k][1] * f->v[1][1] + kEta[k][2] * f->v[2][1];
+    const double r6 = pow(rmin, 6);
+    for (int k = 0; k < 3; k++)
+        for (int l = k; l < 3; l++) {
+            const double mag_r = py[k] - y_wall;
+            double force_mag = 12 * r6 * emin * (pow(mag_r, -7) - r6 * pow(mag_r, -13));
+            force_mag *= -1;
+            fpm[k][l] = force_mag;
+            fpm[l][k] = force_mag;
+        }
+    const double asq = f->area * f->area;
+    for (int j = 0; j < 3; j++) {
+        double fy = 0.0;
+        for (int k = 0; k < 3; k++)
+            for (int l = 0; l < 3; l++) fy += kW * kW * kEta[l][j] * fpm[k][l];
+        ff[j][1] += fy * asq;
+    }
+}
+
 int oracle_ssint(int num_nodes, const double *pos, int num_faces, const int *faces, const int *face_apex,
                  const int *face_blob, const int *face_type, int num_types, const double *emin, const double *rmin,
                  const double *k0, int num_blobs, double h, int nx, int ny, int nz, int inc_self, int ssint_type,
-                 double steric_factor, double steric_dr, double *node_force, double *energy, long long *pairs_out)
+                 double steric_factor, double steric_dr, const double *blob_corr, int sticky_wall, double *node_force,
+                 double *energy, long long *pairs_out)
 {
+    if (sticky_wall && ny < 2) return -2; /* FFEA's row loop (y += Ny - 1) would not end */
     static const int adj[27][3] = {{-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {-1, 0, -1}, {-1, 0, 0}, {-1, 0, 1},
                                    {-1, 1, -1},  {-1, 1, 0},  {-1, 1, 1},  {0, -1, -1}, {0, -1, 0}, {0, -1, 1},
                                    {0, 0, -1},   {0, 0, 0},   {0, 0, 1},   {0, 1, -1},  {0, 1, 0},  {0, 1, 1},
@@ -274,10 +325,14 @@ int oracle_ssint(int num_nodes, const double *pos, int num_faces, const int *fac
                 if (!inc_self && ba == bb) continue;
                 if (A->normal[0] * B->normal[0] + A->normal[1] * B->normal[1] + A->normal[2] * B->normal[2] > 0.0)
                     continue;
+                /* periodic corrections of the pair: [b1][b2] and [b2][b1] */
+                const double *c12 = blob_corr ? blob_corr + 3 * ((long)ba * num_blobs + bb) : NULL;
+                const double *c21 = blob_corr ? blob_corr + 3 * ((long)bb * num_blobs + ba) : NULL;
                 if (ssint_type != SS_LJ) {
                     /* faces in front of each other; no shared node within a blob */
                     double sep[3];
-                    for (int d = 0; d < 3; d++) sep[d] = B->centroid[d] - A->centroid[d];
+                    for (int d = 0; d < 3; d++)
+                        sep[d] = c12 ? B->centroid[d] - A->centroid[d] - c12[d] : B->centroid[d] - A->centroid[d];
                     if (sep[0] * A->normal[0] + sep[1] * A->normal[1] + sep[2] * A->normal[2] < 0 &&
                         sep[0] * B->normal[0] + sep[1] * B->normal[1] + sep[2] * B->normal[2] > 0)
                         continue;
@@ -293,8 +348,10 @@ int oracle_ssint(int num_nodes, const double *pos, int num_faces, const int *fac
                 int done = 0;
                 if (ssint_type != SS_LJ) {
                     /* steric where the element tetrahedra overlap */
-                    double vol, f1[4][3], f2[4][3];
-                    if (steric_pair((const double (*)[3])A->v, (const double (*)[3])B->v, steric_dr, steric_factor,
+                    double vol, f1[4][3], f2[4][3], Bv[4][3];
+                    for (int u = 0; u < 4; u++)
+                        for (int d = 0; d < 3; d++) Bv[u][d] = c12 ? B->v[u][d] - c12[d] : B->v[u][d];
+                    if (steric_pair((const double (*)[3])A->v, (const double (*)[3])Bv, steric_dr, steric_factor,
                                     &vol, f1, f2)) {
                         for (int u = 0; u < 4; u++)
                             for (int d = 0; d < 3; d++) {
@@ -306,15 +363,26 @@ int oracle_ssint(int num_nodes, const double *pos, int num_faces, const int *fac
                     }
                 }
                 if (!done && (ssint_type == SS_LJ || ssint_type == SS_LJSTERIC)) {
-                    energy[ba * num_blobs + bb] += lj_pair(A, B, emin[t], rmin[t], fforce[i], fforce[j]);
+                    energy[ba * num_blobs + bb] += lj_pair(A, B, c21, emin[t], rmin[t], fforce[i], fforce[j]);
                     done = 1;
                 } else if (!done && ssint_type == SS_GENSOFT) {
-                    energy[ba * num_blobs + bb] += gensoft_pair(A, B, emin[t], rmin[t], k0[t], fforce[i], fforce[j]);
+                    energy[ba * num_blobs + bb] +=
+                        gensoft_pair(A, B, c21, emin[t], rmin[t], k0[t], fforce[i], fforce[j]);
                     done = 1;
                 }
                 pairs += done;
             }
         }
+    }
+    if (sticky_wall) {
+        /* the bottom row of cells, then the top one, each cell's stack in turn */
+        for (int y = 0; y < ny; y += ny - 1)
+            for (int z = 0; z < nz; z++)
+                for (int x = 0; x < nx; x++)
+                    for (int f = root[((long)x * ny + y) * nz + z]; f >= 0; f = next[f]) {
+                        const int t = face_type[pool[f].face] * num_types + face_type[pool[f].face];
+                        sticky_face(&pool[f], y == 0, y == 0 ? 0.0 : h * ny, emin[t], rmin[t], fforce[f]);
+                    }
     }
     for (int i = 0; i < np; i++)
         for (int k = 0; k < 4; k++) {
@@ -338,5 +406,22 @@ int oracle_ssint_lj(int num_nodes, const double *pos, int num_faces, const int *
                     long long *pairs_out)
 {
     return oracle_ssint(num_nodes, pos, num_faces, faces, NULL, face_blob, face_type, num_types, emin, rmin, NULL,
-                        num_blobs, h, nx, ny, nz, inc_self, SS_LJ, 0.0, 0.0, node_force, energy, pairs_out);
+                        num_blobs, h, nx, ny, nz, inc_self, SS_LJ, 0.0, 0.0, NULL, 0, node_force, energy, pairs_out);
+}
+
+/* World::calc_blob_corr_matrix (src/World.cpp:4460-4483): for blob centroids
+ * c (3 per blob) and the box, blob_corr[i][j] = box * floor((c_j - c_i +
+ * box / 2) / box) per axis for i < j, its negation for j < i, 0 on the
+ * diagonal. */
+void oracle_blob_corr(int num_blobs, const double *c, const double box[3], double *blob_corr)
+{
+    for (int i = 0; i < num_blobs; ++i) {
+        for (int d = 0; d < 3; d++) blob_corr[3 * ((long)i * num_blobs + i) + d] = 0.0;
+        for (int j = i + 1; j < num_blobs; ++j)
+            for (int d = 0; d < 3; d++) {
+                const double v = box[d] * floor((c[3 * j + d] - c[3 * i + d] + 0.5 * box[d]) / box[d]);
+                blob_corr[3 * ((long)i * num_blobs + j) + d] = v;
+                blob_corr[3 * ((long)j * num_blobs + i) + d] = -1 * v;
+            }
+    }
 }

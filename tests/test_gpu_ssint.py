@@ -243,3 +243,81 @@ def test_steric_types_match_oracle(ssint_type, inc_self):
     if ssint_type != 1:
         _, e_st, p_st = oracle.ssint(pos, faces, blob, ftype, emin, rmin, 2, h, grid, inc_self, 1, apex, 50.0, 5e-3)
         assert 0 < p_st < p_ref
+
+
+@pytest.mark.parametrize("ssint_type", [0, 1, 2, 3])
+def test_periodic_corrections_match_oracle(ssint_type):
+    """force_pbc: the second sphere translated by one box length in x and
+    minus one in z, the blob corrections from the blobs' centroids
+    (SurfaceSolver.blob_corr, the library's World::calc_blob_corr_matrix).
+    The GPU against the oracle with the same corrections (forces to 1e-9 of
+    the largest, energies to 1e-9, pair counts exactly), and against the
+    untranslated pass without corrections (the same geometry: 1e-9)."""
+    from tests.test_steric_oracle import overlapping_spheres
+    pos, faces, apex, blob, h, grid = overlapping_spheres()
+    rng = np.random.default_rng(13)
+    T = 2
+    emin = rng.uniform(0.5, 2.0, (T, T))
+    emin = 0.5 * (emin + emin.T)
+    rmin = np.full((T, T), nm(1.0))
+    k0 = np.full((T, T), 0.3)
+    ftype = rng.integers(0, T, len(faces)).astype(np.int32)
+    kw = dict(num_nodes=len(pos), faces=faces, face_blob=blob, face_type=ftype, emin=emin, rmin=rmin, num_blobs=2,
+              cell_size=h, grid=grid, inc_self=1, ssint_type=ssint_type, face_apex=apex, steric_factor=50.0,
+              steric_dr=5e-3, k0=k0)
+    s = _solver(**kw)
+    f0, e0, p0 = s.forces(pos)
+    n = len(pos) // 2
+    moved = pos.copy()
+    moved[n:] += np.array([1.0, 0.0, -1.0]) * s.box
+    bc = s.blob_corr(np.array([moved[:n].mean(0), moved[n:].mean(0)]))
+    assert np.array_equal(bc[0, 1], np.array([1.0, 0.0, -1.0]) * s.box)
+    s.set_pbc(bc)
+    f1, e1, p1 = s.forces(moved)
+    s.set_pbc(None)
+    f2, e2, p2 = s.forces(pos)
+    s.close()
+    f_ref, e_ref, p_ref = oracle.ssint(moved, faces, blob, ftype, emin, rmin, 2, h, grid, 1, ssint_type, apex, 50.0,
+                                       5e-3, k0, blob_corr=bc)
+    scale = np.abs(f_ref).max()
+    assert p1 == p_ref == p0 == p2 and p0 > 0
+    np.testing.assert_allclose(f1, f_ref, rtol=0, atol=1e-9 * scale)
+    np.testing.assert_allclose(e1, e_ref, rtol=1e-9, atol=1e-9 * np.abs(e_ref).max())
+    np.testing.assert_allclose(f1, f0, rtol=0, atol=1e-9 * scale)
+    assert np.array_equal(f2, f0)  # turned off again
+
+
+@pytest.mark.parametrize("ssint_type", [0, 2])
+def test_sticky_wall_matches_oracle(ssint_type):
+    """sticky_wall_xz: a sphere resting 0.4 nm above y = 0 in a 6^3 grid, plus
+    the pair pass; the GPU against the oracle (forces to 1e-10 of the
+    largest); the walls need two rows of cells."""
+    from ffea_gb300._lib import FfeaGpuError
+    from ffea_gb300.mesh import sphere_mesh
+    from ffea_gb300.surface import surface_faces
+    m = sphere_mesh(2.5, seed=8)
+    tri, apex = surface_faces(m.pos, m.topology, with_apex=True)
+    tri = tri.astype(np.int32)
+    h = nm(1.5)
+    grid = (6, 6, 6)
+    pos = m.pos - m.pos.mean(0) + np.array([3.0, 0.0, 3.0]) * h
+    pos[:, 1] += -pos[:, 1].min() + nm(0.4)
+    rng = np.random.default_rng(2)
+    ftype = rng.integers(0, 2, len(tri)).astype(np.int32)
+    emin = np.array([[1.0, 0.7], [0.7, 1.3]])
+    rmin = np.full((2, 2), nm(0.6))
+    blob = np.zeros(len(tri), np.int32)
+    kw = dict(num_nodes=len(pos), faces=tri, face_blob=blob, face_type=ftype, emin=emin, rmin=rmin, num_blobs=1,
+              cell_size=h, grid=grid, inc_self=1, ssint_type=ssint_type, face_apex=apex, steric_factor=50.0,
+              steric_dr=5e-3, sticky_wall=True)
+    s = _solver(**kw)
+    f_gpu, e_gpu, p_gpu = s.forces(pos)
+    s.close()
+    f_ref, e_ref, p_ref = oracle.ssint(pos, tri, blob, ftype, emin, rmin, 1, h, grid, 1, ssint_type, apex, 50.0, 5e-3,
+                                       sticky_wall=True)
+    f_nowall, _, _ = oracle.ssint(pos, tri, blob, ftype, emin, rmin, 1, h, grid, 1, ssint_type, apex, 50.0, 5e-3)
+    assert p_gpu == p_ref and np.abs(f_ref - f_nowall).max() > 0
+    np.testing.assert_allclose(f_gpu, f_ref, rtol=0, atol=1e-10 * np.abs(f_ref).max())
+    kw["grid"] = (6, 1, 6)
+    with pytest.raises(FfeaGpuError, match="two rows"):
+        _solver(**kw)
