@@ -557,6 +557,14 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
         CK(cudaMemcpy(d.phi, H.phi.data(), H.phi.size() * sizeof(float), cudaMemcpyHostToDevice));
         CK(A.alloc(d.coarse_A, (size_t)coarse_total));
         CK(A.alloc(d.coarse_X, (size_t)coarse_total));
+        if (!d.cg_reg) {
+            // the memory-resident kernel reads X every iteration from global
+            // memory: an FP16 copy, scaled to unit diagonal, halves that read
+            size_t dofs = 0;
+            for (const BlobParams &bp : H.bp) dofs += (size_t)bp.coarse_n;
+            CK(A.alloc(d.coarse_Xh, (size_t)H.coarse_htotal));
+            CK(A.alloc(d.coarse_s, dofs));
+        }
         // Newton-Schulz scratch for a run of equal-size blobs at once
         CK(A.alloc(d.coarse_T, std::max((size_t)coarse_nmax * coarse_nmax, (size_t)coarse_total)));
         CK(A.alloc(d.coarse_Xn, std::max((size_t)coarse_nmax * coarse_nmax, (size_t)coarse_total)));

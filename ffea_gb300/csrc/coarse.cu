@@ -15,10 +15,12 @@
 //   coarse_refresh     X ~ A_c^-1 by Newton-Schulz, X <- 2X - X A_c X (two
 //                      FP32 GEMMs, k_sgemm below) from the previous step's
 //                      X; `init` starts from X = I / ||A_c||_inf and
-//                      iterates to convergence
+//                      iterates to convergence; for the memory-resident
+//                      CG kernel, then the FP16 copy it reads (k_coarse_half)
 //
 // The matrix enters in the same difference form as the solver's SpMV:
 // (A v)_p = sum_q K_pq (v_q - v_p) + zeta_p v_p over the free rows.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -219,6 +221,32 @@ __global__ void k_symmetrize(const float *__restrict__ src, float *__restrict__ 
     if (i >= n || j >= n) return;
     const size_t o = (size_t)blockIdx.z * n * n;
     dst[o + (size_t)i * n + j] = 0.5f * (src[o + (size_t)i * n + j] + src[o + (size_t)j * n + i]);
+}
+
+// The scale of coarse dof i: sqrt(X_ii), 1 where that is not a positive
+// finite number.
+__device__ __forceinline__ float coarse_scale(float xii)
+{
+    return (xii > 0.f && xii < INFINITY) ? sqrtf(xii) : 1.f;
+}
+
+// Xh = S^-1 X S^-1 rounded to FP16 (unit diagonal, |entries| about 1 at most
+// for an SPD X) with rows padded with zeros to nh halves, and s = diag(S);
+// one n x n matrix per blockIdx.z (X n^2 apart, Xh n nh apart, s n apart).
+// S Xh S is symmetric like X, and its entries keep FP16's relative precision
+// whatever the magnitude of X.
+__global__ void k_coarse_half(const float *__restrict__ X, __half *__restrict__ Xh, float *__restrict__ sv, int n,
+                              int nh)
+{
+    const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || j >= nh) return;
+    X += (size_t)blockIdx.z * n * n;
+    Xh += (size_t)blockIdx.z * n * nh;
+    const float si = coarse_scale(X[(size_t)i * n + i]);
+    if (j == 0) sv[(size_t)blockIdx.z * n + i] = si;
+    float v = 0.f;
+    if (j < n) v = X[(size_t)i * n + j] / (si * coarse_scale(X[(size_t)j * n + j]));
+    Xh[(size_t)i * nh + j] = __float2half_rn(v);
 }
 
 // X = I / ||A||_inf (the Newton-Schulz start, convergent for an SPD A), one
@@ -508,6 +536,13 @@ int coarse_refresh(const DeviceBatch &d, const std::vector<BlobParams> &bps, cud
             sgemm_batched(X, Tm, X, Xn, n, batch, -1.f, 2.f, d.coarse_part, s);
             dim3 grid((n + 255) / 256, n, batch);
             k_symmetrize<<<grid, 256, 0, s>>>(Xn, X, n);
+            count_launches(1);
+        }
+        if (d.coarse_Xh) {
+            const int nh = (n + 7) / 8 * 8;
+            dim3 grid((nh + 255) / 256, n, batch);
+            k_coarse_half<<<grid, 256, 0, s>>>(X, reinterpret_cast<__half *>(d.coarse_Xh) + bp.coarse_hxoff,
+                                               d.coarse_s + bp.coarse_off, n, nh);
             count_launches(1);
         }
     });

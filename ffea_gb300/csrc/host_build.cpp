@@ -213,15 +213,18 @@ int64_t build_coarse(HostBatch &H)
         H.seg_nbr.insert(H.seg_nbr.end(), nb.begin(), nb.end());
         H.seg_nbr_ptr[s + 1] = (int32_t)H.seg_nbr.size();
     }
-    int64_t coff = 0, xoff = 0;
+    int64_t coff = 0, xoff = 0, hxoff = 0;
     for (int b = 0; b < H.num_blobs; b++) {
         BlobParams &bp = H.bp[b];
         bp.coarse_off = (int32_t)coff;
         bp.coarse_n = 6 * bp.seg_cnt;
         bp.coarse_xoff = (int32_t)xoff;
+        bp.coarse_hxoff = (int32_t)hxoff;
         coff += bp.coarse_n;
         xoff += (int64_t)bp.coarse_n * bp.coarse_n;
+        hxoff += (int64_t)bp.coarse_n * ((bp.coarse_n + 7) / 8 * 8);
     }
+    H.coarse_htotal = hxoff;
     return xoff;
 }
 

@@ -55,6 +55,7 @@ struct HostBatch {
     std::vector<int32_t> seg_of_row;
     std::vector<float> phi;                                // 4 per padded row
     std::vector<int32_t> seg_nbr_ptr, seg_nbr;
+    int64_t coarse_htotal = 0;                             // halves of the FP16 scaled inverses
     int32_t num_streams = 0;
     std::vector<uint32_t> stream_state;                   // 6 per stream
     std::vector<mrg::JumpMat> stream_step;                // per stream: A^(draws per step)
@@ -85,9 +86,9 @@ int32_t plan_cg_segments(HostBatch &H);
 
 // Coarse-space data of the two-level preconditioner for the planned
 // segments (call after plan_cg_segments): seg_of_row, phi (smoother weight
-// 1), seg_nbr_*, and per blob coarse_off / coarse_n / coarse_xoff (6 rigid
-// modes per segment).  Returns the total size of the per-blob dense coarse
-// matrices (sum of coarse_n^2).
+// 1), seg_nbr_*, per blob coarse_off / coarse_n / coarse_xoff / coarse_hxoff
+// (6 rigid modes per segment), and coarse_htotal.  Returns the total size of
+// the per-blob dense coarse matrices (sum of coarse_n^2).
 int64_t build_coarse(HostBatch &H);
 
 // World::init's six seed words (src/World.cpp:299-305).

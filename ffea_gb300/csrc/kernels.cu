@@ -20,6 +20,7 @@
 // Reductions are deterministic: fixed butterflies inside warps and CTAs, one
 // partial per node tile, and fixed-order per-blob sums.  No floating-point
 // atomics are used anywhere.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -1804,6 +1805,19 @@ __device__ __forceinline__ void coarse_u_of(const float4 f, const float *c, cons
     for (int k = 0; k < 3; k++) u[k] = (T)f.w * dinv[k] * r[k] + pc[k];
 }
 
+// acc + sum_t h_t g_t over the eight FP16 values h of one 16-byte load
+// (lowest address first), in order
+__device__ __forceinline__ float dot8_half(const uint4 raw, const float (&g)[8], float acc)
+{
+    const unsigned int w[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        acc = fmaf(__half2float(__ushort_as_half((unsigned short)(w[q] & 0xffffu))), g[2 * q], acc);
+        acc = fmaf(__half2float(__ushort_as_half((unsigned short)(w[q] >> 16))), g[2 * q + 1], acc);
+    }
+    return acc;
+}
+
 // The coarse corrections of the CTA's segments for the next update
 // (memory-resident kernel), after the iteration's partial sums and the CG
 // transitions.  First, for every blob k of the CTA (state ACTIVE or RESTART,
@@ -1837,13 +1851,14 @@ __device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const floa
             for (int i = tid; i < n; i += blockDim.x) {
                 const float *sl = part + (size_t)d.part_stride * (bp.seg_off + i / 6);
                 const float pr = __ldcg(sl + 8 + i % 6);
+                const float sc = d.coarse_Xh ? __ldg(&d.coarse_s[bp.coarse_off + i]) : 1.f;
                 if (restart) {
                     h[i] = 0.f;
-                    g[i] = pr;
+                    g[i] = sc * pr;
                 } else {
                     const float hn = __ldcg(sl + 14 + i % 6) + be * h[i];
                     h[i] = hn;
-                    g[i] = pr - a * hn;
+                    g[i] = sc * (pr - a * hn);
                 }
             }
         }
@@ -1865,11 +1880,27 @@ __device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const floa
             if (n > 0 && (prologue || st == CG_ACTIVE || st == CG_RESTART)) {  // warp-uniform
                 const float *g = cv.g + cv.hoff[k];
                 const float *Xr = d.coarse_X + bp.coarse_xoff + (size_t)(6 * (s_sid[j] - bp.seg_off)) * n;
-#pragma unroll 4
-                for (int i = sub * 32 + lane; i < n; i += wps * 32) {
-                    const float gi = g[i];
+                if (d.coarse_Xh) {
+                    // the FP16 copy S^-1 X S^-1 (g holds S g): eight coarse
+                    // dofs a lane and 16-byte load, rows padded to nh
+                    const int nh = (n + 7) & ~7, n8 = nh >> 3;
+                    const uint4 *X8 = reinterpret_cast<const uint4 *>(d.coarse_Xh + bp.coarse_hxoff +
+                                                                      (size_t)(6 * (s_sid[j] - bp.seg_off)) * nh);
+#pragma unroll 2
+                    for (int i = sub * 32 + lane; i < n8; i += wps * 32) {
+                        float gv[8];
 #pragma unroll
-                    for (int l = 0; l < 6; l++) v[l] = fmaf(__ldcg(Xr + (size_t)l * n + i), gi, v[l]);
+                        for (int t = 0; t < 8; t++) gv[t] = 8 * i + t < n ? g[8 * i + t] : 0.f;
+#pragma unroll
+                        for (int l = 0; l < 6; l++) v[l] = dot8_half(__ldcg(X8 + (size_t)l * n8 + i), gv, v[l]);
+                    }
+                } else {
+#pragma unroll 4
+                    for (int i = sub * 32 + lane; i < n; i += wps * 32) {
+                        const float gi = g[i];
+#pragma unroll
+                        for (int l = 0; l < 6; l++) v[l] = fmaf(__ldcg(Xr + (size_t)l * n + i), gi, v[l]);
+                    }
                 }
             }
         }
@@ -1882,6 +1913,10 @@ __device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const floa
             if (q0 + jj < nt) {
                 float sum = 0.f;
                 for (int w = 0; w < wps; w++) sum += cv.red[(jj * wps + w) * 8 + l];
+                if (d.coarse_Xh) {
+                    const BlobParams &bp = d.bp[s_blob[s_tslot[q0 + jj]]];
+                    sum *= __ldg(&d.coarse_s[bp.coarse_off + 6 * (s_sid[q0 + jj] - bp.seg_off) + l]);
+                }
                 cv.cvec[8 * (q0 + jj) + l] = sum;
             }
         }

@@ -34,6 +34,10 @@ struct DeviceBatch {
     int32_t *seg_of_row = nullptr;
     int32_t *seg_nbr_ptr = nullptr, *seg_nbr = nullptr;   // segments coupled to each segment (itself included)
     float *coarse_A = nullptr, *coarse_X = nullptr;       // per blob: A_c and X ~ A_c^-1 (coarse_xoff)
+    // memory-resident CG kernel: X read as S Xh S, S = diag(sqrt(X_ii)) per
+    // coarse dof (coarse_off), Xh = S^-1 X S^-1 in FP16 (coarse_hxoff)
+    uint16_t *coarse_Xh = nullptr;
+    float *coarse_s = nullptr;
     float *coarse_T = nullptr, *coarse_Xn = nullptr;      // Newton-Schulz scratch (coarse_nmax^2)
     float *coarse_part = nullptr;                         // split-K partial products of the Newton-Schulz GEMMs
     float *coarse_asm = nullptr;                          // partial A_c blocks: 36 floats x CG_SEG_MAX_ROWS / 256 per neighbour entry

@@ -49,6 +49,8 @@ struct BlobParams {
     int32_t seg_off, seg_cnt;               // CG segments of this blob
     int32_t coarse_off, coarse_n;           // two-level: first coarse dof, number of coarse dofs (6 per segment)
     int32_t coarse_xoff;                    // offset of the blob's dense coarse matrices (coarse_n^2 floats)
+    int32_t coarse_hxoff;                   // offset of the blob's FP16 scaled inverse (coarse_n rows of
+                                            // coarse_n rounded up to 8 halves)
     int32_t num_nodes_total;                // N_t of the reference (linear + secondary)
     int32_t noise_node_off;                 // first node of the blob's node draws in the node-noise buffer
     int32_t true_residual;
