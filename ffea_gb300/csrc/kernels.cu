@@ -1870,6 +1870,14 @@ __device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const floa
     const int per_round = 32 / wps;
     for (int q0 = 0; q0 < nt; q0 += per_round) {
         const int j = q0 + warp / wps, sub = warp % wps;
+        // the row scale of the FP16 copy for the final sums below, loaded
+        // ahead so that its latency overlaps the products
+        float srow = 1.f;
+        if (d.coarse_Xh && tid < 6 * per_round && q0 + tid / 6 < nt) {
+            const int jj = q0 + tid / 6;
+            const BlobParams &bp = d.bp[s_blob[s_tslot[jj]]];
+            if (bp.coarse_n > 0) srow = __ldg(&d.coarse_s[bp.coarse_off + 6 * (s_sid[jj] - bp.seg_off) + tid % 6]);
+        }
         float v[8];
 #pragma unroll
         for (int l = 0; l < 8; l++) v[l] = 0.f;
@@ -1913,11 +1921,7 @@ __device__ __forceinline__ void coarse_mem_step(const DeviceBatch &d, const floa
             if (q0 + jj < nt) {
                 float sum = 0.f;
                 for (int w = 0; w < wps; w++) sum += cv.red[(jj * wps + w) * 8 + l];
-                if (d.coarse_Xh) {
-                    const BlobParams &bp = d.bp[s_blob[s_tslot[q0 + jj]]];
-                    sum *= __ldg(&d.coarse_s[bp.coarse_off + 6 * (s_sid[q0 + jj] - bp.seg_off) + l]);
-                }
-                cv.cvec[8 * (q0 + jj) + l] = sum;
+                cv.cvec[8 * (q0 + jj) + l] = sum * srow;
             }
         }
         __syncthreads();
