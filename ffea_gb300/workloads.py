@@ -1,6 +1,6 @@
 """The synthetic blob workloads the measurements and the large parity tests use.
 
-Every workload is a set of NoMass blobs at BASELINE physics: density
+Every workload is a set of NoMass blobs with one set of physics: density
 1.5e3 kg/m^3, shear/bulk modulus 3.7e8/1.1e9 Pa (scaled per blob in the
 ensemble), shear/bulk viscosity 1e-3 Pa s, kT at 300 K, dt 1e-14 s, thermal
 noise and Stokes drag on.  Meshes are Freudenthal-split cube grids at a

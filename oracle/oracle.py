@@ -2,8 +2,8 @@
 built, the reference objects (oracle/_ref/libffea_ref.so).
 
 TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's
-cpu_baseline / --impl reference legs use this module as the checker.  The
-product (ffea_gb300) never imports it.
+cpu_baseline / --impl reference legs use this module to check and time the
+CPU algorithm.  The product (ffea_gb300) never imports it.
 """
 from __future__ import annotations
 

@@ -1,8 +1,8 @@
 /* ssint_oracle.c -- CPU restatement of FFEA's surface-surface Lennard-Jones
  * interaction ("vdw_type = lennard-jones"), for tests only.
  *
- * This is test infrastructure: the tests and the bench's CPU leg call it as
- * the checker of the GPU kernels in ffea_gb300/csrc/ssint.cu.  Nothing in the
+ * This is test infrastructure: the tests and the bench's CPU leg compare the
+ * GPU kernels in ffea_gb300/csrc/ssint.cu against it.  Nothing in the
  * product links it.
  *
  * It follows one single-threaded pass of VdW_solver::solve

@@ -1,8 +1,8 @@
 /* steric_oracle.c -- CPU restatement of FFEA's steric, LJ-steric and
  * soft-potential ("gensoft") surface interactions, for tests only.
  *
- * This is test infrastructure: the tests call it as the checker of the GPU
- * kernels in ffea_gb300/csrc/ssint.cu.  Nothing in the product links it.
+ * This is test infrastructure: the tests compare the GPU kernels in
+ * ffea_gb300/csrc/ssint.cu against it.  Nothing in the product links it.
  *
  * The three interaction types share VdW_solver::solve's pass over the
  * nearest-neighbour grid (src/VdW_solver.cpp:168-210, restated in

@@ -6,8 +6,8 @@ that drives it through a `Solver *` exactly as Blob does: init on a
 one-element mesh built from FFEA's classes, then solve.  Without a GPU the
 library refuses the handle, and init must return FFEA_ERROR with the
 library's message (FFEA's error convention); with one, the solve must
-return FFEA_OK.  Needs the FFEA sources and g++; skipped where they are
-absent (the GPU machine has no FFEA sources)."""
+return FFEA_OK.  Needs the FFEA sources and g++; skipped on machines
+without them."""
 import os
 import shutil
 import subprocess
