@@ -113,6 +113,9 @@ SIGNATURES = {
     "ffea_gpu_diag_spmv": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _dp]),
     "ffea_gpu_diag_coarse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
                                             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "ffea_gpu_diag_coarse_half": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                                 ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_uint16),
+                                                 ctypes.POINTER(ctypes.c_float)]),
     "ffea_gpu_script_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
     "ffea_gpu_script_free": (None, [ctypes.c_void_p]),
     "ffea_gpu_script_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScriptParams)]),

@@ -1377,6 +1377,24 @@ extern "C" int ffea_gpu_diag_coarse(ffea_gpu_t *h, int32_t blob, int32_t *n, flo
     return FFEA_GPU_OK;
 }
 
+extern "C" int ffea_gpu_diag_coarse_half(ffea_gpu_t *h, int32_t blob, int32_t *n, int32_t *row_len,
+                                         uint16_t *half_inverse, float *scale)
+{
+    if (!h || !n || !row_len) return fail("bad arguments");
+    if (blob < 0 || blob >= (int32_t)h->host.bp.size()) return fail("blob index %d out of range", blob);
+    const BlobParams &bp = h->host.bp[blob];
+    *n = h->dev.coarse && h->dev.coarse_Xh ? bp.coarse_n : 0;
+    *row_len = (*n + 7) / 8 * 8;
+    if (*n == 0) return FFEA_GPU_OK;
+    CK(cudaStreamSynchronize(h->stream));
+    if (half_inverse)
+        CK(cudaMemcpy(half_inverse, h->dev.coarse_Xh + bp.coarse_hxoff, sizeof(uint16_t) * (size_t)*n * *row_len,
+                      cudaMemcpyDeviceToHost));
+    if (scale)
+        CK(cudaMemcpy(scale, h->dev.coarse_s + bp.coarse_off, sizeof(float) * (size_t)*n, cudaMemcpyDeviceToHost));
+    return FFEA_GPU_OK;
+}
+
 extern "C" int ffea_gpu_diag_sgemm(const float *a, const float *b, const float *d, float *c, int32_t n, int32_t batch,
                                    float alpha, float beta, void *stream)
 {

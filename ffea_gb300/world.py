@@ -195,6 +195,23 @@ class World:
                                              x.ctypes.data_as(fp)), "diag_coarse")
         return a, x
 
+    def coarse_half(self, blob: int = 0):
+        """(Xh, s) of a blob's FP16 coarse inverse as read by the memory-resident
+        solve: Xh float16 (n x n rounded up to 8 columns, zero padded) holding
+        X_ij / (s_i s_j), s float32 (n), or None when the handle keeps none."""
+        n, w = ctypes.c_int32(), ctypes.c_int32()
+        L.check(L.lib().ffea_gpu_diag_coarse_half(self._h, int(blob), ctypes.byref(n), ctypes.byref(w), None, None),
+                "diag_coarse_half")
+        if n.value == 0:
+            return None
+        xh = np.zeros((n.value, w.value), np.uint16)
+        sv = np.zeros(n.value, np.float32)
+        L.check(L.lib().ffea_gpu_diag_coarse_half(self._h, int(blob), ctypes.byref(n), ctypes.byref(w),
+                                                  xh.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)),
+                                                  sv.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+                "diag_coarse_half")
+        return xh.view(np.float16), sv
+
     def set_timing(self, on: bool):
         L.check(L.lib().ffea_gpu_set_timing(self._h, 1 if on else 0))
 

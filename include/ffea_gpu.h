@@ -392,6 +392,17 @@ int ffea_gpu_diag_spmv(ffea_gpu_t *h, int32_t variant, int32_t reps, double *us_
  * n = 0 when the handle has no coarse space.  No reference counterpart. */
 int ffea_gpu_diag_coarse(ffea_gpu_t *h, int32_t blob, int32_t *n, float *coarse_matrix, float *inverse);
 
+/* The FP16 copy of a blob's coarse inverse that the memory-resident CG
+ * kernel reads: scale[i] = sqrt(X_ii) (1 where X_ii is not a positive finite
+ * number) and half_inverse = X_ij / (scale[i] scale[j]) rounded to FP16 (IEEE
+ * binary16 bit patterns), n rows of *row_len halves (n rounded up to 8, the
+ * padding zero), copied to host arrays (either may be NULL; query n and
+ * *row_len first with both NULL).  n = 0 when the handle keeps no such copy
+ * (no coarse space, or the register-resident kernel).  No reference
+ * counterpart. */
+int ffea_gpu_diag_coarse_half(ffea_gpu_t *h, int32_t blob, int32_t *n, int32_t *row_len, uint16_t *half_inverse,
+                              float *scale);
+
 /* The coarse space's dense product on DEVICE arrays: c = alpha a b + beta d
  * for `batch` row-major n x n FP32 matrices n^2 apart (d may be NULL when
  * beta = 0; c may be d), enqueued on `stream` (cudaStream_t).  No reference

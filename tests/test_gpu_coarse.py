@@ -78,3 +78,43 @@ def test_coarse_inverse_after_create(gpulib, radius, replicas):
         a, x = w.coarse(0)
         _check_inverse(a, x)
     assert len(sizes) == 1
+
+
+def _check_half(x, xh, s):
+    """xh, s against the FP16 rounding of X_ij / (s_i s_j), s_i = sqrt(X_ii)
+    in FP32 (1 where X_ii is not positive), bit for bit, padding zero."""
+    n = x.shape[0]
+    d = np.diag(x)
+    s_ref = np.where((d > 0) & np.isfinite(d), np.sqrt(d), np.float32(1.0)).astype(np.float32)
+    assert np.array_equal(s.view(np.uint32), s_ref.view(np.uint32))
+    ref = (x / (s_ref[:, None] * s_ref[None, :])).astype(np.float16)
+    assert xh.shape == (n, (n + 7) // 8 * 8)
+    assert np.array_equal(xh[:, :n].view(np.uint16), ref.view(np.uint16))
+    assert not xh[:, n:].view(np.uint16).any()
+    # unit diagonal up to the rounding of s_i^2, and S Xh S symmetric as X
+    assert np.allclose(np.diag(xh[:, :n]).astype(np.float64), 1.0, atol=2e-3)
+    assert np.array_equal(xh[:, :n], xh[:, :n].T)
+
+
+@pytest.mark.parametrize("radius,max_ctas", [(8.0, "2"), (12.0, "3")])
+def test_memory_resident_half_inverse(gpulib, monkeypatch, radius, max_ctas):
+    """The memory-resident solve reads the coarse inverse from an FP16 copy
+    scaled to unit diagonal (k_coarse_half): after creation and after a
+    refresh it is the IEEE rounding of the current FP32 inverse, row by row;
+    the register-resident solve keeps no such copy."""
+    from ffea_gb300 import params as P
+    from ffea_gb300.world import PRECOND_TWO_LEVEL, World
+    from tests.helpers import spec
+    s = spec(radius_nm=radius, precision=P.PRECISION_MIXED, epsilon=1e-6)
+    with World([s], preconditioner=PRECOND_TWO_LEVEL) as w:
+        assert w.coarse_half(0) is None
+    monkeypatch.setenv("FFEA_GPU_CG_MEMORY_STATE", "1")
+    monkeypatch.setenv("FFEA_GPU_CG_MAX_CTAS", max_ctas)
+    with World([s], preconditioner=PRECOND_TWO_LEVEL) as w:
+        assert w.preconditioner() == PRECOND_TWO_LEVEL
+        for _ in range(2):
+            _, x = w.coarse(0)
+            xh, sv = w.coarse_half(0)
+            _check_half(x, xh, sv)
+            w.run(12)  # moves the mesh and refreshes the inverse
+            assert w.blob(0).status()["fail_bits"] == 0
