@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdlib>
 #include <limits>
 #include <cstdio>
@@ -389,7 +390,10 @@ int ffea_gpu_create_batch(int32_t num_blobs, const ffea_gpu_mesh *meshes, const 
     if (want < FFEA_GPU_PRECOND_JACOBI || want > FFEA_GPU_PRECOND_LEARNED) return fail("unknown preconditioner");
     const int64_t coarse_total = build_coarse(H);
     int coarse_nmax = 0;
-    bool coarse_ok = want != FFEA_GPU_PRECOND_JACOBI && H.precision == PREC_MIXED && !H.any_mass && !H.any_lumped;
+    // (the per-blob offsets of the dense coarse matrices are int32: a batch
+    // whose matrices together pass that range runs Jacobi)
+    bool coarse_ok = want != FFEA_GPU_PRECOND_JACOBI && H.precision == PREC_MIXED && !H.any_mass && !H.any_lumped &&
+                     coarse_total <= INT32_MAX && H.coarse_htotal <= INT32_MAX;
     for (const BlobParams &bp : H.bp) coarse_nmax = std::max(coarse_nmax, (int)bp.coarse_n);
     const bool coarse_reg_ok = coarse_ok && coarse_nmax <= CG_THREADS;
     // phi per row, the CTA's six rows of X, c, 6 x 32 reduction floats and
