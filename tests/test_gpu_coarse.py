@@ -91,9 +91,11 @@ def _check_half(x, xh, s):
     assert xh.shape == (n, (n + 7) // 8 * 8)
     assert np.array_equal(xh[:, :n].view(np.uint16), ref.view(np.uint16))
     assert not xh[:, n:].view(np.uint16).any()
-    # unit diagonal up to the rounding of s_i^2, and S Xh S symmetric as X
+    # unit diagonal up to the rounding of s_i^2, and S Xh S symmetric and
+    # positive definite as X (so the preconditioner stays SPD)
     assert np.allclose(np.diag(xh[:, :n]).astype(np.float64), 1.0, atol=2e-3)
     assert np.array_equal(xh[:, :n], xh[:, :n].T)
+    assert np.linalg.eigvalsh(xh[:, :n].astype(np.float64)).min() > 0
 
 
 @pytest.mark.parametrize("radius,max_ctas", [(8.0, "2"), (12.0, "3")])
