@@ -65,6 +65,47 @@ def test_host_rejects_corner_midpoint_mixup(lib):
         World([bad])
 
 
+def _with(s, **over):
+    d = {"mesh": {"pos": s.mesh.pos, "topology": s.mesh.topology}, "material": s.material, "drag": s.drag,
+         "pinned": None, "params": s.params}
+    for k, v in over.items():
+        if k in ("pos", "topology"):
+            d["mesh"][k] = v
+        else:
+            d[k] = v
+    return d
+
+
+@pytest.mark.parametrize("case,match", [
+    ("pinned_high", "pinned node index out of range"),
+    ("pinned_negative", "pinned node index out of range"),
+    ("repeated_corner", "repeats a corner node"),
+    ("negative_index", "out of bounds node index"),
+    ("empty", "empty mesh"),
+])
+def test_host_rejects_invalid_blobs(lib, case, match):
+    """Each invalid blob is refused by ffea_gpu_create_batch on the host, with
+    FFEA_ERROR and a message naming the fault, before any device work."""
+    from ffea_gb300 import _lib as L
+    from ffea_gb300.world import World
+    s = make_blob(sphere_mesh(2.5, seed=0), P.SimulationParams())
+    t = s.mesh.topology.copy()
+    if case == "pinned_high":
+        bad = _with(s, pinned=np.array([s.mesh.num_nodes + 3], np.int32))
+    elif case == "pinned_negative":
+        bad = _with(s, pinned=np.array([-1], np.int32))
+    elif case == "repeated_corner":
+        t[0, 1] = t[0, 0]
+        bad = _with(s, topology=t)
+    elif case == "negative_index":
+        t[2, 2] = -1
+        bad = _with(s, topology=t)
+    else:
+        bad = _with(s, topology=np.zeros((0, 10), np.int32), material=np.zeros((0, 5)))
+    with pytest.raises(L.FfeaGpuError, match=match):
+        World([bad])
+
+
 def test_ffea_seed_through_the_abi(lib, oracle):
     from ffea_gb300.world import ffea_seed
     for s in (0, 44, 123456789):
