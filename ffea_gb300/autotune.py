@@ -106,9 +106,10 @@ def tune(specs: Sequence, preconditioner: int = 0, space: Iterable[dict] | None 
             table = json.load(fh)
         if key in table:
             return table[key]
-    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    if space is None:
+        space = candidates(torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count)
     best, results = None, []
-    for cfg in (space if space is not None else candidates(sms)):
+    for cfg in space:
         t = time_config(specs, cfg, preconditioner, steps=steps, weights=weights)
         results.append((t, cfg))
         if log:
